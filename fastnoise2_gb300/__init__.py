@@ -1,0 +1,343 @@
+"""fastnoise2_gb300 -- GB300 (sm_103a) backend for FastNoise2 node trees.
+
+Python host mirror of FastNoise2's API for the node-tree generation path,
+bound to the C-ABI in ``include/FastNoise/FastNoise_C.h`` (the same entry
+points as the reference's ``FastNoise_C.h`` plus device-pointer additions).
+
+    import fastnoise2_gb300 as fn
+    node = fn.Node.from_encoded("...")            # FastNoise::NewFromEncodedNodeTree
+    simplex = fn.Node.new("Simplex")              # FastNoise::New<Simplex>()
+    simplex.set("Feature Scale", 50.0)            # SetScale(50)
+    out, (mn, mx) = simplex.gen_uniform_grid_3d((0, 0, 0), (64, 64, 64), (1, 1, 1), 1337)
+
+Generation always runs on the GPU.  If the native library is missing the
+import fails; if a call cannot run on the GPU, :class:`FastNoiseError` is raised.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from typing import Optional, Sequence, Tuple, Union
+
+import numpy as np
+
+__all__ = ["Node", "FastNoiseError", "lib", "library_path", "metadata_count", "metadata_name", "node_id"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_lib", "libfastnoise_gb300.so")
+
+
+class FastNoiseError(RuntimeError):
+    """A GPU generation call failed (status code and message from the library)."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"fastnoise_gb300 error {code}: {message}")
+        self.code = code
+        self.message = message
+
+
+def library_path() -> str:
+    return _LIB_PATH
+
+
+_lib = None
+_FP = ctypes.POINTER(ctypes.c_float)
+
+
+def _declare(L):
+    c_int, c_float, vp, cp, c_bool, c_uint = ctypes.c_int, ctypes.c_float, ctypes.c_void_p, ctypes.c_char_p, ctypes.c_bool, ctypes.c_uint
+    sig = {
+        "fnNewFromEncodedNodeTree": (vp, [cp, c_uint]),
+        "fnDeleteNodeRef": (None, [vp]),
+        "fnGetActiveFeatureSet": (c_uint, [vp]),
+        "fnGetMetadataID": (c_int, [vp]),
+        "fnGenUniformGrid2D": (None, [vp, _FP, c_float, c_float, c_int, c_int, c_float, c_float, c_int, _FP]),
+        "fnGenUniformGrid3D": (None, [vp, _FP, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, _FP]),
+        "fnGenUniformGrid4D": (None, [vp, _FP] + [c_float] * 4 + [c_int] * 4 + [c_float] * 4 + [c_int, _FP]),
+        "fnGenPositionArray2D": (None, [vp, _FP, c_int, _FP, _FP, c_float, c_float, c_int, _FP]),
+        "fnGenPositionArray3D": (None, [vp, _FP, c_int, _FP, _FP, _FP, c_float, c_float, c_float, c_int, _FP]),
+        "fnGenPositionArray4D": (None, [vp, _FP, c_int, _FP, _FP, _FP, _FP, c_float, c_float, c_float, c_float, c_int, _FP]),
+        "fnGenTileable2D": (None, [vp, _FP, c_int, c_int, c_float, c_float, c_int, _FP]),
+        "fnGenSingle2D": (c_float, [vp, c_float, c_float, c_int]),
+        "fnGenSingle3D": (c_float, [vp, c_float, c_float, c_float, c_int]),
+        "fnGenSingle4D": (c_float, [vp, c_float, c_float, c_float, c_float, c_int]),
+        "fnGetMetadataCount": (c_int, []),
+        "fnGetMetadataName": (cp, [c_int]),
+        "fnNewFromMetadata": (vp, [c_int, c_uint]),
+        "fnGetMetadataVariableCount": (c_int, [c_int]),
+        "fnGetMetadataVariableName": (cp, [c_int, c_int]),
+        "fnGetMetadataVariableType": (c_int, [c_int, c_int]),
+        "fnGetMetadataVariableDimensionIdx": (c_int, [c_int, c_int]),
+        "fnGetMetadataEnumCount": (c_int, [c_int, c_int]),
+        "fnGetMetadataEnumName": (cp, [c_int, c_int, c_int]),
+        "fnSetVariableFloat": (c_bool, [vp, c_int, c_float]),
+        "fnSetVariableIntEnum": (c_bool, [vp, c_int, c_int]),
+        "fnGetMetadataNodeLookupCount": (c_int, [c_int]),
+        "fnGetMetadataNodeLookupName": (cp, [c_int, c_int]),
+        "fnGetMetadataNodeLookupDimensionIdx": (c_int, [c_int, c_int]),
+        "fnSetNodeLookup": (c_bool, [vp, c_int, vp]),
+        "fnGetMetadataHybridCount": (c_int, [c_int]),
+        "fnGetMetadataHybridName": (cp, [c_int, c_int]),
+        "fnGetMetadataHybridDimensionIdx": (c_int, [c_int, c_int]),
+        "fnSetHybridNodeLookup": (c_bool, [vp, c_int, vp]),
+        "fnSetHybridFloat": (c_bool, [vp, c_int, c_float]),
+        "fnGetMetadataDescription": (cp, [c_int]),
+        "fnGetMetadataGroupCount": (c_int, [c_int]),
+        "fnGetMetadataGroupName": (cp, [c_int, c_int]),
+        "fnGetMetadataVariableDescription": (cp, [c_int, c_int]),
+        "fnGetMetadataVariableDefaultFloat": (c_float, [c_int, c_int]),
+        "fnGetMetadataVariableDefaultIntEnum": (c_int, [c_int, c_int]),
+        "fnGetMetadataVariableMinFloat": (c_float, [c_int, c_int]),
+        "fnGetMetadataVariableMaxFloat": (c_float, [c_int, c_int]),
+        "fnGetMetadataNodeLookupDescription": (cp, [c_int, c_int]),
+        "fnGetMetadataHybridDescription": (cp, [c_int, c_int]),
+        "fnGetMetadataHybridDefault": (c_float, [c_int, c_int]),
+        "fnGetLastError": (c_int, []),
+        "fnGetLastErrorString": (cp, []),
+        "fnSerialiseNodeTree": (c_int, [vp, ctypes.c_char_p, c_int]),
+        "fnPrepare": (c_int, [vp, c_int]),
+        "fnCompileInfo": (c_int, [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
+        "fnGenUniformGrid2DDevice": (c_int, [vp, vp, c_float, c_float, c_int, c_int, c_float, c_float, c_int, vp, vp]),
+        "fnGenUniformGrid3DDevice": (c_int, [vp, vp, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, vp, vp]),
+        "fnGenUniformGrid4DDevice": (c_int, [vp, vp] + [c_float] * 4 + [c_int] * 4 + [c_float] * 4 + [c_int, vp, vp]),
+        "fnGenPositionArray2DDevice": (c_int, [vp, vp, c_int, vp, vp, c_float, c_float, c_int, vp, vp]),
+        "fnGenPositionArray3DDevice": (c_int, [vp, vp, c_int, vp, vp, vp, c_float, c_float, c_float, c_int, vp, vp]),
+        "fnGenPositionArray4DDevice": (c_int, [vp, vp, c_int, vp, vp, vp, vp, c_float, c_float, c_float, c_float, c_int, vp, vp]),
+        "fnGenTileable2DDevice": (c_int, [vp, vp, c_int, c_int, c_float, c_float, c_int, vp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    return L
+
+
+def lib():
+    """The loaded native library (raises ImportError if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB_PATH):
+            raise ImportError(f"{_LIB_PATH} is missing: build it with `python -m fastnoise2_gb300.build` "
+                              "(this package has no CPU fallback)")
+        _lib = _declare(ctypes.CDLL(_LIB_PATH))
+    return _lib
+
+
+def _check():
+    L = lib()
+    code = L.fnGetLastError()
+    if code:
+        raise FastNoiseError(code, L.fnGetLastErrorString().decode())
+
+
+def _fp(a: np.ndarray):
+    return a.ctypes.data_as(_FP)
+
+
+def metadata_count() -> int:
+    return lib().fnGetMetadataCount()
+
+
+def metadata_name(node_id: int) -> str:
+    return lib().fnGetMetadataName(node_id).decode()
+
+
+def node_id(name: str) -> int:
+    for i in range(metadata_count()):
+        if metadata_name(i) == name:
+            return i
+    raise KeyError(name)
+
+
+class Node:
+    """Reference-counted handle to a node (FastNoise::SmartNode<>)."""
+
+    def __init__(self, handle: int):
+        if not handle:
+            raise ValueError("null node handle")
+        self._h = handle
+
+    # -- construction -------------------------------------------------------
+    @classmethod
+    def new(cls, name_or_id: Union[str, int]) -> "Node":
+        nid = node_id(name_or_id) if isinstance(name_or_id, str) else int(name_or_id)
+        h = lib().fnNewFromMetadata(nid, 0)
+        if not h:
+            raise KeyError(name_or_id)
+        return cls(h)
+
+    @classmethod
+    def from_encoded(cls, encoded: str) -> Optional["Node"]:
+        h = lib().fnNewFromEncodedNodeTree(encoded.encode(), 0)
+        return cls(h) if h else None
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.fnDeleteNodeRef(self._h)
+            self._h = None
+
+    @property
+    def handle(self) -> int:
+        return self._h
+
+    @property
+    def id(self) -> int:
+        return lib().fnGetMetadataID(self._h)
+
+    @property
+    def name(self) -> str:
+        return metadata_name(self.id)
+
+    # -- members -----------------------------------------------------------
+    def _find(self, kind: str, name: str, dim: Optional[int]) -> int:
+        L, nid = lib(), self.id
+        count = {"var": L.fnGetMetadataVariableCount, "lookup": L.fnGetMetadataNodeLookupCount,
+                 "hybrid": L.fnGetMetadataHybridCount}[kind](nid)
+        getn = {"var": L.fnGetMetadataVariableName, "lookup": L.fnGetMetadataNodeLookupName,
+                "hybrid": L.fnGetMetadataHybridName}[kind]
+        getd = {"var": L.fnGetMetadataVariableDimensionIdx, "lookup": L.fnGetMetadataNodeLookupDimensionIdx,
+                "hybrid": L.fnGetMetadataHybridDimensionIdx}[kind]
+        for i in range(count):
+            if getn(nid, i).decode() == name and (dim is None or getd(nid, i) == dim):
+                return i
+        return -1
+
+    def set(self, name: str, value, dim: Optional[int] = None) -> "Node":
+        """Set a member variable, node lookup or hybrid by its metadata name."""
+        L = lib()
+        i = self._find("var", name, dim)
+        if i >= 0:
+            vtype = L.fnGetMetadataVariableType(self.id, i)
+            if isinstance(value, str):
+                names = [L.fnGetMetadataEnumName(self.id, i, e).decode() for e in range(L.fnGetMetadataEnumCount(self.id, i))]
+                value = names.index(value)
+            ok = L.fnSetVariableFloat(self._h, i, float(value)) if vtype == 0 else L.fnSetVariableIntEnum(self._h, i, int(value))
+        elif (i := self._find("lookup", name, dim)) >= 0:
+            ok = L.fnSetNodeLookup(self._h, i, value.handle)
+        elif (i := self._find("hybrid", name, dim)) >= 0:
+            ok = L.fnSetHybridNodeLookup(self._h, i, value.handle) if isinstance(value, Node) else L.fnSetHybridFloat(self._h, i, float(value))
+        else:
+            raise KeyError(f"{self.name} has no member {name!r}")
+        if not ok:
+            raise ValueError(f"{self.name}.{name} rejected {value!r}")
+        return self
+
+    def set_var_bits(self, index: int, bits: int) -> "Node":
+        """fnSetVariableIntEnum with raw ValueUnion bits (how encoded trees set variables)."""
+        lib().fnSetVariableIntEnum(self._h, index, int(np.int32(np.uint32(bits & 0xFFFFFFFF))))
+        return self
+
+    def encode(self) -> str:
+        L = lib()
+        n = L.fnSerialiseNodeTree(self._h, None, 0)
+        if n < 0:
+            _check()
+        buf = ctypes.create_string_buffer(n + 1)
+        L.fnSerialiseNodeTree(self._h, buf, n + 1)
+        return buf.value.decode()
+
+    def compile_info(self, dim: int) -> Tuple[int, int]:
+        """(instructions, registers) of the device program for `dim` (host-only compile)."""
+        ni, nr = ctypes.c_int(0), ctypes.c_int(0)
+        if lib().fnCompileInfo(self._h, dim, ctypes.byref(ni), ctypes.byref(nr)) != 0:
+            _check()
+        return ni.value, nr.value
+
+    def prepare(self, dim: int) -> None:
+        if lib().fnPrepare(self._h, dim) != 0:
+            _check()
+
+    # -- generation (host memory, reference-compatible) ----------------------
+    def gen_uniform_grid(self, offset: Sequence[float], count: Sequence[int], step: Sequence[float], seed: int,
+                         out: Optional[np.ndarray] = None) -> Tuple[np.ndarray, Tuple[float, float]]:
+        dim = len(count)
+        total = int(np.prod([max(int(c), 0) for c in count]))
+        if out is None:
+            out = np.empty(max(total, 1), np.float32)
+        mm = np.zeros(2, np.float32)
+        L = lib()
+        if dim == 2:
+            L.fnGenUniformGrid2D(self._h, _fp(out), *map(float, offset), *map(int, count), *map(float, step), int(np.int32(seed)), _fp(mm))
+        elif dim == 3:
+            L.fnGenUniformGrid3D(self._h, _fp(out), *map(float, offset), *map(int, count), *map(float, step), int(np.int32(seed)), _fp(mm))
+        elif dim == 4:
+            L.fnGenUniformGrid4D(self._h, _fp(out), *map(float, offset), *map(int, count), *map(float, step), int(np.int32(seed)), _fp(mm))
+        else:
+            raise ValueError("dimension must be 2, 3 or 4")
+        _check()
+        return out[:total], (float(mm[0]), float(mm[1]))
+
+    def gen_uniform_grid_2d(self, offset, count, step, seed, out=None):
+        return self.gen_uniform_grid(offset, count, step, seed, out)
+
+    def gen_uniform_grid_3d(self, offset, count, step, seed, out=None):
+        return self.gen_uniform_grid(offset, count, step, seed, out)
+
+    def gen_uniform_grid_4d(self, offset, count, step, seed, out=None):
+        return self.gen_uniform_grid(offset, count, step, seed, out)
+
+    def gen_position_array(self, positions: Sequence[np.ndarray], offset: Sequence[float], seed: int,
+                           out: Optional[np.ndarray] = None) -> Tuple[np.ndarray, Tuple[float, float]]:
+        dim = len(positions)
+        arrs = [np.ascontiguousarray(p, np.float32) for p in positions]
+        count = len(arrs[0])
+        if out is None:
+            out = np.empty(max(count, 1), np.float32)
+        mm = np.zeros(2, np.float32)
+        L = lib()
+        s = int(np.int32(seed))
+        if dim == 2:
+            L.fnGenPositionArray2D(self._h, _fp(out), count, *map(_fp, arrs), *map(float, offset), s, _fp(mm))
+        elif dim == 3:
+            L.fnGenPositionArray3D(self._h, _fp(out), count, *map(_fp, arrs), *map(float, offset), s, _fp(mm))
+        elif dim == 4:
+            L.fnGenPositionArray4D(self._h, _fp(out), count, *map(_fp, arrs), *map(float, offset), s, _fp(mm))
+        else:
+            raise ValueError("dimension must be 2, 3 or 4")
+        _check()
+        return out[:count], (float(mm[0]), float(mm[1]))
+
+    def gen_tileable_2d(self, size: Sequence[int], step: Sequence[float], seed: int,
+                        out: Optional[np.ndarray] = None) -> Tuple[np.ndarray, Tuple[float, float]]:
+        total = max(int(size[0]), 0) * max(int(size[1]), 0)
+        if out is None:
+            out = np.empty(max(total, 1), np.float32)
+        mm = np.zeros(2, np.float32)
+        lib().fnGenTileable2D(self._h, _fp(out), int(size[0]), int(size[1]), float(step[0]), float(step[1]), int(np.int32(seed)), _fp(mm))
+        _check()
+        return out[:total], (float(mm[0]), float(mm[1]))
+
+    def gen_single(self, pos: Sequence[float], seed: int) -> float:
+        L = lib()
+        s = int(np.int32(seed))
+        p = list(map(float, pos))
+        v = {2: L.fnGenSingle2D, 3: L.fnGenSingle3D, 4: L.fnGenSingle4D}[len(p)](self._h, *p, s)
+        _check()
+        return float(v)
+
+    # -- generation into device memory (additions) ---------------------------
+    def gen_uniform_grid_device(self, out_ptr: int, offset, count, step, seed: int, minmax_ptr: int = 0,
+                                stream: int = 0) -> None:
+        """Queue a grid into device memory `out_ptr` on `stream` (a cudaStream_t value)."""
+        L = lib()
+        dim = len(count)
+        f = {2: L.fnGenUniformGrid2DDevice, 3: L.fnGenUniformGrid3DDevice, 4: L.fnGenUniformGrid4DDevice}[dim]
+        rc = f(self._h, out_ptr, *map(float, offset), *map(int, count), *map(float, step), int(np.int32(seed)),
+               minmax_ptr or None, stream or None)
+        if rc != 0:
+            _check()
+
+    def gen_position_array_device(self, out_ptr: int, count: int, pos_ptrs: Sequence[int], offset, seed: int,
+                                  minmax_ptr: int = 0, stream: int = 0) -> None:
+        L = lib()
+        dim = len(pos_ptrs)
+        f = {2: L.fnGenPositionArray2DDevice, 3: L.fnGenPositionArray3DDevice, 4: L.fnGenPositionArray4DDevice}[dim]
+        rc = f(self._h, out_ptr, int(count), *pos_ptrs, *map(float, offset), int(np.int32(seed)), minmax_ptr or None, stream or None)
+        if rc != 0:
+            _check()
+
+    def gen_tileable_2d_device(self, out_ptr: int, size, step, seed: int, minmax_ptr: int = 0, stream: int = 0) -> None:
+        rc = lib().fnGenTileable2DDevice(self._h, out_ptr, int(size[0]), int(size[1]), float(step[0]), float(step[1]),
+                                         int(np.int32(seed)), minmax_ptr or None, stream or None)
+        if rc != 0:
+            _check()

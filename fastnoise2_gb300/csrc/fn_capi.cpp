@@ -1,0 +1,553 @@
+// fn_capi.cpp -- the FastNoise_C entry points (include/FastNoise/FastNoise_C.h).
+//
+// Part 1 mirrors reference src/FastNoise/FastNoise_C.cpp:41-476 (same names,
+// argument meaning, sentinel return values).  Generation runs on the GPU
+// through the program interpreter; host output arrays are filled by a
+// device->host copy on this thread's stream.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <string>
+
+#include "../../include/FastNoise/FastNoise_C.h"
+#include "fn_runtime.h"
+
+using namespace fn;
+
+namespace {
+
+Node* N(void* p) { return static_cast<Node*>(p); }
+const Node* N(const void* p) { return static_cast<const Node*>(p); }
+
+float f_of(int32_t bits) { float f; std::memcpy(&f, &bits, 4); return f; }
+int32_t bits_of(float f) { int32_t i; std::memcpy(&i, &f, 4); return i; }
+
+void store_minmax(float* mm, float mn, float mx)   // FastNoise_C.cpp:32-39
+{
+    if (mm) { mm[0] = mn; mm[1] = mx; }
+}
+
+void fill_nan(float* out, long long n, float* mm)
+{
+    const float q = std::numeric_limits<float>::quiet_NaN();
+    if (out) for (long long i = 0; i < n; ++i) out[i] = q;
+    store_minmax(mm, q, q);
+}
+
+bool ensure(float*& buf, size_t& cap, size_t n)
+{
+    if (n <= cap) return true;
+    if (buf) cudaFree(buf);
+    buf = nullptr;
+    cap = 0;
+    size_t want = n < 4096 ? 4096 : n;
+    if (!cuda_ok(cudaMalloc(&buf, want * sizeof(float)), "cudaMalloc(output)")) return false;
+    cap = want;
+    return true;
+}
+
+// Run one host-memory generation call end to end.
+void gen_host(const void* node, PointArgs args, float* out, float* minmax, const float* const* hpos)
+{
+    clear_error();
+    const long long total = args.total;
+    if (!node || total < 0 || (total > 0 && !out)) { set_error(FN_ERR_ARG, "invalid arguments"); fill_nan(out, total > 0 ? total : 0, minmax); return; }
+    ThreadCtx* ctx = thread_ctx();
+    DeviceProgram prog;
+    if (!ctx || !get_program(N(node), args.dim, prog)) { fill_nan(out, total, minmax); return; }
+    MinMaxWork* work = work_for_stream(ctx->stream);
+    if (!work || !ensure(ctx->dbuf, ctx->dbuf_cap, (size_t)total)) { fill_nan(out, total, minmax); return; }
+    if (args.src == kSrcPositions && total > 0) {
+        if ((size_t)total > ctx->dpos_cap) {
+            for (float*& p : ctx->dpos) { if (p) cudaFree(p); p = nullptr; }
+            ctx->dpos_cap = 0;
+            for (int k = 0; k < args.dim; ++k)
+                if (!cuda_ok(cudaMalloc(&ctx->dpos[k], (size_t)total * 4), "cudaMalloc(positions)")) { fill_nan(out, total, minmax); return; }
+            ctx->dpos_cap = (size_t)total;
+        }
+        for (int k = 0; k < args.dim; ++k) {
+            if (!hpos[k]) { set_error(FN_ERR_ARG, "null position array"); fill_nan(out, total, minmax); return; }
+            if (!cuda_ok(cudaMemcpyAsync(ctx->dpos[k], hpos[k], (size_t)total * 4, cudaMemcpyHostToDevice, ctx->stream), "copy positions")) {
+                fill_nan(out, total, minmax);
+                return;
+            }
+            args.pos[k] = ctx->dpos[k];
+        }
+    }
+    if (!cuda_ok(launch_interpreter(prog.dptr, prog.bytes, args, ctx->dbuf, work, nullptr, ctx->stream), "launch")) { fill_nan(out, total, minmax); return; }
+    if (total > 0 && !cuda_ok(cudaMemcpyAsync(out, ctx->dbuf, (size_t)total * 4, cudaMemcpyDeviceToHost, ctx->stream), "copy output")) { fill_nan(out, total, minmax); return; }
+    if (!cuda_ok(cudaMemcpyAsync(ctx->hminmax, work->result, 8, cudaMemcpyDeviceToHost, ctx->stream), "copy minmax") ||
+        !cuda_ok(cudaStreamSynchronize(ctx->stream), "synchronize")) {
+        fill_nan(out, total, minmax);
+        return;
+    }
+    store_minmax(minmax, ctx->hminmax[0], ctx->hminmax[1]);
+}
+
+int gen_device(const void* node, PointArgs args, float* dout, float* dminmax, void* stream)
+{
+    clear_error();
+    if (!node || args.total < 0 || (args.total > 0 && !dout)) { set_error(FN_ERR_ARG, "invalid arguments"); return FN_ERR_ARG; }
+    if (!thread_ctx()) return FN_ERR_CUDA;
+    DeviceProgram prog;
+    if (!get_program(N(node), args.dim, prog)) return last_error();
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    MinMaxWork* work = work_for_stream(s);
+    if (!work) return FN_ERR_CUDA;
+    if (!cuda_ok(launch_interpreter(prog.dptr, prog.bytes, args, dout, work, dminmax, s), "launch")) return FN_ERR_CUDA;
+    return FN_OK;
+}
+
+PointArgs grid_args(int dim, const float* off, const int* cnt, const float* step, int seed)
+{
+    PointArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.src = kSrcGrid;
+    a.dim = dim;
+    a.seed = seed;
+    long long total = 1;
+    for (int k = 0; k < dim; ++k) {
+        a.count[k] = cnt[k];
+        a.offset[k] = off[k];
+        a.step[k] = step[k];
+        total *= cnt[k] > 0 ? cnt[k] : 0;
+    }
+    a.total = total;
+    return a;
+}
+
+PointArgs tile_args(int xSize, int ySize, float xStep, float yStep, int seed)
+{
+    PointArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.src = kSrcTileable;
+    a.dim = 4;
+    a.seed = seed;
+    a.count[0] = xSize;
+    a.count[1] = ySize;
+    const float pi2Recip = 0.15915493667f;                    // Generator.inl:386-392
+    const float xSizePi = (float)xSize * pi2Recip;
+    const float ySizePi = (float)ySize * pi2Recip;
+    a.tfreq[0] = xSizePi * xStep;
+    a.tfreq[1] = ySizePi * yStep;
+    a.tmul[0] = 1 / xSizePi;
+    a.tmul[1] = 1 / ySizePi;
+    a.total = (long long)(xSize > 0 ? xSize : 0) * (ySize > 0 ? ySize : 0);
+    return a;
+}
+
+PointArgs pos_args(int dim, int count, const float* off, int seed)
+{
+    PointArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.src = kSrcPositions;
+    a.dim = dim;
+    a.seed = seed;
+    a.total = count > 0 ? count : 0;
+    for (int k = 0; k < dim; ++k) a.offset[k] = off[k];
+    return a;
+}
+
+float gen_single(const void* node, int dim, const float* p, int seed)
+{
+    const int cnt[4] = {1, 1, 1, 1};
+    const float step[4] = {0, 0, 0, 0};
+    float out = 0.0f;
+    gen_host(node, grid_args(dim, p, cnt, step, seed), &out, nullptr, nullptr);   // fma(0, 0, p) == p
+    return out;
+}
+
+const NodeMeta* M(int id) { return meta_by_id(id); }
+
+}  // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------------ lifetime
+
+void* fnNewFromEncodedNodeTree(const char* encodedString, unsigned)
+{
+    return decode_tree(encodedString);
+}
+
+void fnDeleteNodeRef(void* node)
+{
+    if (node) node_unref(N(node));
+}
+
+unsigned fnGetActiveFeatureSet(const void*) { return FN_GB300_FEATURE_SET; }
+
+int fnGetMetadataID(const void* node) { return node ? N(node)->meta->id : -1; }
+
+// ------------------------------------------------------------------ generation (host memory)
+
+void fnGenUniformGrid2D(const void* node, float* noiseOut, float xOffset, float yOffset, int xCount, int yCount,
+                        float xStepSize, float yStepSize, int seed, float* outputMinMax)
+{
+    const float off[2] = {xOffset, yOffset};
+    const int cnt[2] = {xCount, yCount};
+    const float st[2] = {xStepSize, yStepSize};
+    gen_host(node, grid_args(2, off, cnt, st, seed), noiseOut, outputMinMax, nullptr);
+}
+
+void fnGenUniformGrid3D(const void* node, float* noiseOut, float xOffset, float yOffset, float zOffset, int xCount,
+                        int yCount, int zCount, float xStepSize, float yStepSize, float zStepSize, int seed,
+                        float* outputMinMax)
+{
+    const float off[3] = {xOffset, yOffset, zOffset};
+    const int cnt[3] = {xCount, yCount, zCount};
+    const float st[3] = {xStepSize, yStepSize, zStepSize};
+    gen_host(node, grid_args(3, off, cnt, st, seed), noiseOut, outputMinMax, nullptr);
+}
+
+void fnGenUniformGrid4D(const void* node, float* noiseOut, float xOffset, float yOffset, float zOffset, float wOffset,
+                        int xCount, int yCount, int zCount, int wCount, float xStepSize, float yStepSize,
+                        float zStepSize, float wStepSize, int seed, float* outputMinMax)
+{
+    const float off[4] = {xOffset, yOffset, zOffset, wOffset};
+    const int cnt[4] = {xCount, yCount, zCount, wCount};
+    const float st[4] = {xStepSize, yStepSize, zStepSize, wStepSize};
+    gen_host(node, grid_args(4, off, cnt, st, seed), noiseOut, outputMinMax, nullptr);
+}
+
+void fnGenPositionArray2D(const void* node, float* noiseOut, int count, const float* xPosArray, const float* yPosArray,
+                          float xOffset, float yOffset, int seed, float* outputMinMax)
+{
+    const float off[2] = {xOffset, yOffset};
+    const float* p[4] = {xPosArray, yPosArray, nullptr, nullptr};
+    gen_host(node, pos_args(2, count, off, seed), noiseOut, outputMinMax, p);
+}
+
+void fnGenPositionArray3D(const void* node, float* noiseOut, int count, const float* xPosArray, const float* yPosArray,
+                          const float* zPosArray, float xOffset, float yOffset, float zOffset, int seed,
+                          float* outputMinMax)
+{
+    const float off[3] = {xOffset, yOffset, zOffset};
+    const float* p[4] = {xPosArray, yPosArray, zPosArray, nullptr};
+    gen_host(node, pos_args(3, count, off, seed), noiseOut, outputMinMax, p);
+}
+
+void fnGenPositionArray4D(const void* node, float* noiseOut, int count, const float* xPosArray, const float* yPosArray,
+                          const float* zPosArray, const float* wPosArray, float xOffset, float yOffset, float zOffset,
+                          float wOffset, int seed, float* outputMinMax)
+{
+    const float off[4] = {xOffset, yOffset, zOffset, wOffset};
+    const float* p[4] = {xPosArray, yPosArray, zPosArray, wPosArray};
+    gen_host(node, pos_args(4, count, off, seed), noiseOut, outputMinMax, p);
+}
+
+void fnGenTileable2D(const void* node, float* noiseOut, int xSize, int ySize, float xStepSize, float yStepSize, int seed,
+                     float* outputMinMax)
+{
+    gen_host(node, tile_args(xSize, ySize, xStepSize, yStepSize, seed), noiseOut, outputMinMax, nullptr);
+}
+
+float fnGenSingle2D(const void* node, float x, float y, int seed)
+{
+    const float p[2] = {x, y};
+    return gen_single(node, 2, p, seed);
+}
+
+float fnGenSingle3D(const void* node, float x, float y, float z, int seed)
+{
+    const float p[3] = {x, y, z};
+    return gen_single(node, 3, p, seed);
+}
+
+float fnGenSingle4D(const void* node, float x, float y, float z, float w, int seed)
+{
+    const float p[4] = {x, y, z, w};
+    return gen_single(node, 4, p, seed);
+}
+
+// ------------------------------------------------------------------ metadata (FastNoise_C.cpp:117-476)
+
+int fnGetMetadataCount(void) { return (int)all_meta().size(); }
+
+const char* fnGetMetadataName(int id)
+{
+    const NodeMeta* m = M(id);
+    return m ? m->name : "INVALID NODE ID";
+}
+
+void* fnNewFromMetadata(int id, unsigned)
+{
+    return node_new(id);
+}
+
+int fnGetMetadataVariableCount(int id)
+{
+    const NodeMeta* m = M(id);
+    return m ? (int)m->vars.size() : -1;
+}
+
+const char* fnGetMetadataVariableName(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    if (!m) return "INVALID NODE ID";
+    return (size_t)i < m->vars.size() ? m->vars[i].name : "INVALID VARIABLE INDEX";
+}
+
+int fnGetMetadataVariableType(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    return (m && (size_t)i < m->vars.size()) ? (int)m->vars[i].type : -1;
+}
+
+int fnGetMetadataVariableDimensionIdx(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    return (m && (size_t)i < m->vars.size()) ? m->vars[i].dim : -1;
+}
+
+int fnGetMetadataEnumCount(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    return (m && (size_t)i < m->vars.size()) ? (int)m->vars[i].enums.size() : -1;
+}
+
+const char* fnGetMetadataEnumName(int id, int i, int e)
+{
+    const NodeMeta* m = M(id);
+    if (!m) return "INVALID NODE ID";
+    if ((size_t)i >= m->vars.size()) return "INVALID VARIABLE INDEX";
+    return (size_t)e < m->vars[i].enums.size() ? m->vars[i].enums[e] : "INVALID ENUM INDEX";
+}
+
+bool fnSetVariableFloat(void* node, int i, float value)
+{
+    return node && N(node)->set_var(i, bits_of(value));      // ValueUnion(float)
+}
+
+bool fnSetVariableIntEnum(void* node, int i, int value)
+{
+    return node && N(node)->set_var(i, value);               // ValueUnion(int)
+}
+
+int fnGetMetadataNodeLookupCount(int id)
+{
+    const NodeMeta* m = M(id);
+    return m ? (int)m->lookups.size() : -1;
+}
+
+const char* fnGetMetadataNodeLookupName(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    if (!m) return "INVALID NODE ID";
+    return (size_t)i < m->lookups.size() ? m->lookups[i].name : "INVALID NODE LOOKUP INDEX";
+}
+
+int fnGetMetadataNodeLookupDimensionIdx(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    return (m && (size_t)i < m->lookups.size()) ? m->lookups[i].dim : -1;
+}
+
+bool fnSetNodeLookup(void* node, int i, const void* lookup)
+{
+    return node && N(node)->set_lookup(i, const_cast<Node*>(N(lookup)));
+}
+
+int fnGetMetadataHybridCount(int id)
+{
+    const NodeMeta* m = M(id);
+    return m ? (int)m->hybrids.size() : -1;
+}
+
+const char* fnGetMetadataHybridName(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    if (!m) return "INVALID NODE ID";
+    return (size_t)i < m->hybrids.size() ? m->hybrids[i].name : "INVALID HYBRID INDEX";
+}
+
+int fnGetMetadataHybridDimensionIdx(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    return (m && (size_t)i < m->hybrids.size()) ? m->hybrids[i].dim : -1;
+}
+
+bool fnSetHybridNodeLookup(void* node, int i, const void* lookup)
+{
+    return node && N(node)->set_hybrid_node(i, const_cast<Node*>(N(lookup)));
+}
+
+bool fnSetHybridFloat(void* node, int i, float value)
+{
+    return node && N(node)->set_hybrid_float(i, value);
+}
+
+const char* fnGetMetadataDescription(int id)
+{
+    const NodeMeta* m = M(id);
+    return m ? m->description : "INVALID NODE ID";
+}
+
+int fnGetMetadataGroupCount(int id)
+{
+    const NodeMeta* m = M(id);
+    return m ? (int)m->groups.size() : -1;
+}
+
+const char* fnGetMetadataGroupName(int id, int g)
+{
+    const NodeMeta* m = M(id);
+    if (!m) return "INVALID NODE ID";
+    return (size_t)g < m->groups.size() ? m->groups[g] : "INVALID GROUP INDEX";
+}
+
+const char* fnGetMetadataVariableDescription(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    if (!m) return "INVALID NODE ID";
+    return (size_t)i < m->vars.size() ? m->vars[i].description : "INVALID VARIABLE INDEX";
+}
+
+float fnGetMetadataVariableDefaultFloat(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    return (m && (size_t)i < m->vars.size()) ? f_of(m->vars[i].def) : 0.0f;
+}
+
+int fnGetMetadataVariableDefaultIntEnum(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    return (m && (size_t)i < m->vars.size()) ? m->vars[i].def : 0;
+}
+
+float fnGetMetadataVariableMinFloat(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    return (m && (size_t)i < m->vars.size()) ? f_of(m->vars[i].vmin) : 0.0f;
+}
+
+float fnGetMetadataVariableMaxFloat(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    return (m && (size_t)i < m->vars.size()) ? f_of(m->vars[i].vmax) : 0.0f;
+}
+
+const char* fnGetMetadataNodeLookupDescription(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    if (!m) return "INVALID NODE ID";
+    return (size_t)i < m->lookups.size() ? m->lookups[i].description : "INVALID NODE LOOKUP INDEX";
+}
+
+const char* fnGetMetadataHybridDescription(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    if (!m) return "INVALID NODE ID";
+    return (size_t)i < m->hybrids.size() ? m->hybrids[i].description : "INVALID HYBRID INDEX";
+}
+
+float fnGetMetadataHybridDefault(int id, int i)
+{
+    const NodeMeta* m = M(id);
+    return (m && (size_t)i < m->hybrids.size()) ? m->hybrids[i].def : 0.0f;
+}
+
+// ------------------------------------------------------------------ additions
+
+int fnGetLastError(void) { return last_error(); }
+const char* fnGetLastErrorString(void) { return last_error_string(); }
+
+int fnSerialiseNodeTree(const void* node, char* buffer, int bufferSize)
+{
+    clear_error();
+    if (!node) { set_error(FN_ERR_ARG, "null node"); return FN_ERR_ARG; }
+    std::string s = encode_tree(N(node));
+    if (s.empty()) { set_error(FN_ERR_ARG, "tree has an unset source"); return FN_ERR_ARG; }
+    if (buffer && bufferSize > (int)s.size()) std::memcpy(buffer, s.c_str(), s.size() + 1);
+    return (int)s.size();
+}
+
+int fnCompileInfo(const void* node, int dimension, int* nInstr, int* nRegs)
+{
+    clear_error();
+    if (!node) { set_error(FN_ERR_ARG, "null node"); return FN_ERR_ARG; }
+    CompiledProgram p;
+    std::string err;
+    if (!compile_program(N(node), dimension, p, err)) { set_error(FN_ERR_COMPILE, err); return FN_ERR_COMPILE; }
+    if (nInstr) *nInstr = p.n_instr;
+    if (nRegs) *nRegs = p.n_regs;
+    return FN_OK;
+}
+
+int fnPrepare(const void* node, int dimension)
+{
+    clear_error();
+    DeviceProgram p;
+    if (!thread_ctx()) return FN_ERR_CUDA;
+    return get_program(N(node), dimension, p) ? FN_OK : last_error();
+}
+
+int fnGenUniformGrid2DDevice(const void* node, float* dOut, float xOffset, float yOffset, int xCount, int yCount,
+                             float xStepSize, float yStepSize, int seed, float* dMinMax, void* stream)
+{
+    const float off[2] = {xOffset, yOffset};
+    const int cnt[2] = {xCount, yCount};
+    const float st[2] = {xStepSize, yStepSize};
+    return gen_device(node, grid_args(2, off, cnt, st, seed), dOut, dMinMax, stream);
+}
+
+int fnGenUniformGrid3DDevice(const void* node, float* dOut, float xOffset, float yOffset, float zOffset, int xCount,
+                             int yCount, int zCount, float xStepSize, float yStepSize, float zStepSize, int seed,
+                             float* dMinMax, void* stream)
+{
+    const float off[3] = {xOffset, yOffset, zOffset};
+    const int cnt[3] = {xCount, yCount, zCount};
+    const float st[3] = {xStepSize, yStepSize, zStepSize};
+    return gen_device(node, grid_args(3, off, cnt, st, seed), dOut, dMinMax, stream);
+}
+
+int fnGenUniformGrid4DDevice(const void* node, float* dOut, float xOffset, float yOffset, float zOffset, float wOffset,
+                             int xCount, int yCount, int zCount, int wCount, float xStepSize, float yStepSize,
+                             float zStepSize, float wStepSize, int seed, float* dMinMax, void* stream)
+{
+    const float off[4] = {xOffset, yOffset, zOffset, wOffset};
+    const int cnt[4] = {xCount, yCount, zCount, wCount};
+    const float st[4] = {xStepSize, yStepSize, zStepSize, wStepSize};
+    return gen_device(node, grid_args(4, off, cnt, st, seed), dOut, dMinMax, stream);
+}
+
+int fnGenPositionArray2DDevice(const void* node, float* dOut, int count, const float* dX, const float* dY, float xOffset,
+                               float yOffset, int seed, float* dMinMax, void* stream)
+{
+    const float off[2] = {xOffset, yOffset};
+    PointArgs a = pos_args(2, count, off, seed);
+    a.pos[0] = dX; a.pos[1] = dY;
+    if (a.total > 0 && (!dX || !dY)) { set_error(FN_ERR_ARG, "null position array"); return FN_ERR_ARG; }
+    return gen_device(node, a, dOut, dMinMax, stream);
+}
+
+int fnGenPositionArray3DDevice(const void* node, float* dOut, int count, const float* dX, const float* dY,
+                               const float* dZ, float xOffset, float yOffset, float zOffset, int seed, float* dMinMax,
+                               void* stream)
+{
+    const float off[3] = {xOffset, yOffset, zOffset};
+    PointArgs a = pos_args(3, count, off, seed);
+    a.pos[0] = dX; a.pos[1] = dY; a.pos[2] = dZ;
+    if (a.total > 0 && (!dX || !dY || !dZ)) { set_error(FN_ERR_ARG, "null position array"); return FN_ERR_ARG; }
+    return gen_device(node, a, dOut, dMinMax, stream);
+}
+
+int fnGenPositionArray4DDevice(const void* node, float* dOut, int count, const float* dX, const float* dY,
+                               const float* dZ, const float* dW, float xOffset, float yOffset, float zOffset,
+                               float wOffset, int seed, float* dMinMax, void* stream)
+{
+    const float off[4] = {xOffset, yOffset, zOffset, wOffset};
+    PointArgs a = pos_args(4, count, off, seed);
+    a.pos[0] = dX; a.pos[1] = dY; a.pos[2] = dZ; a.pos[3] = dW;
+    if (a.total > 0 && (!dX || !dY || !dZ || !dW)) { set_error(FN_ERR_ARG, "null position array"); return FN_ERR_ARG; }
+    return gen_device(node, a, dOut, dMinMax, stream);
+}
+
+int fnGenTileable2DDevice(const void* node, float* dOut, int xSize, int ySize, float xStepSize, float yStepSize,
+                          int seed, float* dMinMax, void* stream)
+{
+    return gen_device(node, tile_args(xSize, ySize, xStepSize, yStepSize, seed), dOut, dMinMax, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,1123 @@
+// fn_device.cuh -- FastNoise2 node math for sm_103a.
+//
+// Device-side restatement of the node generators in
+// include/FastNoise/Generators/*.inl (FastNoise2 v1.1.1).  Every function here
+// evaluates ONE point in registers; the interpreter kernel (fn_kernels.cu) and
+// the run-time specialised kernels (fn_jit.cpp) both call them.
+//
+// Arithmetic contract (matches the reference's strict-FP build):
+//   * the whole translation unit is compiled with -fmad=false, so a*b+c is a
+//     multiply and an add; FS::FMulAdd / FNMulAdd / FMulSub become fmaf();
+//   * FS::Convert<int32> rounds to nearest-even and returns INT_MIN for NaN or
+//     |x| >= 2^31 (x86 cvtps2dq);
+//   * FS::Min(a,b)=a<b?a:b, FS::Max(a,b)=a>b?a:b (minps/maxps operand order);
+//   * InvSqrt / Reciprocal / Sqrt / division are the correctly rounded IEEE ops;
+//   * Sin / Cos / Pow use the project's own polynomial kernels below, shared
+//     bit-for-bit with the CPU restatement used for testing.
+#pragma once
+
+#ifndef FN_DEVICE_NO_STDINT
+#include <stdint.h>
+#endif
+
+#define FND __device__ __forceinline__
+
+namespace fnd {
+
+constexpr int kPrimeX = (int)0xF797C5C7;   // Utils.inl:8-11
+constexpr int kPrimeY = (int)0x6C060C89;
+constexpr int kPrimeZ = (int)0x465FD04F;
+constexpr int kPrimeW = (int)0xF7A62279;
+constexpr int kHashA = (int)0xB7E0A5F5;     // Utils.inl:18
+
+constexpr double kRoot2 = 1.4142135623730950488016887242097;
+constexpr double kRoot3 = 1.7320508075688772935274463415059;
+constexpr double kRoot5 = 2.2360679774997896964091736687313;
+constexpr float kValueBounds = 2147483648.f;
+
+// ---------------------------------------------------------------- primitives
+
+FND float fmin_(float a, float b) { return a < b ? a : b; }
+FND float fmax_(float a, float b) { return a > b ? a : b; }
+FND float fabs_(float a) { return __int_as_float(__float_as_int(a) & 0x7FFFFFFF); }
+FND float flip(float v, int s) { return __int_as_float(__float_as_int(v) ^ (s & (int)0x80000000)); }
+FND float flipm(float v, bool m) { return m ? __int_as_float(__float_as_int(v) ^ (int)0x80000000) : v; }
+FND int cvti(float x)
+{
+    int r = __float2int_rn(x);
+    return (x >= -2147483648.0f && x < 2147483648.0f) ? r : (int)0x80000000;
+}
+FND float cvtf(int i) { return __int2float_rn(i); }
+FND unsigned srl(int a, int s) { return (unsigned)a >> s; }
+FND int imul(int a, int b) { return (int)((unsigned)a * (unsigned)b); }
+FND int iadd(int a, int b) { return (int)((unsigned)a + (unsigned)b); }
+FND float invsqrt(float x) { return 1.0f / sqrtf(x); }
+
+FND int hash(int seed, int a, int b) { int h = imul(seed ^ a ^ b, kHashA); return (h >> 15) ^ h; }
+FND int hash(int seed, int a, int b, int c) { int h = imul(seed ^ a ^ b ^ c, kHashA); return (h >> 15) ^ h; }
+FND int hash(int seed, int a, int b, int c, int d) { int h = imul(seed ^ a ^ b ^ c ^ d, kHashA); return (h >> 15) ^ h; }
+FND int hashhb(int seed, int a, int b) { return imul(seed ^ a ^ b, kHashA); }
+FND int hashhb(int seed, int a, int b, int c) { return imul(seed ^ a ^ b ^ c, kHashA); }
+FND int hashhb(int seed, int a, int b, int c, int d) { return imul(seed ^ a ^ b ^ c ^ d, kHashA); }
+FND float valcoord(int h) { return cvtf(imul(h, imul(h, kHashA))); }   // Utils.inl:243-250
+
+FND float lerp(float a, float b, float t) { return fmaf(t, b - a, a); }
+FND float hermite(float t) { return t * t * fmaf(-t, 2.0f, 3.0f); }
+FND float quintic(float t) { return t * t * t * fmaf(t, fmaf(t, 6.0f, -15.0f), 10.0f); }
+
+// GetGradientDotCommon, portable branch (Utils.inl:132-158)
+FND float grad3(int h, float x, float y, float z)
+{
+    int h13 = h & 13;
+    float u = h13 > 7 ? y : x;
+    float v = h13 == 12 ? x : z;
+    v = h13 < 2 ? y : v;
+    return flip(u, h << 31) + flip(v, (h >> 1) << 31);
+}
+// GetGradientDotPerlin 2D, portable branch (Utils.inl:181-190)
+FND float grad2(int h, float x, float y)
+{
+    x = flip(x, h << 31);
+    y = flip(y, (h >> 1) << 31);
+    bool s = (h << 29) < 0;
+    return fmaf(1.0f + (float)kRoot2, s ? y : x, s ? x : y);
+}
+// GetGradientDotPerlin 4D, portable branch (Utils.inl:205-218)
+FND float grad4(int h, float x, float y, float z, float w)
+{
+    int p = h & (3 << 3);
+    float a = p > 0 ? x : y;
+    float b = (h << 27) < 0 ? y : z;
+    float c = p > (2 << 3) ? z : w;
+    return (flip(a, h << 31) + flip(b, (h >> 1) << 31)) + flip(c, (h >> 2) << 31);
+}
+
+// Sin / Cos: Cody-Waite reduction by pi/2 (three-part constant), Taylor
+// polynomials on [-pi/4, pi/4] evaluated by Horner with fmaf.
+FND float sc_reduce(float x, int& q)
+{
+    float k = rintf(x * 0x1.45f306p-1f);
+    float r = fmaf(-k, 0x1.921fb6p+0f, x);
+    r = fmaf(-k, -0x1.777a5cp-25f, r);
+    r = fmaf(-k, -0x1.ee59dap-50f, r);
+    q = (int)(long long)k & 3;
+    return r;
+}
+FND float sin_poly(float r)
+{
+    float r2 = r * r;
+    float p = fmaf(r2, -0x1.ae6456p-26f, 0x1.71de3ap-19f);
+    p = fmaf(r2, p, -0x1.a01a02p-13f);
+    p = fmaf(r2, p, 0x1.111112p-7f);
+    p = fmaf(r2, p, -0x1.555556p-3f);
+    return fmaf(r * r2, p, r);
+}
+FND float cos_poly(float r)
+{
+    float r2 = r * r;
+    float p = fmaf(r2, 0x1.1eed8ep-29f, -0x1.27e4fcp-22f);
+    p = fmaf(r2, p, 0x1.a01a02p-16f);
+    p = fmaf(r2, p, -0x1.6c16c2p-10f);
+    p = fmaf(r2, p, 0x1.555556p-5f);
+    p = fmaf(r2, p, -0.5f);
+    return fmaf(r2, p, 1.0f);
+}
+FND float sin_(float x)
+{
+    int q;
+    float r = sc_reduce(x, q);
+    float s = (q & 1) ? cos_poly(r) : sin_poly(r);
+    return (q & 2) ? -s : s;
+}
+FND float cos_(float x)
+{
+    int q;
+    float r = sc_reduce(x, q);
+    float c = (q & 1) ? sin_poly(r) : cos_poly(r);
+    return ((q + 1) & 2) ? -c : c;
+}
+
+// Pow for the strict build: 2^(y*log2 x), log2 via the atanh series on
+// m in [sqrt(1/2), sqrt(2)), exp2 via a nearest-integer split.
+FND float log2_pos(float x)
+{
+    unsigned u = __float_as_uint(x);
+    int e = (int)((u >> 23) & 0xFF);
+    if (e == 0) { x *= 0x1p23f; u = __float_as_uint(x); e = (int)((u >> 23) & 0xFF) - 23; }
+    int ex = e - 127;
+    float m = __uint_as_float((u & 0x007FFFFFu) | 0x3F800000u);
+    if (m > 1.41421356f) { m *= 0.5f; ex += 1; }
+    float s = (m - 1.0f) / (m + 1.0f);
+    float s2 = s * s;
+    float p = fmaf(s2, 0x1.745d18p-4f, 0x1.c71c72p-4f);
+    p = fmaf(s2, p, 0x1.24924ap-3f);
+    p = fmaf(s2, p, 0x1.99999ap-3f);
+    p = fmaf(s2, p, 0x1.555556p-2f);
+    p = fmaf(s2, p, 1.0f);
+    float ln = 2.0f * s * p;
+    return fmaf(ln, 0x1.715476p+0f, (float)ex);
+}
+FND float exp2_any(float t)
+{
+    if (!(t < 128.0f)) return (t != t) ? t : __int_as_float(0x7F800000);
+    if (t < -150.0f) return 0.0f;
+    float n = rintf(t);
+    float f = t - n;
+    float a = f * 0x1.62e430p-1f;
+    float p = fmaf(a, 0x1.a01a02p-13f, 0x1.6c16c2p-10f);
+    p = fmaf(a, p, 0x1.111112p-7f);
+    p = fmaf(a, p, 0x1.555556p-5f);
+    p = fmaf(a, p, 0x1.555556p-3f);
+    p = fmaf(a, p, 0.5f);
+    p = fmaf(a, p, 1.0f);
+    p = fmaf(a, p, 1.0f);
+    int ni = (int)n;
+    int n1 = ni / 2, n2 = ni - n1;
+    return p * __uint_as_float((unsigned)(n1 + 127) << 23) * __uint_as_float((unsigned)(n2 + 127) << 23);
+}
+FND float pow_(float x, float y)
+{
+    if (y == 0.0f) return 1.0f;
+    if (x != x || y != y) return x + y;
+    if (x == 0.0f) return y > 0.0f ? 0.0f : __int_as_float(0x7F800000);
+    if (x < 0.0f) return __int_as_float(0x7FC00000);
+    if (x == __int_as_float(0x7F800000)) return y > 0.0f ? x : 0.0f;
+    return exp2_any(y * log2_pos(x));
+}
+FND float mod_(float a, float b) { return a - truncf(a / b) * b; }
+
+// VariableRange::ScaleOutput (BasicGenerators.inl:27-30); mul = (1/(max-min))*rangeScale
+FND float scale_out(float v, float nmin, float mul, float rmin) { return fmaf(mul, v - nmin, rmin); }
+
+// ---------------------------------------------------------------- Simplex
+
+FND float simplex2(int seed, float x, float y)
+{
+    constexpr double kSkew2 = 1.0 / (kRoot3 + 1.0);
+    constexpr double kUnskew2 = -1.0 / (kRoot3 + 3.0);
+    float skewDelta = (float)kSkew2 * (x + y);
+    float xs = x + skewDelta, ys = y + skewDelta;
+    float xb = floorf(xs), yb = floorf(ys);
+    float dxs = xs - xb, dys = ys - yb;
+    int xp = imul(cvti(xb), kPrimeX), yp = imul(cvti(yb), kPrimeY);
+    bool xgey = dxs >= dys;
+    float unskew = (float)kUnskew2 * (dxs + dys);
+    float dx0 = dxs + unskew, dy0 = dys + unskew;
+    float dx1 = (xgey ? dx0 : dx0 + 1.0f) - (float)(kUnskew2 + 1);
+    float dy1 = (xgey ? dy0 + 1.0f : dy0) - (float)(kUnskew2 + 1);
+    float dx2 = dx0 - (float)(kUnskew2 * 2 + 1);
+    float dy2 = dy0 - (float)(kUnskew2 * 2 + 1);
+    float f0 = fmaf(-dx0, dx0, fmaf(-dy0, dy0, 0.5f));
+    float f1 = fmaf(-dx1, dx1, fmaf(-dy1, dy1, 0.5f));
+    float f2 = f0 + fmaf(unskew, (float)(-4.0 * (kRoot3 + 2.0) / (kRoot3 + 3.0)), (float)(-2.0 / 3.0));
+    f0 = fmax_(f0, 0.0f); f1 = fmax_(f1, 0.0f); f2 = fmax_(f2, 0.0f);
+    f0 *= f0; f0 *= f0; f1 *= f1; f1 *= f1; f2 *= f2; f2 *= f2;
+    float g0 = grad2(hash(seed, xp, yp), dx0, dy0);
+    float g1 = grad2(hash(seed, xgey ? iadd(xp, kPrimeX) : xp, xgey ? yp : iadd(yp, kPrimeY)), dx1, dy1);
+    float g2 = grad2(hash(seed, iadd(xp, kPrimeX), iadd(yp, kPrimeY)), dx2, dy2);
+    return fmaf(g0, f0, fmaf(g1, f1, g2 * f2));
+}
+
+FND float simplex3(int seed, float x, float y, float z)
+{
+    constexpr double kReflect = -1.0 / 2.0;
+    float skewDelta = (float)(1.0 / 3.0) * (x + y + z);
+    float xs = x + skewDelta, ys = y + skewDelta, zs = z + skewDelta;
+    float xb = floorf(xs), yb = floorf(ys), zb = floorf(zs);
+    float dxs = xs - xb, dys = ys - yb, dzs = zs - zb;
+    int xp = imul(cvti(xb), kPrimeX), yp = imul(cvti(yb), kPrimeY), zp = imul(cvti(zb), kPrimeZ);
+    bool xgey = dxs >= dys, ygez = dys >= dzs, xgez = dxs >= dzs;
+    float unskew = (float)kReflect * (dxs + dys + dzs);
+    float dx0 = dxs + unskew, dy0 = dys + unskew, dz0 = dzs + unskew;
+    bool mx1 = xgey && xgez, my1 = ygez && !xgey, mz1 = xgez || ygez;
+    bool nx2 = xgey || xgez, ny2 = xgey && !ygez, nz2 = xgez && ygez;
+    constexpr float c3 = (float)(kReflect * 3 + 1);
+    float dx3 = dx0 - c3, dy3 = dy0 - c3, dz3 = dz0 - c3;
+    float dx1 = mx1 ? dx3 - 1.0f : dx3;
+    float dy1 = my1 ? dy3 - 1.0f : dy3;
+    float dz1 = mz1 ? dz3 : dz3 - 1.0f;
+    float dx2 = nx2 ? dx0 : dx0 + 1.0f;
+    float dy2 = ny2 ? dy0 + 1.0f : dy0;
+    float dz2 = nz2 ? dz0 + 1.0f : dz0;
+    constexpr float R = (float)0.6;
+    float f0 = fmaf(-dz0, dz0, fmaf(-dy0, dy0, fmaf(-dx0, dx0, R)));
+    float f1 = fmaf(-dz1, dz1, fmaf(-dy1, dy1, fmaf(-dx1, dx1, R)));
+    float f2 = fmaf(-dz2, dz2, fmaf(-dy2, dy2, fmaf(-dx2, dx2, R)));
+    float f3 = f0 - (unskew + (float)(3.0 / 4.0));
+    f0 = fmax_(f0, 0.0f); f1 = fmax_(f1, 0.0f); f2 = fmax_(f2, 0.0f); f3 = fmax_(f3, 0.0f);
+    f0 *= f0; f0 *= f0; f1 *= f1; f1 *= f1; f2 *= f2; f2 *= f2; f3 *= f3; f3 *= f3;
+    float g0 = grad3(hash(seed, xp, yp, zp), dx0, dy0, dz0);
+    float g1 = grad3(hash(seed, mx1 ? iadd(xp, kPrimeX) : xp, my1 ? iadd(yp, kPrimeY) : yp, mz1 ? zp : iadd(zp, kPrimeZ)), dx1, dy1, dz1);
+    float g2 = grad3(hash(seed, nx2 ? iadd(xp, kPrimeX) : xp, ny2 ? yp : iadd(yp, kPrimeY), nz2 ? zp : iadd(zp, kPrimeZ)), dx2, dy2, dz2);
+    float g3 = grad3(hash(seed, iadd(xp, kPrimeX), iadd(yp, kPrimeY), iadd(zp, kPrimeZ)), dx3, dy3, dz3);
+    return fmaf(g3, f3, fmaf(g2, f2, fmaf(g1, f1, g0 * f0)));
+}
+
+FND float simplex4(int seed, float x, float y, float z, float w)
+{
+    constexpr double kSkew4 = 1.0 / (kRoot5 + 1.0);
+    constexpr double kUnskew4 = -1.0 / (kRoot5 + 5.0);
+    float skewDelta = (float)kSkew4 * (x + y + z + w);
+    float xs = x + skewDelta, ys = y + skewDelta, zs = z + skewDelta, ws = w + skewDelta;
+    float xb = floorf(xs), yb = floorf(ys), zb = floorf(zs), wb = floorf(ws);
+    float dxs = xs - xb, dys = ys - yb, dzs = zs - zb, dws = ws - wb;
+    int xp = imul(cvti(xb), kPrimeX), yp = imul(cvti(yb), kPrimeY), zp = imul(cvti(zb), kPrimeZ), wp = imul(cvti(wb), kPrimeW);
+    float unskew = (float)kUnskew4 * (dxs + dys + dzs + dws);
+    float dx0 = dxs + unskew, dy0 = dys + unskew, dz0 = dzs + unskew, dw0 = dws + unskew;
+    int rx = 0, ry = 0, rz = 0, rw = 0;
+    if (dx0 >= dy0) rx++; else ry++;
+    if (dx0 >= dz0) rx++; else rz++;
+    if (dx0 >= dw0) rx++; else rw++;
+    if (dy0 >= dz0) ry++; else rz++;
+    if (dy0 >= dw0) ry++; else rw++;
+    if (dz0 >= dw0) rz++; else rw++;
+    constexpr float u1 = (float)kUnskew4, u2 = (float)(kUnskew4 * 2), u3 = (float)(kUnskew4 * 3), u4 = (float)(kUnskew4 * 4 + 1);
+    float dx1 = (rx > 2 ? dx0 - 1.0f : dx0) - u1, dy1 = (ry > 2 ? dy0 - 1.0f : dy0) - u1;
+    float dz1 = (rz > 2 ? dz0 - 1.0f : dz0) - u1, dw1 = (rw > 2 ? dw0 - 1.0f : dw0) - u1;
+    float dx2 = (rx > 1 ? dx0 - 1.0f : dx0) - u2, dy2 = (ry > 1 ? dy0 - 1.0f : dy0) - u2;
+    float dz2 = (rz > 1 ? dz0 - 1.0f : dz0) - u2, dw2 = (rw > 1 ? dw0 - 1.0f : dw0) - u2;
+    float dx3 = (rx > 0 ? dx0 - 1.0f : dx0) - u3, dy3 = (ry > 0 ? dy0 - 1.0f : dy0) - u3;
+    float dz3 = (rz > 0 ? dz0 - 1.0f : dz0) - u3, dw3 = (rw > 0 ? dw0 - 1.0f : dw0) - u3;
+    float dx4 = dx0 - u4, dy4 = dy0 - u4, dz4 = dz0 - u4, dw4 = dw0 - u4;
+    constexpr float R = (float)0.6;
+    float f0 = fmaf(-dw0, dw0, fmaf(-dz0, dz0, fmaf(-dy0, dy0, fmaf(-dx0, dx0, R))));
+    float f1 = fmaf(-dw1, dw1, fmaf(-dz1, dz1, fmaf(-dy1, dy1, fmaf(-dx1, dx1, R))));
+    float f2 = fmaf(-dw2, dw2, fmaf(-dz2, dz2, fmaf(-dy2, dy2, fmaf(-dx2, dx2, R))));
+    float f3 = fmaf(-dw3, dw3, fmaf(-dz3, dz3, fmaf(-dy3, dy3, fmaf(-dx3, dx3, R))));
+    float f4 = f0 + fmaf(unskew, (float)(-4.0 * (kRoot5 + 3.0) / (kRoot5 + 5.0)), (float)(-4.0 / 5.0));
+    f0 = fmax_(f0, 0.0f); f1 = fmax_(f1, 0.0f); f2 = fmax_(f2, 0.0f); f3 = fmax_(f3, 0.0f); f4 = fmax_(f4, 0.0f);
+    f0 *= f0; f0 *= f0; f1 *= f1; f1 *= f1; f2 *= f2; f2 *= f2; f3 *= f3; f3 *= f3; f4 *= f4; f4 *= f4;
+    float g0 = grad4(hash(seed, xp, yp, zp, wp), dx0, dy0, dz0, dw0);
+    float g1 = grad4(hash(seed, rx > 2 ? iadd(xp, kPrimeX) : xp, ry > 2 ? iadd(yp, kPrimeY) : yp, rz > 2 ? iadd(zp, kPrimeZ) : zp, rw > 2 ? iadd(wp, kPrimeW) : wp), dx1, dy1, dz1, dw1);
+    float g2 = grad4(hash(seed, rx > 1 ? iadd(xp, kPrimeX) : xp, ry > 1 ? iadd(yp, kPrimeY) : yp, rz > 1 ? iadd(zp, kPrimeZ) : zp, rw > 1 ? iadd(wp, kPrimeW) : wp), dx2, dy2, dz2, dw2);
+    float g3 = grad4(hash(seed, rx > 0 ? iadd(xp, kPrimeX) : xp, ry > 0 ? iadd(yp, kPrimeY) : yp, rz > 0 ? iadd(zp, kPrimeZ) : zp, rw > 0 ? iadd(wp, kPrimeW) : wp), dx3, dy3, dz3, dw3);
+    float g4 = grad4(hash(seed, iadd(xp, kPrimeX), iadd(yp, kPrimeY), iadd(zp, kPrimeZ), iadd(wp, kPrimeW)), dx4, dy4, dz4, dw4);
+    return fmaf(g0, f0, fmaf(g1, f1, fmaf(g2, f2, fmaf(g3, f3, g4 * f4))));
+}
+
+// ---------------------------------------------------------------- SuperSimplex (OpenSimplex2S)
+
+FND float supersimplex2(int seed, float x, float y)
+{
+    constexpr double kSkew2 = 1.0 / (kRoot3 + 1.0);
+    constexpr double kUnskew2 = -1.0 / (kRoot3 + 3.0);
+    constexpr float R = (float)(2.0 / 3.0);
+    float skewDelta = (float)kSkew2 * (x + y);
+    float xs = x + skewDelta, ys = y + skewDelta;
+    float xb = floorf(xs), yb = floorf(ys);
+    float dxs = xs - xb, dys = ys - yb;
+    int xp = imul(cvti(xb), kPrimeX), yp = imul(cvti(yb), kPrimeY);
+    bool fxy = dxs + dys > 1.0f;
+    float boundary = fxy ? -1.0f : 0.0f;
+    bool fx = fmaf(dxs, -2.0f, dys) < boundary;
+    bool fy = fmaf(dys, -2.0f, dxs) < boundary;
+    float unskew = (float)kUnskew2 * (dxs + dys);
+    float dxb = dxs + unskew, dyb = dys + unskew;
+    float fb0 = fmaf(-dxb, dxb, fmaf(-dyb, dyb, R));
+    float value;
+    {
+        float g = grad2(hash(seed, xp, yp), dxb, dyb);
+        float f = fb0; f *= f; f *= f;
+        value = f * g;
+    }
+    {
+        float g = grad2(hash(seed, iadd(xp, kPrimeX), iadd(yp, kPrimeY)), dxb - (float)(2 * kUnskew2 + 1), dyb - (float)(2 * kUnskew2 + 1));
+        float f = fmaf(unskew, (float)(-4.0 * (kRoot3 + 2.0) / (kRoot3 + 3.0)), fb0 - R);
+        f *= f; f *= f;
+        value = fmaf(f, g, value);
+    }
+    float xyd = fxy ? (float)(kUnskew2 + 1) : (float)(-kUnskew2);
+    dxb = dxb - xyd;
+    dyb = dyb - xyd;
+    {
+        int xa = fx ? iadd(xp, (int)((unsigned)kPrimeX * 2u)) : xp;
+        int h = hash(seed, fxy ? xa : iadd(xa, -kPrimeX), fxy ? iadd(yp, kPrimeY) : yp);
+        float dx = dxb - (fx ? (float)(1 + 2 * kUnskew2) : -1.0f);
+        float dy = fx ? dyb - (float)(2 * kUnskew2) : dyb;
+        float g = grad2(h, dx, dy);
+        float f = fmax_(fmaf(-dx, dx, fmaf(-dy, dy, R)), 0.0f);
+        f *= f; f *= f;
+        value = fmaf(f, g, value);
+    }
+    {
+        int ya = fy ? iadd(yp, (int)((unsigned)kPrimeY * 2u)) : yp;
+        int h = hash(seed, fxy ? iadd(xp, kPrimeX) : xp, fxy ? ya : iadd(ya, -kPrimeY));
+        float dx = fy ? dxb - (float)(2 * kUnskew2) : dxb;
+        float dy = dyb - (fy ? (float)(1 + 2 * kUnskew2) : -1.0f);
+        float g = grad2(h, dx, dy);
+        float f = fmax_(fmaf(-dx, dx, fmaf(-dy, dy, R)), 0.0f);
+        f *= f; f *= f;
+        value = fmaf(f, g, value);
+    }
+    return value;
+}
+
+FND void ss_consider(float& maxScore, int& bits, float score, int b)
+{
+    bits = score > maxScore ? b : bits;
+    maxScore = fmax_(maxScore, score);
+}
+
+FND float supersimplex3(int seed, float x, float y, float z)
+{
+    constexpr double kReflect = -1.0 / 2.0;
+    constexpr double kTwice = -1.0 / 4.0;
+    constexpr double kDA = 3.0 / 4.0, kDB = 1.0;
+    float skewDelta = (float)(1.0 / 3.0) * (x + y + z);
+    float xs = x + skewDelta, ys = y + skewDelta, zs = z + skewDelta;
+    float xb = floorf(xs), yb = floorf(ys), zb = floorf(zs);
+    float dxs = xs - xb, dys = ys - yb, dzs = zs - zb;
+    {
+        float t = (float)kTwice * (dxs + dys + dzs);
+        float xn = dxs + t, yn = dys + t, zn = dzs + t, xyzn = -t;
+        float maxScore = 0.375f;
+        int bits = xyzn > maxScore ? -1 : 0;
+        maxScore = fmax_(maxScore, xyzn);
+        ss_consider(maxScore, bits, xn, 1);
+        ss_consider(maxScore, bits, yn, 2);
+        ss_consider(maxScore, bits, zn, 4);
+        maxScore += 0.125f - xyzn;
+        ss_consider(maxScore, bits, -zn, 3);
+        ss_consider(maxScore, bits, -yn, 5);
+        ss_consider(maxScore, bits, -xn, 6);
+        if (bits & 1) { xb += 1.0f; dxs -= 1.0f; }
+        if (bits & 2) { yb += 1.0f; dys -= 1.0f; }
+        if (bits & 4) { zb += 1.0f; dzs -= 1.0f; }
+    }
+    int xp = imul(cvti(xb), kPrimeX), yp = imul(cvti(yb), kPrimeY), zp = imul(cvti(zb), kPrimeZ);
+    float sum = dxs + dys + dzs;
+    float t = (float)kTwice * sum;
+    float xn = dxs + t, yn = dys + t, zn = dzs + t, xyzn = -t;
+    float unskew = (float)kReflect * sum;
+    float dx = dxs + unskew, dy = dys + unskew, dz = dzs + unskew;
+    float cs = (float)(1 + 3 * kReflect) * sum;
+    float value, stemA, stemB;
+    {
+        float g = grad3(hash(seed, xp, yp, zp), dx, dy, dz);
+        float fb = fmaf(-dz, dz, fmaf(-dy, dy, fmaf(-dx, dx, (float)kDA))) * 0.5f;
+        stemA = fb - (float)(kDA * 0.5);
+        stemB = fb - (float)(kDB * 0.5);
+        value = (fb * fb) * (fb * fb) * g;
+    }
+    {
+        bool m = xyzn < 0.0f;
+        float off = flipm((float)(3 * kReflect + 1), m);
+        float g = grad3(hash(seed, iadd(xp, m ? -kPrimeX : kPrimeX), iadd(yp, m ? -kPrimeY : kPrimeY), iadd(zp, m ? -kPrimeZ : kPrimeZ)), dx - off, dy - off, dz - off);
+        float fb = fmax_(fmaf(off, cs, stemA), 0.0f);
+        value = fmaf((fb * fb) * (fb * fb), g, value);
+    }
+    {
+        bool m = xyzn < zn;
+        float o0 = flipm((float)(2 * kReflect), m);
+        float g = grad3(hash(seed, iadd(xp, m ? -kPrimeX : kPrimeX), iadd(yp, m ? -kPrimeY : kPrimeY), zp), dx, dy, dz - o0);
+        float fb = fmin_(flipm(dz, m) - stemB, 0.0f);
+        value = fmaf((fb * fb) * (fb * fb), g, value);
+    }
+    {
+        bool m = xyzn < yn;
+        float o0 = flipm((float)(2 * kReflect), m);
+        float g = grad3(hash(seed, iadd(xp, m ? -kPrimeX : kPrimeX), yp, iadd(zp, m ? -kPrimeZ : kPrimeZ)), dx, dy - o0, dz);
+        float fb = fmin_(flipm(dy, m) - stemB, 0.0f);
+        value = fmaf((fb * fb) * (fb * fb), g, value);
+    }
+    {
+        bool m = xyzn < xn;
+        float o0 = flipm((float)(2 * kReflect), m);
+        float g = grad3(hash(seed, xp, iadd(yp, m ? -kPrimeY : kPrimeY), iadd(zp, m ? -kPrimeZ : kPrimeZ)), dx - o0, dy, dz);
+        float fb = fmin_(flipm(dx, m) - stemB, 0.0f);
+        value = fmaf((fb * fb) * (fb * fb), g, value);
+    }
+    {
+        bool m = xn < 0.0f;
+        float o0 = flipm((float)kReflect, m);
+        float g = grad3(hash(seed, iadd(xp, m ? -kPrimeX : kPrimeX), yp, zp), dx + o0, dy - o0, dz - o0);
+        float fb = fmax_(fmaf(o0, cs, stemA) + flipm(dx, m), 0.0f);
+        value = fmaf((fb * fb) * (fb * fb), g, value);
+    }
+    {
+        bool m = yn < 0.0f;
+        float o0 = flipm((float)kReflect, m);
+        float g = grad3(hash(seed, xp, iadd(yp, m ? -kPrimeY : kPrimeY), zp), dx - o0, dy + o0, dz - o0);
+        float fb = fmax_(fmaf(o0, cs, stemA) + flipm(dy, m), 0.0f);
+        value = fmaf((fb * fb) * (fb * fb), g, value);
+    }
+    {
+        bool m = zn < 0.0f;
+        float o0 = flipm((float)kReflect, m);
+        float g = grad3(hash(seed, xp, yp, iadd(zp, m ? -kPrimeZ : kPrimeZ)), dx - o0, dy - o0, dz + o0);
+        float fb = fmax_(fmaf(o0, cs, stemA) + flipm(dz, m), 0.0f);
+        value = fmaf((fb * fb) * (fb * fb), g, value);
+    }
+    return value;
+}
+
+FND float supersimplex4(int seed, float x, float y, float z, float w)
+{
+    constexpr double kSkew4 = 1.0 / (kRoot5 + 1.0);
+    constexpr double kU = -1.0 / (kRoot5 + 5.0);
+    constexpr double kTwice = -1.0 / 5.0;
+    constexpr double kDA = 4.0 / 5.0, kDB = 6.0 / 5.0;
+    float skewDelta = (float)kSkew4 * (x + y + z + w);
+    float xs = x + skewDelta, ys = y + skewDelta, zs = z + skewDelta, ws = w + skewDelta;
+    float xb = floorf(xs), yb = floorf(ys), zb = floorf(zs), wb = floorf(ws);
+    float dxs = xs - xb, dys = ys - yb, dzs = zs - zb, dws = ws - wb;
+    {
+        float t = (float)kTwice * (dxs + dys + dzs + dws);
+        float xn = dxs + t, yn = dys + t, zn = dzs + t, wn = dws + t, xyzwn = -t;
+        float ms = 0.6f - xyzwn;
+        int bits = 0.2f > ms ? -1 : 0;
+        ms = fmax_(ms, 0.2f);
+        ss_consider(ms, bits, -wn, 7);
+        ss_consider(ms, bits, -zn, 11);
+        ss_consider(ms, bits, -yn, 13);
+        ss_consider(ms, bits, -xn, 14);
+        ms += xyzwn - 0.2f;
+        ss_consider(ms, bits, xn, 1);
+        ss_consider(ms, bits, yn, 2);
+        ss_consider(ms, bits, zn, 4);
+        ss_consider(ms, bits, wn, 8);
+        ms += 0.2f - xn;
+        ss_consider(ms, bits, yn, 3);
+        ss_consider(ms, bits, zn, 5);
+        ss_consider(ms, bits, wn, 9);
+        ms += xn;
+        ss_consider(ms, bits, yn + zn, 6);
+        ms -= wn;
+        ss_consider(ms, bits, yn, 10);
+        ss_consider(ms, bits, zn, 12);
+        if (bits & 1) { xb += 1.0f; dxs -= 1.0f; }
+        if (bits & 2) { yb += 1.0f; dys -= 1.0f; }
+        if (bits & 4) { zb += 1.0f; dzs -= 1.0f; }
+        if (bits & 8) { wb += 1.0f; dws -= 1.0f; }
+    }
+    int xp = imul(cvti(xb), kPrimeX), yp = imul(cvti(yb), kPrimeY), zp = imul(cvti(zb), kPrimeZ), wp = imul(cvti(wb), kPrimeW);
+    float sum = dxs + dys + dzs + dws;
+    float t = (float)kTwice * sum;
+    float xn = dxs + t, yn = dys + t, zn = dzs + t, wn = dws + t, xyzwn = -t;
+    float ud = (float)kU * sum;
+    float dx = dxs + ud, dy = dys + ud, dz = dzs + ud, dw = dws + ud;
+    float cs = (float)(1 + 4 * kU) * sum;
+    float value, stemA, stemB;
+    {
+        float g = grad4(hash(seed, xp, yp, zp, wp), dx, dy, dz, dw);
+        float fb = fmaf(-dw, dw, fmaf(-dz, dz, fmaf(-dy, dy, fmaf(-dx, dx, (float)kDA)))) * 0.5f;
+        stemA = fb - (float)(kDA * 0.5);
+        stemB = fb - (float)(kDB * 0.5);
+        value = (fb * fb) * (fb * fb) * g;
+    }
+#define FND_P(m, base, P) iadd(base, (m) ? -(P) : (P))
+#define FND_ACC(fbexpr, gexpr) { float g_ = (gexpr); float fb_ = fmax_((fbexpr), 0.0f); value = fmaf((fb_ * fb_) * (fb_ * fb_), g_, value); }
+    {
+        bool m = xyzwn < 0.0f;
+        float o = flipm((float)(4 * kU + 1), m);
+        FND_ACC(fmaf(o, cs, stemA), grad4(hash(seed, FND_P(m, xp, kPrimeX), FND_P(m, yp, kPrimeY), FND_P(m, zp, kPrimeZ), FND_P(m, wp, kPrimeW)), dx - o, dy - o, dz - o, dw - o));
+    }
+    {
+        bool m = xyzwn < wn;
+        float o1 = flipm((float)(3 * kU + 1), m), o0 = flipm((float)(3 * kU), m);
+        FND_ACC(fmaf(o1, cs, stemB) - flipm(dw, m), grad4(hash(seed, FND_P(m, xp, kPrimeX), FND_P(m, yp, kPrimeY), FND_P(m, zp, kPrimeZ), wp), dx - o1, dy - o1, dz - o1, dw - o0));
+    }
+    {
+        bool m = xyzwn < zn;
+        float o1 = flipm((float)(3 * kU + 1), m), o0 = flipm((float)(3 * kU), m);
+        FND_ACC(fmaf(o1, cs, stemB) - flipm(dz, m), grad4(hash(seed, FND_P(m, xp, kPrimeX), FND_P(m, yp, kPrimeY), zp, FND_P(m, wp, kPrimeW)), dx - o1, dy - o1, dz - o0, dw - o1));
+    }
+    {
+        bool m = xyzwn < yn;
+        float o1 = flipm((float)(3 * kU + 1), m), o0 = flipm((float)(3 * kU), m);
+        FND_ACC(fmaf(o1, cs, stemB) - flipm(dy, m), grad4(hash(seed, FND_P(m, xp, kPrimeX), yp, FND_P(m, zp, kPrimeZ), FND_P(m, wp, kPrimeW)), dx - o1, dy - o0, dz - o1, dw - o1));
+    }
+    {
+        bool m = xyzwn < xn;
+        float o1 = flipm((float)(3 * kU + 1), m), o0 = flipm((float)(3 * kU), m);
+        FND_ACC(fmaf(o1, cs, stemB) - flipm(dx, m), grad4(hash(seed, xp, FND_P(m, yp, kPrimeY), FND_P(m, zp, kPrimeZ), FND_P(m, wp, kPrimeW)), dx - o0, dy - o1, dz - o1, dw - o1));
+    }
+    {
+        bool m = xn < 0.0f;
+        float o1 = flipm((float)(kU + 1), m), o0 = flipm((float)kU, m);
+        FND_ACC(fmaf(o0, cs, stemA) + flipm(dx, m), grad4(hash(seed, FND_P(m, xp, kPrimeX), yp, zp, wp), dx - o1, dy - o0, dz - o0, dw - o0));
+    }
+    {
+        bool m = xn < -yn;
+        float o1 = flipm((float)(2 * kU + 1), m), o0 = flipm((float)(2 * kU), m);
+        FND_ACC(fmaf(o0, cs, stemB) + flipm(dx + dy, m), grad4(hash(seed, FND_P(m, xp, kPrimeX), FND_P(m, yp, kPrimeY), zp, wp), dx - o1, dy - o1, dz - o0, dw - o0));
+    }
+    {
+        bool m = xn < -zn;
+        float o1 = flipm((float)(2 * kU + 1), m), o0 = flipm((float)(2 * kU), m);
+        FND_ACC(fmaf(o0, cs, stemB) + flipm(dx + dz, m), grad4(hash(seed, FND_P(m, xp, kPrimeX), yp, FND_P(m, zp, kPrimeZ), wp), dx - o1, dy - o0, dz - o1, dw - o0));
+    }
+    {
+        bool m = xn < -wn;
+        float o1 = flipm((float)(2 * kU + 1), m), o0 = flipm((float)(2 * kU), m);
+        FND_ACC(fmaf(o0, cs, stemB) + flipm(dx + dw, m), grad4(hash(seed, FND_P(m, xp, kPrimeX), yp, zp, FND_P(m, wp, kPrimeW)), dx - o1, dy - o0, dz - o0, dw - o1));
+    }
+    {
+        bool m = yn < 0.0f;
+        float o1 = flipm((float)(kU + 1), m), o0 = flipm((float)kU, m);
+        FND_ACC(fmaf(o0, cs, stemA) + flipm(dy, m), grad4(hash(seed, xp, FND_P(m, yp, kPrimeY), zp, wp), dx - o0, dy - o1, dz - o0, dw - o0));
+    }
+    {
+        bool m = yn < -zn;
+        float o1 = flipm((float)(2 * kU + 1), m), o0 = flipm((float)(2 * kU), m);
+        FND_ACC(fmaf(o0, cs, stemB) + flipm(dy + dz, m), grad4(hash(seed, xp, FND_P(m, yp, kPrimeY), FND_P(m, zp, kPrimeZ), wp), dx - o0, dy - o1, dz - o1, dw - o0));
+    }
+    {
+        bool m = yn < -wn;
+        float o1 = flipm((float)(2 * kU + 1), m), o0 = flipm((float)(2 * kU), m);
+        FND_ACC(fmaf(o0, cs, stemB) + flipm(dy + dw, m), grad4(hash(seed, xp, FND_P(m, yp, kPrimeY), zp, FND_P(m, wp, kPrimeW)), dx - o0, dy - o1, dz - o0, dw - o1));
+    }
+    {
+        bool m = zn < 0.0f;
+        float o1 = flipm((float)(kU + 1), m), o0 = flipm((float)kU, m);
+        FND_ACC(fmaf(o0, cs, stemA) + flipm(dz, m), grad4(hash(seed, xp, yp, FND_P(m, zp, kPrimeZ), wp), dx - o0, dy - o0, dz - o1, dw - o0));
+    }
+    {
+        bool m = zn < -wn;
+        float o1 = flipm((float)(2 * kU + 1), m), o0 = flipm((float)(2 * kU), m);
+        FND_ACC(fmaf(o0, cs, stemB) + flipm(dz + dw, m), grad4(hash(seed, xp, yp, FND_P(m, zp, kPrimeZ), FND_P(m, wp, kPrimeW)), dx - o0, dy - o0, dz - o1, dw - o1));
+    }
+    {
+        bool m = wn < 0.0f;
+        float o1 = flipm((float)(kU + 1), m), o0 = flipm((float)kU, m);
+        FND_ACC(fmaf(o0, cs, stemA) + flipm(dw, m), grad4(hash(seed, xp, yp, zp, FND_P(m, wp, kPrimeW)), dx - o0, dy - o0, dz - o0, dw - o1));
+    }
+#undef FND_P
+#undef FND_ACC
+    return value;
+}
+
+// ---------------------------------------------------------------- Perlin / Value
+
+FND float perlin2(int seed, float x, float y)
+{
+    float xs = floorf(x), ys = floorf(y);
+    int x0 = imul(cvti(xs), kPrimeX), y0 = imul(cvti(ys), kPrimeY);
+    int x1 = iadd(x0, kPrimeX), y1 = iadd(y0, kPrimeY);
+    float xf0 = x - xs, yf0 = y - ys, xf1 = xf0 - 1.0f, yf1 = yf0 - 1.0f;
+    float u = quintic(xf0), v = quintic(yf0);
+    return lerp(lerp(grad2(hash(seed, x0, y0), xf0, yf0), grad2(hash(seed, x1, y0), xf1, yf0), u),
+                lerp(grad2(hash(seed, x0, y1), xf0, yf1), grad2(hash(seed, x1, y1), xf1, yf1), u), v);
+}
+
+FND float perlin3(int seed, float x, float y, float z)
+{
+    float xs = floorf(x), ys = floorf(y), zs = floorf(z);
+    int x0 = imul(cvti(xs), kPrimeX), y0 = imul(cvti(ys), kPrimeY), z0 = imul(cvti(zs), kPrimeZ);
+    int x1 = iadd(x0, kPrimeX), y1 = iadd(y0, kPrimeY), z1 = iadd(z0, kPrimeZ);
+    float xf0 = x - xs, yf0 = y - ys, zf0 = z - zs;
+    float xf1 = xf0 - 1.0f, yf1 = yf0 - 1.0f, zf1 = zf0 - 1.0f;
+    float u = quintic(xf0), v = quintic(yf0), s = quintic(zf0);
+    return lerp(lerp(lerp(grad3(hash(seed, x0, y0, z0), xf0, yf0, zf0), grad3(hash(seed, x1, y0, z0), xf1, yf0, zf0), u),
+                     lerp(grad3(hash(seed, x0, y1, z0), xf0, yf1, zf0), grad3(hash(seed, x1, y1, z0), xf1, yf1, zf0), u), v),
+                lerp(lerp(grad3(hash(seed, x0, y0, z1), xf0, yf0, zf1), grad3(hash(seed, x1, y0, z1), xf1, yf0, zf1), u),
+                     lerp(grad3(hash(seed, x0, y1, z1), xf0, yf1, zf1), grad3(hash(seed, x1, y1, z1), xf1, yf1, zf1), u), v), s);
+}
+
+FND float perlin4(int seed, float x, float y, float z, float w)
+{
+    float xs = floorf(x), ys = floorf(y), zs = floorf(z), ws = floorf(w);
+    int x0 = imul(cvti(xs), kPrimeX), y0 = imul(cvti(ys), kPrimeY), z0 = imul(cvti(zs), kPrimeZ), w0 = imul(cvti(ws), kPrimeW);
+    int x1 = iadd(x0, kPrimeX), y1 = iadd(y0, kPrimeY), z1 = iadd(z0, kPrimeZ), w1 = iadd(w0, kPrimeW);
+    float xf0 = x - xs, yf0 = y - ys, zf0 = z - zs, wf0 = w - ws;
+    float xf1 = xf0 - 1.0f, yf1 = yf0 - 1.0f, zf1 = zf0 - 1.0f, wf1 = wf0 - 1.0f;
+    float u = quintic(xf0), v = quintic(yf0), s = quintic(zf0), q = quintic(wf0);
+#define G(a, b, c, d, fa, fb, fc, fd) grad4(hash(seed, a, b, c, d), fa, fb, fc, fd)
+    return lerp(
+        lerp(lerp(lerp(G(x0, y0, z0, w0, xf0, yf0, zf0, wf0), G(x1, y0, z0, w0, xf1, yf0, zf0, wf0), u),
+                  lerp(G(x0, y1, z0, w0, xf0, yf1, zf0, wf0), G(x1, y1, z0, w0, xf1, yf1, zf0, wf0), u), v),
+             lerp(lerp(G(x0, y0, z1, w0, xf0, yf0, zf1, wf0), G(x1, y0, z1, w0, xf1, yf0, zf1, wf0), u),
+                  lerp(G(x0, y1, z1, w0, xf0, yf1, zf1, wf0), G(x1, y1, z1, w0, xf1, yf1, zf1, wf0), u), v), s),
+        lerp(lerp(lerp(G(x0, y0, z0, w1, xf0, yf0, zf0, wf1), G(x1, y0, z0, w1, xf1, yf0, zf0, wf1), u),
+                  lerp(G(x0, y1, z0, w1, xf0, yf1, zf0, wf1), G(x1, y1, z0, w1, xf1, yf1, zf0, wf1), u), v),
+             lerp(lerp(G(x0, y0, z1, w1, xf0, yf0, zf1, wf1), G(x1, y0, z1, w1, xf1, yf0, zf1, wf1), u),
+                  lerp(G(x0, y1, z1, w1, xf0, yf1, zf1, wf1), G(x1, y1, z1, w1, xf1, yf1, zf1, wf1), u), v), s), q);
+#undef G
+}
+
+FND float value2(int seed, float x, float y)
+{
+    float xs = floorf(x), ys = floorf(y);
+    int x0 = imul(cvti(xs), kPrimeX), y0 = imul(cvti(ys), kPrimeY);
+    int x1 = iadd(x0, kPrimeX), y1 = iadd(y0, kPrimeY);
+    float u = hermite(x - xs), v = hermite(y - ys);
+    return lerp(lerp(valcoord(seed ^ x0 ^ y0), valcoord(seed ^ x1 ^ y0), u),
+                lerp(valcoord(seed ^ x0 ^ y1), valcoord(seed ^ x1 ^ y1), u), v);
+}
+
+FND float value3(int seed, float x, float y, float z)
+{
+    float xs = floorf(x), ys = floorf(y), zs = floorf(z);
+    int x0 = imul(cvti(xs), kPrimeX), y0 = imul(cvti(ys), kPrimeY), z0 = imul(cvti(zs), kPrimeZ);
+    int x1 = iadd(x0, kPrimeX), y1 = iadd(y0, kPrimeY), z1 = iadd(z0, kPrimeZ);
+    float u = hermite(x - xs), v = hermite(y - ys), s = hermite(z - zs);
+    return lerp(lerp(lerp(valcoord(seed ^ x0 ^ y0 ^ z0), valcoord(seed ^ x1 ^ y0 ^ z0), u),
+                     lerp(valcoord(seed ^ x0 ^ y1 ^ z0), valcoord(seed ^ x1 ^ y1 ^ z0), u), v),
+                lerp(lerp(valcoord(seed ^ x0 ^ y0 ^ z1), valcoord(seed ^ x1 ^ y0 ^ z1), u),
+                     lerp(valcoord(seed ^ x0 ^ y1 ^ z1), valcoord(seed ^ x1 ^ y1 ^ z1), u), v), s);
+}
+
+FND float value4(int seed, float x, float y, float z, float w)
+{
+    float xs = floorf(x), ys = floorf(y), zs = floorf(z), ws = floorf(w);
+    int x0 = imul(cvti(xs), kPrimeX), y0 = imul(cvti(ys), kPrimeY), z0 = imul(cvti(zs), kPrimeZ), w0 = imul(cvti(ws), kPrimeW);
+    int x1 = iadd(x0, kPrimeX), y1 = iadd(y0, kPrimeY), z1 = iadd(z0, kPrimeZ), w1 = iadd(w0, kPrimeW);
+    float u = hermite(x - xs), v = hermite(y - ys), s = hermite(z - zs), q = hermite(w - ws);
+#define V(a, b, c, d) valcoord(seed ^ a ^ b ^ c ^ d)
+    return lerp(
+        lerp(lerp(lerp(V(x0, y0, z0, w0), V(x1, y0, z0, w0), u), lerp(V(x0, y1, z0, w0), V(x1, y1, z0, w0), u), v),
+             lerp(lerp(V(x0, y0, z1, w0), V(x1, y0, z1, w0), u), lerp(V(x0, y1, z1, w0), V(x1, y1, z1, w0), u), v), s),
+        lerp(lerp(lerp(V(x0, y0, z0, w1), V(x1, y0, z0, w1), u), lerp(V(x0, y1, z0, w1), V(x1, y1, z0, w1), u), v),
+             lerp(lerp(V(x0, y0, z1, w1), V(x1, y0, z1, w1), u), lerp(V(x0, y1, z1, w1), V(x1, y1, z1, w1), u), v), s), q);
+#undef V
+}
+
+// ---------------------------------------------------------------- distances (Utils.inl:281-335)
+
+enum DistFunc { kEuclidean = 0, kEuclideanSq, kManhattan, kHybrid, kMaxAxis, kMinkowski };
+
+// Distance over D components; `sqrt_euclid` mirrors CalcDistance<DO_SQRT>.
+// Minkowski takes its exponent `mp` (already evaluated by the caller).
+template <int D>
+FND float distance(int df, bool sqrt_euclid, const float* p, float mp)
+{
+    if (df == kManhattan) {
+        float tail = fabs_(p[D - 1]);
+#pragma unroll
+        for (int k = D - 2; k >= 1; --k) tail = fabs_(p[k]) + tail;
+        return fabs_(p[0]) + tail;
+    }
+    if (df == kHybrid) {
+        float both = fmaf(p[0], p[0], fabs_(p[0]));
+#pragma unroll
+        for (int k = 1; k < D; ++k) both = both + fmaf(p[k], p[k], fabs_(p[k]));
+        return both;
+    }
+    if (df == kMaxAxis) {
+        float m = fabs_(p[0]);
+#pragma unroll
+        for (int k = 1; k < D; ++k) m = fmax_(fabs_(p[k]), m);
+        return m;
+    }
+    if (df == kMinkowski) {
+        float tail = pow_(fabs_(p[D - 1]), mp);
+#pragma unroll
+        for (int k = D - 2; k >= 1; --k) tail = pow_(fabs_(p[k]), mp) + tail;
+        return pow_(pow_(fabs_(p[0]), mp) + tail, 1.0f / mp);
+    }
+    float d = p[0] * p[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) d = fmaf(p[k], p[k], d);
+    return (df != kEuclideanSq && sqrt_euclid) ? sqrtf(d) : d;
+}
+
+// ---------------------------------------------------------------- Cellular (Cellular.inl)
+
+constexpr float kJitter2D = 0.437016f, kJitter3D = 0.396144f, kJitter4D = 0.366025f;
+
+template <int D> struct CellConst;
+template <> struct CellConst<2> { static constexpr float jitter = kJitter2D; static constexpr float size = -1.f / 0x3ff; };
+template <> struct CellConst<3> { static constexpr float jitter = kJitter3D; static constexpr float size = -1.f / 0xffff; };
+template <> struct CellConst<4> { static constexpr float jitter = kJitter4D; static constexpr float size = -1.f / 0xfffff; };
+
+__device__ constexpr int kPrimes[4] = {kPrimeX, kPrimeY, kPrimeZ, kPrimeW};
+
+template <int D>
+FND int cell_hash(int seed, const int* c)
+{
+    if (D == 2) return hashhb(seed, c[0], c[1]);
+    if (D == 3) return hashhb(seed, c[0], c[1], c[2]);
+    return hashhb(seed, c[0], c[1], c[2], c[3]);
+}
+
+// Jittered cell-point direction scaled by jitter/|dir| (Cellular.inl:55-58, 141-145, 239-244)
+template <int D>
+FND void cell_dir(int h, float jitter, float* d)
+{
+    if (D == 2) {
+        d[0] = cvtf(h & 0x7ff) - (0x7ff / 2.0f);
+        d[1] = cvtf((int)srl(h, 21)) - (0x7ff / 2.0f);
+        float inv = jitter * invsqrt(fmaf(d[0], d[0], d[1] * d[1]));
+        d[2] = inv;
+    } else if (D == 3) {
+        d[0] = cvtf(h & 0x3ff) - (0x3ff / 2.0f);
+        d[1] = cvtf((h >> 11) & 0x3ff) - (0x3ff / 2.0f);
+        d[2] = cvtf((int)srl(h, 22)) - (0x3ff / 2.0f);
+        d[3] = jitter * invsqrt(fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2])));
+    } else {
+        d[0] = cvtf(h & 0xff) - (0xff / 2.0f);
+        d[1] = cvtf((h >> 8) & 0xff) - (0xff / 2.0f);
+        d[2] = cvtf((h >> 16) & 0xff) - (0xff / 2.0f);
+        d[3] = cvtf((int)srl(h, 24)) - (0xff / 2.0f);
+        d[4] = jitter * invsqrt(fmaf(d[0], d[0], fmaf(d[1], d[1], fmaf(d[2], d[2], d[3] * d[3]))));
+    }
+}
+
+template <int D>
+FND float size_factor(int h, float sj)
+{
+    float dj = D == 2 ? cvtf((h >> 11) & 0x3ff) : (D == 3 ? cvtf(h & 0xffff) : cvtf(h & 0xfffff));
+    return fmaf(-sj, dj, 1.0f);
+}
+
+// The 3^D neighbourhood walk shared by the three cellular nodes.  `mode`:
+// 0 = CellularValue (offset base = cell - pos, incremented),
+// 1 = CellularDistance (offset = running cell - pos),
+// 2 = CellularLookup (cell point, then - pos).
+struct CellParams {
+    float freq;        // ScalableGenerator::mFrequency
+    float jitter;      // kJitterND * grid jitter (already multiplied)
+    float sizeJitter;  // size jitter * -1/mask (already multiplied), used if sizeActive
+    bool sizeActive;
+    int distFunc;
+    float minkowski;   // constant Minkowski P
+};
+
+template <int D>
+FND float cellular_value(int seed, const float* pin, const CellParams& cp, int valueIndex)
+{
+    float p[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) p[k] = pin[k] * cp.freq;
+    float dist[4] = {__int_as_float(0x7F800000), __int_as_float(0x7F800000), __int_as_float(0x7F800000), __int_as_float(0x7F800000)};
+    int vh[4] = {0, 0, 0, 0};
+    int cb[D];
+    float cfb[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        cb[k] = iadd(cvti(p[k]), -1);
+        cfb[k] = cvtf(cb[k]) - p[k];
+        cb[k] = imul(cb[k], kPrimes[k]);
+    }
+    int c[D];
+    float cf[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) { c[k] = cb[k]; cf[k] = cfb[k]; }
+    constexpr int total = D == 2 ? 9 : (D == 3 ? 27 : 81);
+    int idx[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) idx[k] = 0;
+#pragma unroll 1
+    for (int it = 0; it < total; ++it) {
+        int h = cell_hash<D>(seed, c);
+        float d[D + 1];
+        cell_dir<D>(h, cp.jitter, d);
+        float off[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) off[k] = fmaf(d[k], d[D], cf[k]);
+        float nd = distance<D>(cp.distFunc, D == 2, off, cp.minkowski);
+        if (cp.sizeActive) nd *= size_factor<D>(h, cp.sizeJitter);
+        int nh = h;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            bool closer = nd < dist[i];
+            float ld = dist[i];
+            int lh = vh[i];
+            dist[i] = closer ? nd : dist[i];
+            vh[i] = closer ? nh : vh[i];
+            if (i >= valueIndex) break;
+            nd = closer ? ld : nd;
+            nh = closer ? lh : nh;
+        }
+#pragma unroll
+        for (int k = D - 1; k >= 0; --k) {
+            if (++idx[k] < 3) { cf[k] += 1.0f; c[k] = iadd(c[k], kPrimes[k]); break; }
+            idx[k] = 0; cf[k] = cfb[k]; c[k] = cb[k];
+        }
+    }
+    int sel = vh[0];
+#pragma unroll
+    for (int i = 1; i < 4; ++i) sel = valueIndex == i ? vh[i] : sel;
+    return cvtf(sel);
+}
+
+template <int D>
+FND void cellular_distances(int seed, const float* pin, const CellParams& cp, float* dist)
+{
+    float p[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) p[k] = pin[k] * cp.freq;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) dist[i] = __int_as_float(0x7F800000);
+    int cb[D];
+    float cfb[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        cb[k] = iadd(cvti(p[k]), -1);
+        cfb[k] = cvtf(cb[k]);
+        cb[k] = imul(cb[k], kPrimes[k]);
+    }
+    int c[D];
+    float cf[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) { c[k] = cb[k]; cf[k] = cfb[k]; }
+    constexpr int total = D == 2 ? 9 : (D == 3 ? 27 : 81);
+    int idx[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) idx[k] = 0;
+#pragma unroll 1
+    for (int it = 0; it < total; ++it) {
+        int h = cell_hash<D>(seed, c);
+        float d[D + 1];
+        cell_dir<D>(h, cp.jitter, d);
+        float off[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) off[k] = fmaf(d[k], d[D], cf[k] - p[k]);
+        float nd = distance<D>(cp.distFunc, false, off, cp.minkowski);
+        if (cp.sizeActive) nd *= size_factor<D>(h, cp.sizeJitter);
+#pragma unroll
+        for (int i = 3; i > 0; i--) dist[i] = fmax_(fmin_(dist[i], nd), dist[i - 1]);
+        dist[0] = fmin_(dist[0], nd);
+#pragma unroll
+        for (int k = D - 1; k >= 0; --k) {
+            if (++idx[k] < 3) { cf[k] += 1.0f; c[k] = iadd(c[k], kPrimes[k]); break; }
+            idx[k] = 0; cf[k] = cfb[k]; c[k] = cb[k];
+        }
+    }
+}
+
+// CellularDistance::GetReturn (Cellular.inl:531-565) without the final ScaleOutput;
+// returns the combined distance and writes the native max through `nmax`.
+template <int D>
+FND float cellular_return(float* dist, int distFunc, int i0, int i1, int ret, float& nmax)
+{
+    float maxDist = 1 + CellConst<D>::jitter;
+    float d0 = dist[0], d1 = dist[0];
+#pragma unroll
+    for (int i = 1; i < 4; ++i) { d0 = i0 == i ? dist[i] : d0; d1 = i1 == i ? dist[i] : d1; }
+    if (distFunc == kEuclidean) {
+        d0 = d0 * invsqrt(d0);
+        // both indices alias the same slot when i0 == i1: the reference scales it twice
+        d1 = (i1 == i0) ? d0 * invsqrt(d0) : d1 * invsqrt(d1);
+        if (i1 == i0) d0 = d1;
+    }
+    maxDist *= maxDist;
+    switch (ret) {
+    case 1: nmax = maxDist * 2; return d0 + d1;
+    case 2: nmax = maxDist; return fabs_(d0 - d1);
+    case 3: nmax = maxDist * maxDist; return d0 * d1;
+    case 4: nmax = maxDist; return d0 * (1.0f / d1);
+    default: nmax = maxDist; return d0;
+    }
+}
+
+template <int D>
+FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, float scale, float* out)
+{
+    float p[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) p[k] = pin[k] * cp.freq;
+    float best = 3.40282347e+38f;
+    float cell[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) cell[k] = 0.0f;
+    int cb[D];
+    float cfb[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        cb[k] = iadd(cvti(p[k]), -1);
+        cfb[k] = cvtf(cb[k]);
+        cb[k] = imul(cb[k], kPrimes[k]);
+    }
+    int c[D];
+    float cf[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) { c[k] = cb[k]; cf[k] = cfb[k]; }
+    constexpr int total = D == 2 ? 9 : (D == 3 ? 27 : 81);
+    int idx[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k) idx[k] = 0;
+#pragma unroll 1
+    for (int it = 0; it < total; ++it) {
+        int h = cell_hash<D>(seed, c);
+        float d[D + 1];
+        cell_dir<D>(h, cp.jitter, d);
+        float local[D], off[D];
+#pragma unroll
+        for (int k = 0; k < D; ++k) { local[k] = fmaf(d[k], d[D], cf[k]); off[k] = local[k] - p[k]; }
+        float nd = distance<D>(cp.distFunc, false, off, cp.minkowski);
+        if (cp.sizeActive) nd *= size_factor<D>(h, cp.sizeJitter);
+        bool closer = nd < best;
+        best = fmin_(nd, best);
+#pragma unroll
+        for (int k = 0; k < D; ++k) cell[k] = closer ? local[k] : cell[k];
+#pragma unroll
+        for (int k = D - 1; k >= 0; --k) {
+            if (++idx[k] < 3) { cf[k] += 1.0f; c[k] = iadd(c[k], kPrimes[k]); break; }
+            idx[k] = 0; cf[k] = cfb[k]; c[k] = cb[k];
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) out[k] = cell[k] * scale;
+}
+
+// ---------------------------------------------------------------- DomainWarpGradient::Warp (DomainWarp.inl:33-206)
+
+template <int D>
+FND float warp_gradient(int seed, float amp, const float* sp, const float* axis, float* io)
+{
+    float s[D][2];
+    int c[D][2];
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        float fl = floorf(sp[k]);
+        c[k][0] = imul(cvti(fl), kPrimes[k]);
+        c[k][1] = iadd(c[k][0], kPrimes[k]);
+        s[k][1] = hermite(sp[k] - fl);
+        s[k][0] = 1.0f - s[k][1];
+    }
+    float wv[D];
+    constexpr float normalise = D == 2 ? 1.0f / (0xffff / 2.0f) : (D == 3 ? 1.0f / (0x3ff / 2.0f) : 1.0f / (0xff / 2.0f));
+#pragma unroll
+    for (int corner = 0; corner < (1 << D); ++corner) {
+        const int b0 = corner & 1, b1 = (corner >> 1) & 1, b2 = (corner >> 2) & 1, b3 = (corner >> 3) & 1;
+        int h;
+        float contrib, comp[D];
+        if (D == 2) {
+            h = hashhb(seed, c[0][b0], c[1][b1]);
+            contrib = s[0][b0] * s[1][b1];
+            comp[0] = cvtf(h & 0xffff);
+            comp[1] = cvtf((int)srl(h, 16));
+        } else if (D == 3) {
+            h = hashhb(seed, c[0][b0], c[1][b1], c[2 % D][b2]);
+            contrib = s[0][b0] * s[1][b1] * s[2 % D][b2];
+            comp[0] = cvtf(h & 0x3ff);
+            comp[1] = cvtf((h >> 11) & 0x3ff);
+            comp[2 % D] = cvtf((int)srl(h, 22));
+        } else {
+            h = hashhb(seed, c[0][b0], c[1][b1], c[2 % D][b2], c[3 % D][b3]);
+            contrib = s[0][b0] * s[1][b1] * s[2 % D][b2] * s[3 % D][b3];
+            comp[0] = cvtf(h & 0xff);
+            comp[1] = cvtf((h >> 8) & 0xff);
+            comp[2 % D] = cvtf((h >> 16) & 0xff);
+            comp[3 % D] = cvtf((int)srl(h, 24));
+        }
+#pragma unroll
+        for (int k = 0; k < D; ++k) wv[k] = corner == 0 ? contrib * comp[k] : fmaf(contrib, comp[k], wv[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) wv[k] = fmaf(wv[k], normalise, -1.0f);
+#pragma unroll
+    for (int k = 0; k < D; ++k) io[k] = fmaf(wv[k], amp * axis[k], io[k]);
+    float r = wv[D - 1] * wv[D - 1];
+#pragma unroll
+    for (int k = D - 2; k >= 0; --k) r = fmaf(wv[k], wv[k], r);
+    return r;
+}
+
+// ---------------------------------------------------------------- basic generators
+
+template <int D>
+FND float white(int seed, const float* p)
+{
+    int h = seed;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+        int b = __float_as_int(p[k]);
+        h ^= imul(b ^ (b >> 16), kPrimes[k]);
+    }
+    return valcoord(h);
+}
+
+template <int D>
+FND float checkerboard(const float* p, float freq)
+{
+    int v = 0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) v ^= cvti(p[k] * freq);
+    return __int_as_float((v & 1) << 30);
+}
+
+template <int D>
+FND float sine_wave(const float* p, float freq)
+{
+    float t = sin_(p[D - 1] * freq);
+#pragma unroll
+    for (int k = D - 2; k >= 0; --k) t = sin_(p[k] * freq) * t;
+    return t;
+}
+
+// ---------------------------------------------------------------- modifiers
+
+FND void rotate_plane(int type, float& x, float& y, float& z)   // Modifiers.inl:354-388
+{
+    float nx = x, ny = y, nz = z;
+    if (type == 0) {
+        float xy = x + y;
+        float s2 = xy * -0.211324865405187f;
+        nz = z * 0.577350269189626f;
+        nx = x + s2 - nz;
+        ny = y + s2 - nz;
+        nz = nz + xy * 0.577350269189626f;
+    } else if (type == 1) {
+        float xz = x + z;
+        float s2 = xz * -0.211324865405187f;
+        ny = y * 0.577350269189626f;
+        nx = x + s2 - ny;
+        nz = z + s2 - ny;
+        ny = ny + xz * 0.577350269189626f;
+    }
+    x = nx; y = ny; z = nz;
+}
+
+// Terrace (Modifiers.inl:134-181).  recip = 1 + 1/smoothness (constant) or computed.
+FND float terrace_smooth(float rounded, float source, float recip)
+{
+    float diff = rounded - source;
+    bool neg = diff < 0.0f;
+    diff = fabs_(diff);
+    diff = 0.5f - diff;
+    diff = diff * recip;
+    diff = fmin_(diff, 0.5f);
+    diff = neg ? 0.5f - diff : diff - 0.5f;
+    return rounded + diff;
+}
+
+FND float min_smooth(float a, float b, float smooth)   // Blends.inl:130-141
+{
+    float sm = fmax_(1.17549435e-38f, fabs_(smooth));
+    float h = fmax_(sm - fabs_(a - b), 0.0f);
+    h = h * (1.0f / sm);
+    return fmaf(-(1.0f / 6.0f), h * h * h * sm, fmin_(a, b));
+}
+
+FND float fade_t(float fade, float fmn, float fmx, int interp)   // Blends.inl:172-195
+{
+    float range = fmx - fmn;
+    fade = (fade - fmn) / range;
+    fade = fmax_(0.0f, fmin_(1.0f, fade));
+    if (interp == 1) fade = hermite(fade);
+    else if (interp == 2) fade = quintic(fade);
+    return range == 0.0f ? 0.5f : fade;
+}
+
+FND float remap(float s, float fromMin, float fromMax, float toMin, float toMax, bool clampOut)
+{
+    float r = toMin + ((s - fromMin) / (fromMax - fromMin) * (toMax - toMin));
+    if (clampOut) { r = fmax_(r, toMin); r = fmin_(r, toMax); }
+    return r;
+}
+
+FND float ping_pong(float t)
+{
+    t = t - floorf(t * 0.5f) * 2.0f;
+    return t < 1.0f ? t : 2.0f - t;
+}
+
+FND float to_rgba8(float s, float mn, float mx)   // Modifiers.inl:107-126
+{
+    s = fmin_(s, mx);
+    s = fmax_(s, mn);
+    s = s - mn;
+    s = s * (255.0f / (mx - mn));
+    int b = cvti(s);
+    unsigned o = 0xFF000000u | (unsigned)b | ((unsigned)b << 8) | ((unsigned)b << 16);
+    return __uint_as_float(o);
+}
+
+FND float signed_sqrt(float v)
+{
+    return __uint_as_float(__float_as_uint(sqrtf(fabs_(v))) | (__float_as_uint(v) & 0x80000000u));
+}
+
+}  // namespace fnd

@@ -1,0 +1,178 @@
+/*
+ * FastNoise_C.h -- C-ABI of the GB300 FastNoise2 backend (libfastnoise_gb300.so).
+ *
+ * Drop-in for FastNoise2's own C-ABI (reference include/FastNoise/FastNoise_C.h,
+ * implemented in src/FastNoise/FastNoise_C.cpp).  Every function in the first
+ * part keeps the reference's name, argument meaning and error behaviour; the
+ * citation beside each one is the reference declaration it replaces.  Node
+ * handles are opaque, reference counted, and may be shared between threads for
+ * generation (README.md:39-40 of the reference).  Node trees are evaluated on
+ * the current CUDA device; output arrays in this part are HOST memory.
+ *
+ * The second part adds entry points that the reference does not have: device
+ * pointer variants (output stays in GPU memory), tree serialisation, batched
+ * generation and a request server.  They return an int status (0 = ok,
+ * negative = error, text via fnGetLastErrorString()).
+ *
+ * Where the reference would compute on the CPU, this library never does: if
+ * the GPU path cannot run (no device, a node without a GPU implementation) the
+ * output is filled with NaN, the min/max with NaN, a message is printed to
+ * stderr and fnGetLastError() returns non-zero.
+ */
+#ifndef FASTNOISE_GB300_C_H
+#define FASTNOISE_GB300_C_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(_WIN32)
+#define FASTNOISE_API __declspec(dllexport)
+#else
+#define FASTNOISE_API __attribute__((visibility("default")))
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#else
+#include <stdbool.h>
+#endif
+
+/* ---------------------------------------------------------------------------
+ * Part 1: reference-compatible entry points
+ * ------------------------------------------------------------------------- */
+
+/* FastNoise_C.h:27 -- decode an encoded node tree; NULL on failure.  maxFeatureSet is accepted and ignored. */
+FASTNOISE_API void* fnNewFromEncodedNodeTree(const char* encodedString, unsigned maxFeatureSet);
+/* FastNoise_C.h:32 -- release one reference; NULL is a no-op. */
+FASTNOISE_API void fnDeleteNodeRef(void* node);
+/* FastNoise_C.h:38 -- feature set of the node; this backend reports FN_GB300_FEATURE_SET. */
+FASTNOISE_API unsigned fnGetActiveFeatureSet(const void* node);
+/* FastNoise_C.h:44 */
+FASTNOISE_API int fnGetMetadataID(const void* node);
+
+/* FastNoise_C.h:66-80 -- out[y*xCount + x]; outputMinMax is NULL or float[2] */
+FASTNOISE_API void fnGenUniformGrid2D(const void* node, float* noiseOut, float xOffset, float yOffset, int xCount,
+                                      int yCount, float xStepSize, float yStepSize, int seed, float* outputMinMax);
+/* FastNoise_C.h:91-106 */
+FASTNOISE_API void fnGenUniformGrid3D(const void* node, float* noiseOut, float xOffset, float yOffset, float zOffset,
+                                      int xCount, int yCount, int zCount, float xStepSize, float yStepSize,
+                                      float zStepSize, int seed, float* outputMinMax);
+/* FastNoise_C.h:120-138 */
+FASTNOISE_API void fnGenUniformGrid4D(const void* node, float* noiseOut, float xOffset, float yOffset, float zOffset,
+                                      float wOffset, int xCount, int yCount, int zCount, int wCount, float xStepSize,
+                                      float yStepSize, float zStepSize, float wStepSize, int seed, float* outputMinMax);
+/* FastNoise_C.h:164-170 */
+FASTNOISE_API void fnGenPositionArray2D(const void* node, float* noiseOut, int count, const float* xPosArray,
+                                        const float* yPosArray, float xOffset, float yOffset, int seed,
+                                        float* outputMinMax);
+/* FastNoise_C.h:193-199 */
+FASTNOISE_API void fnGenPositionArray3D(const void* node, float* noiseOut, int count, const float* xPosArray,
+                                        const float* yPosArray, const float* zPosArray, float xOffset, float yOffset,
+                                        float zOffset, int seed, float* outputMinMax);
+/* FastNoise_C.h:224-231 */
+FASTNOISE_API void fnGenPositionArray4D(const void* node, float* noiseOut, int count, const float* xPosArray,
+                                        const float* yPosArray, const float* zPosArray, const float* wPosArray,
+                                        float xOffset, float yOffset, float zOffset, float wOffset, int seed,
+                                        float* outputMinMax);
+/* FastNoise_C.h:250-253 */
+FASTNOISE_API void fnGenTileable2D(const void* node, float* noiseOut, int xSize, int ySize, float xStepSize,
+                                   float yStepSize, int seed, float* outputMinMax);
+/* FastNoise_C.h:267, 281, 298 */
+FASTNOISE_API float fnGenSingle2D(const void* node, float x, float y, int seed);
+FASTNOISE_API float fnGenSingle3D(const void* node, float x, float y, float z, int seed);
+FASTNOISE_API float fnGenSingle4D(const void* node, float x, float y, float z, float w, int seed);
+
+/* Metadata, FastNoise_C.h:307-651.  Invalid ids / indices return -1, false,
+ * 0 or the reference's sentinel strings ("INVALID NODE ID", ...). */
+FASTNOISE_API int fnGetMetadataCount(void);
+FASTNOISE_API const char* fnGetMetadataName(int id);
+FASTNOISE_API void* fnNewFromMetadata(int id, unsigned maxFeatureSet);
+FASTNOISE_API int fnGetMetadataVariableCount(int id);
+FASTNOISE_API const char* fnGetMetadataVariableName(int id, int variableIndex);
+FASTNOISE_API int fnGetMetadataVariableType(int id, int variableIndex);
+FASTNOISE_API int fnGetMetadataVariableDimensionIdx(int id, int variableIndex);
+FASTNOISE_API int fnGetMetadataEnumCount(int id, int variableIndex);
+FASTNOISE_API const char* fnGetMetadataEnumName(int id, int variableIndex, int enumIndex);
+FASTNOISE_API bool fnSetVariableFloat(void* node, int variableIndex, float value);
+FASTNOISE_API bool fnSetVariableIntEnum(void* node, int variableIndex, int value);
+FASTNOISE_API int fnGetMetadataNodeLookupCount(int id);
+FASTNOISE_API const char* fnGetMetadataNodeLookupName(int id, int nodeLookupIndex);
+FASTNOISE_API int fnGetMetadataNodeLookupDimensionIdx(int id, int nodeLookupIndex);
+FASTNOISE_API bool fnSetNodeLookup(void* node, int nodeLookupIndex, const void* nodeLookup);
+FASTNOISE_API int fnGetMetadataHybridCount(int id);
+FASTNOISE_API const char* fnGetMetadataHybridName(int id, int hybridIndex);
+FASTNOISE_API int fnGetMetadataHybridDimensionIdx(int id, int hybridIndex);
+FASTNOISE_API bool fnSetHybridNodeLookup(void* node, int hybridIndex, const void* nodeLookup);
+FASTNOISE_API bool fnSetHybridFloat(void* node, int hybridIndex, float value);
+FASTNOISE_API const char* fnGetMetadataDescription(int id);
+FASTNOISE_API int fnGetMetadataGroupCount(int id);
+FASTNOISE_API const char* fnGetMetadataGroupName(int id, int groupIndex);
+FASTNOISE_API const char* fnGetMetadataVariableDescription(int id, int variableIndex);
+FASTNOISE_API float fnGetMetadataVariableDefaultFloat(int id, int variableIndex);
+FASTNOISE_API int fnGetMetadataVariableDefaultIntEnum(int id, int variableIndex);
+FASTNOISE_API float fnGetMetadataVariableMinFloat(int id, int variableIndex);
+FASTNOISE_API float fnGetMetadataVariableMaxFloat(int id, int variableIndex);
+FASTNOISE_API const char* fnGetMetadataNodeLookupDescription(int id, int nodeLookupIndex);
+FASTNOISE_API const char* fnGetMetadataHybridDescription(int id, int hybridIndex);
+FASTNOISE_API float fnGetMetadataHybridDefault(int id, int hybridIndex);
+
+/* ---------------------------------------------------------------------------
+ * Part 2: additions of the GB300 backend (no reference counterpart)
+ * ------------------------------------------------------------------------- */
+
+#define FN_GB300_FEATURE_SET 0x47423330u   /* value of fnGetActiveFeatureSet */
+
+#define FN_OK 0
+#define FN_ERR_ARG (-1)           /* bad argument (null node, negative count, ...) */
+#define FN_ERR_COMPILE (-2)       /* tree cannot be evaluated on the GPU (see message) */
+#define FN_ERR_CUDA (-3)          /* CUDA runtime error */
+#define FN_ERR_CAPACITY (-4)      /* request does not fit a pool / queue / scratch limit */
+#define FN_ERR_TIMEOUT (-5)       /* a bounded wait ran out */
+#define FN_ERR_STATE (-6)         /* object in the wrong state (closed server, ...) */
+
+/* Last status of this thread (0 after a successful call), and its message. */
+FASTNOISE_API int fnGetLastError(void);
+FASTNOISE_API const char* fnGetLastErrorString(void);
+
+/* Serialise like Metadata::SerialiseNodeData (reference src/FastNoise/Metadata.cpp:297-308).
+ * Writes a NUL-terminated string if it fits; returns its length (excluding NUL) or a negative status. */
+FASTNOISE_API int fnSerialiseNodeTree(const void* node, char* buffer, int bufferSize);
+
+/* Device-pointer variants of the generation calls.  `dOut` is device memory
+ * (count floats); `dMinMax` is NULL or device float[2]; `stream` is a
+ * cudaStream_t (NULL = this thread's stream).  The call is asynchronous:
+ * it returns once the work is queued on the stream. */
+FASTNOISE_API int fnGenUniformGrid2DDevice(const void* node, float* dOut, float xOffset, float yOffset, int xCount,
+                                           int yCount, float xStepSize, float yStepSize, int seed, float* dMinMax,
+                                           void* stream);
+FASTNOISE_API int fnGenUniformGrid3DDevice(const void* node, float* dOut, float xOffset, float yOffset, float zOffset,
+                                           int xCount, int yCount, int zCount, float xStepSize, float yStepSize,
+                                           float zStepSize, int seed, float* dMinMax, void* stream);
+FASTNOISE_API int fnGenUniformGrid4DDevice(const void* node, float* dOut, float xOffset, float yOffset, float zOffset,
+                                           float wOffset, int xCount, int yCount, int zCount, int wCount,
+                                           float xStepSize, float yStepSize, float zStepSize, float wStepSize, int seed,
+                                           float* dMinMax, void* stream);
+FASTNOISE_API int fnGenPositionArray2DDevice(const void* node, float* dOut, int count, const float* dX, const float* dY,
+                                             float xOffset, float yOffset, int seed, float* dMinMax, void* stream);
+FASTNOISE_API int fnGenPositionArray3DDevice(const void* node, float* dOut, int count, const float* dX, const float* dY,
+                                             const float* dZ, float xOffset, float yOffset, float zOffset, int seed,
+                                             float* dMinMax, void* stream);
+FASTNOISE_API int fnGenPositionArray4DDevice(const void* node, float* dOut, int count, const float* dX, const float* dY,
+                                             const float* dZ, const float* dW, float xOffset, float yOffset,
+                                             float zOffset, float wOffset, int seed, float* dMinMax, void* stream);
+FASTNOISE_API int fnGenTileable2DDevice(const void* node, float* dOut, int xSize, int ySize, float xStepSize,
+                                        float yStepSize, int seed, float* dMinMax, void* stream);
+
+/* Compile `node` for dimensionality 2/3/4 on the host only (no CUDA call) and report the
+ * program size: returns 0 and fills nInstr / nRegs (either may be NULL), or a negative status. */
+FASTNOISE_API int fnCompileInfo(const void* node, int dimension, int* nInstr, int* nRegs);
+
+/* Compile (and cache on the device) the program for `node` at dimensionality 2/3/4.
+ * Generation calls do this on demand; calling it ahead moves the cost out of the first call. */
+FASTNOISE_API int fnPrepare(const void* node, int dimension);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FASTNOISE_GB300_C_H */

@@ -1,0 +1,166 @@
+"""ctypes front-end to the C oracle (TEST INFRASTRUCTURE, never shipped).
+
+Builds ``oracle/fn_oracle.c`` into ``oracle/_build/libfn_oracle.so`` with the
+recipe in :func:`build` (plain gcc, ``-ffp-contract=off`` so that only the
+explicit ``fmaf`` calls fuse), instantiates a :class:`oracle.tree.Node` tree by
+replaying its setter calls in order, and exposes the reference's batch drivers
+(``Generator.inl`` GenUniformGrid2D/3D/4D, GenPositionArray2D/3D/4D,
+GenTileable2D, GenSingle*), each returning ``(values, (min, max))``.
+
+Parity is unpinned: see the header of ``fn_oracle.c``.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import platform
+import subprocess
+from typing import Dict, Optional, Sequence, Tuple
+
+import numpy as np
+
+from .tree import Node, walk
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libfn_oracle.so")
+SRC = os.path.join(HERE, "fn_oracle.c")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle shared library (a few seconds)."""
+    os.makedirs(BUILD, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
+        return LIB
+    flags = ["-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-fvisibility=hidden"]
+    if platform.machine() in ("x86_64", "AMD64"):
+        flags.append("-mfma")            # hardware fmaf; the result is the same IEEE fused op
+    tmp = LIB + f".tmp{os.getpid()}"
+    subprocess.run(["gcc", *flags, "-o", tmp, SRC, "-lm", "-lpthread"], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB)
+        vp, fp, ip, c_int, c_float = ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_float
+        L.on_new.restype = vp
+        L.on_new.argtypes = [c_int]
+        L.on_free.argtypes = [vp]
+        L.on_set_var.argtypes = [vp, c_int, ctypes.c_int32]
+        L.on_set_lookup.argtypes = [vp, c_int, vp]
+        L.on_set_hybrid_node.argtypes = [vp, c_int, vp]
+        L.on_set_hybrid_float.argtypes = [vp, c_int, c_float]
+        L.on_set_unfused.argtypes = [c_int]
+        L.on_gen_grid.argtypes = [vp, c_int, fp, fp, ip, fp, c_int, c_int, fp]
+        L.on_gen_positions.argtypes = [vp, c_int, fp, ctypes.c_int64, ctypes.POINTER(fp), fp, c_int, c_int, fp]
+        L.on_gen_tileable.argtypes = [vp, fp, c_int, c_int, c_float, c_float, c_int, c_int, fp]
+        L.on_gen_single.restype = c_float
+        L.on_gen_single.argtypes = [vp, c_int, fp, c_int]
+        L.fn_sinf.restype = c_float
+        L.fn_sinf.argtypes = [c_float]
+        L.fn_cosf.restype = c_float
+        L.fn_cosf.argtypes = [c_float]
+        L.fn_powf.restype = c_float
+        L.fn_powf.argtypes = [c_float, c_float]
+        _lib = L
+    return _lib
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class OracleTree:
+    """A tree instantiated inside the C oracle."""
+
+    def __init__(self, root: Node, unfused: bool = False):
+        L = lib()
+        self.unfused = unfused
+        self._handles: Dict[int, int] = {}
+        for node in walk(root):
+            h = L.on_new(node.meta.id)
+            self._handles[id(node)] = h
+            for kind, idx, arg in node.ops:
+                if kind == "var":
+                    L.on_set_var(h, idx, int(arg))
+                elif kind == "lookup":
+                    L.on_set_lookup(h, idx, self._handles[id(arg)])
+                elif kind == "hnode":
+                    L.on_set_hybrid_node(h, idx, self._handles[id(arg)])
+                elif kind == "hfloat":
+                    L.on_set_hybrid_float(h, idx, float(arg))
+        self.root = self._handles[id(root)]
+
+    def __del__(self):
+        if _lib is not None:
+            for h in self._handles.values():
+                _lib.on_free(h)
+
+    def _mode(self):
+        lib().on_set_unfused(1 if self.unfused else 0)
+
+    def grid(self, offset: Sequence[float], count: Sequence[int], step: Sequence[float], seed: int,
+             threads: int = 0) -> Tuple[np.ndarray, Tuple[float, float]]:
+        """GenUniformGrid{2,3,4}D: out[(..*Y + y)*X + x], x fastest."""
+        dim = len(count)
+        total = int(np.prod([max(c, 0) for c in count]))
+        out = np.empty(max(total, 1), np.float32)
+        off = np.asarray(offset, np.float32)
+        cnt = np.asarray(count, np.int32)
+        st = np.asarray(step, np.float32)
+        mm = np.zeros(2, np.float32)
+        self._mode()
+        lib().on_gen_grid(self.root, dim, _fptr(out), _fptr(off), cnt.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                          _fptr(st), int(np.int32(seed)), threads or os.cpu_count(), _fptr(mm))
+        return out[:total], (float(mm[0]), float(mm[1]))
+
+    def positions(self, pos: Sequence[np.ndarray], offset: Sequence[float], seed: int,
+                  threads: int = 0) -> Tuple[np.ndarray, Tuple[float, float]]:
+        """GenPositionArray{2,3,4}D."""
+        dim = len(pos)
+        arrs = [np.ascontiguousarray(p, np.float32) for p in pos]
+        count = len(arrs[0])
+        out = np.empty(max(count, 1), np.float32)
+        ptrs = (ctypes.POINTER(ctypes.c_float) * 4)(*[_fptr(a) for a in arrs], *([None] * (4 - dim)))
+        off = np.asarray(offset, np.float32)
+        mm = np.zeros(2, np.float32)
+        self._mode()
+        lib().on_gen_positions(self.root, dim, _fptr(out), count, ptrs, _fptr(off), int(np.int32(seed)),
+                               threads or os.cpu_count(), _fptr(mm))
+        return out[:count], (float(mm[0]), float(mm[1]))
+
+    def tileable(self, x_size: int, y_size: int, x_step: float, y_step: float, seed: int,
+                 threads: int = 0) -> Tuple[np.ndarray, Tuple[float, float]]:
+        """GenTileable2D."""
+        total = max(x_size, 0) * max(y_size, 0)
+        out = np.empty(max(total, 1), np.float32)
+        mm = np.zeros(2, np.float32)
+        self._mode()
+        lib().on_gen_tileable(self.root, _fptr(out), x_size, y_size, x_step, y_step, int(np.int32(seed)),
+                              threads or os.cpu_count(), _fptr(mm))
+        return out[:total], (float(mm[0]), float(mm[1]))
+
+    def single(self, pos: Sequence[float], seed: int) -> float:
+        """GenSingle{2,3,4}D."""
+        p = np.zeros(4, np.float32)
+        p[:len(pos)] = pos
+        self._mode()
+        return float(lib().on_gen_single(self.root, len(pos), _fptr(p), int(np.int32(seed))))
+
+
+def sinf(x: float) -> float:
+    return float(lib().fn_sinf(x))
+
+
+def cosf(x: float) -> float:
+    return float(lib().fn_cosf(x))
+
+
+def powf(x: float, y: float) -> float:
+    return float(lib().fn_powf(x, y))

@@ -1,0 +1,64 @@
+"""Shared comparison helpers: run a tree through the GPU (product C-ABI) and the
+CPU oracle on the same inputs and check the result.
+
+Tolerance: max |gpu - oracle| <= 1e-5 (absolute, the path's stated bound), or
+1e-6 relative for values whose magnitude exceeds 10.  Both sides implement the
+same IEEE operation sequence, so in practice outputs are bit-identical; the
+bit-exact fraction is reported with every comparison.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from oracle.oracle import OracleTree
+from tests.trees import to_product
+
+ABS_TOL = 1e-5
+REL_TOL = 1e-6
+
+
+def close(gpu: np.ndarray, ref: np.ndarray):
+    gpu = np.asarray(gpu, np.float32)
+    ref = np.asarray(ref, np.float32)
+    assert gpu.shape == ref.shape
+    both_nan = np.isnan(gpu) & np.isnan(ref)
+    diff = np.abs(gpu.astype(np.float64) - ref.astype(np.float64))
+    diff[both_nan] = 0.0
+    tol = np.maximum(ABS_TOL, REL_TOL * np.abs(ref.astype(np.float64)))
+    bad = ~(diff <= tol)
+    exact = np.mean(gpu.view(np.uint32) == ref.view(np.uint32)) if gpu.size else 1.0
+    return (not bad.any()), float(np.nanmax(diff)) if diff.size else 0.0, float(exact), int(bad.sum())
+
+
+def minmax_equal(a, b):
+    def eq(x, y):
+        return (np.isnan(x) and np.isnan(y)) or x == y
+    return eq(a[0], b[0]) and eq(a[1], b[1])
+
+
+def run_grid(root, offset, count, step, seed):
+    prod = to_product(root)
+    g, gmm = prod.gen_uniform_grid(offset, count, step, seed)
+    o, omm = OracleTree(root).grid(offset, count, step, seed)
+    return g, gmm, o, omm
+
+
+def run_positions(root, pos, offset, seed):
+    prod = to_product(root)
+    g, gmm = prod.gen_position_array(pos, offset, seed)
+    o, omm = OracleTree(root).positions(pos, offset, seed)
+    return g, gmm, o, omm
+
+
+def run_tileable(root, size, step, seed):
+    prod = to_product(root)
+    g, gmm = prod.gen_tileable_2d(size, step, seed)
+    o, omm = OracleTree(root).tileable(size[0], size[1], step[0], step[1], seed)
+    return g, gmm, o, omm
+
+
+def assert_parity(g, gmm, o, omm, label=""):
+    ok, maxerr, exact, nbad = close(g, o)
+    assert ok, f"{label}: {nbad} points beyond tolerance, max abs err {maxerr:.3e}, bit-exact {exact:.4f}"
+    assert minmax_equal(gmm, omm), f"{label}: minmax {gmm} != oracle {omm}"
+    return maxerr, exact

@@ -1,0 +1,39 @@
+"""Host-side tree compiler (CPU only): every tested tree flattens into a device program."""
+import pytest
+
+from oracle.tree import N, decode
+from tests import trees
+from tests.test_gpu_parity import COMPOSITE, SINGLE
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+@pytest.mark.parametrize("name", sorted({**SINGLE, **COMPOSITE}))
+def test_tree_compiles(native, name, dim):
+    prod = trees.to_product({**SINGLE, **COMPOSITE}[name]())
+    n_instr, n_regs = prod.compile_info(dim)
+    assert 1 <= n_instr and 1 <= n_regs <= 64
+
+
+def test_workload_trees_compile(native):
+    for make in trees.MIX_TREES:
+        for dim in (2, 3, 4):
+            trees.to_product(make()).compile_info(dim)
+    trees.to_product(decode(trees.DEMO_CAVES)).compile_info(3)
+
+
+def test_unsupported_nodes_report_compile_error(native):
+    node = native.Node.from_encoded(trees.DEMO_MOUNTAIN)
+    with pytest.raises(native.FastNoiseError) as e:
+        node.compile_info(2)
+    assert e.value.code == -2 and "DomainWarpSimplex" in e.value.message
+
+
+def test_missing_source_is_a_compile_error(native):
+    with pytest.raises(native.FastNoiseError):
+        native.Node.new("FractalFBm").compile_info(3)
+
+
+def test_octave_count_scales_program(native):
+    short = trees.to_product(N("FractalFBm", Source=N("Perlin"), Octaves=2)).compile_info(3)[0]
+    long = trees.to_product(N("FractalFBm", Source=N("Perlin"), Octaves=9)).compile_info(3)[0]
+    assert long > short

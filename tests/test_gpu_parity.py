@@ -1,0 +1,202 @@
+"""GPU parity: every node kind, dimensionality and batch driver against the CPU oracle.
+
+Runs through the reference-facing C-ABI (fnGenUniformGrid*/fnGenPositionArray*/
+fnGenTileable2D/fnGenSingle*) with host buffers, on seeded inputs small enough
+for the oracle to finish in seconds.
+"""
+import numpy as np
+import pytest
+
+from oracle.tree import N, decode
+from tests import trees
+from tests.parity import assert_parity, run_grid, run_positions, run_tileable
+
+pytestmark = pytest.mark.gpu
+
+GRID = {2: ((-7.5, 3.25), (37, 29), (1.5, 0.75)),
+        3: ((-7.5, 3.25, 11.0), (13, 11, 9), (1.5, 0.75, 1.25)),
+        4: ((-7.5, 3.25, 11.0, -2.0), (7, 6, 5, 4), (1.5, 0.75, 1.25, 2.0))}
+
+
+def noise(name, scale=3.7, **kw):
+    return N(name, Feature_Scale=scale, **kw)
+
+
+def cellular(name, df="Euclidean Squared", **kw):
+    n = N(name, Feature_Scale=3.1)
+    n.set("Distance Function", df)
+    for k, v in kw.items():
+        n.set(k.replace("_", " "), v)
+    return n
+
+
+SINGLE = {
+    "Constant": lambda: N("Constant", Value=0.625),
+    "White": lambda: N("White", Seed_Offset=3),
+    "Checkerboard": lambda: noise("Checkerboard", 2.5),
+    "SineWave": lambda: noise("SineWave", 5.0),
+    "Gradient": lambda: N("Gradient").set("Multiplier", 0.25, 0).set("Multiplier", -0.5, 1).set("Multiplier", 0.125, 2)
+                                    .set("Multiplier", 1.0, 3).set("Offset", 3.0, 0),
+    "DistanceToPoint": lambda: N("DistanceToPoint").set("Point", 1.5, 0).set("Point", -2.0, 1),
+    "Simplex": lambda: noise("Simplex"),
+    "SuperSimplex": lambda: noise("SuperSimplex"),
+    "Perlin": lambda: noise("Perlin"),
+    "Value": lambda: noise("Value"),
+    "SimplexRange": lambda: noise("Simplex", Seed_Offset=-17, Output_Min=0.2, Output_Max=3.5),
+    "CellularValue": lambda: cellular("CellularValue"),
+    "CellularValueIdx2": lambda: cellular("CellularValue", "Manhattan", Value_Index=2),
+    "CellularDistance": lambda: cellular("CellularDistance"),
+    "CellularDistanceSub": lambda: cellular("CellularDistance", "Euclidean", Return_Type="Index0Sub1"),
+    "CellularDistanceHybrid": lambda: cellular("CellularDistance", "Hybrid", Return_Type="Index0Add1", Distance_Index_1=2),
+    "CellularDistanceMax": lambda: cellular("CellularDistance", "Max Axis", Return_Type="Index0Mul1"),
+    "CellularDistanceDiv": lambda: cellular("CellularDistance", "Euclidean", Return_Type="Index0Div1", Distance_Index_0=1, Distance_Index_1=3),
+    "CellularDistanceMinkowski": lambda: cellular("CellularDistance", "Minkowski", Minkowski_P=1.7),
+    "CellularJitter": lambda: cellular("CellularDistance", Grid_Jitter=0.6, Size_Jitter=0.4),
+    "CellularLookup": lambda: N("CellularLookup", Feature_Scale=4.0, Lookup=noise("Perlin", 9.0)),
+}
+
+COMPOSITE = {
+    "FBm": lambda: N("FractalFBm", Source=noise("Simplex"), Octaves=4, Lacunarity=1.87, Gain=0.6, Weighted_Strength=0.3),
+    "Ridged": lambda: N("FractalRidged", Source=noise("Perlin"), Octaves=3, Weighted_Strength=0.7),
+    "FBmGainNode": lambda: N("FractalFBm", Source=noise("Value"), Gain=noise("Simplex", 20.0)),
+    "PingPong": lambda: N("PingPong", Source=noise("Simplex"), Ping_Pong_Strength=2.7),
+    "WarpGradient": lambda: N("DomainWarpGradient", Source=noise("Simplex"), Warp_Amplitude=4.0, Feature_Scale=6.0, Seed_Offset=5),
+    "WarpProgressive": lambda: N("DomainWarpFractalProgressive",
+                                 Domain_Warp_Source=N("DomainWarpGradient", Source=noise("Perlin"), Warp_Amplitude=3.0, Feature_Scale=7.0),
+                                 Octaves=3, Weighted_Strength=0.4),
+    "WarpIndependent": lambda: N("DomainWarpFractalIndependent",
+                                 Domain_Warp_Source=N("DomainWarpGradient", Source=noise("Value"), Warp_Amplitude=2.0, Feature_Scale=5.0),
+                                 Octaves=4, Gain=0.7),
+    "Add": lambda: N("Add", LHS=noise("Simplex"), RHS=noise("Perlin")),
+    "Subtract": lambda: N("Subtract", LHS=noise("Simplex"), RHS=0.25),
+    "Multiply": lambda: N("Multiply", LHS=noise("Simplex"), RHS=noise("Value")),
+    "Divide": lambda: N("Divide", LHS=noise("Simplex"), RHS=1.7),
+    "Modulus": lambda: N("Modulus", LHS=noise("Simplex", 9.0), RHS=0.3),
+    "Min": lambda: N("Min", LHS=noise("Simplex"), RHS=noise("Perlin")),
+    "Max": lambda: N("Max", LHS=noise("Simplex"), RHS=0.1),
+    "MinSmooth": lambda: N("MinSmooth", LHS=noise("Simplex"), RHS=noise("Perlin"), Smoothness=0.35),
+    "MaxSmooth": lambda: N("MaxSmooth", LHS=noise("Simplex"), RHS=noise("Value"), Smoothness=0.2),
+    "Abs": lambda: N("Abs", Source=noise("Simplex")),
+    "SignedSquareRoot": lambda: N("SignedSquareRoot", Source=noise("Perlin")),
+    "PowFloat": lambda: N("PowFloat", Value=noise("Simplex"), Pow=1.6),
+    "PowInt": lambda: N("PowInt", Value=noise("Simplex"), Pow=5),
+    "DomainScale": lambda: N("DomainScale", Source=noise("Simplex"), Scaling=1.37),
+    "DomainOffset": lambda: N("DomainOffset", Source=noise("Simplex")).set("Offset", 2.5, 0).set("Offset", noise("Perlin", 8.0), 1),
+    "DomainRotate": lambda: N("DomainRotate", Source=noise("Simplex"), Yaw=0.7, Pitch=0.3, Roll=-0.4),
+    "DomainRotateYaw": lambda: N("DomainRotate", Source=noise("Simplex"), Yaw=1.1),
+    "DomainAxisScale": lambda: N("DomainAxisScale", Source=noise("Simplex")).set("Scaling", 0.5, 0).set("Scaling", 2.0, 2),
+    "SeedOffset": lambda: N("SeedOffset", Source=noise("Simplex"), Seed_Offset=99),
+    "ConvertRGBA8": lambda: N("ConvertRGBA8", Source=noise("Simplex")),
+    "GeneratorCache": lambda: N("GeneratorCache", Source=noise("Simplex")),
+    "Fade": lambda: N("Fade", A=noise("Simplex"), B=noise("Perlin"), Fade=noise("Value", 11.0), Interpolation="Quintic"),
+    "FadeConst": lambda: N("Fade", A=noise("Simplex"), B=noise("Perlin"), Fade=0.25, Interpolation="Hermite"),
+    "Remap": lambda: N("Remap", Source=noise("Simplex"), From_Min=-0.5, To_Max=4.0, Clamp_Output="True"),
+    "Terrace": lambda: N("Terrace", Source=noise("Simplex"), Step_Count=5.0, Smoothness=0.45),
+    "TerraceDynamic": lambda: N("Terrace", Source=noise("Simplex"), Step_Count=3.0, Smoothness=noise("Perlin", 13.0)),
+    "AddDimension": lambda: N("AddDimension", Source=noise("Simplex"), New_Dimension_Position=noise("Value", 5.0)),
+    "RemoveDimension": lambda: N("RemoveDimension", Source=noise("Simplex"), Remove_Dimension="X"),
+    "DomainRotatePlane": lambda: N("DomainRotatePlane", Source=noise("Simplex"), Rotation_Type="Improve XZ Planes"),
+    "Terrain": trees.terrain_c2,
+}
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+@pytest.mark.parametrize("name", sorted(SINGLE))
+def test_single_node_grid(gpu, name, dim):
+    off, cnt, st = GRID[dim]
+    assert_parity(*run_grid(SINGLE[name](), off, cnt, st, 1337), label=f"{name}/{dim}D")
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+@pytest.mark.parametrize("name", sorted(COMPOSITE))
+def test_composite_grid(gpu, name, dim):
+    off, cnt, st = GRID[dim]
+    assert_parity(*run_grid(COMPOSITE[name](), off, cnt, st, -42), label=f"{name}/{dim}D")
+
+
+@pytest.mark.parametrize("seed", [0, 1337, -1, 2**31 - 1, -(2**31)])
+def test_seeds(gpu, seed):
+    assert_parity(*run_grid(COMPOSITE["Terrain"](), (0, 0, 0), (9, 8, 7), (3.0, 3.0, 3.0), seed), label=f"seed {seed}")
+
+
+def test_workload0_simplex_64cubed(gpu):
+    """Simplex, scale 50, 64^3 from the origin, seed 1337 (the reference's config-0 case)."""
+    assert_parity(*run_grid(trees.simplex_c0(), (0, 0, 0), (64, 64, 64), (1, 1, 1), 1337), label="c0")
+
+
+def test_workload1_fbm_perlin_reduced(gpu):
+    assert_parity(*run_grid(trees.fbm_perlin_c1(), (-128, -128, -128), (40, 36, 32), (1, 1, 1), 42), label="c1")
+
+
+def test_workload2_terrain_tileable_reduced(gpu):
+    assert_parity(*run_tileable(trees.terrain_c2(), (96, 80), (1.0, 1.0), 7), label="c2 tileable")
+
+
+def test_workload2_terrain_grid_reduced(gpu):
+    assert_parity(*run_grid(trees.terrain_c2(), (0, 0, 0), (24, 24, 24), (1, 1, 1), 7), label="c2 3D")
+
+
+def test_demo_caves_tree(gpu):
+    root = decode(trees.DEMO_CAVES)
+    assert_parity(*run_grid(root, (-40, 12, 5), (48, 40, 12), (1, 1, 1), 1337), label="caves")
+
+
+def test_demo_mountain_tree_needs_domain_warp_simplex(gpu):
+    """DomainWarpSimplex has no GPU kernel yet: the call must fail loudly, never fall back to the CPU."""
+    import fastnoise2_gb300 as fn
+    node = fn.Node.from_encoded(trees.DEMO_MOUNTAIN)
+    with pytest.raises(fn.FastNoiseError) as e:
+        node.gen_uniform_grid((0, 0), (8, 8), (1, 1), 1)
+    assert e.value.code == -2
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+def test_position_arrays(gpu, dim):
+    rng = np.random.default_rng(20261203 + dim)
+    count = 3001
+    pos = [rng.uniform(-1e4, 1e4, count).astype(np.float32) for _ in range(dim)]
+    off = [0.5, -3.0, 7.25, 1.0][:dim]
+    assert_parity(*run_positions(COMPOSITE["FBm"](), pos, off, 77), label=f"positions {dim}D")
+
+
+def test_position_array_matches_grid(gpu):
+    """GenPositionArray3D over the grid's own positions reproduces GenUniformGrid3D."""
+    from tests.trees import to_product
+    root = trees.fbm_perlin_c1()
+    prod = to_product(root)
+    g, gmm = prod.gen_uniform_grid((0, 0, 0), (16, 8, 4), (1, 1, 1), 5)
+    z, y, x = np.meshgrid(np.arange(4), np.arange(8), np.arange(16), indexing="ij")
+    p, pmm = prod.gen_position_array([x.ravel().astype(np.float32), y.ravel().astype(np.float32),
+                                      z.ravel().astype(np.float32)], (0, 0, 0), 5)
+    assert np.array_equal(g.view(np.uint32), p.view(np.uint32))
+    assert gmm == pmm
+
+
+def test_single_matches_grid(gpu):
+    from tests.trees import to_product
+    prod = to_product(trees.terrain_c2())
+    g, _ = prod.gen_uniform_grid((3, 4, 5), (4, 3, 2), (1, 1, 1), 7)
+    idx = 1 * 12 + 2 * 4 + 3        # z=1, y=2, x=3
+    assert prod.gen_single((6.0, 6.0, 6.0), 7) == g[idx]
+
+
+@pytest.mark.parametrize("cnt", [(1, 1), (1, 7), (33, 1), (257, 3), (0, 5)])
+def test_ragged_and_empty_2d(gpu, cnt):
+    g, gmm, o, omm = run_grid(N("Simplex", Feature_Scale=2.0), (0.5, 0.25), cnt, (1, 1), 3)
+    if cnt[0] * cnt[1] == 0:
+        assert g.size == 0 and gmm == (float("inf"), float("-inf"))
+    else:
+        assert_parity(g, gmm, o, omm, label=str(cnt))
+
+
+def test_large_coordinates(gpu):
+    assert_parity(*run_grid(COMPOSITE["Terrain"](), (-1.0e6, 2.5e6, 7.0e5), (9, 9, 9), (97.0, 31.0, 11.0), 11), label="far")
+
+
+def test_unfused_oracle_mode_is_close(gpu):
+    """The scalar-build (unfused) reading of FS::FMulAdd stays within the tolerance of the fused one."""
+    from oracle.oracle import OracleTree
+    root = trees.fbm_perlin_c1()
+    a, _ = OracleTree(root).grid((0, 0, 0), (16, 16, 16), (1, 1, 1), 42)
+    b, _ = OracleTree(root, unfused=True).grid((0, 0, 0), (16, 16, 16), (1, 1, 1), 42)
+    assert np.max(np.abs(a - b)) < 1e-5
