@@ -62,7 +62,7 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
         if ((size_t)total > ctx->dpos_cap) {
             for (float*& p : ctx->dpos) { if (p) cudaFree(p); p = nullptr; }
             ctx->dpos_cap = 0;
-            for (int k = 0; k < args.dim; ++k)
+            for (int k = 0; k < 4; ++k)      // all four axes, so any dimensionality fits
                 if (!cuda_ok(cudaMalloc(&ctx->dpos[k], (size_t)total * 4), "cudaMalloc(positions)")) { fill_nan(out, total, minmax); return; }
             ctx->dpos_cap = (size_t)total;
         }

@@ -49,7 +49,11 @@ typedef int32_t i32;
 #define OC_TICK(n) ((void)0)
 #endif
 
+#ifdef __cplusplus
+#define OC_EXPORT extern "C" __attribute__((visibility("default")))
+#else
 #define OC_EXPORT __attribute__((visibility("default")))
+#endif
 
 /* ------------------------------------------------------------------------- */
 /* FS-level primitives                                                        */
@@ -1729,7 +1733,7 @@ static f32 eval_node(const on_node* n, i32 seed, int dim, const f32* p)
     }
     case N_SIGNEDSQRT: {
         f32 v = gen_n(n->lookup[0], seed, dim, p);
-        return bits_f(f_bits(fs_sqrt(fs_abs(v))) | (f_bits(v) & 0x80000000u));
+        return bits_f(f_bits((float)fs_sqrt(fs_abs(v))) | (f_bits((float)v) & 0x80000000u));
     }
     case N_POWFLOAT: {
         f32 v = fs_max(fs_abs(hyb_n(n, 0, seed, dim, p)), FLT_MIN);

@@ -26,7 +26,11 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libfn_oracle.so")
 SRC = os.path.join(HERE, "fn_oracle.c")
 
+LIB_COUNT = os.path.join(BUILD, "libfn_oracle_count.so")
+OPCOUNT_H = os.path.join(HERE, "opcount.h")
+
 _lib = None
+_lib_count = None
 
 
 def build(force: bool = False) -> str:
@@ -41,6 +45,60 @@ def build(force: bool = False) -> str:
     subprocess.run(["gcc", *flags, "-o", tmp, SRC, "-lm", "-lpthread"], check=True)
     os.replace(tmp, LIB)
     return LIB
+
+
+def build_count(force: bool = False) -> str:
+    """Compile the oracle as C++ with the counting scalar type (opcount.h)."""
+    os.makedirs(BUILD, exist_ok=True)
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(OPCOUNT_H))
+    if not force and os.path.exists(LIB_COUNT) and os.path.getmtime(LIB_COUNT) >= newest:
+        return LIB_COUNT
+    tmp = LIB_COUNT + f".tmp{os.getpid()}"
+    subprocess.run(["g++", "-x", "c++", "-std=c++17", "-O2", "-DOC_COUNT", f"-I{HERE}", "-ffp-contract=off",
+                    "-fPIC", "-shared", "-fvisibility=hidden", "-o", tmp, SRC, "-lm", "-lpthread"], check=True)
+    os.replace(tmp, LIB_COUNT)
+    return LIB_COUNT
+
+
+def count_ops(root: Node, points: np.ndarray, seed: int) -> float:
+    """Mean FS-level operations per point of `root` over the rows of `points` (n x dim)."""
+    global _lib_count
+    if _lib_count is None:
+        build_count()
+        L = ctypes.CDLL(LIB_COUNT)
+        L.on_new.restype = ctypes.c_void_p
+        L.on_new.argtypes = [ctypes.c_int]
+        L.on_set_var.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int32]
+        L.on_set_lookup.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.on_set_hybrid_node.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.on_set_hybrid_float.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_float]
+        L.on_free.argtypes = [ctypes.c_void_p]
+        L.on_count_ops.restype = ctypes.c_double
+        L.on_count_ops.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+        _lib_count = L
+    L = _lib_count
+    handles = {}
+    for node in walk(root):
+        h = L.on_new(node.meta.id)
+        handles[id(node)] = h
+        for kind, idx, arg in node.ops:
+            if kind == "var":
+                L.on_set_var(h, idx, int(arg))
+            elif kind == "lookup":
+                L.on_set_lookup(h, idx, handles[id(arg)])
+            elif kind == "hnode":
+                L.on_set_hybrid_node(h, idx, handles[id(arg)])
+            else:
+                L.on_set_hybrid_float(h, idx, float(arg))
+    pts = np.ascontiguousarray(points, np.float32)
+    total = 0.0
+    for row in pts:
+        p = np.zeros(4, np.float32)
+        p[:len(row)] = row
+        total += L.on_count_ops(handles[id(root)], len(row), _fptr(p), int(np.int32(seed)))
+    for h in handles.values():
+        L.on_free(h)
+    return total / max(len(pts), 1)
 
 
 def lib():
