@@ -104,6 +104,10 @@ def _declare(L):
         "fnGenPositionArray3DDevice": (c_int, [vp, vp, c_int, vp, vp, vp, c_float, c_float, c_float, c_int, vp, vp]),
         "fnGenPositionArray4DDevice": (c_int, [vp, vp, c_int, vp, vp, vp, vp, c_float, c_float, c_float, c_float, c_int, vp, vp]),
         "fnGenTileable2DDevice": (c_int, [vp, vp, c_int, c_int, c_float, c_float, c_int, vp, vp]),
+        "fnGenBatchDevice": (c_int, [vp, c_int, vp, c_int]),
+        "fnAutotuneBatch": (c_int, [vp, c_int, vp]),
+        "fnAutotuneLoad": (c_int, [cp]),
+        "fnAutotuneSave": (c_int, [cp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -132,6 +136,48 @@ def _check():
 
 def _fp(a: np.ndarray):
     return a.ctypes.data_as(_FP)
+
+
+KIND_GRID2D, KIND_GRID3D, KIND_GRID4D, KIND_TILEABLE2D, KIND_POSITIONS2D, KIND_POSITIONS3D, KIND_POSITIONS4D = range(7)
+BATCH_SYNC, BATCH_NO_GRAPH = 1, 2
+
+
+class GenRequest(ctypes.Structure):
+    """fnGenRequest: one request of a batched launch (include/FastNoise/FastNoise_C.h)."""
+    _fields_ = [("node", ctypes.c_void_p), ("kind", ctypes.c_int), ("seed", ctypes.c_int),
+                ("count", ctypes.c_int * 4), ("offset", ctypes.c_float * 4), ("step", ctypes.c_float * 4),
+                ("positions", ctypes.c_void_p * 4), ("out", ctypes.c_void_p), ("minMax", ctypes.POINTER(ctypes.c_float))]
+
+
+def make_request(node: "Node", kind: int, out_ptr: int, seed: int, count=(0, 0, 0, 0), offset=(0, 0, 0, 0),
+                 step=(1, 1, 1, 1), positions=(0, 0, 0, 0), minmax: Optional[np.ndarray] = None) -> GenRequest:
+    r = GenRequest()
+    r.node = node.handle
+    r.kind = kind
+    r.seed = int(np.int32(seed))
+    for k in range(4):
+        r.count[k] = int(count[k]) if k < len(count) else 0
+        r.offset[k] = float(offset[k]) if k < len(offset) else 0.0
+        r.step[k] = float(step[k]) if k < len(step) else 0.0
+        r.positions[k] = int(positions[k]) if k < len(positions) and positions[k] else None
+    r.out = out_ptr
+    if minmax is not None:
+        r.minMax = minmax.ctypes.data_as(_FP)
+    return r
+
+
+def gen_batch(requests, stream: int = 0, sync: bool = True, graph: bool = True) -> None:
+    """fnGenBatchDevice over a sequence of GenRequest."""
+    arr = (GenRequest * len(requests))(*requests)
+    flags = (BATCH_SYNC if sync else 0) | (0 if graph else BATCH_NO_GRAPH)
+    if lib().fnGenBatchDevice(arr, len(requests), stream or None, flags) != 0:
+        _check()
+
+
+def autotune_batch(requests, stream: int = 0) -> None:
+    arr = (GenRequest * len(requests))(*requests)
+    if lib().fnAutotuneBatch(arr, len(requests), stream or None) != 0:
+        _check()
 
 
 def metadata_count() -> int:

@@ -1,0 +1,242 @@
+// fn_batch.cpp -- descriptor staging, graph capture and autotuning for the
+// batched persistent launch (kernel in fn_kernels.cu).
+#include "fn_batch.h"
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+
+namespace fn {
+
+namespace {
+size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+}  // namespace
+
+uint32_t tiles_for(long long total, uint32_t tile_points)
+{
+    if (total <= 0) return 1;                      // one empty tile still finalises min/max
+    return (uint32_t)((total + tile_points - 1) / tile_points);
+}
+
+uint64_t batch_signature(const std::vector<BatchItem>& items, const std::vector<DeviceProgram>& progs)
+{
+    // multiset of (program, size class): independent of request order and of node addresses
+    std::vector<uint64_t> keys;
+    keys.reserve(items.size());
+    for (size_t i = 0; i < items.size(); ++i) {
+        int lg = 0;
+        while ((1ll << lg) < items[i].args.total && lg < 62) ++lg;
+        keys.push_back(progs[i].hash * 0x9E3779B97F4A7C15ull ^ ((uint64_t)items[i].args.src << 60) ^ ((uint64_t)lg << 48));
+    }
+    std::sort(keys.begin(), keys.end());
+    return fnv1a64(keys.data(), keys.size() * sizeof(uint64_t));
+}
+
+BatchRunner::BatchRunner() {}
+
+BatchRunner::~BatchRunner()
+{
+    if (exec_) cudaGraphExecDestroy(exec_);
+    if (graph_) cudaGraphDestroy(graph_);
+    if (staged_) cudaEventDestroy(staged_);
+    if (capture_stream_) cudaStreamDestroy(capture_stream_);
+    if (d_buf_) cudaFree(d_buf_);
+    if (h_buf_) cudaFreeHost(h_buf_);
+}
+
+bool BatchRunner::reserve(size_t n_req, size_t n_items)
+{
+    if (n_req <= cap_req_ && n_items <= cap_items_) return true;
+    size_t req = std::max(n_req, std::max<size_t>(cap_req_ * 2, 64));
+    size_t items = std::max(n_items, std::max<size_t>(cap_items_ * 2, 4096));
+    size_t off_req = align_up(sizeof(BatchHeader), 256);
+    size_t off_state = align_up(off_req + req * sizeof(BatchRequest), 256);
+    size_t off_items = align_up(off_state + req * sizeof(BatchState), 256);
+    size_t bytes = align_up(off_items + items * sizeof(uint2), 256);
+    char* d = nullptr;
+    char* h = nullptr;
+    if (!cuda_ok(cudaMalloc(&d, bytes), "cudaMalloc(batch descriptors)")) return false;
+    if (!cuda_ok(cudaMallocHost(&h, bytes), "cudaMallocHost(batch staging)")) { cudaFree(d); return false; }
+    if (d_buf_) cudaFree(d_buf_);
+    if (h_buf_) cudaFreeHost(h_buf_);
+    d_buf_ = d; h_buf_ = h;
+    cap_req_ = req; cap_items_ = items; cap_bytes_ = bytes;
+    off_req_ = off_req; off_state_ = off_state; off_items_ = off_items;
+    d_states_ = reinterpret_cast<BatchState*>(d_buf_ + off_state_);
+    if (exec_) { cudaGraphExecDestroy(exec_); exec_ = nullptr; }   // kernel arguments changed: recapture
+    if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
+    return true;
+}
+
+int BatchRunner::launch_graph(cudaStream_t stream, size_t bytes, int grid, uint32_t smem)
+{
+    auto* hdr = reinterpret_cast<BatchHeader*>(d_buf_);
+    auto* reqs = reinterpret_cast<BatchRequest*>(d_buf_ + off_req_);
+    auto* items = reinterpret_cast<uint2*>(d_buf_ + off_items_);
+    if (!exec_) {
+        if (!capture_stream_ && !cuda_ok(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking), "stream")) return -3;
+        if (!cuda_ok(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal), "begin capture")) return -3;
+        cudaMemcpyAsync(d_buf_, h_buf_, bytes, cudaMemcpyHostToDevice, capture_stream_);
+        launch_batch(hdr, reqs, d_states_, items, smem, grid, 256, capture_stream_);
+        if (!cuda_ok(cudaStreamEndCapture(capture_stream_, &graph_), "end capture")) return -3;
+        if (!cuda_ok(cudaGraphInstantiate(&exec_, graph_, 0), "graph instantiate")) return -3;
+        size_t n = 0;
+        cudaGraphGetNodes(graph_, nullptr, &n);
+        std::vector<cudaGraphNode_t> nodes(n);
+        cudaGraphGetNodes(graph_, nodes.data(), &n);
+        for (auto nd : nodes) {
+            cudaGraphNodeType t;
+            cudaGraphNodeGetType(nd, &t);
+            if (t == cudaGraphNodeTypeMemcpy) copy_node_ = nd;
+            if (t == cudaGraphNodeTypeKernel) kernel_node_ = nd;
+        }
+        if (!copy_node_ || !kernel_node_) { set_error(-3, "unexpected graph shape"); return -3; }
+    } else {
+        if (!cuda_ok(cudaGraphExecMemcpyNodeSetParams1D(exec_, copy_node_, d_buf_, h_buf_, bytes, cudaMemcpyHostToDevice), "graph memcpy update"))
+            return -3;
+        cudaKernelNodeParams kp;
+        if (!cuda_ok(cudaGraphKernelNodeGetParams(kernel_node_, &kp), "graph kernel params")) return -3;
+        kp.gridDim = dim3((unsigned)grid);
+        kp.sharedMemBytes = smem;
+        if (!cuda_ok(cudaGraphExecKernelNodeSetParams(exec_, kernel_node_, &kp), "graph kernel update")) return -3;
+    }
+    return cuda_ok(cudaGraphLaunch(exec_, stream), "graph launch") ? 0 : -3;
+}
+
+int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream, const BatchTuning* tuning_in, bool use_graph)
+{
+    const size_t n = items.size();
+    if (n == 0) return 0;
+    std::vector<DeviceProgram> progs(n);
+    uint32_t max_bytes = 16;
+    points_ = 0;
+    for (size_t i = 0; i < n; ++i) {
+        if (!items[i].node || items[i].args.total < 0 || (items[i].args.total > 0 && !items[i].dout)) {
+            set_error(-1, "batch request " + std::to_string(i) + ": invalid arguments");
+            return -1;
+        }
+        if (!get_program(items[i].node, items[i].args.dim, progs[i])) return last_error();
+        max_bytes = std::max(max_bytes, progs[i].bytes);
+        points_ += (uint64_t)std::max(0ll, items[i].args.total);
+    }
+    signature_ = batch_signature(items, progs);
+    BatchTuning tuning;
+    if (tuning_in) tuning = *tuning_in;
+    else Autotuner::instance().lookup(signature_, tuning);
+    const uint32_t tp = std::max<uint32_t>(256, tuning.tile_points);
+    size_t n_items = 0;
+    for (size_t i = 0; i < n; ++i) n_items += tiles_for(items[i].args.total, tp);
+    if (n_items > 0xFFFFFFFFull) { set_error(-4, "batch too large"); return -4; }
+    if (!reserve(n, n_items)) return -3;
+
+    // The staging buffer is reused: the previous launch's upload must have been consumed.
+    if (!staged_ && !cuda_ok(cudaEventCreateWithFlags(&staged_, cudaEventDisableTiming), "event")) return -3;
+    cudaEventSynchronize(staged_);
+
+    auto* hdr = reinterpret_cast<BatchHeader*>(h_buf_);
+    auto* reqs = reinterpret_cast<BatchRequest*>(h_buf_ + off_req_);
+    auto* states = reinterpret_cast<BatchState*>(h_buf_ + off_state_);
+    auto* its = reinterpret_cast<uint2*>(h_buf_ + off_items_);
+    std::memset(hdr, 0, sizeof(BatchHeader));
+    hdr->n_req = (unsigned)n;
+    hdr->n_items = (unsigned)n_items;
+    hdr->tile_points = tp;
+    hdr->max_prog_bytes = max_bytes;
+    size_t k = 0;
+    last_minmax_.resize(n);
+    for (size_t i = 0; i < n; ++i) {
+        BatchRequest& r = reqs[i];
+        std::memset(&r, 0, sizeof r);
+        r.args = items[i].args;
+        r.prog = progs[i].dptr;
+        r.prog_bytes = progs[i].bytes;
+        r.out = items[i].dout;
+        r.minmax = items[i].dminmax;
+        r.host_minmax = items[i].host_minmax;
+        r.host_done = items[i].host_done;
+        r.n_tiles = tiles_for(items[i].args.total, tp);
+        states[i].mn_enc = 0xFFFFFFFFu;
+        states[i].mx_enc = 0u;
+        states[i].tiles_done = 0u;
+        states[i].pad = 0u;
+        for (uint32_t t = 0; t < r.n_tiles; ++t) its[k++] = make_uint2((unsigned)i, t);
+        last_minmax_[i] = items[i].dminmax;
+    }
+    const size_t bytes = off_items_ + n_items * sizeof(uint2);
+    const int occ = tuning.ctas_per_sm > 0 ? tuning.ctas_per_sm : batch_occupancy(256, max_bytes);
+    long long grid = (long long)num_sms() * occ;
+    if (grid > (long long)n_items) grid = (long long)n_items;
+    if (grid < 1) grid = 1;
+    int rc;
+    if (use_graph) {
+        rc = launch_graph(stream, bytes, (int)grid, max_bytes);
+    } else {
+        rc = cuda_ok(cudaMemcpyAsync(d_buf_, h_buf_, bytes, cudaMemcpyHostToDevice, stream), "upload batch") &&
+                     cuda_ok(launch_batch(reinterpret_cast<BatchHeader*>(d_buf_), reinterpret_cast<BatchRequest*>(d_buf_ + off_req_),
+                                          d_states_, reinterpret_cast<uint2*>(d_buf_ + off_items_), max_bytes, (int)grid, 256, stream),
+                             "launch batch")
+                 ? 0
+                 : -3;
+    }
+    if (rc == 0) cudaEventRecord(staged_, stream);
+    return rc;
+}
+
+// ------------------------------------------------------------------ autotuner
+
+Autotuner& Autotuner::instance()
+{
+    static Autotuner a;
+    return a;
+}
+
+bool Autotuner::lookup(uint64_t sig, BatchTuning& out)
+{
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = table_.find(sig);
+    if (it == table_.end()) return false;
+    out = it->second.first;
+    return true;
+}
+
+void Autotuner::store(uint64_t sig, const BatchTuning& t, double ms)
+{
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = table_.find(sig);
+    if (it == table_.end() || ms < it->second.second) table_[sig] = {t, ms};
+}
+
+std::vector<BatchTuning> Autotuner::candidates() const
+{
+    std::vector<BatchTuning> c;
+    for (uint32_t tp : {1024u, 2048u, 4096u, 8192u})
+        for (int ctas : {0, 1}) c.push_back(BatchTuning{tp, ctas});
+    return c;
+}
+
+bool Autotuner::load(const std::string& path)
+{
+    std::ifstream f(path);
+    if (!f) return false;
+    std::lock_guard<std::mutex> lk(mu_);
+    unsigned long long sig;
+    unsigned tp;
+    int ctas;
+    double ms;
+    while (f >> std::hex >> sig >> std::dec >> tp >> ctas >> ms) table_[sig] = {BatchTuning{tp, ctas}, ms};
+    return true;
+}
+
+bool Autotuner::save(const std::string& path) const
+{
+    std::ofstream f(path);
+    if (!f) return false;
+    for (const auto& kv : table_)
+        f << std::hex << kv.first << std::dec << ' ' << kv.second.first.tile_points << ' ' << kv.second.first.ctas_per_sm << ' '
+          << kv.second.second << '\n';
+    return true;
+}
+
+}  // namespace fn

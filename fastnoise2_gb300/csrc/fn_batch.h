@@ -1,0 +1,87 @@
+// fn_batch.h -- many generation requests in one persistent launch.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "fn_kernels.cuh"
+#include "fn_runtime.h"
+
+namespace fn {
+
+struct BatchItem {
+    const Node* node = nullptr;
+    PointArgs args{};
+    float* dout = nullptr;
+    float* dminmax = nullptr;          // device float[2] or null
+    float* host_minmax = nullptr;      // mapped pinned float[2] or null
+    unsigned int* host_done = nullptr; // mapped pinned completion flag or null
+};
+
+struct BatchTuning {
+    uint32_t tile_points = 2048;
+    int ctas_per_sm = 0;               // 0 = occupancy limit
+};
+
+// Owns the device/pinned descriptor buffers and a captured graph; not thread safe
+// (one runner per host thread or per server stream).
+class BatchRunner {
+public:
+    BatchRunner();
+    ~BatchRunner();
+    BatchRunner(const BatchRunner&) = delete;
+    BatchRunner& operator=(const BatchRunner&) = delete;
+
+    // Resolve programs, build descriptors and queue one launch on `stream`.
+    // Returns FN_OK or a negative status (set_error has the message).
+    // `tuning` null = the autotuner's choice for this batch signature, else defaults.
+    int launch(const std::vector<BatchItem>& items, cudaStream_t stream, const BatchTuning* tuning, bool use_graph);
+
+    // Device copy of the last launch's per-request state (for min/max read-back).
+    BatchState* device_states() const { return d_states_; }
+    const std::vector<float*>& last_device_minmax() const { return last_minmax_; }
+    uint64_t last_signature() const { return signature_; }
+    uint64_t last_points() const { return points_; }
+
+private:
+    bool reserve(size_t n_req, size_t n_items);
+    int launch_graph(cudaStream_t stream, size_t bytes, int grid, uint32_t smem);
+
+    char* d_buf_ = nullptr;            // device: header | reqs | states | items
+    char* h_buf_ = nullptr;            // pinned staging with the same layout
+    size_t cap_req_ = 0, cap_items_ = 0, cap_bytes_ = 0;
+    size_t off_req_ = 0, off_state_ = 0, off_items_ = 0;
+    BatchState* d_states_ = nullptr;
+    cudaStream_t capture_stream_ = nullptr;
+    cudaEvent_t staged_ = nullptr;      // recorded after each upload: guards reuse of h_buf_
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    cudaGraphNode_t copy_node_ = nullptr, kernel_node_ = nullptr;
+    std::vector<float*> last_minmax_;
+    uint64_t signature_ = 0;
+    uint64_t points_ = 0;
+};
+
+// Tuning cache keyed by a batch signature (program hashes and size classes).
+class Autotuner {
+public:
+    static Autotuner& instance();
+    bool lookup(uint64_t signature, BatchTuning& out);
+    void store(uint64_t signature, const BatchTuning& t, double ms);
+    std::vector<BatchTuning> candidates() const;
+    bool load(const std::string& path);
+    bool save(const std::string& path) const;
+
+private:
+    std::mutex mu_;
+    std::map<uint64_t, std::pair<BatchTuning, double>> table_;
+};
+
+uint64_t batch_signature(const std::vector<BatchItem>& items, const std::vector<DeviceProgram>& progs);
+uint32_t tiles_for(long long total, uint32_t tile_points);
+
+}  // namespace fn

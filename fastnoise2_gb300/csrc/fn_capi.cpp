@@ -11,6 +11,7 @@
 #include <string>
 
 #include "../../include/FastNoise/FastNoise_C.h"
+#include "fn_batch.h"
 #include "fn_runtime.h"
 
 using namespace fn;
@@ -159,6 +160,100 @@ float gen_single(const void* node, int dim, const float* p, int seed)
 }
 
 const NodeMeta* M(int id) { return meta_by_id(id); }
+
+// ------------------------------------------------------------------ batches
+
+bool request_args(const fnGenRequest& r, PointArgs& a)
+{
+    switch (r.kind) {
+    case FN_KIND_GRID2D: case FN_KIND_GRID3D: case FN_KIND_GRID4D:
+        a = grid_args(2 + (r.kind - FN_KIND_GRID2D), r.offset, r.count, r.step, r.seed);
+        return true;
+    case FN_KIND_TILEABLE2D:
+        a = tile_args(r.count[0], r.count[1], r.step[0], r.step[1], r.seed);
+        return true;
+    case FN_KIND_POSITIONS2D: case FN_KIND_POSITIONS3D: case FN_KIND_POSITIONS4D: {
+        const int dim = 2 + (r.kind - FN_KIND_POSITIONS2D);
+        a = pos_args(dim, r.count[0], r.offset, r.seed);
+        for (int k = 0; k < dim; ++k) {
+            if (a.total > 0 && !r.positions[k]) return false;
+            a.pos[k] = r.positions[k];
+        }
+        return true;
+    }
+    default:
+        return false;
+    }
+}
+
+struct BatchCtx {
+    BatchRunner runner;
+    float* dminmax = nullptr;
+    float* hminmax = nullptr;
+    size_t cap = 0;
+    ~BatchCtx()
+    {
+        if (dminmax) cudaFree(dminmax);
+        if (hminmax) cudaFreeHost(hminmax);
+    }
+};
+thread_local BatchCtx* t_batch = nullptr;
+
+BatchCtx* batch_ctx(size_t n)
+{
+    if (!t_batch) t_batch = new BatchCtx();
+    BatchCtx* b = t_batch;
+    if (n > b->cap) {
+        if (b->dminmax) cudaFree(b->dminmax);
+        if (b->hminmax) cudaFreeHost(b->hminmax);
+        b->dminmax = nullptr; b->hminmax = nullptr; b->cap = 0;
+        size_t want = n < 256 ? 256 : n;
+        if (!cuda_ok(cudaMalloc(&b->dminmax, want * 2 * sizeof(float)), "cudaMalloc(batch minmax)") ||
+            !cuda_ok(cudaMallocHost(&b->hminmax, want * 2 * sizeof(float)), "cudaMallocHost(batch minmax)"))
+            return nullptr;
+        b->cap = want;
+    }
+    return b;
+}
+
+int build_items(const fnGenRequest* reqs, int n, BatchCtx* b, std::vector<BatchItem>& items)
+{
+    items.resize((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        BatchItem& it = items[(size_t)i];
+        it.node = N(reqs[i].node);
+        if (!it.node || !request_args(reqs[i], it.args)) {
+            set_error(FN_ERR_ARG, "batch request " + std::to_string(i) + ": invalid node, kind or positions");
+            return FN_ERR_ARG;
+        }
+        it.dout = reqs[i].out;
+        it.dminmax = b->dminmax + 2 * i;
+    }
+    return FN_OK;
+}
+
+int run_batch(const fnGenRequest* reqs, int n, void* stream, int flags, const BatchTuning* tuning)
+{
+    if (n < 0 || (n > 0 && !reqs)) { set_error(FN_ERR_ARG, "invalid request list"); return FN_ERR_ARG; }
+    if (n == 0) return FN_OK;
+    if (!thread_ctx()) return FN_ERR_CUDA;
+    BatchCtx* b = batch_ctx((size_t)n);
+    if (!b) return FN_ERR_CUDA;
+    std::vector<BatchItem> items;
+    int rc = build_items(reqs, n, b, items);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    rc = b->runner.launch(items, s, tuning, !(flags & FN_BATCH_NO_GRAPH));
+    if (rc) return rc;
+    if (flags & FN_BATCH_SYNC) {
+        if (!cuda_ok(cudaMemcpyAsync(b->hminmax, b->dminmax, (size_t)n * 2 * sizeof(float), cudaMemcpyDeviceToHost, s), "copy minmax") ||
+            !cuda_ok(cudaStreamSynchronize(s), "synchronize"))
+            return FN_ERR_CUDA;
+        for (int i = 0; i < n; ++i)
+            if (reqs[i].minMax) { reqs[i].minMax[0] = b->hminmax[2 * i]; reqs[i].minMax[1] = b->hminmax[2 * i + 1]; }
+    }
+    return FN_OK;
+}
 
 }  // namespace
 
@@ -462,6 +557,43 @@ int fnSerialiseNodeTree(const void* node, char* buffer, int bufferSize)
     if (buffer && bufferSize > (int)s.size()) std::memcpy(buffer, s.c_str(), s.size() + 1);
     return (int)s.size();
 }
+
+int fnGenBatchDevice(const fnGenRequest* requests, int count, void* stream, int flags)
+{
+    clear_error();
+    return run_batch(requests, count, stream, flags, nullptr);
+}
+
+int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream)
+{
+    clear_error();
+    if (count <= 0 || !requests) return FN_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaEvent_t e0, e1;
+    if (!cuda_ok(cudaEventCreate(&e0), "event") || !cuda_ok(cudaEventCreate(&e1), "event")) return FN_ERR_CUDA;
+    BatchTuning best;
+    double best_ms = 1e30;
+    uint64_t sig = 0;
+    for (const BatchTuning& t : Autotuner::instance().candidates()) {
+        int rc = run_batch(requests, count, stream, 0, &t);            // warm (first use compiles/captures)
+        if (rc) return rc;
+        cudaEventRecord(e0, s);
+        for (int rep = 0; rep < 2 && rc == 0; ++rep) rc = run_batch(requests, count, stream, 0, &t);
+        cudaEventRecord(e1, s);
+        if (rc || !cuda_ok(cudaEventSynchronize(e1), "synchronize")) return rc ? rc : FN_ERR_CUDA;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        sig = t_batch->runner.last_signature();
+        if (ms < best_ms) { best_ms = ms; best = t; }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    Autotuner::instance().store(sig, best, best_ms / 2);
+    return FN_OK;
+}
+
+int fnAutotuneLoad(const char* path) { return path && Autotuner::instance().load(path) ? FN_OK : FN_ERR_ARG; }
+int fnAutotuneSave(const char* path) { return path && Autotuner::instance().save(path) ? FN_OK : FN_ERR_ARG; }
 
 int fnCompileInfo(const void* node, int dimension, int* nInstr, int* nRegs)
 {

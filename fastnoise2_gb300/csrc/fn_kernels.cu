@@ -387,7 +387,126 @@ __global__ void __launch_bounds__(kThreads) interp_kernel(const FnProgramHeader*
 
 int g_num_sms = 0;
 
+// Order-preserving float <-> uint encoding for atomicMin/atomicMax.
+__device__ __forceinline__ unsigned int enc_ordered(float f)
+{
+    const unsigned int b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float dec_ordered(unsigned int u)
+{
+    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+constexpr int kBatchThreads = 256;
+
+__global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchHeader* hdr, const BatchRequest* __restrict__ reqs,
+                                                              BatchState* states, const uint2* __restrict__ items)
+{
+    extern __shared__ uint4 sprog[];
+    __shared__ unsigned int s_item;
+    __shared__ float smn[kBatchThreads / 32], smx[kBatchThreads / 32];
+    const FnProgramHeader* loaded = nullptr;
+    const unsigned int n_items = hdr->n_items;
+    const unsigned int tile_points = hdr->tile_points;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&hdr->head, 1u);
+        __syncthreads();
+        const unsigned int it = s_item;
+        if (it >= n_items) break;
+        const uint2 item = items[it];
+        const BatchRequest& rq = reqs[item.x];
+        const FnProgramHeader* gprog = rq.prog;
+        if (gprog != loaded) {                               // stage this request's program
+            const uint4* src = reinterpret_cast<const uint4*>(gprog);
+            for (uint32_t w = threadIdx.x; w < rq.prog_bytes / 16; w += blockDim.x) sprog[w] = src[w];
+            loaded = gprog;
+        }
+        __syncthreads();
+        const FnProgramHeader* h = reinterpret_cast<const FnProgramHeader*>(sprog);
+        const FnInstr* ins = fn_program_instrs(h);
+        const float* P = fn_program_params(h);
+        const PointArgs args = rq.args;
+        const long long begin = (long long)item.y * tile_points;
+        long long end = begin + tile_points;
+        if (end > args.total) end = args.total;
+
+        float mn = kInf, mx = -kInf;
+        float R[FN_MAX_REGS];
+        for (long long i = begin + threadIdx.x; i < end; i += blockDim.x) {
+            root_position(args, i, R);
+            exec_program(ins, h->n_instr, P, R, args.seed);
+            const float v = R[h->out_reg];
+            rq.out[i] = v;
+            mn = v < mn ? v : mn;
+            mx = mx < v ? v : mx;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fmin_(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = fmax_(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        }
+        if (lane == 0) { smn[warp] = mn; smx[warp] = mx; }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            for (int w = 1; w < kBatchThreads / 32; ++w) { mn = fmin_(mn, smn[w]); mx = fmax_(mx, smx[w]); }
+            BatchState* st = states + item.x;
+            if (mn <= mx) {                                  // tile had at least one non-NaN value
+                atomicMin(&st->mn_enc, enc_ordered(mn));
+                atomicMax(&st->mx_enc, enc_ordered(mx));
+            }
+            __threadfence();
+            const unsigned int done = atomicAdd(&st->tiles_done, 1u);
+            if (done + 1 == rq.n_tiles) {                    // last tile of this request
+                __threadfence();
+                const unsigned int me = atomicAdd(&st->mn_enc, 0u), xe = atomicAdd(&st->mx_enc, 0u);
+                const float fmn = me == 0xFFFFFFFFu ? kInf : dec_ordered(me);
+                const float fmx = xe == 0u ? -kInf : dec_ordered(xe);
+                if (rq.minmax) { rq.minmax[0] = fmn; rq.minmax[1] = fmx; }
+                if (rq.host_minmax) {
+                    volatile float* hm = rq.host_minmax;
+                    hm[0] = fmn; hm[1] = fmx;
+                }
+                __threadfence_system();
+                if (rq.host_done) atomicExch_system(rq.host_done, 1u);
+                atomicAdd(&hdr->requests_done, 1u);
+            }
+        }
+        // the next iteration's __syncthreads orders smem reuse
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_batch(BatchHeader* hdr, const BatchRequest* reqs, BatchState* states, const uint2* items,
+                         uint32_t max_prog_bytes, int grid, int block, cudaStream_t stream)
+{
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    if (block != kBatchThreads || max_prog_bytes > 96 * 1024) return cudaErrorInvalidValue;
+    batch_kernel<<<grid, block, max_prog_bytes, stream>>>(hdr, reqs, states, items);
+    return cudaGetLastError();
+}
+
+int batch_occupancy(int block, uint32_t smem)
+{
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_kernel, block, smem) != cudaSuccess || n < 1) n = 1;
+    return n;
+}
+
+cudaError_t batch_kernel_node_params(void** func)
+{
+    *func = reinterpret_cast<void*>(batch_kernel);
+    return cudaSuccess;
+}
+
 
 int num_sms()
 {

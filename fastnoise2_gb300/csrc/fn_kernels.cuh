@@ -47,4 +47,52 @@ cudaError_t launch_interpreter(const FnProgramHeader* prog, uint32_t prog_bytes,
 
 int num_sms();
 
+// ---------------------------------------------------------------- batched persistent launch
+//
+// A batch is N requests (each: one tree program, one point source, one output
+// array) cut into tiles of `tile_points` points.  Work items (request, tile)
+// are listed in `items`; persistent CTAs pull the next item index from
+// `hdr->head` with one atomicAdd, so CTAs that draw cheap tiles simply take
+// more of them.  Each request's min/max is folded with order-preserving
+// integer atomics; the CTA that finishes a request's last tile decodes it,
+// writes it to `minmax` (device) and to `host_minmax` / `host_done` (mapped
+// pinned memory, visible to the host as soon as the request is done).
+
+struct BatchRequest {
+    PointArgs args;
+    const FnProgramHeader* prog;
+    float* out;
+    float* minmax;               // device float[2] or null
+    float* host_minmax;          // mapped pinned float[2] or null
+    unsigned int* host_done;     // mapped pinned flag or null (set to 1 on completion)
+    uint32_t prog_bytes;
+    uint32_t n_tiles;
+    uint32_t pad[4];
+};
+
+struct BatchState {              // per-request mutable state, zeroed by the host upload
+    unsigned int mn_enc;         // order-preserving encodings (host sets 0xFFFFFFFF / 0)
+    unsigned int mx_enc;
+    unsigned int tiles_done;
+    unsigned int pad;
+};
+
+struct BatchHeader {
+    unsigned int n_req;
+    unsigned int n_items;
+    unsigned int tile_points;
+    unsigned int head;           // next work item (host uploads 0)
+    unsigned int requests_done;
+    unsigned int max_prog_bytes;
+    unsigned int pad[2];
+};
+
+// items[i] = (request index, tile index within the request)
+cudaError_t launch_batch(BatchHeader* hdr, const BatchRequest* reqs, BatchState* states, const uint2* items,
+                         uint32_t max_prog_bytes, int grid, int block, cudaStream_t stream);
+
+// CTAs per SM the batch kernel can keep resident for `block` threads and `smem` bytes.
+int batch_occupancy(int block, uint32_t smem);
+cudaError_t batch_kernel_node_params(void** func);
+
 }  // namespace fn

@@ -163,6 +163,40 @@ FASTNOISE_API int fnGenPositionArray4DDevice(const void* node, float* dOut, int 
 FASTNOISE_API int fnGenTileable2DDevice(const void* node, float* dOut, int xSize, int ySize, float xStepSize,
                                         float yStepSize, int seed, float* dMinMax, void* stream);
 
+/* ---- batched generation: many requests, one persistent launch ---------------------------- */
+
+#define FN_KIND_GRID2D 0
+#define FN_KIND_GRID3D 1
+#define FN_KIND_GRID4D 2
+#define FN_KIND_TILEABLE2D 3        /* count[0..1] = x/y size, step[0..1] = x/y step */
+#define FN_KIND_POSITIONS2D 4       /* count[0] = points, positions[0..1] device arrays */
+#define FN_KIND_POSITIONS3D 5
+#define FN_KIND_POSITIONS4D 6
+
+typedef struct fnGenRequest {
+    const void* node;               /* tree to evaluate (any mix of trees per batch) */
+    int kind;                       /* FN_KIND_* */
+    int seed;
+    int count[4];                   /* grid counts (x fastest) or as noted above */
+    float offset[4];
+    float step[4];
+    const float* positions[4];      /* device arrays for FN_KIND_POSITIONS*D */
+    float* out;                     /* device output, one float per point */
+    float* minMax;                  /* NULL or host float[2]; filled by FN_BATCH_SYNC calls */
+} fnGenRequest;
+
+#define FN_BATCH_SYNC 1             /* wait for the batch and fill every minMax */
+#define FN_BATCH_NO_GRAPH 2         /* plain stream launches instead of the captured CUDA graph */
+
+/* Evaluate `count` requests in one persistent launch on `stream` (NULL = default stream).
+ * Tile size and CTAs per SM come from the autotuner's entry for this batch's signature
+ * (set by fnAutotuneBatch), else defaults. */
+FASTNOISE_API int fnGenBatchDevice(const fnGenRequest* requests, int count, void* stream, int flags);
+/* Time each tuning candidate on this batch and remember the fastest for its signature. */
+FASTNOISE_API int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream);
+FASTNOISE_API int fnAutotuneLoad(const char* path);
+FASTNOISE_API int fnAutotuneSave(const char* path);
+
 /* Compile `node` for dimensionality 2/3/4 on the host only (no CUDA call) and report the
  * program size: returns 0 and fills nInstr / nRegs (either may be NULL), or a negative status. */
 FASTNOISE_API int fnCompileInfo(const void* node, int dimension, int* nInstr, int* nRegs);
