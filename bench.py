@@ -1,26 +1,32 @@
 #!/usr/bin/env python3
 """Benchmark: FastNoise2 node-tree evaluation on GB300.
 
-Default workload (the reference's configs[1]): FractalFBm over Perlin, 5 octaves,
-gain 0.5, lacunarity 2, GenUniformGrid3D 256^3 from (-128,-128,-128), step 1,
-seed 42.  A step is one pass over the 16,777,216-point grid.
+Default workload "chunk-mix" (the metric's served-vs-per-call case): 4096
+generation requests, sizes uniform over {16^3, 32^3, 64^3} 3D and {32^2,
+128^2, 512^2} 2D grids, each with one of eight trees, random seeds and chunk
+origins (tests/chunkmix.py; 395M points per step).  A step is one pass over
+all 4096 requests.
 
-  value  -- Mpoints/s of the device-resident path (fnGenUniformGrid3DDevice into
-            HBM), CUDA-event timed per step on the launching stream, L2 flushed
-            between steps (256 MiB write outside the timed events).
-  e2e    -- the same metric through the reference-facing C-ABI call
-            fnGenUniformGrid3D with a pinned host output buffer: launch, kernel,
-            device->host copy of the 64 MiB result and the min/max read are all
-            inside the timed region.
+  value      Mpoints/s of the batched path: all requests in one persistent
+             launch (fnGenBatchDevice, captured CUDA graph, autotuned tiles),
+             outputs resident in HBM, CUDA events on the launching stream.
+  per_call   the same requests as 4096 plain launches (fnGenEachDevice).
+  served     the request server (fnServer*): closed loop (all requests
+             submitted at once) and open loop (Poisson arrivals), with
+             p50/p99 submit-to-completion latency.
+  e2e        the batched path through the public API with the device->host
+             copy of every output into pinned host memory inside the timed region.
+
+Other workloads (--workload): fbm-perlin-256 (FractalFBm(Perlin) 256^3, the
+reference's configs[1]), simplex-64, terrain-tileable-1024, terrain-128.
 
 --impl reference times the CPU restatement of the reference's algorithm
-(oracle/, "port"; the reference itself cannot be built here because its
-FastSIMD dependency is not vendored) with every host thread on the same
-workload, each step a bounded z-slab sample.
+(oracle/, "port": the reference binary cannot be built here because its
+FastSIMD dependency is not vendored) with every host thread on a bounded
+sample of the same workload.
 
-Multi-GPU: points are independent, so --gpus N runs N replicas (one process per
-GPU under torchrun, no collective on the data path); value = all points / max
-rank time.
+Multi-GPU: requests are independent, so --gpus N runs N replicas (one process
+per GPU, no collective on the data path); value = all points / max rank time.
 """
 from __future__ import annotations
 
@@ -39,15 +45,17 @@ sys.path.insert(0, ROOT)
 
 import numpy as np  # noqa: E402
 
-WORKLOADS = {
-    # name: (tree factory name, kind, args, seed)
+GRID_WORKLOADS = {
     "fbm-perlin-256": ("fbm_perlin_c1", "grid", ((-128.0, -128.0, -128.0), (256, 256, 256), (1.0, 1.0, 1.0)), 42),
     "simplex-64": ("simplex_c0", "grid", ((0.0, 0.0, 0.0), (64, 64, 64), (1.0, 1.0, 1.0)), 1337),
     "terrain-tileable-1024": ("terrain_c2", "tile", ((1024, 1024), (1.0, 1.0)), 7),
     "terrain-128": ("terrain_c2", "grid", ((0.0, 0.0, 0.0), (128, 128, 128), (1.0, 1.0, 1.0)), 7),
 }
+WORKLOADS = ["chunk-mix", *GRID_WORKLOADS]
 L2_FLUSH_BYTES = 256 << 20
 
+
+# ---------------------------------------------------------------- helpers
 
 def load_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -57,29 +65,13 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
-def npoints(kind, args):
-    if kind == "grid":
-        return int(np.prod(args[1]))
-    return int(args[0][0] * args[0][1])
-
-
-def tree_for(name):
+def tree_named(name):
     from tests import trees
-    return getattr(trees, WORKLOADS[name][0])()
-
-
-def lane_ops_per_point(name):
-    """FS-level operations per point, counted by the oracle's op counter."""
-    from oracle.oracle import count_ops
-    tname, kind, args, seed = WORKLOADS[name]
-    dim = 4 if kind == "tile" else len(args[1])
-    rng = np.random.default_rng(1)
-    pts = rng.uniform(-200, 200, (32, dim))
-    return count_ops(tree_for(name), pts, seed)
+    return getattr(trees, name)()
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle sampling during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
     def __init__(self, index=0):
         self.index = index
@@ -130,7 +122,7 @@ class ClockSampler:
 
 
 def read_traffic(name):
-    """DRAM bytes per launch from the committed ncu summary, if present."""
+    """DRAM bytes per launch of the dominant kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     if not os.path.exists(path):
         return None
@@ -143,44 +135,7 @@ def read_traffic(name):
     return None
 
 
-def cpu_baseline(name, seconds=8.0, max_points=None):
-    """Time the CPU restatement (all host threads) on a bounded sample of the workload."""
-    from oracle.oracle import OracleTree
-    tname, kind, args, seed = WORKLOADS[name]
-    t = OracleTree(tree_for(name))
-    threads = os.cpu_count()
-    done = 0
-    t0 = time.perf_counter()
-    slab = 0
-    if kind == "grid":
-        off, cnt, st = args
-        plane = int(np.prod(cnt[:-1]))
-        zs = max(1, min(cnt[-1], 8))
-        while time.perf_counter() - t0 < seconds:
-            z0 = (slab * zs) % cnt[-1]
-            z = min(zs, cnt[-1] - z0)
-            o = list(off)
-            o[-1] = float(np.float32(off[-1]) + np.float32(z0) * np.float32(st[-1]))
-            t.grid(o, list(cnt[:-1]) + [z], st, seed, threads=threads)
-            done += plane * z
-            slab += 1
-            if max_points and done >= max_points:
-                break
-        sample = f"{slab} z-slabs of {zs} planes ({done} points) of the {'x'.join(map(str, cnt))} grid"
-    else:
-        (xs, ys), (sx, sy) = args
-        while time.perf_counter() - t0 < seconds:
-            t.tileable(xs, ys, sx, sy, seed, threads=threads)
-            done += xs * ys
-            slab += 1
-            if max_points and done >= max_points:
-                break
-        sample = f"{slab} full {xs}x{ys} tileable passes ({done} points)"
-    dt = time.perf_counter() - t0
-    return {"value": done / dt / 1e6, "unit": "Mpoints/s", "cores": threads, "kind": "port", "sample": sample}
-
-
-def dist_setup(n):
+def dist_setup():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -206,42 +161,262 @@ def allmax(x, world):
     return float(t.item())
 
 
+def ops_per_point(tree, dim, seed):
+    """FS-level operations per point (oracle op counter, oracle/opcount.h)."""
+    from oracle.oracle import count_ops
+    rng = np.random.default_rng(1)
+    return count_ops(tree, rng.uniform(-200, 200, (24, dim)), seed)
+
+
+# ---------------------------------------------------------------- CPU side
+
+def cpu_sample(workload, seconds):
+    """The CPU restatement (all host threads) on a bounded sample of the workload."""
+    from oracle.oracle import OracleTree
+    from tests import chunkmix, trees
+    threads = os.cpu_count()
+    t0 = time.perf_counter()
+    done = 0
+    if workload == "chunk-mix":
+        chunks = chunkmix.make_mix(4096)
+        otrees = [OracleTree(m()) for m in trees.MIX_TREES]
+        n = 0
+        while time.perf_counter() - t0 < seconds and n < len(chunks):
+            c = chunks[n]
+            otrees[c.tree].grid(c.offset, c.count, (1.0,) * len(c.count), c.seed, threads=threads)
+            done += c.points
+            n += 1
+        sample = f"first {n} requests of the 4096-request chunk mix ({done} points)"
+    else:
+        tname, kind, args, seed = GRID_WORKLOADS[workload]
+        t = OracleTree(tree_named(tname))
+        slab = 0
+        if kind == "grid":
+            off, cnt, st = args
+            plane = int(np.prod(cnt[:-1]))
+            zs = max(1, min(cnt[-1], 8))
+            while time.perf_counter() - t0 < seconds:
+                z0 = (slab * zs) % cnt[-1]
+                z = min(zs, cnt[-1] - z0)
+                o = list(off)
+                o[-1] = float(np.float32(off[-1]) + np.float32(z0) * np.float32(st[-1]))
+                t.grid(o, list(cnt[:-1]) + [z], st, seed, threads=threads)
+                done += plane * z
+                slab += 1
+            sample = f"{slab} z-slabs of {zs} planes ({done} points) of the {'x'.join(map(str, cnt))} grid"
+        else:
+            (xs, ys), (sx, sy) = args
+            while time.perf_counter() - t0 < seconds:
+                t.tileable(xs, ys, sx, sy, seed, threads=threads)
+                done += xs * ys
+                slab += 1
+            sample = f"{slab} full {xs}x{ys} tileable passes ({done} points)"
+    dt = time.perf_counter() - t0
+    return {"value": done / dt / 1e6, "unit": "Mpoints/s", "cores": threads, "kind": "port",
+            "sample": sample + "; CPU restatement of FastNoise2 (oracle/), the reference binary needs the unvendored FastSIMD"}
+
+
+def points_per_step(workload):
+    if workload == "chunk-mix":
+        from tests import chunkmix
+        return sum(c.points for c in chunkmix.make_mix(4096))
+    tname, kind, args, seed = GRID_WORKLOADS[workload]
+    return int(np.prod(args[1])) if kind == "grid" else int(args[0][0] * args[0][1])
+
+
 def run_reference(a):
-    rank, world, _ = dist_setup(a.gpus)
+    rank, world, _ = dist_setup()
     if rank != 0:
         return
-    name = a.workload
-    kind, args = WORKLOADS[name][1], WORKLOADS[name][2]
-    per_step = []
     for _ in range(a.warmup):
-        cpu_baseline(name, seconds=0.5)
-    for _ in range(a.steps):
-        per_step.append(cpu_baseline(name, seconds=a.cpu_seconds / max(a.steps, 1)))
+        cpu_sample(a.workload, 0.3)
+    per_step = [cpu_sample(a.workload, a.cpu_seconds / max(a.steps, 1)) for _ in range(a.steps)]
     v = statistics.median(s["value"] for s in per_step)
+    pts = points_per_step(a.workload)
     line = {
         "impl": "reference", "metric": "Mpoints/s", "value": v, "unit": "Mpoints/s", "n_gpus": a.gpus,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": npoints(kind, args) / (v * 1e6) * 1e3,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": name, "points_per_step": npoints(kind, args)},
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": pts / (v * 1e6) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": a.workload, "points_per_step": pts},
         "cpu_baseline": {"value": v, "unit": "Mpoints/s", "cores": per_step[0]["cores"], "kind": "port",
-                         "sample": per_step[0]["sample"] + " per step; CPU restatement of FastNoise2 (oracle/), "
-                                   "the reference binary needs the unvendored FastSIMD"},
+                         "sample": per_step[0]["sample"] + " (per step)"},
         "e2e": {"value": v, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
 
-def run_gpu(a):
-    import torch
-    rank, world, local = dist_setup(a.gpus)
-    torch.cuda.set_device(local)
-    import fastnoise2_gb300 as fn
-    from tests.trees import to_product
+# ---------------------------------------------------------------- GPU: chunk mix
 
-    name = a.workload
-    tname, kind, args, seed = WORKLOADS[name]
-    pts = npoints(kind, args)
-    root = tree_for(name)
+def run_chunkmix(a, rank, world, local):
+    import torch
+    import fastnoise2_gb300 as fn
+    from tests import chunkmix, trees
+
+    dev = torch.device("cuda", local)
+    chunks = chunkmix.make_mix(4096)
+    nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
+    pts = sum(c.points for c in chunks)
+    out = torch.empty(pts, dtype=torch.float32, device=dev)
+    base = out.data_ptr()
+    reqs, off = [], 0
+    for c in chunks:
+        kind = fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D
+        reqs.append(fn.make_request(nodes[c.tree], kind, base + 4 * off, c.seed + rank, c.count, c.offset, (1, 1, 1, 1)))
+        off += c.points
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    fn.gen_each(reqs, sptr, sync=True)                 # compiles and uploads every program
+    fn.autotune_batch(reqs, sptr)
+    for _ in range(max(a.warmup, 3)):
+        fn.gen_batch(reqs, sptr, sync=False)
+        fn.gen_each(reqs, sptr, sync=False)
+    torch.cuda.synchronize(dev)
+
+    def timed(fnc, steps):
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        for i in range(steps):
+            flush.zero_()
+            st[i].record(stream)
+            fnc()
+            en[i].record(stream)
+        torch.cuda.synchronize(dev)
+        return statistics.mean(s.elapsed_time(e) for s, e in zip(st, en))
+
+    sampler = ClockSampler(local)
+    with sampler:
+        barrier(world)
+        torch.cuda.synchronize(dev)
+        batch_ms = timed(lambda: fn.gen_batch(reqs, sptr, sync=False), a.steps)
+        percall_ms = timed(lambda: fn.gen_each(reqs, sptr, sync=False), max(2, a.steps // 2))
+        barrier(world)
+    clocks = sampler.summary()
+    batch_ms_max = allmax(batch_ms, world)
+    value = pts * world / (batch_ms_max * 1e-3) / 1e6
+    percall_value = pts * world / (allmax(percall_ms, world) * 1e-3) / 1e6
+
+    # served: closed loop (everything submitted at once), then open loop (Poisson arrivals)
+    del flush
+    served = run_served(fn, chunks, nodes, rank, a)
+
+    # end to end: batched path + device->host copy of all outputs into pinned memory
+    host = torch.empty(pts, dtype=torch.float32, pin_memory=True)
+    e2e = []
+    for i in range(2 + a.e2e_steps):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        fn.gen_batch(reqs, sptr, sync=True)
+        host.copy_(out, non_blocking=True)
+        torch.cuda.synchronize(dev)
+        if i >= 2:
+            e2e.append((time.perf_counter() - t0) * 1e3)
+    e2e_ms = allmax(statistics.median(e2e), world) if e2e else None
+
+    if rank != 0:
+        return
+    peaks, peak_src = load_peaks()
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
+    peak_lane = n_sm * 128 * sm_max * 1e6 / 1e12
+    tree_ops = [ops_per_point(m(), 3, 1) for m in trees.MIX_TREES]
+    tree_ops2 = [ops_per_point(m(), 2, 1) for m in trees.MIX_TREES]
+    work = sum(c.points * (tree_ops[c.tree] if len(c.count) == 3 else tree_ops2[c.tree]) for c in chunks)
+    achieved = work / (batch_ms * 1e-3) / 1e12
+    hbm_gbs = pts * 4 / (batch_ms * 1e-3) / 1e9
+    cpu = cpu_sample("chunk-mix", a.cpu_seconds) if a.cpu_seconds > 0 else None
+    line = {
+        "metric": "Mpoints/s", "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": batch_ms_max, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "chunk-mix", "requests": len(chunks), "points_per_step": pts,
+                   "trees": [m.__name__ for m in trees.MIX_TREES], "rng": "numpy PCG64(20261203)",
+                   "l2": "flushed between steps (256 MiB write outside the timed events)",
+                   "path": "batched persistent launch (fnGenBatchDevice), interpreter, CUDA graph"},
+        "per_call": {"value": percall_value, "unit": "Mpoints/s", "ms_per_step": percall_ms,
+                     "api": "fnGenEachDevice: one launch per request"},
+        "batched_vs_per_call": value / percall_value,
+        "served": served,
+        "roofline": {"bound": "fp32-issue", "achieved": achieved, "peak": peak_lane, "unit": "Tlane-op/s",
+                     "frac": achieved / peak_lane, "traffic": read_traffic("chunk-mix"),
+                     "work_per_point": work / pts, "work_source": "FS-level ops per point counted by oracle/opcount.h, per tree and dimensionality",
+                     "peak_source": f"{n_sm} SMs x 128 FP32 lanes x {sm_max:.0f} MHz ({peak_src} sm_max_mhz)",
+                     "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": float(peaks.get("hbm_gbs", 6800.0)),
+                             "frac": hbm_gbs / float(peaks.get("hbm_gbs", 6800.0)), "algorithmic_bytes_per_point": 4}},
+        "e2e": {"value": pts * world / (e2e_ms * 1e-3) / 1e6 if e2e_ms else None, "unit": "Mpoints/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": pts * 4, "ms_per_step": e2e_ms,
+                "api": "fnGenBatchDevice + copy of all outputs to pinned host memory"},
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "gpu_launches": a.steps,
+    }
+    print(json.dumps(line))
+
+
+def run_served(fn, chunks, nodes, rank, a):
+    """Closed-loop throughput and open-loop latency through the request server."""
+    pool = int(a.pool_gb * (1 << 30))
+    srv = fn.Server(pool_bytes=pool, streams=a.streams, max_batch_requests=a.max_batch_requests)
+    reqs = []
+    for c in chunks:
+        kind = fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D
+        reqs.append(fn.make_request(nodes[c.tree], kind, 0, c.seed + rank, c.count, c.offset, (1, 1, 1, 1)))
+    pts = sum(c.points for c in chunks)
+    # warm: one full pass
+    for t in [srv.submit(r) for r in reqs]:
+        srv.wait(t)
+        srv.release(t)
+    srv.reset_stats()
+    t0 = time.perf_counter()
+    tickets = [srv.submit(r) for r in reqs]
+    for t in tickets:
+        srv.wait(t)
+    closed_s = time.perf_counter() - t0
+    closed = srv.stats()
+    for t in tickets:
+        srv.release(t)
+    result = {"closed_loop": {"value": pts / closed_s / 1e6, "unit": "Mpoints/s", "wall_ms": closed_s * 1e3,
+                              "p50_ms": closed["p50Micros"] / 1e3, "p99_ms": closed["p99Micros"] / 1e3,
+                              "batches": closed["batches"]}}
+    open_loop = []
+    rng = np.random.default_rng(5)
+    for rate in a.rates:
+        srv.reset_stats()
+        n = min(len(reqs), max(200, int(rate * a.open_seconds)))
+        gaps = rng.exponential(1.0 / rate, n)
+        t_start = time.perf_counter()
+        due = t_start
+        tickets = []
+        for k in range(n):
+            due += gaps[k]
+            while time.perf_counter() < due:
+                pass
+            tickets.append(srv.submit(reqs[k % len(reqs)]))
+        for t in tickets:
+            srv.wait(t)
+        wall = time.perf_counter() - t_start
+        st = srv.stats()
+        for t in tickets:
+            srv.release(t)
+        served_pts = sum(chunks[k % len(chunks)].points for k in range(n))
+        open_loop.append({"rate_req_s": rate, "achieved_req_s": n / wall, "requests": n,
+                          "p50_ms": st["p50Micros"] / 1e3, "p99_ms": st["p99Micros"] / 1e3,
+                          "max_ms": st["maxMicros"] / 1e3, "Mpoints_s": served_pts / wall / 1e6, "batches": st["batches"]})
+    srv.close()
+    result["open_loop"] = open_loop
+    result["config"] = {"pool_gb": a.pool_gb, "streams": a.streams, "max_batch_requests": a.max_batch_requests}
+    return result
+
+
+# ---------------------------------------------------------------- GPU: single grids
+
+def run_grid(a, rank, world, local):
+    import torch
+    from tests.trees import to_product
+    tname, kind, args, seed = GRID_WORKLOADS[a.workload]
+    pts = int(np.prod(args[1])) if kind == "grid" else int(args[0][0] * args[0][1])
+    root = tree_named(tname)
     node = to_product(root)
     node.prepare(4 if kind == "tile" else len(args[1]))
     dev = torch.device("cuda", local)
@@ -260,73 +435,63 @@ def run_gpu(a):
     for _ in range(max(a.warmup, 3)):
         step()
     torch.cuda.synchronize(dev)
-
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
     sampler = ClockSampler(local)
     with sampler:
         barrier(world)
         torch.cuda.synchronize(dev)
-        w0 = time.perf_counter()
         for i in range(a.steps):
-            flush.zero_()                       # evict L2 between steps (outside the timed events)
+            flush.zero_()
             starts[i].record(stream)
             step()
             ends[i].record(stream)
         torch.cuda.synchronize(dev)
         barrier(world)
-        wall = time.perf_counter() - w0
     clocks = sampler.summary()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
-    ms = statistics.mean(step_ms)
+    ms = statistics.mean(s.elapsed_time(e) for s, e in zip(starts, ends))
     ms_max = allmax(ms, world)
     value = pts * world / (ms_max * 1e-3) / 1e6
 
-    # end to end through the reference-facing C-ABI with pinned host memory
-    e2e_med, e2e_value = None, None
+    e2e_ms = None
     if a.e2e_steps > 0:
         host = torch.empty(pts, dtype=torch.float32, pin_memory=True).numpy()
-        e2e_ms = []
-        for i in range(max(a.warmup, 3) + a.e2e_steps):
+        samples = []
+        for i in range(3 + a.e2e_steps):
             t0 = time.perf_counter()
             if kind == "grid":
                 node.gen_uniform_grid(*args, seed + rank, out=host)
             else:
                 node.gen_tileable_2d(args[0], args[1], seed + rank, out=host)
-            if i >= max(a.warmup, 3):
-                e2e_ms.append((time.perf_counter() - t0) * 1e3)
-        e2e_med = allmax(statistics.median(e2e_ms), world)
-        e2e_value = pts * world / (e2e_med * 1e-3) / 1e6
-
+            if i >= 3:
+                samples.append((time.perf_counter() - t0) * 1e3)
+        e2e_ms = allmax(statistics.median(samples), world)
     if rank != 0:
         return
     peaks, peak_src = load_peaks()
-    ops = lane_ops_per_point(name)
     sm_max = float(peaks.get("sm_max_mhz", 2070.0))
     n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
-    peak_lane = n_sm * 128 * sm_max * 1e6 / 1e12          # Tlane-op/s: FP32 lanes x max clock
+    peak_lane = n_sm * 128 * sm_max * 1e6 / 1e12
+    ops = ops_per_point(root, 4 if kind == "tile" else len(args[1]), seed)
     achieved = pts * ops / (ms * 1e-3) / 1e12
-    hbm_bytes = pts * 4
-    hbm_gbs = hbm_bytes / (ms * 1e-3) / 1e9
-    traffic = read_traffic(name)
-    cpu = cpu_baseline(name, seconds=a.cpu_seconds) if a.cpu_seconds > 0 else None
+    hbm_gbs = pts * 4 / (ms * 1e-3) / 1e9
     line = {
         "metric": "Mpoints/s", "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": name, "points_per_step": pts, "tree": tname, "seed": seed,
+        "config": {"workload": a.workload, "points_per_step": pts, "tree": tname, "seed": seed,
                    "l2": "flushed between steps (256 MiB write outside the timed events)",
-                   "path": "interpreter kernel, device-resident output"},
-        "wall_ms_per_step_incl_flush": wall * 1e3 / a.steps,
+                   "path": "per-call interpreter kernel, device-resident output"},
         "roofline": {"bound": "fp32-issue", "achieved": achieved, "peak": peak_lane, "unit": "Tlane-op/s",
-                     "frac": achieved / peak_lane, "traffic": traffic,
-                     "work_per_point": ops, "work_source": "FS-level ops per point counted by oracle/opcount.h",
+                     "frac": achieved / peak_lane, "traffic": read_traffic(a.workload), "work_per_point": ops,
+                     "work_source": "FS-level ops per point counted by oracle/opcount.h",
                      "peak_source": f"{n_sm} SMs x 128 FP32 lanes x {sm_max:.0f} MHz ({peak_src} sm_max_mhz)",
                      "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": float(peaks.get("hbm_gbs", 6800.0)),
                              "frac": hbm_gbs / float(peaks.get("hbm_gbs", 6800.0)), "algorithmic_bytes_per_point": 4}},
-        "e2e": {"value": e2e_value, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": pts * 4 + 8,
-                "ms_per_step": e2e_med, "api": "fnGenUniformGrid3D / fnGenTileable2D into pinned host memory"},
-        "cpu_baseline": cpu,
+        "e2e": {"value": pts * world / (e2e_ms * 1e-3) / 1e6 if e2e_ms else None, "unit": "Mpoints/s",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": pts * 4 + 8, "ms_per_step": e2e_ms,
+                "api": "fnGenUniformGrid3D / fnGenTileable2D into pinned host memory"},
+        "cpu_baseline": cpu_sample(a.workload, a.cpu_seconds) if a.cpu_seconds > 0 else None,
         "clocks": clocks,
         "gpu_launches": a.steps,
     }
@@ -336,17 +501,28 @@ def run_gpu(a):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="fbm-perlin-256", choices=sorted(WORKLOADS))
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--workload", default="chunk-mix", choices=WORKLOADS)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--pool-gb", type=float, default=4.0)
+    ap.add_argument("--streams", type=int, default=3)
+    ap.add_argument("--max-batch-requests", type=int, default=512)
+    ap.add_argument("--rates", type=float, nargs="*", default=[1000.0, 5000.0, 20000.0])
+    ap.add_argument("--open-seconds", type=float, default=0.5)
     a = ap.parse_args()
     if a.impl == "reference":
         run_reference(a)
+        return
+    import torch
+    rank, world, local = dist_setup()
+    torch.cuda.set_device(local)
+    if a.workload == "chunk-mix":
+        run_chunkmix(a, rank, world, local)
     else:
-        run_gpu(a)
+        run_grid(a, rank, world, local)
 
 
 if __name__ == "__main__":

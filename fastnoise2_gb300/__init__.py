@@ -106,6 +106,16 @@ def _declare(L):
         "fnGenTileable2DDevice": (c_int, [vp, vp, c_int, c_int, c_float, c_float, c_int, vp, vp]),
         "fnGenBatchDevice": (c_int, [vp, c_int, vp, c_int]),
         "fnAutotuneBatch": (c_int, [vp, c_int, vp]),
+        "fnGenEachDevice": (c_int, [vp, c_int, vp, c_int]),
+        "fnServerCreate": (vp, [vp]),
+        "fnServerDestroy": (None, [vp]),
+        "fnServerSubmit": (c_int, [vp, vp, vp]),
+        "fnServerPoll": (c_int, [vp, ctypes.c_ulonglong]),
+        "fnServerWait": (c_int, [vp, ctypes.c_ulonglong, c_int, _FP, vp]),
+        "fnServerCancel": (c_int, [vp, ctypes.c_ulonglong]),
+        "fnServerRelease": (c_int, [vp, ctypes.c_ulonglong]),
+        "fnServerGetStats": (c_int, [vp, vp]),
+        "fnServerResetStats": (c_int, [vp]),
         "fnAutotuneLoad": (c_int, [cp]),
         "fnAutotuneSave": (c_int, [cp]),
     }
@@ -174,10 +184,86 @@ def gen_batch(requests, stream: int = 0, sync: bool = True, graph: bool = True) 
         _check()
 
 
+def gen_each(requests, stream: int = 0, sync: bool = True) -> None:
+    """fnGenEachDevice: one plain launch per request (the per-call path)."""
+    arr = (GenRequest * len(requests))(*requests)
+    if lib().fnGenEachDevice(arr, len(requests), stream or None, BATCH_SYNC if sync else 0) != 0:
+        _check()
+
+
 def autotune_batch(requests, stream: int = 0) -> None:
     arr = (GenRequest * len(requests))(*requests)
     if lib().fnAutotuneBatch(arr, len(requests), stream or None) != 0:
         _check()
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("poolBytes", ctypes.c_ulonglong), ("streams", ctypes.c_int), ("maxBatchRequests", ctypes.c_int),
+                ("maxBatchPoints", ctypes.c_longlong), ("idleWaitMicros", ctypes.c_int)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_ulonglong), ("completed", ctypes.c_ulonglong), ("failed", ctypes.c_ulonglong),
+                ("batches", ctypes.c_ulonglong), ("points", ctypes.c_ulonglong), ("p50Micros", ctypes.c_double),
+                ("p99Micros", ctypes.c_double), ("maxMicros", ctypes.c_double), ("meanMicros", ctypes.c_double),
+                ("poolUsed", ctypes.c_ulonglong), ("poolCapacity", ctypes.c_ulonglong), ("queueDepth", ctypes.c_int),
+                ("inflight", ctypes.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Server:
+    """Continuous-batching request server (fnServerCreate ... fnServerDestroy)."""
+
+    def __init__(self, pool_bytes: int = 1 << 30, streams: int = 3, max_batch_requests: int = 1024,
+                 max_batch_points: int = 64 << 20, idle_wait_us: int = 50):
+        cfg = ServerConfig(pool_bytes, streams, max_batch_requests, max_batch_points, idle_wait_us)
+        self._h = lib().fnServerCreate(ctypes.byref(cfg))
+        if not self._h:
+            _check()
+            raise FastNoiseError(-3, "server could not start")
+
+    def close(self):
+        if self._h:
+            lib().fnServerDestroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            self.close()
+
+    def submit(self, request: GenRequest) -> int:
+        t = ctypes.c_ulonglong(0)
+        if lib().fnServerSubmit(self._h, ctypes.byref(request), ctypes.byref(t)) != 0:
+            _check()
+        return t.value
+
+    def poll(self, ticket: int) -> int:
+        return lib().fnServerPoll(self._h, ticket)
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """Returns (min, max, device output pointer); raises FastNoiseError on failure or timeout."""
+        mm = np.zeros(2, np.float32)
+        ptr = ctypes.c_void_p(0)
+        rc = lib().fnServerWait(self._h, ticket, timeout_ms, _fp(mm), ctypes.byref(ptr))
+        if rc != 0:
+            raise FastNoiseError(rc, lib().fnGetLastErrorString().decode())
+        return float(mm[0]), float(mm[1]), ptr.value
+
+    def cancel(self, ticket: int) -> int:
+        return lib().fnServerCancel(self._h, ticket)
+
+    def release(self, ticket: int) -> int:
+        return lib().fnServerRelease(self._h, ticket)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        lib().fnServerGetStats(self._h, ctypes.byref(s))
+        return s.as_dict()
+
+    def reset_stats(self) -> None:
+        lib().fnServerResetStats(self._h)
 
 
 def metadata_count() -> int:

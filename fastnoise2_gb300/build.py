@@ -25,7 +25,7 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["fn_kernels.cu"]
-CPP_SOURCES = ["fn_node.cpp", "fn_compile.cpp", "fn_runtime.cpp", "fn_batch.cpp", "fn_capi.cpp"]
+CPP_SOURCES = ["fn_node.cpp", "fn_compile.cpp", "fn_runtime.cpp", "fn_batch.cpp", "fn_server.cpp", "fn_capi.cpp"]
 
 CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fvisibility=hidden", "-Wall",
             f"-I{CUDA_HOME}/include", f"-I{ROOT}/include"]

@@ -13,6 +13,7 @@
 #include "../../include/FastNoise/FastNoise_C.h"
 #include "fn_batch.h"
 #include "fn_runtime.h"
+#include "fn_server.h"
 
 using namespace fn;
 
@@ -564,6 +565,31 @@ int fnGenBatchDevice(const fnGenRequest* requests, int count, void* stream, int 
     return run_batch(requests, count, stream, flags, nullptr);
 }
 
+int fnGenEachDevice(const fnGenRequest* requests, int count, void* stream, int flags)
+{
+    clear_error();
+    if (count < 0 || (count > 0 && !requests)) { set_error(FN_ERR_ARG, "invalid request list"); return FN_ERR_ARG; }
+    if (count == 0) return FN_OK;
+    if (!thread_ctx()) return FN_ERR_CUDA;
+    BatchCtx* b = batch_ctx((size_t)count);
+    if (!b) return FN_ERR_CUDA;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    for (int i = 0; i < count; ++i) {
+        PointArgs a;
+        if (!requests[i].node || !request_args(requests[i], a)) { set_error(FN_ERR_ARG, "invalid request"); return FN_ERR_ARG; }
+        int rc = gen_device(requests[i].node, a, requests[i].out, b->dminmax + 2 * i, stream);
+        if (rc) return rc;
+    }
+    if (flags & FN_BATCH_SYNC) {
+        if (!cuda_ok(cudaMemcpyAsync(b->hminmax, b->dminmax, (size_t)count * 2 * sizeof(float), cudaMemcpyDeviceToHost, s), "copy minmax") ||
+            !cuda_ok(cudaStreamSynchronize(s), "synchronize"))
+            return FN_ERR_CUDA;
+        for (int i = 0; i < count; ++i)
+            if (requests[i].minMax) { requests[i].minMax[0] = b->hminmax[2 * i]; requests[i].minMax[1] = b->hminmax[2 * i + 1]; }
+    }
+    return FN_OK;
+}
+
 int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream)
 {
     clear_error();
@@ -589,6 +615,92 @@ int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream)
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     Autotuner::instance().store(sig, best, best_ms / 2);
+    return FN_OK;
+}
+
+void* fnServerCreate(const fnServerConfig* config)
+{
+    clear_error();
+    ServerConfig c;
+    if (config) {
+        if (config->poolBytes) c.pool_bytes = (size_t)config->poolBytes;
+        if (config->streams > 0) c.streams = config->streams;
+        if (config->maxBatchRequests > 0) c.max_batch_requests = config->maxBatchRequests;
+        if (config->maxBatchPoints > 0) c.max_batch_points = config->maxBatchPoints;
+        if (config->idleWaitMicros > 0) c.idle_wait_us = config->idleWaitMicros;
+    }
+    Server* s = new Server(c);
+    if (!s->ok()) {
+        delete s;
+        if (!last_error()) set_error(FN_ERR_CUDA, "server could not start");
+        return nullptr;
+    }
+    return s;
+}
+
+void fnServerDestroy(void* server) { delete static_cast<Server*>(server); }
+
+int fnServerSubmit(void* server, const fnGenRequest* request, unsigned long long* ticket)
+{
+    clear_error();
+    if (!server || !request || !ticket) { set_error(FN_ERR_ARG, "invalid arguments"); return FN_ERR_ARG; }
+    BatchItem it;
+    it.node = N(request->node);
+    if (!it.node || !request_args(*request, it.args)) { set_error(FN_ERR_ARG, "invalid node, kind or positions"); return FN_ERR_ARG; }
+    it.dout = request->out;
+    uint64_t t = 0;
+    int rc = static_cast<Server*>(server)->submit(it, t);
+    *ticket = t;
+    return rc;
+}
+
+int fnServerPoll(void* server, unsigned long long ticket)
+{
+    return server ? static_cast<Server*>(server)->poll(ticket) : FN_ERR_ARG;
+}
+
+int fnServerWait(void* server, unsigned long long ticket, int timeoutMs, float* minMax, float** dOut)
+{
+    clear_error();
+    if (!server) { set_error(FN_ERR_ARG, "null server"); return FN_ERR_ARG; }
+    return static_cast<Server*>(server)->wait(ticket, timeoutMs, minMax, dOut);
+}
+
+int fnServerCancel(void* server, unsigned long long ticket)
+{
+    return server ? static_cast<Server*>(server)->cancel(ticket) : FN_ERR_ARG;
+}
+
+int fnServerRelease(void* server, unsigned long long ticket)
+{
+    return server ? static_cast<Server*>(server)->release(ticket) : FN_ERR_ARG;
+}
+
+int fnServerGetStats(void* server, fnServerStats* out)
+{
+    if (!server || !out) return FN_ERR_ARG;
+    ServerStats s;
+    static_cast<Server*>(server)->stats(s);
+    out->submitted = s.submitted;
+    out->completed = s.completed;
+    out->failed = s.failed;
+    out->batches = s.batches;
+    out->points = s.points;
+    out->p50Micros = s.p50_us;
+    out->p99Micros = s.p99_us;
+    out->maxMicros = s.max_us;
+    out->meanMicros = s.mean_us;
+    out->poolUsed = s.pool_used;
+    out->poolCapacity = s.pool_capacity;
+    out->queueDepth = s.queue_depth;
+    out->inflight = s.inflight;
+    return FN_OK;
+}
+
+int fnServerResetStats(void* server)
+{
+    if (!server) return FN_ERR_ARG;
+    static_cast<Server*>(server)->reset_stats();
     return FN_OK;
 }
 

@@ -192,10 +192,50 @@ typedef struct fnGenRequest {
  * Tile size and CTAs per SM come from the autotuner's entry for this batch's signature
  * (set by fnAutotuneBatch), else defaults. */
 FASTNOISE_API int fnGenBatchDevice(const fnGenRequest* requests, int count, void* stream, int flags);
+/* The per-call path for the same request list: one plain launch per request, queued in
+ * order on `stream` (what a caller looping over fnGen*Device would do), for comparison
+ * with fnGenBatchDevice.  minMax pointers are filled when FN_BATCH_SYNC is set. */
+FASTNOISE_API int fnGenEachDevice(const fnGenRequest* requests, int count, void* stream, int flags);
 /* Time each tuning candidate on this batch and remember the fastest for its signature. */
 FASTNOISE_API int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream);
 FASTNOISE_API int fnAutotuneLoad(const char* path);
 FASTNOISE_API int fnAutotuneSave(const char* path);
+
+/* ---- request server: continuous batching over a device memory pool ------------------------ */
+
+typedef struct fnServerConfig {
+    unsigned long long poolBytes;   /* device pool for server-owned outputs (default 1 GiB) */
+    int streams;                    /* batches in flight at once (default 3) */
+    int maxBatchRequests;           /* requests per launch (default 1024) */
+    long long maxBatchPoints;       /* points per launch (default 64 Mi) */
+    int idleWaitMicros;             /* request-loop poll interval when idle (default 50) */
+} fnServerConfig;
+
+typedef struct fnServerStats {
+    unsigned long long submitted, completed, failed, batches, points;
+    double p50Micros, p99Micros, maxMicros, meanMicros;   /* submit -> completion latency */
+    unsigned long long poolUsed, poolCapacity;
+    int queueDepth, inflight;
+} fnServerStats;
+
+/* NULL config = defaults.  Returns NULL (error set) if the device or pool is unavailable. */
+FASTNOISE_API void* fnServerCreate(const fnServerConfig* config);
+/* Waits for batches in flight; requests never admitted are cancelled. */
+FASTNOISE_API void fnServerDestroy(void* server);
+/* Queue one request.  request->out NULL = the server allocates the output from its pool
+ * (admission waits for pool memory).  Tree errors are reported here (FN_ERR_COMPILE). */
+FASTNOISE_API int fnServerSubmit(void* server, const fnGenRequest* request, unsigned long long* ticket);
+/* 1 = done, 0 = pending, negative = failed / cancelled / unknown ticket. */
+FASTNOISE_API int fnServerPoll(void* server, unsigned long long ticket);
+/* Wait up to timeoutMs (negative = forever); on success fills minMax (host float[2]) and
+ * *dOut (device output pointer), either may be NULL.  FN_ERR_TIMEOUT when the wait runs out. */
+FASTNOISE_API int fnServerWait(void* server, unsigned long long ticket, int timeoutMs, float* minMax, float** dOut);
+/* Cancel a request that has not been admitted yet (FN_ERR_STATE otherwise). */
+FASTNOISE_API int fnServerCancel(void* server, unsigned long long ticket);
+/* Forget a finished request and return its pool memory. */
+FASTNOISE_API int fnServerRelease(void* server, unsigned long long ticket);
+FASTNOISE_API int fnServerGetStats(void* server, fnServerStats* stats);
+FASTNOISE_API int fnServerResetStats(void* server);
 
 /* Compile `node` for dimensionality 2/3/4 on the host only (no CUDA call) and report the
  * program size: returns 0 and fills nInstr / nRegs (either may be NULL), or a negative status. */

@@ -1,0 +1,102 @@
+"""Batched persistent launch (fnGenBatchDevice): each request's output and min/max
+equal the per-call path's, alone and inside a mix of trees, kinds and sizes."""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleTree
+from tests import chunkmix, trees
+from tests.parity import assert_parity
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    return torch
+
+
+def requests_for(fn, torch, chunks, nodes):
+    reqs, outs, mms = [], [], []
+    for c in chunks:
+        out = torch.empty(c.points, dtype=torch.float32, device="cuda")
+        mm = np.zeros(2, np.float32)
+        kind = fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D
+        reqs.append(fn.make_request(nodes[c.tree], kind, out.data_ptr(), c.seed, c.count, c.offset, (1, 1, 1, 1), minmax=mm))
+        outs.append(out)
+        mms.append(mm)
+    return reqs, outs, mms
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_matches_per_call(gpu, torch_cuda, graph):
+    fn, torch = gpu, torch_cuda
+    sizes = [(16, 16, 16), (9, 7, 5), (32, 32), (50, 3), (1, 1, 1), (0, 4, 4)]
+    chunks = chunkmix.make_mix(48, seed=7, sizes=sizes)
+    nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
+    reqs, outs, mms = requests_for(fn, torch, chunks, nodes)
+    fn.gen_batch(reqs, sync=True, graph=graph)
+    for c, out, mm in zip(chunks, outs, mms):
+        ref, rmm = nodes[c.tree].gen_uniform_grid(c.offset, c.count, (1,) * len(c.count), c.seed)
+        got = out.cpu().numpy()
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), c
+        assert (mm[0], mm[1]) == rmm, (c, mm, rmm)
+
+
+def test_batch_against_oracle(gpu, torch_cuda):
+    fn, torch = gpu, torch_cuda
+    chunks = chunkmix.make_mix(16, seed=11, sizes=[(12, 10, 8), (40, 24)])
+    nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
+    reqs, outs, mms = requests_for(fn, torch, chunks, nodes)
+    fn.gen_batch(reqs, sync=True)
+    for c, out, mm in zip(chunks, outs, mms):
+        o, omm = OracleTree(trees.MIX_TREES[c.tree]()).grid(c.offset, c.count, (1,) * len(c.count), c.seed)
+        assert_parity(out.cpu().numpy(), (float(mm[0]), float(mm[1])), o, omm, label=str(c))
+
+
+def test_batch_mixed_kinds(gpu, torch_cuda):
+    """Tileable and position-array requests ride in the same launch as grids."""
+    fn, torch = gpu, torch_cuda
+    terrain = trees.to_product(trees.terrain_c2())
+    fbm = trees.to_product(trees.fbm_perlin_c1())
+    rng = np.random.default_rng(5)
+    pos = [torch.tensor(rng.uniform(-1e4, 1e4, 5000).astype(np.float32), device="cuda") for _ in range(3)]
+    o1 = torch.empty(64 * 48, device="cuda")
+    o2 = torch.empty(5000, device="cuda")
+    o3 = torch.empty(20 * 20 * 20, device="cuda")
+    m1, m2, m3 = (np.zeros(2, np.float32) for _ in range(3))
+    reqs = [fn.make_request(terrain, fn.KIND_TILEABLE2D, o1.data_ptr(), 7, (64, 48), step=(1.0, 1.0), minmax=m1),
+            fn.make_request(fbm, fn.KIND_POSITIONS3D, o2.data_ptr(), 42, (5000,), offset=(1.0, 2.0, 3.0),
+                            positions=[p.data_ptr() for p in pos], minmax=m2),
+            fn.make_request(fbm, fn.KIND_GRID3D, o3.data_ptr(), 3, (20, 20, 20), offset=(-5, -5, -5), minmax=m3)]
+    fn.gen_batch(reqs, sync=True)
+    t, tmm = terrain.gen_tileable_2d((64, 48), (1.0, 1.0), 7)
+    p, pmm = fbm.gen_position_array([x.cpu().numpy() for x in pos], (1.0, 2.0, 3.0), 42)
+    g, gmm = fbm.gen_uniform_grid((-5, -5, -5), (20, 20, 20), (1, 1, 1), 3)
+    for got, ref, mm, rmm in ((o1, t, m1, tmm), (o2, p, m2, pmm), (o3, g, m3, gmm)):
+        assert np.array_equal(got.cpu().numpy().view(np.uint32), ref.view(np.uint32))
+        assert (mm[0], mm[1]) == rmm
+
+
+def test_autotune_and_reuse(gpu, torch_cuda, tmp_path):
+    fn, torch = gpu, torch_cuda
+    chunks = chunkmix.make_mix(24, seed=3, sizes=[(16, 16, 16), (64, 64)])
+    nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
+    reqs, outs, mms = requests_for(fn, torch, chunks, nodes)
+    fn.autotune_batch(reqs)
+    first = [o.clone() for o in outs]
+    fn.gen_batch(reqs, sync=True)
+    for a, b in zip(first, outs):
+        assert torch.equal(a, b)
+    path = str(tmp_path / "tune.txt")
+    assert fn.lib().fnAutotuneSave(path.encode()) == 0
+    assert fn.lib().fnAutotuneLoad(path.encode()) == 0
+
+
+def test_bad_request_fails_loudly(gpu, torch_cuda):
+    fn = gpu
+    node = fn.Node.from_encoded(trees.DEMO_MOUNTAIN)          # DomainWarpSimplex: no GPU kernel yet
+    out = torch_cuda.empty(16, device="cuda")
+    with pytest.raises(fn.FastNoiseError):
+        fn.gen_batch([fn.make_request(node, fn.KIND_GRID2D, out.data_ptr(), 1, (4, 4))])
