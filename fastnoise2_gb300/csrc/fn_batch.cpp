@@ -151,6 +151,7 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         std::memset(&r, 0, sizeof r);
         r.args = items[i].args;
         r.prog = progs[i].dptr;
+        r.jit_slot = -1;
         r.prog_bytes = progs[i].bytes;
         r.out = items[i].dout;
         r.minmax = items[i].dminmax;

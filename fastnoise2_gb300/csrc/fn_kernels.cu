@@ -11,7 +11,7 @@
 // of a warp executes the same instruction stream (warp-uniform dispatch).
 #include <cuda_runtime.h>
 
-#include "fn_device.cuh"
+#include "fn_eval.cuh"
 #include "fn_kernels.cuh"
 
 namespace fn {
@@ -284,84 +284,11 @@ __device__ __noinline__ void exec_program(const FnInstr* ins, int n, const float
     }
 }
 
-__device__ __forceinline__ void root_position(const PointArgs& a, long long i, float* R)
-{
-    if (a.src == kSrcGrid) {
-        long long r = i;
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (k >= a.dim) break;
-            long long ik = (k == a.dim - 1) ? r : r % a.count[k];
-            r = (k == a.dim - 1) ? 0 : r / a.count[k];
-            R[k] = fmaf(cvtf((int)ik), a.step[k], a.offset[k]);   // Generator.inl:160-162
-        }
-    } else if (a.src == kSrcTileable) {
-        const long long xi = i % a.count[0], yi = i / a.count[0];
-        const float xf = cvtf((int)xi) * a.tmul[0];                 // Generator.inl:400-406
-        const float yf = cvtf((int)yi) * a.tmul[1];
-        R[0] = cos_(xf) * a.tfreq[0];
-        R[1] = cos_(yf) * a.tfreq[1];
-        R[2] = sin_(xf) * a.tfreq[0];
-        R[3] = sin_(yf) * a.tfreq[1];
-    } else {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            if (k >= a.dim) break;
-            R[k] = a.offset[k] + __ldg(a.pos[k] + i);              // Generator.inl:295-297
-        }
-    }
-}
-
-// Block-wide min/max, then the last block folds all per-block partials.
-__device__ __forceinline__ void reduce_minmax(float mn, float mx, MinMaxWork* work, float* dminmax)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn = fmin_(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmax_(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    }
-    __shared__ float smn[kThreads / 32], smx[kThreads / 32];
-    __shared__ bool is_last;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (lane == 0) { smn[warp] = mn; smx[warp] = mx; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { mn = fmin_(mn, smn[w]); mx = fmax_(mx, smx[w]); }
-        work->partial[2 * blockIdx.x] = mn;
-        work->partial[2 * blockIdx.x + 1] = mx;
-        __threadfence();
-        const unsigned t = atomicAdd(&work->counter, 1u);
-        is_last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!is_last) return;
-    __threadfence();
-    mn = kInf; mx = -kInf;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-        mn = fmin_(mn, __ldcg(&work->partial[2 * b]));
-        mx = fmax_(mx, __ldcg(&work->partial[2 * b + 1]));
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        mn = fmin_(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-        mx = fmax_(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-    }
-    __syncthreads();
-    if (lane == 0) { smn[warp] = mn; smx[warp] = mx; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { mn = fmin_(mn, smn[w]); mx = fmax_(mx, smx[w]); }
-        work->result[0] = mn;
-        work->result[1] = mx;
-        if (dminmax) { dminmax[0] = mn; dminmax[1] = mx; }
-        work->counter = 0;
-    }
-}
-
 __global__ void __launch_bounds__(kThreads) interp_kernel(const FnProgramHeader* gprog, uint32_t bytes, PointArgs args,
                                                           float* __restrict__ out, MinMaxWork* work, float* dminmax)
 {
     extern __shared__ uint4 sprog[];
+    __shared__ float smn[kThreads / 32], smx[kThreads / 32];
     const uint4* src = reinterpret_cast<const uint4*>(gprog);
     for (uint32_t w = threadIdx.x; w < bytes / 16; w += blockDim.x) sprog[w] = src[w];
     __syncthreads();
@@ -375,28 +302,16 @@ __global__ void __launch_bounds__(kThreads) interp_kernel(const FnProgramHeader*
     float R[FN_MAX_REGS];
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < args.total; i += stride) {
-        root_position(args, i, R);
+        fne::root_position(args, i, R);
         exec_program(ins, n, P, R, args.seed);
         const float v = R[outr];
         out[i] = v;
-        mn = v < mn ? v : mn;       // OutputMinMax::operator<< (NaN never replaces)
-        mx = mx < v ? v : mx;
+        fne::fold(v, mn, mx);
     }
-    reduce_minmax(mn, mx, work, dminmax);
+    fne::grid_minmax(mn, mx, work, dminmax, smn, smx);
 }
 
 int g_num_sms = 0;
-
-// Order-preserving float <-> uint encoding for atomicMin/atomicMax.
-__device__ __forceinline__ unsigned int enc_ordered(float f)
-{
-    const unsigned int b = __float_as_uint(f);
-    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
-}
-__device__ __forceinline__ float dec_ordered(unsigned int u)
-{
-    return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
-}
 
 constexpr int kBatchThreads = 256;
 
@@ -409,7 +324,6 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchHeader* hdr, 
     const FnProgramHeader* loaded = nullptr;
     const unsigned int n_items = hdr->n_items;
     const unsigned int tile_points = hdr->tile_points;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     for (;;) {
         if (threadIdx.x == 0) s_item = atomicAdd(&hdr->head, 1u);
@@ -418,7 +332,7 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchHeader* hdr, 
         if (it >= n_items) break;
         const uint2 item = items[it];
         const BatchRequest& rq = reqs[item.x];
-        const FnProgramHeader* gprog = rq.prog;
+        const FnProgramHeader* gprog = static_cast<const FnProgramHeader*>(rq.prog);
         if (gprog != loaded) {                               // stage this request's program
             const uint4* src = reinterpret_cast<const uint4*>(gprog);
             for (uint32_t w = threadIdx.x; w < rq.prog_bytes / 16; w += blockDim.x) sprog[w] = src[w];
@@ -436,45 +350,15 @@ __global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchHeader* hdr, 
         float mn = kInf, mx = -kInf;
         float R[FN_MAX_REGS];
         for (long long i = begin + threadIdx.x; i < end; i += blockDim.x) {
-            root_position(args, i, R);
+            fne::root_position(args, i, R);
             exec_program(ins, h->n_instr, P, R, args.seed);
             const float v = R[h->out_reg];
             rq.out[i] = v;
-            mn = v < mn ? v : mn;
-            mx = mx < v ? v : mx;
+            fne::fold(v, mn, mx);
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            mn = fmin_(mn, __shfl_xor_sync(0xffffffffu, mn, o));
-            mx = fmax_(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        }
-        if (lane == 0) { smn[warp] = mn; smx[warp] = mx; }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (int w = 1; w < kBatchThreads / 32; ++w) { mn = fmin_(mn, smn[w]); mx = fmax_(mx, smx[w]); }
-            BatchState* st = states + item.x;
-            if (mn <= mx) {                                  // tile had at least one non-NaN value
-                atomicMin(&st->mn_enc, enc_ordered(mn));
-                atomicMax(&st->mx_enc, enc_ordered(mx));
-            }
-            __threadfence();
-            const unsigned int done = atomicAdd(&st->tiles_done, 1u);
-            if (done + 1 == rq.n_tiles) {                    // last tile of this request
-                __threadfence();
-                const unsigned int me = atomicAdd(&st->mn_enc, 0u), xe = atomicAdd(&st->mx_enc, 0u);
-                const float fmn = me == 0xFFFFFFFFu ? kInf : dec_ordered(me);
-                const float fmx = xe == 0u ? -kInf : dec_ordered(xe);
-                if (rq.minmax) { rq.minmax[0] = fmn; rq.minmax[1] = fmx; }
-                if (rq.host_minmax) {
-                    volatile float* hm = rq.host_minmax;
-                    hm[0] = fmn; hm[1] = fmx;
-                }
-                __threadfence_system();
-                if (rq.host_done) atomicExch_system(rq.host_done, 1u);
-                atomicAdd(&hdr->requests_done, 1u);
-            }
-        }
-        // the next iteration's __syncthreads orders smem reuse
+        fne::block_minmax(mn, mx, smn, smx);
+        if (threadIdx.x == 0) fne::finish_tile(rq, states + item.x, hdr, mn, mx);
+        // the next iteration's __syncthreads orders shared-memory reuse
     }
 }
 
@@ -501,11 +385,6 @@ int batch_occupancy(int block, uint32_t smem)
     return n;
 }
 
-cudaError_t batch_kernel_node_params(void** func)
-{
-    *func = reinterpret_cast<void*>(batch_kernel);
-    return cudaSuccess;
-}
 
 
 int num_sms()
