@@ -99,6 +99,7 @@ def _declare(L):
         "fnCompileInfo": (c_int, [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
         "fnGenUniformGrid2DDevice": (c_int, [vp, vp, c_float, c_float, c_int, c_int, c_float, c_float, c_int, vp, vp]),
         "fnGenUniformGrid3DDevice": (c_int, [vp, vp, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, vp, vp]),
+        "fnGenUniformGrid3DDeviceNoAlloc": (c_int, [vp, vp, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, vp, vp]),
         "fnGenUniformGrid4DDevice": (c_int, [vp, vp] + [c_float] * 4 + [c_int] * 4 + [c_float] * 4 + [c_int, vp, vp]),
         "fnGenPositionArray2DDevice": (c_int, [vp, vp, c_int, vp, vp, c_float, c_float, c_int, vp, vp]),
         "fnGenPositionArray3DDevice": (c_int, [vp, vp, c_int, vp, vp, vp, c_float, c_float, c_float, c_int, vp, vp]),

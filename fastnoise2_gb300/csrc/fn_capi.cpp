@@ -14,6 +14,7 @@
 #include "fn_batch.h"
 #include "fn_runtime.h"
 #include "fn_server.h"
+#include "fn_static_scratch.h"
 
 using namespace fn;
 
@@ -792,6 +793,43 @@ int fnGenTileable2DDevice(const void* node, float* dOut, int xSize, int ySize, f
                           int seed, float* dMinMax, void* stream)
 {
     return gen_device(node, tile_args(xSize, ySize, xStepSize, yStepSize, seed), dOut, dMinMax, stream);
+}
+
+// Allocation-free 3D grid: the program is compiled on the host (cached per
+// thread, host memory only) and copied into the static device scratch of
+// fn_static_scratch.cu on the caller's stream.  No device memory, pinned host
+// memory or stream is created, so this never touches thread_ctx().
+int fnGenUniformGrid3DDeviceNoAlloc(const void* node, float* dOut, float xOffset, float yOffset, float zOffset,
+                                    int xCount, int yCount, int zCount, float xStepSize, float yStepSize,
+                                    float zStepSize, int seed, float* dMinMax, void* stream)
+{
+    clear_error();
+    const float off[3] = {xOffset, yOffset, zOffset};
+    const int cnt[3] = {xCount, yCount, zCount};
+    const float st[3] = {xStepSize, yStepSize, zStepSize};
+    const PointArgs args = grid_args(3, off, cnt, st, seed);
+    if (!node || args.total < 0 || (args.total > 0 && !dOut)) { set_error(FN_ERR_ARG, "invalid arguments"); return FN_ERR_ARG; }
+    struct HostProgram { const Node* node = nullptr; uint64_t epoch = 0; CompiledProgram prog; };
+    thread_local HostProgram cached;
+    const uint64_t epoch = mutation_epoch();
+    if (cached.node != N(node) || cached.epoch != epoch) {
+        cached.node = nullptr;
+        std::string err;
+        if (!compile_program(N(node), 3, cached.prog, err)) { set_error(FN_ERR_COMPILE, err); return FN_ERR_COMPILE; }
+        cached.node = N(node);
+        cached.epoch = epoch;
+    }
+    const size_t bytes = cached.prog.blob.size();
+    if (bytes > kStaticProgramBytes) {
+        set_error(FN_ERR_CAPACITY, "tree program is " + std::to_string(bytes) + " bytes; the allocation-free path holds at most " +
+                                       std::to_string(kStaticProgramBytes) + " bytes (use fnGenUniformGrid3DDevice)");
+        return FN_ERR_CAPACITY;
+    }
+    if (!cuda_ok(launch_interpreter_static(cached.prog.blob.data(), (uint32_t)bytes, args, dOut, dMinMax,
+                                           static_cast<cudaStream_t>(stream)),
+                 "allocation-free launch"))
+        return FN_ERR_CUDA;
+    return FN_OK;
 }
 
 }  // extern "C"
