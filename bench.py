@@ -268,6 +268,13 @@ def run_chunkmix(a, rank, world, local):
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
 
     fn.gen_each(reqs, sptr, sync=True)                 # compiles and uploads every program
+    jit_s = None
+    if a.kernels == "jit":
+        t0 = time.perf_counter()
+        fn.jit_compile([(n, d) for n in nodes for d in (2, 3, 4)])
+        jit_s = time.perf_counter() - t0
+    else:
+        fn.set_jit_enabled(False)
     fn.autotune_batch(reqs, sptr)
     for _ in range(max(a.warmup, 3)):
         fn.gen_batch(reqs, sptr, sync=False)
@@ -292,6 +299,16 @@ def run_chunkmix(a, rank, world, local):
         batch_ms = timed(lambda: fn.gen_batch(reqs, sptr, sync=False), a.steps)
         percall_ms = timed(lambda: fn.gen_each(reqs, sptr, sync=False), max(2, a.steps // 2))
         barrier(world)
+    interp = None
+    if a.kernels == "jit":                              # the same batch through the interpreter, for comparison
+        fn.set_jit_enabled(False)
+        fn.autotune_batch(reqs, sptr)
+        fn.gen_batch(reqs, sptr, sync=True)
+        interp_ms = timed(lambda: fn.gen_batch(reqs, sptr, sync=False), max(2, a.steps // 2))
+        interp_pc_ms = timed(lambda: fn.gen_each(reqs, sptr, sync=False), 2)
+        fn.set_jit_enabled(True)
+        interp = {"batched": pts / (interp_ms * 1e-3) / 1e6, "per_call": pts / (interp_pc_ms * 1e-3) / 1e6,
+                  "unit": "Mpoints/s", "note": "same mix, interpreter kernels (fnSetJitEnabled(0))"}
     clocks = sampler.summary()
     batch_ms_max = allmax(batch_ms, world)
     value = pts * world / (batch_ms_max * 1e-3) / 1e6
@@ -299,7 +316,7 @@ def run_chunkmix(a, rank, world, local):
 
     # served: closed loop (everything submitted at once), then open loop (Poisson arrivals)
     del flush
-    served = run_served(fn, chunks, nodes, rank, a)
+    served = run_served(fn, chunks, nodes, rank, a, dev)
 
     # end to end: batched path + device->host copy of all outputs into pinned memory
     host = torch.empty(pts, dtype=torch.float32, pin_memory=True)
@@ -313,6 +330,7 @@ def run_chunkmix(a, rank, world, local):
         if i >= 2:
             e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = allmax(statistics.median(e2e), world) if e2e else None
+    binfo = fn.batch_info()
 
     if rank != 0:
         return
@@ -333,7 +351,10 @@ def run_chunkmix(a, rank, world, local):
         "config": {"workload": "chunk-mix", "requests": len(chunks), "points_per_step": pts,
                    "trees": [m.__name__ for m in trees.MIX_TREES], "rng": "numpy PCG64(20261203)",
                    "l2": "flushed between steps (256 MiB write outside the timed events)",
-                   "path": "batched persistent launch (fnGenBatchDevice), interpreter, CUDA graph"},
+                   "path": "batched persistent launch (fnGenBatchDevice), CUDA graph, "
+                           + ("specialised kernels (fnJitCompile)" if a.kernels == "jit" else "interpreter kernel"),
+                   "jit_compile_s": jit_s},
+        "interpreter": interp,
         "per_call": {"value": percall_value, "unit": "Mpoints/s", "ms_per_step": percall_ms,
                      "api": "fnGenEachDevice: one launch per request"},
         "batched_vs_per_call": value / percall_value,
@@ -345,8 +366,11 @@ def run_chunkmix(a, rank, world, local):
                      "hbm": {"achieved_gbs": hbm_gbs, "peak_gbs": float(peaks.get("hbm_gbs", 6800.0)),
                              "frac": hbm_gbs / float(peaks.get("hbm_gbs", 6800.0)), "algorithmic_bytes_per_point": 4}},
         "e2e": {"value": pts * world / (e2e_ms * 1e-3) / 1e6 if e2e_ms else None, "unit": "Mpoints/s",
-                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": pts * 4, "ms_per_step": e2e_ms,
-                "api": "fnGenBatchDevice + copy of all outputs to pinned host memory"},
+                "h2d_bytes_per_step": binfo["uploadBytes"], "d2h_bytes_per_step": pts * 4 + 8 * len(chunks),
+                "ms_per_step": e2e_ms,
+                "api": "fnGenBatchDevice (request descriptors uploaded, min/max read back) + copy of all outputs "
+                       "to pinned host memory"},
+        "batch": binfo,
         "cpu_baseline": cpu,
         "clocks": clocks,
         "gpu_launches": a.steps,
@@ -354,7 +378,7 @@ def run_chunkmix(a, rank, world, local):
     print(json.dumps(line))
 
 
-def run_served(fn, chunks, nodes, rank, a):
+def run_served(fn, chunks, nodes, rank, a, dev):
     """Closed-loop throughput and open-loop latency through the request server."""
     pool = int(a.pool_gb * (1 << 30))
     srv = fn.Server(pool_bytes=pool, streams=a.streams, max_batch_requests=a.max_batch_requests)
@@ -379,11 +403,30 @@ def run_served(fn, chunks, nodes, rank, a):
     result = {"closed_loop": {"value": pts / closed_s / 1e6, "unit": "Mpoints/s", "wall_ms": closed_s * 1e3,
                               "p50_ms": closed["p50Micros"] / 1e3, "p99_ms": closed["p99Micros"] / 1e3,
                               "batches": closed["batches"]}}
+    # open loop: the serving mix -- the chunk mix plus, every `extra_every` chunks, one
+    # GenUniformGrid4D 32^4 and one GenPositionArray3D over 1M positions uniform in [-1e4, 1e4]^3
+    import torch
+    prng = np.random.default_rng(20261203)
+    pos = [torch.from_numpy(prng.uniform(-1e4, 1e4, 1 << 20).astype(np.float32)).to(dev) for _ in range(3)]
+    serve, serve_pts = [], []
+    for k, (c, r) in enumerate(zip(chunks, reqs)):
+        serve.append(r)
+        serve_pts.append(c.points)
+        if a.extra_every > 0 and k % a.extra_every == a.extra_every - 1:
+            serve.append(fn.make_request(nodes[c.tree], fn.KIND_GRID4D, 0, c.seed + 1, (32, 32, 32, 32),
+                                         tuple(c.offset) + (0.0,) * (4 - len(c.offset)), (1, 1, 1, 1)))
+            serve_pts.append(32 ** 4)
+            serve.append(fn.make_request(nodes[c.tree], fn.KIND_POSITIONS3D, 0, c.seed + 2, (1 << 20,), (0, 0, 0), (1, 1, 1),
+                                         positions=[p.data_ptr() for p in pos]))
+            serve_pts.append(1 << 20)
+    for t in [srv.submit(r) for r in serve]:           # warm the extra kinds
+        srv.wait(t)
+        srv.release(t)
     open_loop = []
     rng = np.random.default_rng(5)
     for rate in a.rates:
         srv.reset_stats()
-        n = min(len(reqs), max(200, int(rate * a.open_seconds)))
+        n = min(4 * len(serve), max(200, int(rate * a.open_seconds)))
         gaps = rng.exponential(1.0 / rate, n)
         t_start = time.perf_counter()
         due = t_start
@@ -392,20 +435,22 @@ def run_served(fn, chunks, nodes, rank, a):
             due += gaps[k]
             while time.perf_counter() < due:
                 pass
-            tickets.append(srv.submit(reqs[k % len(reqs)]))
+            tickets.append(srv.submit(serve[k % len(serve)]))
         for t in tickets:
             srv.wait(t)
         wall = time.perf_counter() - t_start
         st = srv.stats()
         for t in tickets:
             srv.release(t)
-        served_pts = sum(chunks[k % len(chunks)].points for k in range(n))
+        served_pts = sum(serve_pts[k % len(serve)] for k in range(n))
         open_loop.append({"rate_req_s": rate, "achieved_req_s": n / wall, "requests": n,
                           "p50_ms": st["p50Micros"] / 1e3, "p99_ms": st["p99Micros"] / 1e3,
                           "max_ms": st["maxMicros"] / 1e3, "Mpoints_s": served_pts / wall / 1e6, "batches": st["batches"]})
     srv.close()
     result["open_loop"] = open_loop
-    result["config"] = {"pool_gb": a.pool_gb, "streams": a.streams, "max_batch_requests": a.max_batch_requests}
+    result["config"] = {"pool_gb": a.pool_gb, "streams": a.streams, "max_batch_requests": a.max_batch_requests,
+                        "open_loop_mix": f"chunk mix + per {a.extra_every} chunks one GenUniformGrid4D 32^4 and one "
+                                         "GenPositionArray3D 1M positions U[-1e4,1e4]^3; Poisson arrivals"}
     return result
 
 
@@ -419,6 +464,11 @@ def run_grid(a, rank, world, local):
     root = tree_named(tname)
     node = to_product(root)
     node.prepare(4 if kind == "tile" else len(args[1]))
+    import fastnoise2_gb300 as fn
+    if a.kernels == "jit":
+        fn.jit_compile([(node, 4 if kind == "tile" else len(args[1]))])
+    else:
+        fn.set_jit_enabled(False)
     dev = torch.device("cuda", local)
     out = torch.empty(pts, dtype=torch.float32, device=dev)
     mm = torch.empty(2, dtype=torch.float32, device=dev)
@@ -481,7 +531,8 @@ def run_grid(a, rank, world, local):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": a.workload, "points_per_step": pts, "tree": tname, "seed": seed,
                    "l2": "flushed between steps (256 MiB write outside the timed events)",
-                   "path": "per-call interpreter kernel, device-resident output"},
+                   "path": "per-call " + ("specialised kernel (fnJitCompile)" if a.kernels == "jit" else "interpreter kernel")
+                           + ", device-resident output"},
         "roofline": {"bound": "fp32-issue", "achieved": achieved, "peak": peak_lane, "unit": "Tlane-op/s",
                      "frac": achieved / peak_lane, "traffic": read_traffic(a.workload), "work_per_point": ops,
                      "work_source": "FS-level ops per point counted by oracle/opcount.h",
@@ -506,11 +557,15 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="chunk-mix", choices=WORKLOADS)
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--kernels", default="jit", choices=["jit", "interp"],
+                    help="specialised per-tree kernels (NVRTC) or the program interpreter")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
-    ap.add_argument("--pool-gb", type=float, default=4.0)
+    ap.add_argument("--pool-gb", type=float, default=40.0)
     ap.add_argument("--streams", type=int, default=3)
     ap.add_argument("--max-batch-requests", type=int, default=512)
-    ap.add_argument("--rates", type=float, nargs="*", default=[1000.0, 5000.0, 20000.0])
+    ap.add_argument("--rates", type=float, nargs="*", default=[1000.0, 5000.0, 10000.0, 20000.0, 50000.0])
+    ap.add_argument("--extra-every", type=int, default=64,
+                    help="serving mix: one GenUniformGrid4D 32^4 and one GenPositionArray3D 1M request per this many chunks")
     ap.add_argument("--open-seconds", type=float, default=0.5)
     a = ap.parse_args()
     if a.impl == "reference":

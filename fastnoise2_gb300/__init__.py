@@ -99,6 +99,10 @@ def _declare(L):
         "fnCompileInfo": (c_int, [vp, c_int, ctypes.POINTER(c_int), ctypes.POINTER(c_int)]),
         "fnGenUniformGrid2DDevice": (c_int, [vp, vp, c_float, c_float, c_int, c_int, c_float, c_float, c_int, vp, vp]),
         "fnGenUniformGrid3DDevice": (c_int, [vp, vp, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, vp, vp]),
+        "fnJitCompile": (c_int, [vp, vp, c_int]),
+        "fnGetBatchInfo": (c_int, [vp]),
+        "fnJitCheck": (c_int, [vp, vp, c_int, ctypes.POINTER(c_int)]),
+        "fnSetJitEnabled": (c_int, [c_int]),
         "fnGenUniformGrid3DDeviceNoAlloc": (c_int, [vp, vp, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, vp, vp]),
         "fnGenUniformGrid4DDevice": (c_int, [vp, vp] + [c_float] * 4 + [c_int] * 4 + [c_float] * 4 + [c_int, vp, vp]),
         "fnGenPositionArray2DDevice": (c_int, [vp, vp, c_int, vp, vp, c_float, c_float, c_int, vp, vp]),
@@ -196,6 +200,47 @@ def autotune_batch(requests, stream: int = 0) -> None:
     arr = (GenRequest * len(requests))(*requests)
     if lib().fnAutotuneBatch(arr, len(requests), stream or None) != 0:
         _check()
+
+
+def _jit_arrays(pairs):
+    nodes = (ctypes.c_void_p * len(pairs))(*[n._h for n, _ in pairs])
+    dims = (ctypes.c_int * len(pairs))(*[int(d) for _, d in pairs])
+    return nodes, dims
+
+
+def jit_compile(pairs) -> None:
+    """Build specialised kernels for [(node, dimension), ...] (fnJitCompile)."""
+    nodes, dims = _jit_arrays(pairs)
+    if lib().fnJitCompile(nodes, dims, len(pairs)) != 0:
+        _check()
+
+
+def jit_check(pairs) -> int:
+    """NVRTC-compile the module for [(node, dimension), ...] without loading it; returns cubin bytes."""
+    nodes, dims = _jit_arrays(pairs)
+    n = ctypes.c_int(0)
+    if lib().fnJitCheck(nodes, dims, len(pairs), ctypes.byref(n)) != 0:
+        _check()
+    return n.value
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("requests", ctypes.c_int), ("specialised", ctypes.c_int), ("tilePoints", ctypes.c_int),
+                ("ctas", ctypes.c_int), ("workItems", ctypes.c_ulonglong), ("points", ctypes.c_ulonglong),
+                ("uploadBytes", ctypes.c_ulonglong)]
+
+
+def batch_info() -> dict:
+    """Shape of this thread's last gen_batch launch (fnGetBatchInfo)."""
+    info = BatchInfo()
+    if lib().fnGetBatchInfo(ctypes.byref(info)) != 0:
+        _check()
+    return {k: getattr(info, k) for k, _ in info._fields_}
+
+
+def set_jit_enabled(on: bool) -> bool:
+    """Use specialised kernels where built (True, default) or the interpreter only; returns the old setting."""
+    return bool(lib().fnSetJitEnabled(1 if on else 0))
 
 
 class ServerConfig(ctypes.Structure):

@@ -2,6 +2,8 @@
 // batched persistent launch (kernel in fn_kernels.cu).
 #include "fn_batch.h"
 
+#include "fn_jit.h"
+
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
@@ -70,16 +72,35 @@ bool BatchRunner::reserve(size_t n_req, size_t n_items)
     return true;
 }
 
-int BatchRunner::launch_graph(cudaStream_t stream, size_t bytes, int grid, uint32_t smem)
+cudaError_t BatchRunner::launch_kernel(cudaKernel_t jit, int grid, uint32_t smem, cudaStream_t stream)
 {
     auto* hdr = reinterpret_cast<BatchHeader*>(d_buf_);
     auto* reqs = reinterpret_cast<BatchRequest*>(d_buf_ + off_req_);
     auto* items = reinterpret_cast<uint2*>(d_buf_ + off_items_);
+    if (!jit) return launch_batch(hdr, reqs, d_states_, items, smem, grid, 256, stream);
+    BatchState* states = d_states_;
+    void* params[] = {&hdr, &reqs, &states, &items};
+    return cudaLaunchKernel((const void*)jit, dim3((unsigned)grid), dim3(256), params, 0, stream);
+}
+
+int BatchRunner::launch_graph(cudaStream_t stream, size_t bytes, int grid, uint32_t smem, cudaKernel_t jit)
+{
+    // Recapture when the kernel (interpreter <-> specialised module) or its launch
+    // shape changed; otherwise only the upload node is updated.  (Kernel nodes of
+    // library kernels cannot be read back with cudaGraphKernelNodeGetParams.)
+    if (exec_ && (graph_kernel_ != jit || graph_grid_ != grid || graph_smem_ != smem)) {
+        cudaGraphExecDestroy(exec_);
+        exec_ = nullptr;
+        if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
+    }
     if (!exec_) {
+        graph_kernel_ = jit;
+        graph_grid_ = grid;
+        graph_smem_ = smem;
         if (!capture_stream_ && !cuda_ok(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking), "stream")) return -3;
         if (!cuda_ok(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal), "begin capture")) return -3;
         cudaMemcpyAsync(d_buf_, h_buf_, bytes, cudaMemcpyHostToDevice, capture_stream_);
-        launch_batch(hdr, reqs, d_states_, items, smem, grid, 256, capture_stream_);
+        launch_kernel(jit, grid, smem, capture_stream_);
         if (!cuda_ok(cudaStreamEndCapture(capture_stream_, &graph_), "end capture")) return -3;
         if (!cuda_ok(cudaGraphInstantiate(&exec_, graph_, 0), "graph instantiate")) return -3;
         size_t n = 0;
@@ -96,11 +117,6 @@ int BatchRunner::launch_graph(cudaStream_t stream, size_t bytes, int grid, uint3
     } else {
         if (!cuda_ok(cudaGraphExecMemcpyNodeSetParams1D(exec_, copy_node_, d_buf_, h_buf_, bytes, cudaMemcpyHostToDevice), "graph memcpy update"))
             return -3;
-        cudaKernelNodeParams kp;
-        if (!cuda_ok(cudaGraphKernelNodeGetParams(kernel_node_, &kp), "graph kernel params")) return -3;
-        kp.gridDim = dim3((unsigned)grid);
-        kp.sharedMemBytes = smem;
-        if (!cuda_ok(cudaGraphExecKernelNodeSetParams(exec_, kernel_node_, &kp), "graph kernel update")) return -3;
     }
     return cuda_ok(cudaGraphLaunch(exec_, stream), "graph launch") ? 0 : -3;
 }
@@ -122,6 +138,15 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         points_ += (uint64_t)std::max(0ll, items[i].args.total);
     }
     signature_ = batch_signature(items, progs);
+    // Specialised batch kernel when the active module covers every program of the batch.
+    cudaKernel_t jit = nullptr;
+    std::vector<int> slots;
+    {
+        std::vector<uint64_t> hashes(n);
+        for (size_t i = 0; i < n; ++i) hashes[i] = progs[i].hash;
+        if (!jit_batch_slots(hashes, slots, jit)) jit = nullptr;
+    }
+    if (jit) signature_ = signature_ * 0x100000001B3ull + 0x4A17;   // tuned separately from the interpreter
     BatchTuning tuning;
     if (tuning_in) tuning = *tuning_in;
     else Autotuner::instance().lookup(signature_, tuning);
@@ -151,7 +176,7 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         std::memset(&r, 0, sizeof r);
         r.args = items[i].args;
         r.prog = progs[i].dptr;
-        r.jit_slot = -1;
+        r.jit_slot = jit ? slots[i] : -1;
         r.prog_bytes = progs[i].bytes;
         r.out = items[i].dout;
         r.minmax = items[i].dminmax;
@@ -166,22 +191,32 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         last_minmax_[i] = items[i].dminmax;
     }
     const size_t bytes = off_items_ + n_items * sizeof(uint2);
-    const int occ = tuning.ctas_per_sm > 0 ? tuning.ctas_per_sm : batch_occupancy(256, max_bytes);
+    int occ = tuning.ctas_per_sm;
+    if (occ <= 0 && jit) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)jit, 256, 0) != cudaSuccess || occ < 1) occ = 1;
+    } else if (occ <= 0) {
+        occ = batch_occupancy(256, max_bytes);
+    }
     long long grid = (long long)num_sms() * occ;
     if (grid > (long long)n_items) grid = (long long)n_items;
     if (grid < 1) grid = 1;
     int rc;
     if (use_graph) {
-        rc = launch_graph(stream, bytes, (int)grid, max_bytes);
+        rc = launch_graph(stream, bytes, (int)grid, max_bytes, jit);
     } else {
         rc = cuda_ok(cudaMemcpyAsync(d_buf_, h_buf_, bytes, cudaMemcpyHostToDevice, stream), "upload batch") &&
-                     cuda_ok(launch_batch(reinterpret_cast<BatchHeader*>(d_buf_), reinterpret_cast<BatchRequest*>(d_buf_ + off_req_),
-                                          d_states_, reinterpret_cast<uint2*>(d_buf_ + off_items_), max_bytes, (int)grid, 256, stream),
-                             "launch batch")
+                     cuda_ok(launch_kernel(jit, (int)grid, max_bytes, stream), "launch batch")
                  ? 0
                  : -3;
     }
-    if (rc == 0) cudaEventRecord(staged_, stream);
+    if (rc == 0) {
+        cudaEventRecord(staged_, stream);
+        items_ = n_items;
+        upload_bytes_ = bytes;
+        tile_points_ = tp;
+        grid_ = (int)grid;
+        specialised_ = jit != nullptr;
+    }
     return rc;
 }
 

@@ -46,10 +46,18 @@ public:
     const std::vector<float*>& last_device_minmax() const { return last_minmax_; }
     uint64_t last_signature() const { return signature_; }
     uint64_t last_points() const { return points_; }
+    // Shape of the last launch: work items, bytes uploaded, tile size, CTAs, kernel kind.
+    uint64_t last_items() const { return items_; }
+    uint64_t last_upload_bytes() const { return upload_bytes_; }
+    uint32_t last_tile_points() const { return tile_points_; }
+    int last_grid() const { return grid_; }
+    bool last_specialised() const { return specialised_; }
 
 private:
     bool reserve(size_t n_req, size_t n_items);
-    int launch_graph(cudaStream_t stream, size_t bytes, int grid, uint32_t smem);
+    int launch_graph(cudaStream_t stream, size_t bytes, int grid, uint32_t smem, cudaKernel_t jit);
+    // jit null = the interpreter's batch kernel
+    cudaError_t launch_kernel(cudaKernel_t jit, int grid, uint32_t smem, cudaStream_t stream);
 
     char* d_buf_ = nullptr;            // device: header | reqs | states | items
     char* h_buf_ = nullptr;            // pinned staging with the same layout
@@ -61,9 +69,16 @@ private:
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
     cudaGraphNode_t copy_node_ = nullptr, kernel_node_ = nullptr;
+    cudaKernel_t graph_kernel_ = nullptr;  // kernel the graph was captured with (null = interpreter)
+    int graph_grid_ = 0;                   // and its launch shape
+    uint32_t graph_smem_ = 0;
     std::vector<float*> last_minmax_;
     uint64_t signature_ = 0;
     uint64_t points_ = 0;
+    uint64_t items_ = 0, upload_bytes_ = 0;
+    uint32_t tile_points_ = 0;
+    int grid_ = 0;
+    bool specialised_ = false;
 };
 
 // Tuning cache keyed by a batch signature (program hashes and size classes).

@@ -9,9 +9,11 @@
 #include <cstring>
 #include <limits>
 #include <string>
+#include <vector>
 
 #include "../../include/FastNoise/FastNoise_C.h"
 #include "fn_batch.h"
+#include "fn_jit.h"
 #include "fn_runtime.h"
 #include "fn_server.h"
 #include "fn_static_scratch.h"
@@ -50,6 +52,16 @@ bool ensure(float*& buf, size_t& cap, size_t n)
     return true;
 }
 
+// Launch one generation call: the tree's specialised kernel when one is loaded,
+// the interpreter otherwise.
+cudaError_t launch_points(const DeviceProgram& prog, const PointArgs& args, float* out, MinMaxWork* work, float* dminmax,
+                          cudaStream_t stream)
+{
+    cudaError_t e;
+    if (jit_launch(prog.hash, args, out, work, dminmax, stream, e)) return e;
+    return launch_interpreter(prog.dptr, prog.bytes, args, out, work, dminmax, stream);
+}
+
 // Run one host-memory generation call end to end.
 void gen_host(const void* node, PointArgs args, float* out, float* minmax, const float* const* hpos)
 {
@@ -78,7 +90,7 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
             args.pos[k] = ctx->dpos[k];
         }
     }
-    if (!cuda_ok(launch_interpreter(prog.dptr, prog.bytes, args, ctx->dbuf, work, nullptr, ctx->stream), "launch")) { fill_nan(out, total, minmax); return; }
+    if (!cuda_ok(launch_points(prog, args, ctx->dbuf, work, nullptr, ctx->stream), "launch")) { fill_nan(out, total, minmax); return; }
     if (total > 0 && !cuda_ok(cudaMemcpyAsync(out, ctx->dbuf, (size_t)total * 4, cudaMemcpyDeviceToHost, ctx->stream), "copy output")) { fill_nan(out, total, minmax); return; }
     if (!cuda_ok(cudaMemcpyAsync(ctx->hminmax, work->result, 8, cudaMemcpyDeviceToHost, ctx->stream), "copy minmax") ||
         !cuda_ok(cudaStreamSynchronize(ctx->stream), "synchronize")) {
@@ -98,7 +110,7 @@ int gen_device(const void* node, PointArgs args, float* dout, float* dminmax, vo
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     MinMaxWork* work = work_for_stream(s);
     if (!work) return FN_ERR_CUDA;
-    if (!cuda_ok(launch_interpreter(prog.dptr, prog.bytes, args, dout, work, dminmax, s), "launch")) return FN_ERR_CUDA;
+    if (!cuda_ok(launch_points(prog, args, dout, work, dminmax, s), "launch")) return FN_ERR_CUDA;
     return FN_OK;
 }
 
@@ -793,6 +805,82 @@ int fnGenTileable2DDevice(const void* node, float* dOut, int xSize, int ySize, f
                           int seed, float* dMinMax, void* stream)
 {
     return gen_device(node, tile_args(xSize, ySize, xStepSize, yStepSize, seed), dOut, dMinMax, stream);
+}
+
+// ---------------------------------------------------------------- run-time specialisation
+namespace {
+int jit_programs(const void* const* nodes, const int* dims, int count, std::vector<CompiledProgram>& store,
+                 std::vector<const CompiledProgram*>& progs)
+{
+    if (!nodes || !dims || count <= 0) { set_error(FN_ERR_ARG, "invalid arguments"); return FN_ERR_ARG; }
+    store.resize((size_t)count);
+    for (int i = 0; i < count; ++i) {
+        std::string err;
+        if (!nodes[i] || dims[i] < 2 || dims[i] > 4) { set_error(FN_ERR_ARG, "invalid node or dimension"); return FN_ERR_ARG; }
+        if (!compile_program(N(nodes[i]), dims[i], store[(size_t)i], err)) { set_error(FN_ERR_COMPILE, err); return FN_ERR_COMPILE; }
+    }
+    for (auto& p : store) {
+        bool dup = false;
+        for (auto* q : progs) dup = dup || q->hash == p.hash;
+        if (!dup) progs.push_back(&p);
+    }
+    return FN_OK;
+}
+}  // namespace
+
+int fnGetBatchInfo(fnBatchInfo* info)
+{
+    clear_error();
+    if (!info) { set_error(FN_ERR_ARG, "null info"); return FN_ERR_ARG; }
+    std::memset(info, 0, sizeof *info);
+    if (!t_batch) return FN_OK;
+    const BatchRunner& r = t_batch->runner;
+    info->requests = (int)r.last_device_minmax().size();
+    info->specialised = r.last_specialised() ? 1 : 0;
+    info->tilePoints = (int)r.last_tile_points();
+    info->ctas = r.last_grid();
+    info->workItems = r.last_items();
+    info->points = r.last_points();
+    info->uploadBytes = r.last_upload_bytes();
+    return FN_OK;
+}
+
+int fnJitCompile(const void* const* nodes, const int* dims, int count)
+{
+    clear_error();
+    std::vector<CompiledProgram> store;
+    std::vector<const CompiledProgram*> progs;
+    int rc = jit_programs(nodes, dims, count, store, progs);
+    if (rc) return rc;
+    if (!thread_ctx()) return FN_ERR_CUDA;
+    for (int i = 0; i < count; ++i) {            // device copies for the interpreter paths (batch staging uses them)
+        DeviceProgram dp;
+        if (!get_program(N(nodes[i]), dims[i], dp)) return last_error();
+    }
+    std::string err;
+    if (!jit_build(progs, err)) { set_error(FN_ERR_COMPILE, err); return FN_ERR_COMPILE; }
+    return FN_OK;
+}
+
+int fnJitCheck(const void* const* nodes, const int* dims, int count, int* cubinBytes)
+{
+    clear_error();
+    std::vector<CompiledProgram> store;
+    std::vector<const CompiledProgram*> progs;
+    int rc = jit_programs(nodes, dims, count, store, progs);
+    if (rc) return rc;
+    std::vector<char> cubin;
+    std::string log;
+    if (!jit_compile_cubin(jit_module_source(progs), cubin, log)) { set_error(FN_ERR_COMPILE, "NVRTC: " + log.substr(0, 4000)); return FN_ERR_COMPILE; }
+    if (cubinBytes) *cubinBytes = (int)cubin.size();
+    return FN_OK;
+}
+
+int fnSetJitEnabled(int enabled)
+{
+    const int was = jit_enabled() ? 1 : 0;
+    jit_set_enabled(enabled != 0);
+    return was;
 }
 
 // Allocation-free 3D grid: the program is compiled on the host (cached per

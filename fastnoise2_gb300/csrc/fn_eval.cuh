@@ -13,7 +13,8 @@ using fnd::cvtf;
 using fnd::fmax_;
 using fnd::fmin_;
 
-constexpr float kInf = __builtin_huge_valf();
+// +infinity (a bit pattern, so that NVRTC, which lacks the compiler builtins, accepts it)
+__device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
 
 // Root position of point i (Generator.inl:104-105, 160-162, 225-228, 295-297, 400-406).
 __device__ __forceinline__ void root_position(const fn::PointArgs& a, long long i, float* R)
@@ -87,7 +88,7 @@ __device__ __forceinline__ void grid_minmax(float mn, float mx, fn::MinMaxWork* 
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    mn = kInf; mx = -kInf;
+    mn = inf(); mx = -inf();
     for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
         mn = fmin_(mn, __ldcg(&work->partial[2 * b]));
         mx = fmax_(mx, __ldcg(&work->partial[2 * b + 1]));
@@ -126,8 +127,8 @@ __device__ __forceinline__ void finish_tile(const fn::BatchRequest& rq, fn::Batc
     if (done + 1 == rq.n_tiles) {
         __threadfence();
         const unsigned int me = atomicAdd(&st->mn_enc, 0u), xe = atomicAdd(&st->mx_enc, 0u);
-        const float fmn = me == 0xFFFFFFFFu ? kInf : dec_ordered(me);
-        const float fmx = xe == 0u ? -kInf : dec_ordered(xe);
+        const float fmn = me == 0xFFFFFFFFu ? inf() : dec_ordered(me);
+        const float fmx = xe == 0u ? -inf() : dec_ordered(xe);
         if (rq.minmax) { rq.minmax[0] = fmn; rq.minmax[1] = fmx; }
         if (rq.host_minmax) {
             volatile float* hm = rq.host_minmax;

@@ -1,0 +1,518 @@
+// fn_jit.cpp -- code generation, NVRTC compilation and the module registry of
+// the run-time specialised kernels (see fn_jit.h).
+#include "fn_jit.h"
+
+#include <nvrtc.h>
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <sstream>
+#include <unordered_map>
+
+#include "fn_kernels.cuh"
+#include "fn_runtime.h"
+
+namespace fn {
+
+// The device headers (fn_types.h, fn_device.cuh, fn_eval.cuh) as one source
+// string; the file defining it is generated at build time (build.py).
+const char* embedded_device_source();
+
+namespace {
+
+std::string lit(float f)
+{
+    char b[64];
+    if (std::isfinite(f)) {
+        std::snprintf(b, sizeof b, "%af", (double)f);         // exact hexadecimal literal
+    } else {
+        uint32_t u;
+        std::memcpy(&u, &f, 4);
+        std::snprintf(b, sizeof b, "__int_as_float(0x%08xu)", u);
+    }
+    return b;
+}
+
+std::string r(int i) { return "r" + std::to_string(i); }
+
+const char* noise_fn(int kind)
+{
+    switch (kind) {
+    case FN_NOISE_SIMPLEX: return "simplex";
+    case FN_NOISE_SUPERSIMPLEX: return "supersimplex";
+    case FN_NOISE_PERLIN: return "perlin";
+    default: return "value";
+    }
+}
+
+// One program -> `__device__ float fnjit_eval_<k>(int seed, float x, float y, float z, float w)`.
+void emit_eval(const CompiledProgram& prog, int k, std::ostringstream& o)
+{
+    const FnProgramHeader* h = reinterpret_cast<const FnProgramHeader*>(prog.blob.data());
+    const FnInstr* ins = fn_program_instrs(h);
+    const float* P = fn_program_params(h);
+    const int nregs = h->n_regs;
+    o << "__device__ __noinline__ float fnjit_eval_" << k << "(int seed, float x, float y, float z, float w)\n{\n";
+    o << "    (void)x; (void)y; (void)z; (void)w;\n";
+    const char* root[4] = {"x", "y", "z", "w"};
+    for (int i = 0; i < nregs; ++i) o << "    float " << r(i) << " = " << (i < h->dim ? root[i] : "0.0f") << ";\n";
+    for (int pc = 0; pc < h->n_instr; ++pc) {
+        const FnInstr& I = ins[pc];
+        const int D = I.dim;
+        const std::string sd = "fnd::iadd(seed, " + std::to_string(I.seed) + ")";
+        auto p = [&](int j) { return lit(P[I.prm + j]); };
+        auto pos = [&](int base) {
+            std::string s = "{";
+            for (int j = 0; j < D; ++j) s += (j ? ", " : "") + r(base + j);
+            return s + "}";
+        };
+        auto cellp = [&](int mk_index) {
+            std::ostringstream c;
+            c << "fnd::CellParams cp; cp.freq = " << p(0) << "; cp.jitter = fnd::CellConst<" << D << ">::jitter * " << r(I.b)
+              << "; cp.sizeActive = " << (I.c != FN_REG_NONE ? "true" : "false") << "; cp.sizeJitter = "
+              << (I.c != FN_REG_NONE ? r(I.c) + " * fnd::CellConst<" + std::to_string(D) + ">::size" : std::string("0.0f"))
+              << "; cp.distFunc = " << (I.aux & 15) << "; cp.minkowski = " << p(mk_index) << ";";
+            return c.str();
+        };
+        o << "    { // op " << (int)I.op << "\n";
+        switch (I.op) {
+        case FN_OP_CONST: o << "        " << r(I.dst) << " = " << p(0) << ";\n"; break;
+        case FN_OP_MOV: o << "        " << r(I.dst) << " = " << r(I.a) << ";\n"; break;
+        case FN_OP_SCALE_POS:
+            for (int j = 0; j < D; ++j) o << "        const float t" << j << " = " << r(I.a + j) << " * " << p(0) << ";\n";
+            for (int j = 0; j < D; ++j) o << "        " << r(I.dst + j) << " = t" << j << ";\n";
+            break;
+        case FN_OP_SCALE_POS_V:
+            for (int j = 0; j < D; ++j) o << "        const float t" << j << " = " << r(I.a + j) << " * " << p(j) << ";\n";
+            for (int j = 0; j < D; ++j) o << "        " << r(I.dst + j) << " = t" << j << ";\n";
+            break;
+        case FN_OP_OFFSET_POS: case FN_OP_SUB_POS: {
+            const int off[4] = {I.b, I.c, I.d, I.e};
+            const char* opch = I.op == FN_OP_OFFSET_POS ? " + " : " - ";
+            for (int j = 0; j < D; ++j) o << "        const float t" << j << " = " << r(I.a + j) << opch << r(off[j]) << ";\n";
+            for (int j = 0; j < D; ++j) o << "        " << r(I.dst + j) << " = t" << j << ";\n";
+            break;
+        }
+        case FN_OP_ROTATE2:
+            o << "        const float px = " << r(I.a) << ", py = " << r(I.a + 1) << ";\n";
+            o << "        " << r(I.dst) << " = fmaf(-py, " << p(1) << ", px * " << p(0) << ");\n";
+            o << "        " << r(I.dst + 1) << " = fmaf(px, " << p(1) << ", py * " << p(0) << ");\n";
+            break;
+        case FN_OP_ROTATE3:
+            o << "        const float px = " << r(I.a) << ", py = " << r(I.a + 1) << ", pz = " << (D >= 3 ? r(I.a + 2) : "0.0f") << ";\n";
+            for (int j = 0; j < 3; ++j)
+                o << "        const float n" << j << " = fmaf(px, " << p(3 * j) << ", fmaf(py, " << p(3 * j + 1) << ", pz * " << p(3 * j + 2) << "));\n";
+            for (int j = 0; j < 3; ++j) o << "        " << r(I.dst + j) << " = n" << j << ";\n";
+            break;
+        case FN_OP_ROTPLANE:
+            o << "        float px = " << r(I.a) << ", py = " << r(I.a + 1) << ", pz = " << (D >= 3 ? r(I.a + 2) : "0.0f") << ";\n";
+            if (D == 4) o << "        const float pw = " << r(I.a + 3) << ";\n";
+            o << "        fnd::rotate_plane(" << I.aux << ", px, py, pz);\n";
+            o << "        " << r(I.dst) << " = px; " << r(I.dst + 1) << " = py; " << r(I.dst + 2) << " = pz;\n";
+            if (D == 4) o << "        " << r(I.dst + 3) << " = pw;\n";
+            break;
+        case FN_OP_NOISE: {
+            o << "        const float f = " << p(0) << ";\n";
+            o << "        " << r(I.dst) << " = fnd::scale_out(fnd::" << noise_fn(I.aux) << D << "(" << sd;
+            for (int j = 0; j < D; ++j) o << ", " << r(I.a + j) << " * f";
+            o << "), " << p(1) << ", " << p(2) << ", " << p(3) << ");\n";
+            break;
+        }
+        case FN_OP_WHITE:
+            o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n";
+            o << "        " << r(I.dst) << " = fnd::scale_out(fnd::white<" << D << ">(" << sd << ", pp), -fnd::kValueBounds, " << p(0) << ", " << p(1) << ");\n";
+            break;
+        case FN_OP_CHECKER:
+            o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n";
+            o << "        " << r(I.dst) << " = fnd::scale_out(fnd::checkerboard<" << D << ">(pp, " << p(0) << "), 0.0f, " << p(1) << ", " << p(2) << ");\n";
+            break;
+        case FN_OP_SINE:
+            o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n";
+            o << "        " << r(I.dst) << " = fnd::scale_out(fnd::sine_wave<" << D << ">(pp, " << p(0) << "), -1.0f, " << p(1) << ", " << p(2) << ");\n";
+            break;
+        case FN_OP_CELL_VALUE:
+            o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n        " << cellp(3) << "\n";
+            o << "        " << r(I.dst) << " = fnd::scale_out(fnd::cellular_value<" << D << ">(" << sd << ", pp, cp, " << ((I.aux >> 4) & 3)
+              << "), -fnd::kValueBounds, " << p(1) << ", " << p(2) << ");\n";
+            break;
+        case FN_OP_CELL_DIST:
+            o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n        " << cellp(3) << "\n";
+            o << "        float dist[4]; fnd::cellular_distances<" << D << ">(" << sd << ", pp, cp, dist);\n";
+            o << "        float nmax; const float v = fnd::cellular_return<" << D << ">(dist, cp.distFunc, " << ((I.aux >> 4) & 3) << ", "
+              << ((I.aux >> 8) & 3) << ", " << ((I.aux >> 12) & 7) << ", nmax);\n";
+            o << "        " << r(I.dst) << " = fnd::scale_out(v, 0.0f, " << p(1) << ", " << p(2) << ");\n";
+            break;
+        case FN_OP_CELL_LOOKUP:
+            o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n        " << cellp(2) << "\n";
+            o << "        float oo[" << D << "]; fnd::cellular_lookup_pos<" << D << ">(" << sd << ", pp, cp, " << p(1) << ", oo);\n";
+            for (int j = 0; j < D; ++j) o << "        " << r(I.dst + j) << " = oo[" << j << "];\n";
+            break;
+        case FN_OP_WARP_GRAD:
+            o << "        const float f = " << p(0) << ";\n";
+            o << "        float sp[" << D << "], io[" << D << "];\n";
+            for (int j = 0; j < D; ++j) o << "        sp[" << j << "] = " << r(I.a + j) << " * f; io[" << j << "] = " << r(I.dst + j) << ";\n";
+            o << "        const float axis[" << D << "] = {";
+            for (int j = 0; j < D; ++j) o << (j ? ", " : "") << p(1 + j);
+            o << "};\n        const float st = fnd::warp_gradient<" << D << ">(" << sd << ", " << r(I.b) << ", sp, axis, io);\n";
+            for (int j = 0; j < D; ++j) o << "        " << r(I.dst + j) << " = io[" << j << "];\n";
+            if (I.c != FN_REG_NONE) o << "        " << r(I.c) << " = st;\n";
+            else o << "        (void)st;\n";
+            break;
+        case FN_OP_FRACT_INIT:
+            if (I.aux) o << "        const float nz = fnd::fabs_(" << r(I.a) << "); " << r(I.a) << " = nz; " << r(I.dst) << " = (nz * -2.0f + 1.0f) * 1.0f;\n";
+            else o << "        " << r(I.dst) << " = " << r(I.a) << " * 1.0f;\n";
+            o << "        " << r(I.b) << " = 1.0f;\n";
+            break;
+        case FN_OP_FRACT_AMP:
+            o << "        const float t = " << (I.aux ? "1.0f - " + r(I.a) : "(" + r(I.a) + " + 1.0f) * 0.5f") << ";\n";
+            o << "        const float amp = " << r(I.b) << " * fnd::lerp(1.0f, t, " << r(I.c) << ");\n";
+            o << "        " << r(I.b) << " = amp * " << r(I.d) << ";\n";
+            break;
+        case FN_OP_FRACT_ACC:
+            if (I.aux) o << "        const float nz = fnd::fabs_(" << r(I.a) << "); " << r(I.a) << " = nz; " << r(I.dst) << " = " << r(I.dst) << " + (nz * -2.0f + 1.0f) * " << r(I.b) << ";\n";
+            else o << "        " << r(I.dst) << " = " << r(I.dst) << " + " << r(I.a) << " * " << r(I.b) << ";\n";
+            break;
+        case FN_OP_DWF_AMP:
+            o << "        const float s = sqrtf(" << r(I.a) << "); " << r(I.a) << " = s;\n";
+            o << "        const float amp = " << r(I.b) << " * fnd::lerp(1.0f, 1.0f - s, " << r(I.c) << ");\n";
+            o << "        " << r(I.b) << " = amp * " << r(I.d) << ";\n";
+            break;
+        case FN_OP_ADD: o << "        " << r(I.dst) << " = " << r(I.a) << " + " << r(I.b) << ";\n"; break;
+        case FN_OP_SUB: o << "        " << r(I.dst) << " = " << r(I.a) << " - " << r(I.b) << ";\n"; break;
+        case FN_OP_MUL: o << "        " << r(I.dst) << " = " << r(I.a) << " * " << r(I.b) << ";\n"; break;
+        case FN_OP_DIV: o << "        " << r(I.dst) << " = " << r(I.a) << " / " << r(I.b) << ";\n"; break;
+        case FN_OP_MOD: o << "        " << r(I.dst) << " = fnd::mod_(" << r(I.a) << ", " << r(I.b) << ");\n"; break;
+        case FN_OP_MIN: o << "        " << r(I.dst) << " = fnd::fmin_(" << r(I.a) << ", " << r(I.b) << ");\n"; break;
+        case FN_OP_MAX: o << "        " << r(I.dst) << " = fnd::fmax_(" << r(I.a) << ", " << r(I.b) << ");\n"; break;
+        case FN_OP_ABS: o << "        " << r(I.dst) << " = fnd::fabs_(" << r(I.a) << ");\n"; break;
+        case FN_OP_SSQRT: o << "        " << r(I.dst) << " = fnd::signed_sqrt(" << r(I.a) << ");\n"; break;
+        case FN_OP_POWF: o << "        " << r(I.dst) << " = fnd::pow_(fnd::fmax_(fnd::fabs_(" << r(I.a) << "), 1.17549435e-38f), " << r(I.b) << ");\n"; break;
+        case FN_OP_POWI:
+            o << "        const float v = " << r(I.a) << "; float pw = v * v;\n";
+            o << "        for (int i = 2; i < " << I.aux << "; ++i) pw *= v;\n        " << r(I.dst) << " = pw;\n";
+            break;
+        case FN_OP_MINSMOOTH: o << "        " << r(I.dst) << " = fnd::min_smooth(" << r(I.a) << ", " << r(I.b) << ", " << r(I.c) << ");\n"; break;
+        case FN_OP_MAXSMOOTH: o << "        " << r(I.dst) << " = -fnd::min_smooth(-" << r(I.a) << ", -" << r(I.b) << ", " << r(I.c) << ");\n"; break;
+        case FN_OP_FADE:
+            o << "        " << r(I.dst) << " = fnd::lerp(" << r(I.a) << ", " << r(I.b) << ", fnd::fade_t(" << r(I.c) << ", " << r(I.d) << ", " << r(I.e)
+              << ", " << I.aux << "));\n";
+            break;
+        case FN_OP_REMAP:
+            o << "        " << r(I.dst) << " = fnd::remap(" << r(I.a) << ", " << r(I.b) << ", " << r(I.c) << ", " << r(I.d) << ", " << r(I.e) << ", "
+              << (I.aux ? "true" : "false") << ");\n";
+            break;
+        case FN_OP_TERRACE:
+            o << "        const float src = " << r(I.a) << " * " << p(0) << ";\n        float rounded = rintf(src);\n";
+            if (I.b != FN_REG_NONE)
+                o << "        const float sm = " << r(I.b) << ";\n        if (sm != 0.0f) rounded = fnd::terrace_smooth(rounded, src, 1.0f + 1.0f / sm);\n";
+            else if (I.aux)
+                o << "        rounded = fnd::terrace_smooth(rounded, src, " << p(2) << ");\n";
+            o << "        " << r(I.dst) << " = rounded * " << p(1) << ";\n";
+            break;
+        case FN_OP_PINGPONG: o << "        " << r(I.dst) << " = fnd::ping_pong(" << r(I.a) << " * " << r(I.b) << ");\n"; break;
+        case FN_OP_RGBA8: o << "        " << r(I.dst) << " = fnd::to_rgba8(" << r(I.a) << ", " << p(0) << ", " << p(1) << ");\n"; break;
+        case FN_OP_GRADIENT: {
+            const int off[4] = {I.b, I.c, I.d, I.e};
+            o << "        float acc = 0.0f;\n";
+            for (int j = 0; j < D; ++j) o << "        acc = fmaf(" << r(I.a + j) << " + " << r(off[j]) << ", " << p(j) << ", acc);\n";
+            o << "        " << r(I.dst) << " = acc;\n";
+            break;
+        }
+        case FN_OP_DISTANCE:
+            o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n";
+            o << "        " << r(I.dst) << " = fnd::distance<" << D << ">(" << (I.aux & 15) << ", " << (((I.aux >> 4) & 1) ? "true" : "false")
+              << ", pp, " << (I.b != FN_REG_NONE ? r(I.b) : std::string("0.0f")) << ");\n";
+            break;
+        default:
+            o << "        // unsupported op\n";
+            break;
+        }
+        o << "    }\n";
+    }
+    o << "    return " << r(h->out_reg) << ";\n}\n\n";
+}
+
+// Per-call kernels for program k: grid / position array / tileable.
+//
+// Each warp owns chunks of 32*ppl consecutive points (ppl = points per lane,
+// 1..4, chosen by the host).  Lane l evaluates points chunk + 32*t + l
+// (t < ppl, one point at a time, so the tree's code is not replicated) and
+// parks the values in shared memory; with ppl == 4 the warp then writes the
+// chunk as 32 float4 stores (512 contiguous bytes per warp).  Small calls use
+// ppl == 1 so that their few points spread over as many SMs as possible.
+void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
+{
+    const int D = prog.dim;
+    const char* pv[4] = {"px", "py", "pz", "pw"};
+    std::string call = "fnjit_eval_" + std::to_string(k) + "(A.seed";
+    for (int j = 0; j < 4; ++j) call += std::string(", ") + (j < D ? pv[j] : "0.0f");
+    call += ")";
+
+    auto kernel = [&](const char* name, const std::string& prologue, const std::string& position) {
+        o << "extern \"C\" __global__ void __launch_bounds__(256, 2) " << name << "_" << k
+          << "(fn::PointArgs A, float* __restrict__ out, fn::MinMaxWork* work, float* dminmax, unsigned ppl)\n{\n"
+          << "    __shared__ float4 stage[8][32];\n"
+          << "    __shared__ float smn[8], smx[8];\n"
+          << "    float mn = fne::inf(), mx = -fne::inf();\n"
+          << "    const unsigned total = (unsigned)A.total;\n"
+          << "    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;\n"
+          << "    const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;\n"
+          << "    const bool aligned = (((unsigned long long)out) & 15ull) == 0;\n"
+          << "    float* st = reinterpret_cast<float*>(stage[warp]);\n"
+          << prologue
+          << "    const unsigned chunk = 32u * ppl;\n"
+          << "    for (unsigned base = (((blockIdx.x * blockDim.x) >> 5) + warp) * chunk; base < total; base += nwarps * chunk) {\n"
+          << "#pragma unroll 1\n"
+          << "        for (unsigned t = 0; t < ppl; ++t) {\n"
+          << "            const unsigned i = base + t * 32u + lane;\n"
+          << "            float v = 0.0f;\n"
+          << "            if (i < total) {\n"
+          << position
+          << "                v = " << call << ";\n"
+          << "                fne::fold(v, mn, mx);\n"
+          << "            }\n"
+          << "            st[t * 32u + lane] = v;\n"
+          << "        }\n"
+          << "        __syncwarp();\n"
+          << "        if (ppl == 4u && aligned && base + 128u <= total) {\n"
+          << "            reinterpret_cast<float4*>(out + base)[lane] = stage[warp][lane];\n"
+          << "        } else {\n"
+          << "            for (unsigned q = 0; q < ppl; ++q) {\n"
+          << "                const unsigned j = base + q * 32u + lane;\n"
+          << "                if (j < total) out[j] = st[q * 32u + lane];\n"
+          << "            }\n"
+          << "        }\n"
+          << "        __syncwarp();\n"
+          << "    }\n"
+          << "    fne::grid_minmax(mn, mx, work, dminmax, smn, smx);\n"
+          << "}\n\n";
+    };
+
+    // grid: Generator.inl:79-254, pos_k = fma(float(i_k), step_k, offset_k), x fastest
+    {
+        std::ostringstream pos;
+        pos << "                unsigned r = i;\n";
+        const char* ax = "xyzw";
+        for (int j = 0; j < D; ++j) {
+            if (j < D - 1) pos << "                const unsigned i" << ax[j] << " = r % A.count[" << j << "]; r /= A.count[" << j << "];\n";
+            else pos << "                const unsigned i" << ax[j] << " = r;\n";
+            pos << "                const float " << pv[j] << " = fmaf(fnd::cvtf((int)i" << ax[j] << "), A.step[" << j << "], A.offset[" << j << "]);\n";
+        }
+        kernel("fnjit_grid", "", pos.str());
+    }
+    // position arrays: Generator.inl:256-350, pos_k = offset_k + array_k[i]
+    {
+        std::ostringstream pos;
+        for (int j = 0; j < D; ++j) pos << "                const float " << pv[j] << " = A.offset[" << j << "] + __ldg(A.pos[" << j << "] + i);\n";
+        kernel("fnjit_pos", "", pos.str());
+    }
+    // tileable (4D programs): Generator.inl:370-433
+    if (D == 4) {
+        std::ostringstream pos;
+        pos << "                const unsigned ix = i % A.count[0], iy = i / A.count[0];\n"
+            << "                const float xf = fnd::cvtf((int)ix) * A.tmul[0];\n"
+            << "                const float yf = fnd::cvtf((int)iy) * A.tmul[1];\n"
+            << "                const float px = fnd::cos_(xf) * A.tfreq[0];\n"
+            << "                const float py = fnd::cos_(yf) * A.tfreq[1];\n"
+            << "                const float pz = fnd::sin_(xf) * A.tfreq[0];\n"
+            << "                const float pw = fnd::sin_(yf) * A.tfreq[1];\n";
+        kernel("fnjit_tile", "", pos.str());
+    }
+}
+
+void emit_batch(size_t n, std::ostringstream& o)
+{
+    o << "__device__ __forceinline__ float fnjit_eval_slot(int slot, int seed, const float* p)\n{\n    switch (slot) {\n";
+    for (size_t k = 0; k < n; ++k) o << "    case " << k << ": return fnjit_eval_" << k << "(seed, p[0], p[1], p[2], p[3]);\n";
+    o << "    default: return __int_as_float(0x7fc00000);\n    }\n}\n\n";
+    o << R"(extern "C" __global__ void __launch_bounds__(256) fnjit_batch(fn::BatchHeader* hdr, const fn::BatchRequest* __restrict__ reqs,
+                                                             fn::BatchState* states, const uint2* __restrict__ items)
+{
+    __shared__ unsigned int s_item;
+    __shared__ float smn[8], smx[8];
+    const unsigned int n_items = hdr->n_items;
+    const unsigned int tile_points = hdr->tile_points;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&hdr->head, 1u);
+        __syncthreads();
+        const unsigned int it = s_item;
+        __syncthreads();
+        if (it >= n_items) break;
+        const uint2 item = items[it];
+        const fn::BatchRequest& rq = reqs[item.x];
+        const fn::PointArgs args = rq.args;
+        const int slot = rq.jit_slot;
+        const long long begin = (long long)item.y * tile_points;
+        long long end = begin + tile_points;
+        if (end > args.total) end = args.total;
+        float mn = fne::inf(), mx = -fne::inf();
+        for (long long i = begin + threadIdx.x; i < end; i += blockDim.x) {
+            float pos[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            fne::root_position(args, i, pos);
+            const float v = fnjit_eval_slot(slot, args.seed, pos);
+            rq.out[i] = v;
+            fne::fold(v, mn, mx);
+        }
+        fne::block_minmax(mn, mx, smn, smx);
+        if (threadIdx.x == 0) fne::finish_tile(rq, states + item.x, hdr, mn, mx);
+    }
+}
+)";
+}
+
+struct Module {
+    cudaLibrary_t lib = nullptr;
+    std::vector<uint64_t> hashes;
+};
+
+std::mutex g_jit_mu;
+std::unordered_map<uint64_t, JitKernels> g_kernels;
+std::vector<std::unique_ptr<Module>> g_modules;
+cudaKernel_t g_batch_kernel = nullptr;
+std::unordered_map<uint64_t, int> g_batch_slots;
+std::atomic<bool> g_enabled{true};
+
+}  // namespace
+
+std::string jit_module_source(const std::vector<const CompiledProgram*>& progs)
+{
+    std::ostringstream o;
+    o << "// generated by fn_jit.cpp\n";
+    o << embedded_device_source() << "\n";
+    for (size_t k = 0; k < progs.size(); ++k) emit_eval(*progs[k], (int)k, o);
+    for (size_t k = 0; k < progs.size(); ++k) emit_percall(*progs[k], (int)k, o);
+    emit_batch(progs.size(), o);
+    return o.str();
+}
+
+bool jit_compile_cubin(const std::string& src, std::vector<char>& cubin, std::string& log)
+{
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, src.c_str(), "fastnoise_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
+        log = "nvrtcCreateProgram failed";
+        return false;
+    }
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-fmad=false", "--std=c++17", "-default-device", "-lineinfo",
+                          "-diag-suppress=177"};
+    nvrtcResult rc = nvrtcCompileProgram(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+    size_t loglen = 0;
+    nvrtcGetProgramLogSize(prog, &loglen);
+    log.assign(loglen, '\0');
+    if (loglen) nvrtcGetProgramLog(prog, &log[0]);
+    if (rc != NVRTC_SUCCESS) {
+        nvrtcDestroyProgram(&prog);
+        return false;
+    }
+    size_t n = 0;
+    nvrtcGetCUBINSize(prog, &n);
+    cubin.resize(n);
+    nvrtcGetCUBIN(prog, cubin.data());
+    nvrtcDestroyProgram(&prog);
+    return true;
+}
+
+bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& error)
+{
+    if (progs.empty()) return true;
+    const std::string src = jit_module_source(progs);
+    std::vector<char> cubin;
+    std::string log;
+    if (!jit_compile_cubin(src, cubin, log)) { error = "NVRTC: " + log.substr(0, 2000); return false; }
+    auto mod = std::make_unique<Module>();
+    cudaError_t e = cudaLibraryLoadData(&mod->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+    if (e != cudaSuccess) { error = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e); return false; }
+    std::unordered_map<uint64_t, JitKernels> found;
+    for (size_t k = 0; k < progs.size(); ++k) {
+        JitKernels jk;
+        jk.slot = (int)k;
+        std::string ks = std::to_string(k);
+        if (cudaLibraryGetKernel(&jk.grid, mod->lib, ("fnjit_grid_" + ks).c_str()) != cudaSuccess ||
+            cudaLibraryGetKernel(&jk.positions, mod->lib, ("fnjit_pos_" + ks).c_str()) != cudaSuccess) {
+            error = "kernel lookup failed";
+            return false;
+        }
+        if (progs[k]->dim == 4) cudaLibraryGetKernel(&jk.tileable, mod->lib, ("fnjit_tile_" + ks).c_str());
+        found[progs[k]->hash] = jk;
+        mod->hashes.push_back(progs[k]->hash);
+    }
+    cudaKernel_t batch = nullptr;
+    if (cudaLibraryGetKernel(&batch, mod->lib, "fnjit_batch") != cudaSuccess) { error = "batch kernel lookup failed"; return false; }
+    std::lock_guard<std::mutex> lk(g_jit_mu);
+    for (auto& kv : found) g_kernels[kv.first] = kv.second;
+    g_batch_kernel = batch;
+    g_batch_slots.clear();
+    for (auto& kv : found) g_batch_slots[kv.first] = kv.second.slot;
+    g_modules.push_back(std::move(mod));      // modules stay loaded: kernels may still be queued
+    return true;
+}
+
+bool jit_lookup(uint64_t hash, JitKernels& out)
+{
+    if (!g_enabled.load(std::memory_order_relaxed)) return false;
+    std::lock_guard<std::mutex> lk(g_jit_mu);
+    auto it = g_kernels.find(hash);
+    if (it == g_kernels.end()) return false;
+    out = it->second;
+    return true;
+}
+
+bool jit_batch_kernel(cudaKernel_t& kernel)
+{
+    if (!g_enabled.load(std::memory_order_relaxed)) return false;
+    std::lock_guard<std::mutex> lk(g_jit_mu);
+    kernel = g_batch_kernel;
+    return kernel != nullptr;
+}
+
+bool jit_batch_slots(const std::vector<uint64_t>& hashes, std::vector<int>& slots, cudaKernel_t& kernel)
+{
+    if (!g_enabled.load(std::memory_order_relaxed)) return false;
+    std::lock_guard<std::mutex> lk(g_jit_mu);
+    if (!g_batch_kernel) return false;
+    slots.resize(hashes.size());
+    for (size_t i = 0; i < hashes.size(); ++i) {
+        auto it = g_batch_slots.find(hashes[i]);
+        if (it == g_batch_slots.end()) return false;
+        slots[i] = it->second;
+    }
+    kernel = g_batch_kernel;
+    return true;
+}
+
+int jit_batch_slot(uint64_t hash)
+{
+    std::lock_guard<std::mutex> lk(g_jit_mu);
+    auto it = g_batch_slots.find(hash);
+    return it == g_batch_slots.end() ? -1 : it->second;
+}
+
+void jit_set_enabled(bool on) { g_enabled.store(on); }
+bool jit_enabled() { return g_enabled.load(); }
+
+bool jit_launch(uint64_t hash, const PointArgs& args, float* out, MinMaxWork* work, float* dminmax, cudaStream_t stream,
+                cudaError_t& err)
+{
+    err = cudaSuccess;
+    JitKernels jk;
+    if (args.total <= 0 || args.total > (1ll << 31) || !jit_lookup(hash, jk)) return false;
+    cudaKernel_t k = args.src == kSrcGrid ? jk.grid : args.src == kSrcPositions ? jk.positions : jk.tileable;
+    if (!k) return false;
+    // 4 points per lane (float4 stores) when that still gives every SM a few
+    // warps; 1 point per lane for small calls, which are latency-bound.
+    unsigned ppl = args.total >= (long long)num_sms() * 8 * 128 * 4 ? 4u : 1u;
+    const long long chunks = (args.total + 32 * ppl - 1) / (32 * ppl);   // one warp per chunk
+    long long blocks = (chunks + 7) / 8;
+    const long long cap = (long long)num_sms() * 8;              // beyond this the warps stride over the chunks
+    if (blocks > cap) blocks = cap;
+    if (blocks > kMaxReduceBlocks) blocks = kMaxReduceBlocks;
+    if (blocks < 1) blocks = 1;
+    PointArgs a = args;
+    void* params[] = {&a, &out, &work, &dminmax, &ppl};
+    err = cudaLaunchKernel((const void*)k, dim3((unsigned)blocks), dim3(256), params, 0, stream);
+    return true;
+}
+
+}  // namespace fn

@@ -1,0 +1,61 @@
+// fn_jit.h -- run-time specialised kernels.
+//
+// The interpreter (fn_kernels.cu) evaluates any tree but pays for dispatch and
+// for a register file in local memory.  For trees that will be evaluated many
+// times, the same device program is turned into straight-line CUDA source --
+// one call per instruction to the hand-written node functions of
+// fn_device.cuh, positions and values in registers, parameters as literals --
+// and compiled for sm_103a with NVRTC (-fmad=false, so results are identical
+// to the interpreter's).  A module holds, per tree, grid / position-array /
+// tileable per-call kernels, plus one batch kernel that dispatches on the
+// request's tree slot.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "fn_compile.h"
+#include "fn_types.h"
+
+namespace fn {
+
+struct JitKernels {
+    cudaKernel_t grid = nullptr;      // GenUniformGrid for the program's dimensionality
+    cudaKernel_t positions = nullptr; // GenPositionArray
+    cudaKernel_t tileable = nullptr;  // GenTileable2D (4D programs only)
+    int slot = -1;                    // index in the module's batch kernel
+};
+
+// Generate the CUDA source of a module for `progs` (exposed for tests/tools).
+std::string jit_module_source(const std::vector<const CompiledProgram*>& progs);
+
+// Compile and load a module covering `progs`; on success every program gets
+// per-call kernels and becomes the active batch module.  Thread safe.
+bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& error);
+
+// Kernels for a program hash, or false if none have been built.
+bool jit_lookup(uint64_t hash, JitKernels& out);
+
+// Active batch kernel and the slot of each program in it.
+bool jit_batch_kernel(cudaKernel_t& kernel);
+int jit_batch_slot(uint64_t hash);
+// All-or-nothing: the active batch kernel and the slot of every hash, read
+// under one lock (false if JIT is off or any program has no slot).
+bool jit_batch_slots(const std::vector<uint64_t>& hashes, std::vector<int>& slots, cudaKernel_t& kernel);
+
+// Launch the specialised per-call kernel for `hash` if one is loaded (and JIT
+// is enabled); returns false when the caller should use the interpreter.
+// `err` carries the launch status when true is returned.
+bool jit_launch(uint64_t hash, const PointArgs& args, float* out, MinMaxWork* work, float* dminmax, cudaStream_t stream,
+                cudaError_t& err);
+
+void jit_set_enabled(bool on);
+bool jit_enabled();
+
+// Compile NVRTC source for sm_103a to a cubin (host only; used by tests).
+bool jit_compile_cubin(const std::string& src, std::vector<char>& cubin, std::string& log);
+
+}  // namespace fn

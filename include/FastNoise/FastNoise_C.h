@@ -245,6 +245,34 @@ FASTNOISE_API int fnCompileInfo(const void* node, int dimension, int* nInstr, in
  * Generation calls do this on demand; calling it ahead moves the cost out of the first call. */
 FASTNOISE_API int fnPrepare(const void* node, int dimension);
 
+/* Shape of this thread's last fnGenBatchDevice launch (no counterpart in the reference). */
+typedef struct fnBatchInfo {
+    int requests;
+    int specialised;                /* 1 = the fnJitCompile batch kernel ran, 0 = the interpreter */
+    int tilePoints;                 /* points per work item */
+    int ctas;                       /* persistent CTAs launched */
+    unsigned long long workItems;   /* (request, tile) items in the device queue */
+    unsigned long long points;
+    unsigned long long uploadBytes; /* descriptor bytes copied host -> device for the launch */
+} fnBatchInfo;
+FASTNOISE_API int fnGetBatchInfo(fnBatchInfo* info);
+
+/* Run-time specialisation (no counterpart in the reference, whose trees run through
+ * virtual calls per SIMD block).  Each (node, dimension) pair is compiled to straight-line
+ * CUDA and built for sm_103a with NVRTC into one module: per-tree kernels for the grid,
+ * position-array and tileable calls, and one batch kernel covering all the listed trees.
+ * Later generation calls on these trees (host, device, batch and server paths) use the
+ * specialised kernels; results are bit-identical to the interpreter's.  Building takes
+ * seconds, so do it once at start-up.  A later call replaces the active batch module;
+ * per-tree kernels of earlier calls stay loaded.  Returns FN_OK or FN_ERR_*. */
+FASTNOISE_API int fnJitCompile(const void* const* nodes, const int* dimensions, int count);
+/* Generate and compile the module source with NVRTC without loading it (no GPU needed);
+ * *cubinBytes (may be NULL) receives the size of the compiled code. */
+FASTNOISE_API int fnJitCheck(const void* const* nodes, const int* dimensions, int count, int* cubinBytes);
+/* Turn the use of specialised kernels on (1, the default) or off (0, interpreter only).
+ * Returns the previous setting. */
+FASTNOISE_API int fnSetJitEnabled(int enabled);
+
 /* No counterpart in the reference.  fnGenUniformGrid3DDevice for callers that
  * cannot let the library allocate device memory: code running while a stream is
  * captured into a CUDA graph, applications whose own pool allocator owns all

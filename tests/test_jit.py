@@ -1,0 +1,126 @@
+"""Run-time specialised kernels (fnJitCompile): the generated straight-line CUDA
+compiles for sm_103a for every node kind in 2D/3D/4D (NVRTC runs on the host, so
+that part needs no GPU), and on the GPU its results equal the interpreter's bit
+for bit on every driver, alone and in batches."""
+import numpy as np
+import pytest
+
+from tests import chunkmix, trees
+from tests.parity import assert_parity
+from tests.test_gpu_parity import COMPOSITE, GRID, SINGLE
+
+ALL = {**SINGLE, **COMPOSITE}
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+def test_every_node_kind_compiles(native, dim):
+    fn = native
+    pairs = [(trees.to_product(m()), dim) for m in ALL.values()]
+    assert fn.jit_check(pairs) > 0
+
+
+def test_jit_rejects_bad_arguments(native):
+    fn = native
+    with pytest.raises(fn.FastNoiseError):
+        fn.jit_check([(trees.to_product(trees.simplex_c0()), 5)])
+
+
+@pytest.fixture(scope="module")
+def jit_all(gpu):
+    """Every test tree specialised in 2D/3D/4D (one module per dimensionality)."""
+    fn = gpu
+    nodes = {name: trees.to_product(m()) for name, m in ALL.items()}
+    for dim in (2, 3, 4):
+        fn.jit_compile([(n, dim) for n in nodes.values()])
+    yield fn, nodes
+    fn.set_jit_enabled(True)
+
+
+def _both(fn, call):
+    """Run `call` with the specialised kernels, then with the interpreter only."""
+    fn.set_jit_enabled(True)
+    a = call()
+    fn.set_jit_enabled(False)
+    try:
+        b = call()
+    finally:
+        fn.set_jit_enabled(True)
+    return a, b
+
+
+def _same(a, b, label):
+    (ga, ma), (gb, mb) = a, b
+    assert np.array_equal(np.asarray(ga).view(np.uint32), np.asarray(gb).view(np.uint32)), label
+    assert np.array_equal(np.asarray(ma, np.float32).view(np.uint32), np.asarray(mb, np.float32).view(np.uint32)), label
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3, 4])
+@pytest.mark.parametrize("name", sorted(ALL))
+def test_jit_grid_matches_interpreter(jit_all, name, dim):
+    fn, nodes = jit_all
+    off, cnt, st = GRID[dim]
+    a, b = _both(fn, lambda: nodes[name].gen_uniform_grid(off, cnt, st, 1337))
+    _same(a, b, f"{name} {dim}D")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [2, 3, 4])
+def test_jit_positions_match_interpreter(jit_all, dim):
+    fn, nodes = jit_all
+    rng = np.random.default_rng(dim)
+    pos = [rng.uniform(-1e4, 1e4, 3001).astype(np.float32) for _ in range(dim)]
+    for name in ("Simplex", "CellularDistanceSub", "Terrain", "WarpProgressive", "DomainRotate"):
+        a, b = _both(fn, lambda: nodes[name].gen_position_array(pos, (0.5,) * dim, -9))
+        _same(a, b, f"{name} {dim}D positions")
+    big = [rng.uniform(-1e4, 1e4, 700001).astype(np.float32) for _ in range(dim)]
+    a, b = _both(fn, lambda: nodes["Simplex"].gen_position_array(big, (0.5,) * dim, 3))
+    _same(a, b, f"Simplex {dim}D 700001 positions")
+
+
+@pytest.mark.gpu
+def test_jit_tileable_matches_oracle(jit_all):
+    from oracle.oracle import OracleTree
+    fn, nodes = jit_all
+    root = trees.terrain_c2()
+    g, gmm = nodes["Terrain"].gen_tileable_2d((96, 80), (1.0, 1.0), 7)
+    o, omm = OracleTree(root).tileable(96, 80, 1.0, 1.0, 7)
+    assert_parity(g, gmm, o, omm, label="terrain tileable (specialised)")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cnt", [(1, 1, 1), (5, 3, 2), (129, 1, 1), (16, 16, 16), (33, 17, 9), (97, 89, 73)])
+def test_jit_ragged_grids(jit_all, cnt):
+    """Chunk tails: sizes that are not multiples of the warp chunk (32 points per
+    warp for small calls, 128 with float4 stores from about 0.6 M points on)."""
+    fn, nodes = jit_all
+    a, b = _both(fn, lambda: nodes["FBm"].gen_uniform_grid((-3.0, 2.0, 1.0), cnt, (1.0, 1.0, 1.0), 42))
+    _same(a, b, str(cnt))
+
+
+@pytest.mark.gpu
+def test_jit_batch_matches_interpreter(gpu):
+    torch = pytest.importorskip("torch")
+    fn = gpu
+    nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
+    fn.jit_compile([(n, d) for n in nodes for d in (2, 3)])
+    chunks = chunkmix.make_mix(64, seed=5, sizes=[(16, 16, 16), (9, 7, 5), (32, 32), (50, 3), (0, 4, 4)])
+
+    def run():
+        outs, reqs, mms = [], [], []
+        for c in chunks:
+            out = torch.empty(max(c.points, 1), dtype=torch.float32, device="cuda")
+            mm = np.zeros(2, np.float32)
+            kind = fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D
+            reqs.append(fn.make_request(nodes[c.tree], kind, out.data_ptr(), c.seed, c.count, c.offset, (1, 1, 1, 1), minmax=mm))
+            outs.append(out)
+            mms.append(mm)
+        fn.autotune_batch(reqs)                      # several launches of one signature: graph updates
+        for _ in range(3):
+            fn.gen_batch(reqs, sync=True)
+        return [o.cpu().numpy()[:c.points] for o, c in zip(outs, chunks)], mms
+
+    (ja, jm), (ia, im) = _both(fn, run)
+    for c, x, y, mx, my in zip(chunks, ja, ia, jm, im):
+        assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), c
+        assert np.array_equal(mx.view(np.uint32), my.view(np.uint32)), c
