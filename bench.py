@@ -253,7 +253,7 @@ def run_chunkmix(a, rank, world, local):
     from tests import chunkmix, trees
 
     dev = torch.device("cuda", local)
-    chunks = chunkmix.make_mix(4096)
+    chunks = chunkmix.make_mix(4096)[:a.requests]
     nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
     pts = sum(c.points for c in chunks)
     out = torch.empty(pts, dtype=torch.float32, device=dev)
@@ -281,14 +281,18 @@ def run_chunkmix(a, rank, world, local):
         fn.gen_each(reqs, sptr, sync=False)
     torch.cuda.synchronize(dev)
 
-    def timed(fnc, steps):
+    def timed(fnc, steps, label):
+        # NVTX range per timed region, so a profiler can be limited to it
+        # (ncu --nvtx --nvtx-include "<label>/")
         st = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
         en = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
         for i in range(steps):
             flush.zero_()
+            torch.cuda.nvtx.range_push(label)
             st[i].record(stream)
             fnc()
             en[i].record(stream)
+            torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize(dev)
         return statistics.mean(s.elapsed_time(e) for s, e in zip(st, en))
 
@@ -296,16 +300,16 @@ def run_chunkmix(a, rank, world, local):
     with sampler:
         barrier(world)
         torch.cuda.synchronize(dev)
-        batch_ms = timed(lambda: fn.gen_batch(reqs, sptr, sync=False), a.steps)
-        percall_ms = timed(lambda: fn.gen_each(reqs, sptr, sync=False), max(2, a.steps // 2))
+        batch_ms = timed(lambda: fn.gen_batch(reqs, sptr, sync=False), a.steps, "batched")
+        percall_ms = timed(lambda: fn.gen_each(reqs, sptr, sync=False), max(2, a.steps // 2), "per_call")
         barrier(world)
     interp = None
     if a.kernels == "jit":                              # the same batch through the interpreter, for comparison
         fn.set_jit_enabled(False)
         fn.autotune_batch(reqs, sptr)
         fn.gen_batch(reqs, sptr, sync=True)
-        interp_ms = timed(lambda: fn.gen_batch(reqs, sptr, sync=False), max(2, a.steps // 2))
-        interp_pc_ms = timed(lambda: fn.gen_each(reqs, sptr, sync=False), 2)
+        interp_ms = timed(lambda: fn.gen_batch(reqs, sptr, sync=False), max(2, a.steps // 2), "interp_batched")
+        interp_pc_ms = timed(lambda: fn.gen_each(reqs, sptr, sync=False), 2, "interp_per_call")
         fn.set_jit_enabled(True)
         interp = {"batched": pts / (interp_ms * 1e-3) / 1e6, "per_call": pts / (interp_pc_ms * 1e-3) / 1e6,
                   "unit": "Mpoints/s", "note": "same mix, interpreter kernels (fnSetJitEnabled(0))"}
@@ -316,7 +320,7 @@ def run_chunkmix(a, rank, world, local):
 
     # served: closed loop (everything submitted at once), then open loop (Poisson arrivals)
     del flush
-    served = run_served(fn, chunks, nodes, rank, a, dev)
+    served = run_served(fn, chunks, nodes, rank, a, dev) if a.served else None
 
     # end to end: batched path + device->host copy of all outputs into pinned memory
     host = torch.empty(pts, dtype=torch.float32, pin_memory=True)
@@ -393,16 +397,15 @@ def run_served(fn, chunks, nodes, rank, a, dev):
         srv.release(t)
     srv.reset_stats()
     t0 = time.perf_counter()
-    tickets = [srv.submit(r) for r in reqs]
-    for t in tickets:
-        srv.wait(t)
+    tickets = srv.submit_many(reqs)             # one frame's worth of chunk requests at once
+    srv.wait_many(tickets)
     closed_s = time.perf_counter() - t0
     closed = srv.stats()
     for t in tickets:
         srv.release(t)
     result = {"closed_loop": {"value": pts / closed_s / 1e6, "unit": "Mpoints/s", "wall_ms": closed_s * 1e3,
                               "p50_ms": closed["p50Micros"] / 1e3, "p99_ms": closed["p99Micros"] / 1e3,
-                              "batches": closed["batches"]}}
+                              "batches": closed["batches"], "api": "fnServerSubmitMany + fnServerWaitMany"}}
     # open loop: the serving mix -- the chunk mix plus, every `extra_every` chunks, one
     # GenUniformGrid4D 32^4 and one GenPositionArray3D over 1M positions uniform in [-1e4, 1e4]^3
     import torch
@@ -493,9 +496,11 @@ def run_grid(a, rank, world, local):
         torch.cuda.synchronize(dev)
         for i in range(a.steps):
             flush.zero_()
+            torch.cuda.nvtx.range_push("timed")
             starts[i].record(stream)
             step()
             ends[i].record(stream)
+            torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize(dev)
         barrier(world)
     clocks = sampler.summary()
@@ -567,6 +572,10 @@ def main():
     ap.add_argument("--extra-every", type=int, default=64,
                     help="serving mix: one GenUniformGrid4D 32^4 and one GenPositionArray3D 1M request per this many chunks")
     ap.add_argument("--open-seconds", type=float, default=0.5)
+    ap.add_argument("--requests", type=int, default=4096,
+                    help="chunk mix: use the first N requests of the 4096-request mix (smaller cases for profiling)")
+    ap.add_argument("--no-served", dest="served", action="store_false",
+                    help="chunk mix: leave out the request-server measurements")
     a = ap.parse_args()
     if a.impl == "reference":
         run_reference(a)

@@ -116,6 +116,8 @@ def _declare(L):
         "fnServerDestroy": (None, [vp]),
         "fnServerSubmit": (c_int, [vp, vp, vp]),
         "fnServerPoll": (c_int, [vp, ctypes.c_ulonglong]),
+        "fnServerSubmitMany": (c_int, [vp, vp, c_int, vp]),
+        "fnServerWaitMany": (c_int, [vp, vp, c_int, c_int]),
         "fnServerWait": (c_int, [vp, ctypes.c_ulonglong, c_int, _FP, vp]),
         "fnServerCancel": (c_int, [vp, ctypes.c_ulonglong]),
         "fnServerRelease": (c_int, [vp, ctypes.c_ulonglong]),
@@ -284,6 +286,23 @@ class Server:
         if lib().fnServerSubmit(self._h, ctypes.byref(request), ctypes.byref(t)) != 0:
             _check()
         return t.value
+
+    def submit_many(self, requests) -> list:
+        """Queue many requests at once (all or nothing); returns their tickets."""
+        n = len(requests)
+        arr = (GenRequest * n)(*requests)
+        t = (ctypes.c_ulonglong * n)()
+        if lib().fnServerSubmitMany(self._h, arr, n, t) != 0:
+            _check()
+        return list(t)
+
+    def wait_many(self, tickets, timeout_ms: int = -1) -> None:
+        """Wait until every ticket has finished; raises FastNoiseError on failure or timeout."""
+        n = len(tickets)
+        t = (ctypes.c_ulonglong * n)(*tickets)
+        rc = lib().fnServerWaitMany(self._h, t, n, timeout_ms)
+        if rc != 0:
+            raise FastNoiseError(rc, lib().fnGetLastErrorString().decode())
 
     def poll(self, ticket: int) -> int:
         return lib().fnServerPoll(self._h, ticket)

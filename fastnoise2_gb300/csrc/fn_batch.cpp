@@ -144,7 +144,9 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
     {
         std::vector<uint64_t> hashes(n);
         for (size_t i = 0; i < n; ++i) hashes[i] = progs[i].hash;
-        if (!jit_batch_slots(hashes, slots, jit)) jit = nullptr;
+        bool fits = true;                           // the specialised kernel indexes points with 32 bits
+        for (size_t i = 0; i < n; ++i) fits = fits && items[i].args.total < (1ll << 32);
+        if (!fits || !jit_batch_slots(hashes, slots, jit)) jit = nullptr;
     }
     if (jit) signature_ = signature_ * 0x100000001B3ull + 0x4A17;   // tuned separately from the interpreter
     BatchTuning tuning;

@@ -667,6 +667,33 @@ int fnServerSubmit(void* server, const fnGenRequest* request, unsigned long long
     return rc;
 }
 
+int fnServerSubmitMany(void* server, const fnGenRequest* requests, int count, unsigned long long* tickets)
+{
+    clear_error();
+    if (!server || count < 0 || (count > 0 && (!requests || !tickets))) { set_error(FN_ERR_ARG, "invalid arguments"); return FN_ERR_ARG; }
+    std::vector<BatchItem> items((size_t)count);
+    for (int i = 0; i < count; ++i) {
+        items[i].node = N(requests[i].node);
+        if (!items[i].node || !request_args(requests[i], items[i].args)) {
+            set_error(FN_ERR_ARG, "request " + std::to_string(i) + ": invalid node, kind or positions");
+            return FN_ERR_ARG;
+        }
+        items[i].dout = requests[i].out;
+    }
+    std::vector<uint64_t> t((size_t)count);
+    int rc = static_cast<Server*>(server)->submit_many(items.data(), items.size(), t.data());
+    if (rc == 0) for (int i = 0; i < count; ++i) tickets[i] = t[i];
+    return rc;
+}
+
+int fnServerWaitMany(void* server, const unsigned long long* tickets, int count, int timeoutMs)
+{
+    clear_error();
+    if (!server || count < 0 || (count > 0 && !tickets)) { set_error(FN_ERR_ARG, "invalid arguments"); return FN_ERR_ARG; }
+    std::vector<uint64_t> t(tickets, tickets + count);
+    return static_cast<Server*>(server)->wait_many(t.data(), t.size(), timeoutMs);
+}
+
 int fnServerPoll(void* server, unsigned long long ticket)
 {
     return server ? static_cast<Server*>(server)->poll(ticket) : FN_ERR_ARG;
@@ -869,10 +896,12 @@ int fnJitCheck(const void* const* nodes, const int* dims, int count, int* cubinB
     std::vector<const CompiledProgram*> progs;
     int rc = jit_programs(nodes, dims, count, store, progs);
     if (rc) return rc;
-    std::vector<char> cubin;
-    std::string log;
-    if (!jit_compile_cubin(jit_module_source(progs), cubin, log)) { set_error(FN_ERR_COMPILE, "NVRTC: " + log.substr(0, 4000)); return FN_ERR_COMPILE; }
-    if (cubinBytes) *cubinBytes = (int)cubin.size();
+    std::vector<std::vector<char>> cubins;
+    std::string err;
+    if (!jit_compile_all(progs, cubins, err)) { set_error(FN_ERR_COMPILE, err); return FN_ERR_COMPILE; }
+    size_t bytes = 0;
+    for (auto& c : cubins) bytes += c.size();
+    if (cubinBytes) *cubinBytes = bytes > 0x7FFFFFFF ? 0x7FFFFFFF : (int)bytes;
     return FN_OK;
 }
 

@@ -123,6 +123,15 @@ public:
 
     static int32_t sadd(int32_t a, int32_t b) { return (int32_t)((uint32_t)a + (uint32_t)b); }
 
+    // Warp instruction of a domain-warp node: lattice gradient, or simplex /
+    // super-simplex with the node's vectorization scheme (DomainWarpSimplex.h).
+    static FnOp warp_op(const Node* w) { return w->meta->id == kDomainWarpGradient ? FN_OP_WARP_GRAD : FN_OP_WARP_SIMPLEX; }
+    static uint16_t warp_aux(const Node* w)
+    {
+        if (w->meta->id == kDomainWarpGradient) return 0;
+        return (uint16_t)((w->meta->id == kDomainWarpSuperSimplex ? 1 : 0) | (w->st.vec_scheme == 1 ? 2 : 0));
+    }
+
     int gen(const Node* n, int dim, int32_t seed, int pos);
 };
 
@@ -259,28 +268,25 @@ int Compiler::gen(const Node* n, int dim, int32_t seed, int pos)
         return r;
     }
 
-    case kDomainWarpGradient: {
+    case kDomainWarpGradient: case kDomainWarpSimplex: case kDomainWarpSuperSimplex: {
         // DomainWarp::GenT (DomainWarp.inl:9-17): seed offset applied in GenT and again in Warp
         if (lookup(n, 0) < 0) return 0;
         int amp = hybrid(n, 0, dim, seed, pos);
         int w = copy_pos(pos, dim);
-        emit(FN_OP_WARP_GRAD, dim, w, pos, amp, FN_REG_NONE, FN_REG_NONE, FN_REG_NONE,
-             param_block({s.frequency, s.axis[0], s.axis[1], s.axis[2], s.axis[3]}), 0, sadd(sadd(seed, s.seed_offset), s.seed_offset));
+        emit(warp_op(n), dim, w, pos, amp, FN_REG_NONE, FN_REG_NONE, FN_REG_NONE,
+             param_block({s.frequency, s.axis[0], s.axis[1], s.axis[2], s.axis[3]}), warp_aux(n),
+             sadd(sadd(seed, s.seed_offset), s.seed_offset));
         release(amp, 1);
         int r = gen(n->lookups[0], dim, seed, w);
         release(w, dim);
         return r;
     }
-    case kDomainWarpSimplex: case kDomainWarpSuperSimplex:
-        fail(std::string(n->meta->name) + " has no GPU implementation yet");
-        return 0;
 
     case kDomainWarpFractalProgressive: case kDomainWarpFractalIndependent: {
         // DomainWarpFractal.inl:9-73
         if (lookup(n, 0) < 0) return 0;
         const Node* warp = n->lookups[0];
-        if (warp->meta->id != kDomainWarpGradient) { fail(std::string(warp->meta->name) + " has no GPU implementation yet"); return 0; }
-        if (!warp->lookups[0]) { fail("DomainWarpGradient: source is not set"); return 0; }
+        if (!warp->lookups[0]) { fail(std::string(warp->meta->name) + ": source is not set"); return 0; }
         const bool indep = id == kDomainWarpFractalIndependent;
         const NodeState& ws_ = warp->st;
         int amp = hybrid(warp, 0, dim, seed, pos);
@@ -290,15 +296,15 @@ int Compiler::gen(const Node* n, int dim, int32_t seed, int pos)
         int strength = alloc(1);
         float freq = ws_.frequency;
         const int src = indep ? pos : w;
-        emit(FN_OP_WARP_GRAD, dim, w, src, amp, strength, FN_REG_NONE, FN_REG_NONE,
-             param_block({freq, ws_.axis[0], ws_.axis[1], ws_.axis[2], ws_.axis[3]}), 0, sadd(seed, ws_.seed_offset));
+        emit(warp_op(warp), dim, w, src, amp, strength, FN_REG_NONE, FN_REG_NONE,
+             param_block({freq, ws_.axis[0], ws_.axis[1], ws_.axis[2], ws_.axis[3]}), warp_aux(warp), sadd(seed, ws_.seed_offset));
         int32_t sd = seed;
         for (int i = 1; i < s.octaves; ++i) {
             sd = sadd(sd, 1);
             freq = freq * s.lacunarity;
             emit(FN_OP_DWF_AMP, dim, amp, strength, amp, wstr, gain);
-            emit(FN_OP_WARP_GRAD, dim, w, src, amp, strength, FN_REG_NONE, FN_REG_NONE,
-                 param_block({freq, ws_.axis[0], ws_.axis[1], ws_.axis[2], ws_.axis[3]}), 0, sadd(sd, ws_.seed_offset));
+            emit(warp_op(warp), dim, w, src, amp, strength, FN_REG_NONE, FN_REG_NONE,
+                 param_block({freq, ws_.axis[0], ws_.axis[1], ws_.axis[2], ws_.axis[3]}), warp_aux(warp), sadd(sd, ws_.seed_offset));
         }
         release(amp, 1); release(wstr, 1); release(gain, 1); release(strength, 1);
         int r = gen(warp->lookups[0], dim, seed, w);

@@ -773,6 +773,73 @@ struct CellParams {
     float minkowski;   // constant Minkowski P
 };
 
+// Visit the 3^D cells around the point in the reference's order (last axis
+// fastest): visit(c, cf) gets the primed cell coordinates and the running float
+// cell offsets (cfb[k] + 0, 1, 2).  Nested loops over scalars rather than an
+// odometer over arrays, so the per-cell state stays in registers.
+template <int D, typename F>
+FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
+{
+    if constexpr (D == 2) {
+        int cx = cb[0];
+        float fx = cfb[0];
+#pragma unroll 1
+        for (int xi = 0; xi < 3; ++xi, cx = iadd(cx, kPrimeX), fx += 1.0f) {
+            int cy = cb[1];
+            float fy = cfb[1];
+#pragma unroll 1
+            for (int yi = 0; yi < 3; ++yi, cy = iadd(cy, kPrimeY), fy += 1.0f) {
+                const int c[2] = {cx, cy};
+                const float cf[2] = {fx, fy};
+                visit(c, cf);
+            }
+        }
+    } else if constexpr (D == 3) {
+        int cx = cb[0];
+        float fx = cfb[0];
+#pragma unroll 1
+        for (int xi = 0; xi < 3; ++xi, cx = iadd(cx, kPrimeX), fx += 1.0f) {
+            int cy = cb[1];
+            float fy = cfb[1];
+#pragma unroll 1
+            for (int yi = 0; yi < 3; ++yi, cy = iadd(cy, kPrimeY), fy += 1.0f) {
+                int cz = cb[2];
+                float fz = cfb[2];
+#pragma unroll 1
+                for (int zi = 0; zi < 3; ++zi, cz = iadd(cz, kPrimeZ), fz += 1.0f) {
+                    const int c[3] = {cx, cy, cz};
+                    const float cf[3] = {fx, fy, fz};
+                    visit(c, cf);
+                }
+            }
+        }
+    } else {
+        int cx = cb[0];
+        float fx = cfb[0];
+#pragma unroll 1
+        for (int xi = 0; xi < 3; ++xi, cx = iadd(cx, kPrimeX), fx += 1.0f) {
+            int cy = cb[1];
+            float fy = cfb[1];
+#pragma unroll 1
+            for (int yi = 0; yi < 3; ++yi, cy = iadd(cy, kPrimeY), fy += 1.0f) {
+                int cz = cb[2];
+                float fz = cfb[2];
+#pragma unroll 1
+                for (int zi = 0; zi < 3; ++zi, cz = iadd(cz, kPrimeZ), fz += 1.0f) {
+                    int cw = cb[3];
+                    float fw = cfb[3];
+#pragma unroll 1
+                    for (int wi = 0; wi < 3; ++wi, cw = iadd(cw, kPrimeW), fw += 1.0f) {
+                        const int c[4] = {cx, cy, cz, cw};
+                        const float cf[4] = {fx, fy, fz, fw};
+                        visit(c, cf);
+                    }
+                }
+            }
+        }
+    }
+}
+
 template <int D>
 FND float cellular_value(int seed, const float* pin, const CellParams& cp, int valueIndex)
 {
@@ -789,16 +856,7 @@ FND float cellular_value(int seed, const float* pin, const CellParams& cp, int v
         cfb[k] = cvtf(cb[k]) - p[k];
         cb[k] = imul(cb[k], kPrimes[k]);
     }
-    int c[D];
-    float cf[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) { c[k] = cb[k]; cf[k] = cfb[k]; }
-    constexpr int total = D == 2 ? 9 : (D == 3 ? 27 : 81);
-    int idx[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) idx[k] = 0;
-#pragma unroll 1
-    for (int it = 0; it < total; ++it) {
+    for_each_cell<D>(cb, cfb, [&](const int* c, const float* cf) {
         int h = cell_hash<D>(seed, c);
         float d[D + 1];
         cell_dir<D>(h, cp.jitter, d);
@@ -819,12 +877,7 @@ FND float cellular_value(int seed, const float* pin, const CellParams& cp, int v
             nd = closer ? ld : nd;
             nh = closer ? lh : nh;
         }
-#pragma unroll
-        for (int k = D - 1; k >= 0; --k) {
-            if (++idx[k] < 3) { cf[k] += 1.0f; c[k] = iadd(c[k], kPrimes[k]); break; }
-            idx[k] = 0; cf[k] = cfb[k]; c[k] = cb[k];
-        }
-    }
+    });
     int sel = vh[0];
 #pragma unroll
     for (int i = 1; i < 4; ++i) sel = valueIndex == i ? vh[i] : sel;
@@ -847,16 +900,7 @@ FND void cellular_distances(int seed, const float* pin, const CellParams& cp, fl
         cfb[k] = cvtf(cb[k]);
         cb[k] = imul(cb[k], kPrimes[k]);
     }
-    int c[D];
-    float cf[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) { c[k] = cb[k]; cf[k] = cfb[k]; }
-    constexpr int total = D == 2 ? 9 : (D == 3 ? 27 : 81);
-    int idx[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) idx[k] = 0;
-#pragma unroll 1
-    for (int it = 0; it < total; ++it) {
+    for_each_cell<D>(cb, cfb, [&](const int* c, const float* cf) {
         int h = cell_hash<D>(seed, c);
         float d[D + 1];
         cell_dir<D>(h, cp.jitter, d);
@@ -868,12 +912,7 @@ FND void cellular_distances(int seed, const float* pin, const CellParams& cp, fl
 #pragma unroll
         for (int i = 3; i > 0; i--) dist[i] = fmax_(fmin_(dist[i], nd), dist[i - 1]);
         dist[0] = fmin_(dist[0], nd);
-#pragma unroll
-        for (int k = D - 1; k >= 0; --k) {
-            if (++idx[k] < 3) { cf[k] += 1.0f; c[k] = iadd(c[k], kPrimes[k]); break; }
-            idx[k] = 0; cf[k] = cfb[k]; c[k] = cb[k];
-        }
-    }
+    });
 }
 
 // CellularDistance::GetReturn (Cellular.inl:531-565) without the final ScaleOutput;
@@ -919,16 +958,7 @@ FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, f
         cfb[k] = cvtf(cb[k]);
         cb[k] = imul(cb[k], kPrimes[k]);
     }
-    int c[D];
-    float cf[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) { c[k] = cb[k]; cf[k] = cfb[k]; }
-    constexpr int total = D == 2 ? 9 : (D == 3 ? 27 : 81);
-    int idx[D];
-#pragma unroll
-    for (int k = 0; k < D; ++k) idx[k] = 0;
-#pragma unroll 1
-    for (int it = 0; it < total; ++it) {
+    for_each_cell<D>(cb, cfb, [&](const int* c, const float* cf) {
         int h = cell_hash<D>(seed, c);
         float d[D + 1];
         cell_dir<D>(h, cp.jitter, d);
@@ -941,12 +971,7 @@ FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, f
         best = fmin_(nd, best);
 #pragma unroll
         for (int k = 0; k < D; ++k) cell[k] = closer ? local[k] : cell[k];
-#pragma unroll
-        for (int k = D - 1; k >= 0; --k) {
-            if (++idx[k] < 3) { cf[k] += 1.0f; c[k] = iadd(c[k], kPrimes[k]); break; }
-            idx[k] = 0; cf[k] = cfb[k]; c[k] = cb[k];
-        }
-    }
+    });
 #pragma unroll
     for (int k = 0; k < D; ++k) out[k] = cell[k] * scale;
 }
@@ -1002,6 +1027,615 @@ FND float warp_gradient(int seed, float amp, const float* sp, const float* axis,
     float r = wv[D - 1] * wv[D - 1];
 #pragma unroll
     for (int k = D - 2; k >= 0; --k) r = fmaf(wv[k], wv[k], r);
+    return r;
+}
+
+// ---------------------------------------------------------------- DomainWarpSimplex / DomainWarpSuperSimplex
+//
+// Restatement of DomainWarpSimplex.inl.  The vector-product helpers follow the
+// portable (non-AVX) branches (:40-60, :82-116, :148-191, :221-235, :285-316,
+// :560-695); FS::Masked*(m, a, b) are written as selects and
+// FS::SelectHighBit(m, a, b) as (m < 0 ? a : b).  `v` accumulates the vector.
+
+constexpr float kRoot2f = (float)kRoot2, kRoot3f = (float)kRoot3;
+constexpr float kSkew2f = (float)(1.0 / (kRoot3 + 1.0)), kSkew4f = (float)(1.0 / (kRoot5 + 1.0));
+
+FND int shl(int a, int s) { return (int)((unsigned)a << s); }
+FND float selhb(int m, float a, float b) { return m < 0 ? a : b; }
+
+// ApplyGradientOuterProductVectorProductSimplex 2D (:7-60)
+FND void wgop2(int hash31, float fX, float fY, float mul, float* v)
+{
+    const int hs = (int)srl(hash31, 1);
+    const int ig = imul(hs, 12 >> 2);
+    const int io = imul(hs, (int)0xAAAAAAAB) & (int)0xC0000003;
+    {
+        const float u = selhb(shl(ig, 2), fY, fX);
+        const float w = selhb(shl(ig, 2), fX, fY);
+        const float a = u * selhb(ig, 2.0f, kRoot3f);
+        const float b = flip(w, shl(ig >> 30, 31));
+        const float s = ig >= 0 ? a + b : a;
+        mul = mul * flip(s, shl((ig >> 28) ^ io, 31));
+    }
+    {
+        const float a = mul * selhb(io, 2.0f, kRoot3f);
+        const float b = flip(io >= 0 ? mul : 0.0f, shl(io >> 30, 31));
+        v[0] = v[0] + selhb(shl(io, 30), b, a);
+        v[1] = v[1] + selhb(shl(io, 30), a, b);
+    }
+}
+
+// ApplyGradientOuterProductVectorProductCommon 3D (:62-116)
+FND void wgop3(int hash31, float fX, float fY, float fZ, float mul, float* v)
+{
+    const int hs = (int)srl(hash31, 1);
+    const int ig = (int)srl(imul(hs, 12 >> 2), 28);
+    int io = imul(hs, (int)0xAAAAAAAB) & (int)0xC0000003;
+    io = io | (io >> 28);
+    {
+        const float u = ig >= 8 ? fY : fX;
+        const float w = ig >= 4 ? fZ : fY;
+        mul = mul * (flip(u, shl(ig, 31)) + flip(w, shl(ig >> 1, 31)));
+    }
+    {
+        io &= 0xF;
+        const float s0 = flip(mul, shl(io, 31));
+        const float s1 = flip(mul, shl(io >> 1, 31));
+        const bool notYZ = io < 8, notXY = io >= 4;
+        v[0] = notYZ ? v[0] + s0 : v[0];
+        v[2] = notXY ? v[2] + s1 : v[2];
+        v[1] = (notYZ && notXY) ? v[1] : v[1] + (notXY ? s0 : s1);
+    }
+}
+
+// one 4D outer-product gradient from a [0,20) << 27 table index (:150-171)
+FND void wgop4_vector(int index, float* g)
+{
+    int iA = index & (0x03 << 27);
+    int iB = (index >> 2) & (0x07 << 27);
+    iB ^= iA;
+    const bool extra = iB >= (0x04 << 27);
+    const bool equal = iA == iB;
+    if (equal) iA = -1;
+    const float neutral = (equal || extra) ? (extra ? kSkew4f * -1.0f : kSkew4f) : 0.0f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float t = iA == (k << 27) ? neutral - 1.0f : neutral;
+        g[k] = iB == (k << 27) ? t + 1.0f : t;
+    }
+}
+
+// ApplyGradientOuterProductVectorProductSimplex 4D (:118-191)
+FND void wgop4(int hash, float fX, float fY, float fZ, float fW, float mul, float* v)
+{
+    const int hs = (int)srl(hash, 2);
+    const int ig = imul(hs, 20 >> 2);
+    int io = imul(hs, (int)0xCCCCCCCD);
+    io = imul(io & (int)0xE0000003, 3 | (1 << 27));
+    float g[4];
+    wgop4_vector(ig, g);
+    mul = mul * fmaf(g[3], fW, fmaf(g[2], fZ, fmaf(g[1], fY, g[0] * fX)));
+    wgop4_vector(io, g);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) v[k] = fmaf(mul, g[k], v[k]);
+}
+
+// ApplyOrthogonalGradientMatrixVectorProductSimplex 2D (:193-235)
+FND void wogm2(int hash31, float fX, float fY, float mul, float* v)
+{
+    const int index = imul((int)srl(hash31, 1), 12 >> 2);
+    const int ofThree = (int)srl(index, 30);
+    const float masked = index >= 0 ? kSkew2f : 0.0f;
+    const float gX = flip(ofThree != 0 ? masked + 1.0f : masked, shl(index >> 28, 31));
+    const float gY = flip(ofThree != 1 ? masked + 1.0f : masked, shl(index >> 29, 31));
+    v[0] = fmaf(mul, fmaf(fY, gY, fX * gX), v[0]);
+    mul = flip(mul, shl(hash31, 31));
+    v[1] = fmaf(mul, fmaf(fY, gX, -(fX * gY)), v[1]);
+}
+
+// ApplyOrthogonalGradientMatrixVectorProductCommon 3D (:237-316)
+FND void wogm3(int hash31, float fX, float fY, float fZ, float mul, float* v)
+{
+    constexpr float cA = 2.224744871391589f, cB = -0.224744871391589f, cC = -1.0f, cDE = 1.0f, cF = 2.0f;
+    const int hs = (int)srl(hash31, 1);
+    const int fb = imul(hs, (int)0xAAAAAAAB);
+    const int p2hb = shl(fb, 29);
+    const int p3 = (int)srl(imul(hs, 3), 30);
+    const int sign0 = shl(fb, 31);
+    const int sign1 = shl(fb, 30) & (int)0x80000000;
+    const int notYZ = fb, notXY = shl(fb, 1), either = notYZ | notXY;
+
+    const float aX = selhb(notYZ, cC, flip(cA, sign0));
+    const float aY = selhb(either, selhb(notXY, flip(cB, sign1), flip(cA, sign0)), cC);
+    const float aZ = selhb(notXY, cC, flip(cB, sign1));
+    const float valA = fmaf(aZ, fZ, fmaf(fY, aY, fX * aX));
+    const float bX = selhb(notYZ, cC, flip(cB, sign0));
+    const float bY = selhb(either, selhb(notXY, flip(cA, sign1), flip(cB, sign0)), cC);
+    const float bZ = selhb(notXY, cC, flip(cA, sign1));
+    const float valB = fmaf(bZ, fZ, fmaf(fY, bY, fX * bX));
+    const float cX = selhb(notYZ, cF, flip(cDE, sign0));
+    const float cY = selhb(either, selhb(notXY, flip(cDE, sign1), flip(cDE, sign0)), cF);
+    const float cZ = selhb(notXY, cF, flip(cDE, sign1));
+    const float valC = fmaf(cZ, fZ, fmaf(fY, cY, fX * cX));
+
+    const float valAB = selhb(p2hb, valB, valA);
+    const float valBA = selhb(p2hb, valA, valB);
+    mul = flip(mul, shl(hash31, 31));
+    v[0] = fmaf(mul, p3 == 0 ? valC : valAB, v[0]);
+    v[1] = fmaf(mul, p3 == 1 ? valC : (p3 == 2 ? valBA : valAB), v[1]);
+    v[2] = fmaf(mul, p3 == 2 ? valC : valBA, v[2]);
+}
+
+// ApplyOrthogonalGradientMatrixVectorProductSimplex 4D (:318-695)
+FND void wogm4(int hash31, float fX, float fY, float fZ, float fW, float mul, float* v)
+{
+    constexpr float kNegAB = -0.375999676691291f, kFillAB = 0.222726847849776f;
+    constexpr float kPosD = -kSkew4f, kUnD = kSkew4f;
+    constexpr float kToSingleAB = -0.124000323308709f, kToSingleD = 0.190983005625053f;
+    constexpr float kToExtra = kSkew4f, kABToC = 0.437016024448821f, kToDiag = -kRoot2f;
+
+    const int hs = (int)srl(hash31, 2);
+    const int basis = imul(hs, 20 >> 2);
+    const int p3 = imul(hs, (int)0xD5555556) >> 29;
+    const int p8 = basis >> 24;
+
+    int iPos = basis & (0x03 << 27);
+    int iNeg = (basis >> 2) & (0x03 << 27);
+    iNeg ^= iPos;
+    // (0x10 << 27) wraps to INT_MIN: with signed int32 compares the mask is always set (:567)
+    const bool extraCase = basis >= (int)0x80000000;
+    const bool singleCase = iPos == iNeg;
+    const bool singleNonExtra = basis < (0x04 << 27);
+    if (singleNonExtra) iPos = -1;
+
+    const float offAB = extraCase ? kToSingleAB + kToExtra : kToSingleAB;
+    const float negAB = singleCase ? kNegAB + offAB : kNegAB;
+    const float fillAB = singleCase ? kFillAB + offAB : kFillAB;
+    const float negC = singleCase ? negAB : negAB + kABToC;
+    const float fillC = singleCase ? fillAB : fillAB + kABToC;
+    const float offD = extraCase ? kToSingleD + kToExtra : kToSingleD;
+    const float posD = singleCase ? kPosD + offD : kPosD;
+    const float unD = singleCase ? kUnD + offD : kUnD;
+
+    int counter = -1;
+    float vA = 0.0f, vB = 0.0f, vC = 0.0f, vD = 0.0f;
+    const float f[4] = {fX, fY, fZ, fW};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const bool idxPos = iPos == (k << 27);
+        const bool indexed = idxPos || iNeg == (k << 27);
+        const float icAB = idxPos ? negAB + 1.0f : negAB;
+        const float icC = idxPos ? negC + 1.0f : negC;
+        const float icD = !idxPos ? posD - 1.0f : posD;
+        float uA, uB, uC;
+        if (k == 0) {
+            uA = fillAB + kToDiag; uB = fillAB; uC = fillC;
+        } else if (k == 1) {
+            uA = counter == -2 ? fillAB + kToDiag : fillAB;
+            uB = counter == -1 ? fillAB + kToDiag : fillAB;
+            uC = fillC;
+        } else if (k == 2) {
+            uA = counter == -3 ? fillAB + kToDiag : fillAB;
+            uB = counter == -2 ? fillAB + kToDiag : fillAB;
+            uC = counter == -1 ? fillC + kToDiag : fillC;
+        } else {
+            uA = fillAB;
+            uB = counter == -3 ? fillAB + kToDiag : fillAB;
+            uC = counter == -2 ? fillC + kToDiag : fillC;
+        }
+        const float gA = indexed ? icAB : uA, gB = indexed ? icAB : uB;
+        const float gC = indexed ? icC : uC, gD = indexed ? icD : unD;
+        if (k < 3 && indexed) counter -= 1;
+        if (k == 0) { vA = gA * f[0]; vB = gB * f[0]; vC = gC * f[0]; vD = gD * f[0]; }
+        else { vA = fmaf(gA, f[k], vA); vB = fmaf(gB, f[k], vB); vC = fmaf(gC, f[k], vC); vD = fmaf(gD, f[k], vD); }
+    }
+    const int ix = p8 >> 1;
+    const int iy = iadd(iadd(ix, 1), p3);
+    int iz = p8 & 1;
+    iz = iadd(iadd(ix, 1), iz >= p3 ? iadd(iz, 1) : iz);
+    const int isum = iadd(iadd(ix, iy), iz);
+    mul = flip(mul, shl(hash31, 31));
+    auto pick = [&](int i) { return selhb(shl(i, 31), selhb(shl(i, 30), vD, vB), selhb(shl(i, 30), vC, vA)); };
+    v[0] = fmaf(mul, pick(ix), v[0]);
+    v[1] = fmaf(mul, pick(iy), v[1]);
+    v[2] = fmaf(mul, pick(iz), v[2]);
+    v[3] = fmaf(mul, selhb(shl(isum, 31), selhb(shl(isum, 30), vD, vB), selhb(shl(isum, 30), vA, vC)), v[3]);
+}
+
+template <int D>
+FND void wvec(bool gop, int h, const float* d, float mul, float* v)
+{
+    if (D == 2) { if (gop) wgop2(h, d[0], d[1], mul, v); else wogm2(h, d[0], d[1], mul, v); }
+    else if (D == 3) { if (gop) wgop3(h, d[0], d[1], d[2 % D], mul, v); else wogm3(h, d[0], d[1], d[2 % D], mul, v); }
+    else { if (gop) wgop4(h, d[0], d[1], d[2 % D], d[3 % D], mul, v); else wogm4(h, d[0], d[1], d[2 % D], d[3 % D], mul, v); }
+}
+FND float pow4(float f) { f = f * f; return f * f; }
+FND float fb4(float f) { return (f * f) * (f * f); }
+
+// DomainWarpSimplex::Warp_2D/3D/4D (:771-1089)
+FND void ws_simplex2(bool gop, int seed, const float* p, float* v)
+{
+    constexpr double kSkew2 = 1.0 / (kRoot3 + 1.0), kUnskew2 = -1.0 / (kRoot3 + 3.0), kR2 = 0.5;
+    const float x = p[0], y = p[1];
+    const float skewDelta = (float)kSkew2 * (x + y);
+    const float xs = x + skewDelta, ys = y + skewDelta;
+    const float xb = floorf(xs), yb = floorf(ys);
+    const float dxs = xs - xb, dys = ys - yb;
+    const int xp = imul(cvti(xb), kPrimeX), yp = imul(cvti(yb), kPrimeY);
+    const bool xGEy = dxs >= dys;
+    const float ud = (float)kUnskew2 * (dxs + dys);
+    const float dx0 = dxs + ud, dy0 = dys + ud;
+    const float dx1 = (!xGEy ? dx0 + 1.0f : dx0) - (float)(kUnskew2 + 1);
+    const float dy1 = (xGEy ? dy0 + 1.0f : dy0) - (float)(kUnskew2 + 1);
+    const float dx2 = dx0 - (float)(kUnskew2 * 2 + 1), dy2 = dy0 - (float)(kUnskew2 * 2 + 1);
+    float f0 = fmaf(-dx0, dx0, fmaf(-dy0, dy0, (float)kR2));
+    float f1 = fmaf(-dx1, dx1, fmaf(-dy1, dy1, (float)kR2));
+    float f2 = f0 + fmaf(ud, (float)(-4.0 * (kRoot3 + 2.0) / (kRoot3 + 3.0)), (float)(-2.0 / 3.0));
+    f0 = pow4(fmax_(f0, 0.0f)); f1 = pow4(fmax_(f1, 0.0f)); f2 = pow4(fmax_(f2, 0.0f));
+    v[0] = 0.0f; v[1] = 0.0f;
+    { const float d[2] = {dx0, dy0}; wvec<2>(gop, hash(seed, xp, yp), d, f0, v); }
+    { const float d[2] = {dx1, dy1}; wvec<2>(gop, hash(seed, xGEy ? iadd(xp, kPrimeX) : xp, !xGEy ? iadd(yp, kPrimeY) : yp), d, f1, v); }
+    { const float d[2] = {dx2, dy2}; wvec<2>(gop, hash(seed, iadd(xp, kPrimeX), iadd(yp, kPrimeY)), d, f2, v); }
+}
+
+FND void ws_simplex3(bool gop, int seed, const float* p, float* v)
+{
+    constexpr double kSkew3 = 1.0 / 3.0, kRU3 = -1.0 / 2.0, kR2 = 0.6;
+    const float x = p[0], y = p[1], z = p[2];
+    const float skewDelta = (float)kSkew3 * (x + y + z);
+    const float xs = x + skewDelta, ys = y + skewDelta, zs = z + skewDelta;
+    const float xb = floorf(xs), yb = floorf(ys), zb = floorf(zs);
+    const float dxs = xs - xb, dys = ys - yb, dzs = zs - zb;
+    const int xp = imul(cvti(xb), kPrimeX), yp = imul(cvti(yb), kPrimeY), zp = imul(cvti(zb), kPrimeZ);
+    const bool xGEy = dxs >= dys, yGEz = dys >= dzs, xGEz = dxs >= dzs;
+    const float ud = (float)kRU3 * (dxs + dys + dzs);
+    const float dx0 = dxs + ud, dy0 = dys + ud, dz0 = dzs + ud;
+    const bool mX1 = xGEy && xGEz, mY1 = yGEz && !xGEy, mZ1 = xGEz || yGEz;
+    const bool nX2 = xGEy || xGEz, nY2 = xGEy && !yGEz, nZ2 = xGEz && yGEz;
+    const float dx3 = dx0 - (float)(kRU3 * 3 + 1), dy3 = dy0 - (float)(kRU3 * 3 + 1), dz3 = dz0 - (float)(kRU3 * 3 + 1);
+    const float dx1 = mX1 ? dx3 - 1.0f : dx3, dy1 = mY1 ? dy3 - 1.0f : dy3, dz1 = mZ1 ? dz3 : dz3 - 1.0f;
+    const float dx2 = !nX2 ? dx0 + 1.0f : dx0, dy2 = nY2 ? dy0 + 1.0f : dy0, dz2 = nZ2 ? dz0 + 1.0f : dz0;
+    float f0 = fmaf(-dz0, dz0, fmaf(-dy0, dy0, fmaf(-dx0, dx0, (float)kR2)));
+    float f1 = fmaf(-dz1, dz1, fmaf(-dy1, dy1, fmaf(-dx1, dx1, (float)kR2)));
+    float f2 = fmaf(-dz2, dz2, fmaf(-dy2, dy2, fmaf(-dx2, dx2, (float)kR2)));
+    float f3 = f0 - (ud + (float)(3.0 / 4.0));
+    f0 = pow4(fmax_(f0, 0.0f)); f1 = pow4(fmax_(f1, 0.0f)); f2 = pow4(fmax_(f2, 0.0f)); f3 = pow4(fmax_(f3, 0.0f));
+    v[0] = 0.0f; v[1] = 0.0f; v[2] = 0.0f;
+    { const float d[3] = {dx0, dy0, dz0}; wvec<3>(gop, hash(seed, xp, yp, zp), d, f0, v); }
+    { const float d[3] = {dx1, dy1, dz1};
+      wvec<3>(gop, hash(seed, mX1 ? iadd(xp, kPrimeX) : xp, mY1 ? iadd(yp, kPrimeY) : yp, !mZ1 ? iadd(zp, kPrimeZ) : zp), d, f1, v); }
+    { const float d[3] = {dx2, dy2, dz2};
+      wvec<3>(gop, hash(seed, nX2 ? iadd(xp, kPrimeX) : xp, !nY2 ? iadd(yp, kPrimeY) : yp, !nZ2 ? iadd(zp, kPrimeZ) : zp), d, f2, v); }
+    { const float d[3] = {dx3, dy3, dz3}; wvec<3>(gop, hash(seed, iadd(xp, kPrimeX), iadd(yp, kPrimeY), iadd(zp, kPrimeZ)), d, f3, v); }
+    if (gop) {
+        const float dl = (float)(-2.0 / 2.0) * (v[0] + v[1] + v[2]);
+        v[0] = v[0] + dl; v[1] = v[1] + dl; v[2] = v[2] + dl;
+    }
+}
+
+FND void ws_simplex4(bool gop, int seed, const float* p, float* v)
+{
+    constexpr double kSkew4 = 1.0 / (kRoot5 + 1.0), kUnskew4 = -1.0 / (kRoot5 + 5.0), kR2 = 0.6;
+    const float skewDelta = (float)kSkew4 * (p[0] + p[1] + p[2] + p[3]);
+    float ds[4], d0[4];
+    int pb[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float sk = p[k] + skewDelta;
+        const float b = floorf(sk);
+        ds[k] = sk - b;
+        pb[k] = imul(cvti(b), kPrimes[k]);
+    }
+    const float ud = (float)kUnskew4 * (ds[0] + ds[1] + ds[2] + ds[3]);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) d0[k] = ds[k] + ud;
+    int rank[4] = {0, 0, 0, 0};
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = a + 1; b < 4; ++b) {
+            if (d0[a] >= d0[b]) rank[a]++; else rank[b]++;
+        }
+    v[0] = 0.0f; v[1] = 0.0f; v[2] = 0.0f; v[3] = 0.0f;
+    float f0 = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        float d[4];
+        int c[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const bool m = i == 0 ? false : i == 4 ? true : rank[k] > 3 - i;
+            if (i == 0) d[k] = d0[k];
+            else if (i == 4) d[k] = d0[k] - (float)(kUnskew4 * 4 + 1);
+            else d[k] = (m ? d0[k] - 1.0f : d0[k]) - (float)(kUnskew4 * i);
+            c[k] = m ? iadd(pb[k], kPrimes[k]) : pb[k];
+        }
+        float f;
+        if (i < 4) f = fmaf(-d[3], d[3], fmaf(-d[2], d[2], fmaf(-d[1], d[1], fmaf(-d[0], d[0], (float)kR2))));
+        else f = f0 + fmaf(ud, (float)(-4.0 * (kRoot5 + 3.0) / (kRoot5 + 5.0)), (float)(-4.0 / 5.0));
+        if (i == 0) f0 = f;
+        wvec<4>(gop, hash(seed, c[0], c[1], c[2], c[3]), d, pow4(fmax_(f, 0.0f)), v);
+    }
+}
+
+// DomainWarpSuperSimplex::Warp_2D (:1131-1218)
+FND void ws_super2(bool gop, int seed, const float* p, float* v)
+{
+    constexpr double kSkew2 = 1.0 / (kRoot3 + 1.0), kUnskew2 = -1.0 / (kRoot3 + 3.0), kR2 = 2.0 / 3.0;
+    const float x = p[0], y = p[1];
+    const float skewDelta = (float)kSkew2 * (x + y);
+    const float xs = x + skewDelta, ys = y + skewDelta;
+    const float xb = floorf(xs), yb = floorf(ys);
+    const float dxs = xs - xb, dys = ys - yb;
+    const int xp = imul(cvti(xb), kPrimeX), yp = imul(cvti(yb), kPrimeY);
+    const bool fXY = dxs + dys > 1.0f;
+    const float boundary = fXY ? -1.0f : 0.0f;
+    const bool fX = fmaf(dxs, -2.0f, dys) < boundary;
+    const bool fY = fmaf(dys, -2.0f, dxs) < boundary;
+    const float ud = (float)kUnskew2 * (dxs + dys);
+    float dxB = dxs + ud, dyB = dys + ud;
+    v[0] = 0.0f; v[1] = 0.0f;
+    const float fb0 = fmaf(-dxB, dxB, fmaf(-dyB, dyB, (float)kR2));
+    { const float d[2] = {dxB, dyB}; wvec<2>(gop, hash(seed, xp, yp), d, pow4(fb0), v); }
+    {
+        const float f = fmaf(ud, (float)(-4.0 * (kRoot3 + 2.0) / (kRoot3 + 3.0)), fb0 - (float)kR2);
+        const float d[2] = {dxB - (float)(2 * kUnskew2 + 1), dyB - (float)(2 * kUnskew2 + 1)};
+        wvec<2>(gop, hash(seed, iadd(xp, kPrimeX), iadd(yp, kPrimeY)), d, pow4(f), v);
+    }
+    const float xyDelta = fXY ? (float)(kUnskew2 + 1) : (float)(-kUnskew2);
+    dxB = dxB - xyDelta;
+    dyB = dyB - xyDelta;
+    {
+        int hx = fX ? iadd(xp, imul(kPrimeX, 2)) : xp;
+        hx = fXY ? hx : iadd(hx, -kPrimeX);
+        const float dx = dxB - (fX ? (float)(1 + 2 * kUnskew2) : -1.0f);
+        const float dy = fX ? dyB - (float)(2 * kUnskew2) : dyB;
+        const float f = fmax_(fmaf(-dx, dx, fmaf(-dy, dy, (float)kR2)), 0.0f);
+        const float d[2] = {dx, dy};
+        wvec<2>(gop, hash(seed, hx, fXY ? iadd(yp, kPrimeY) : yp), d, pow4(f), v);
+    }
+    {
+        int hy = fY ? iadd(yp, imul(kPrimeY, 2)) : yp;
+        hy = fXY ? hy : iadd(hy, -kPrimeY);
+        const float dx = fY ? dxB - (float)(2 * kUnskew2) : dxB;
+        const float dy = dyB - (fY ? (float)(1 + 2 * kUnskew2) : -1.0f);
+        const float f = fmax_(fmaf(-dx, dx, fmaf(-dy, dy, (float)kR2)), 0.0f);
+        const float d[2] = {dx, dy};
+        wvec<2>(gop, hash(seed, fXY ? iadd(xp, kPrimeX) : xp, hy), d, pow4(f), v);
+    }
+}
+
+// closest-vertex search of the super-simplex warps: one candidate
+FND void ws_consider(float& maxScore, int& bits, float score, int b)
+{
+    bits = score > maxScore ? b : bits;
+    maxScore = fmax_(maxScore, score);
+}
+
+// DomainWarpSuperSimplex::Warp_3D (:1220-1446)
+FND void ws_super3(bool gop, int seed, const float* p, float* v)
+{
+    constexpr double kSkew3 = 1.0 / 3.0, kRU3 = -1.0 / 2.0, kTU3 = -1.0 / 4.0, kDA = 3.0 / 4.0, kDB = 1.0, kR2 = kDA;
+    const float x = p[0], y = p[1], z = p[2];
+    const float skewDelta = (float)kSkew3 * (x + y + z);
+    const float xs = x + skewDelta, ys = y + skewDelta, zs = z + skewDelta;
+    float b[3] = {floorf(xs), floorf(ys), floorf(zs)};
+    float ds[3] = {xs - b[0], ys - b[1], zs - b[2]};
+    {
+        const float tu = (float)kTU3 * (ds[0] + ds[1] + ds[2]);
+        const float xN = ds[0] + tu, yN = ds[1] + tu, zN = ds[2] + tu, xyzN = -tu;
+        float maxScore = 0.375f;
+        int bits = xyzN > maxScore ? -1 : 0;
+        maxScore = fmax_(maxScore, xyzN);
+        ws_consider(maxScore, bits, xN, 1);
+        ws_consider(maxScore, bits, yN, 2);
+        ws_consider(maxScore, bits, zN, 4);
+        maxScore = maxScore + (0.125f - xyzN);
+        ws_consider(maxScore, bits, -zN, 3);
+        ws_consider(maxScore, bits, -yN, 5);
+        ws_consider(maxScore, bits, -xN, 6);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const bool m = (bits >> k) & 1;
+            b[k] = m ? b[k] + 1.0f : b[k];
+            ds[k] = m ? ds[k] - 1.0f : ds[k];
+        }
+    }
+    int pb[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) pb[k] = imul(cvti(b[k]), kPrimes[k]);
+    const float scs = ds[0] + ds[1] + ds[2];
+    const float tu = (float)kTU3 * scs;
+    const float n[3] = {ds[0] + tu, ds[1] + tu, ds[2] + tu};
+    const float xyzN = -tu;
+    const float ud = (float)kRU3 * scs;
+    const float dB[3] = {ds[0] + ud, ds[1] + ud, ds[2] + ud};
+    const float cs = (float)(1 + 3 * kRU3) * scs;
+    v[0] = 0.0f; v[1] = 0.0f; v[2] = 0.0f;
+    const float fb0 = fmaf(-dB[2], dB[2], fmaf(-dB[1], dB[1], fmaf(-dB[0], dB[0], (float)kR2))) * 0.5f;
+    const float stemA = fb0 - (float)(kDA * 0.5), stemB = fb0 - (float)(kDB * 0.5);
+    wvec<3>(gop, hash(seed, pb[0], pb[1], pb[2]), dB, fb4(fb0), v);
+    {   // <1,1,1> or <-1,-1,-1>
+        const bool sm = xyzN < 0.0f;
+        const float off = flipm((float)(3 * kRU3 + 1), sm);
+        const float fb = fmax_(fmaf(off, cs, stemA), 0.0f);
+        int c[3];
+        float d[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { c[k] = iadd(pb[k], sm ? -kPrimes[k] : kPrimes[k]); d[k] = dB[k] - off; }
+        wvec<3>(gop, hash(seed, c[0], c[1], c[2]), d, fb4(fb), v);
+    }
+    // <1,1,0>, <1,0,1>, <0,1,1> or their negatives: the axis left out is m
+#pragma unroll
+    for (int m = 2; m >= 0; --m) {
+        const bool sm = xyzN < n[m];
+        const float off0 = flipm((float)(2 * kRU3), sm);
+        const float fb = fmin_(flipm(dB[m], sm) - stemB, 0.0f);
+        int c[3];
+        float d[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            c[k] = k == m ? pb[k] : iadd(pb[k], sm ? -kPrimes[k] : kPrimes[k]);
+            d[k] = k == m ? dB[k] - off0 : dB[k];
+        }
+        wvec<3>(gop, hash(seed, c[0], c[1], c[2]), d, fb4(fb), v);
+    }
+    // <1,0,0>, <0,1,0>, <0,0,1> or their negatives
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const bool sm = n[a] < 0.0f;
+        const float off0 = flipm((float)kRU3, sm);
+        const float fb = fmax_(fmaf(off0, cs, stemA) + flipm(dB[a], sm), 0.0f);
+        int c[3];
+        float d[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            c[k] = k == a ? iadd(pb[k], sm ? -kPrimes[k] : kPrimes[k]) : pb[k];
+            d[k] = k == a ? dB[k] + off0 : dB[k] - off0;
+        }
+        wvec<3>(gop, hash(seed, c[0], c[1], c[2]), d, fb4(fb), v);
+    }
+    if (gop) {
+        const float dl = (float)(-2.0 / 3.0) * (v[0] + v[1] + v[2]);
+        v[0] = v[0] + dl; v[1] = v[1] + dl; v[2] = v[2] + dl;
+    }
+}
+
+// DomainWarpSuperSimplex::Warp_4D (:1448-1835): the sixteen vertices around the
+// closest lattice vertex in the reference's order; a vertex is the set of axes
+// it moves along (bit k = axis k), in the direction of its group's sign test.
+FND void ws_super4(bool gop, int seed, const float* p, float* v)
+{
+    constexpr double kSkew4 = 1.0 / (kRoot5 + 1.0), kU4 = -1.0 / (kRoot5 + 5.0), kTU4 = -1.0 / 5.0;
+    constexpr double kDA = 4.0 / 5.0, kDB = 6.0 / 5.0, kR2 = kDA;
+    const float skewDelta = (float)kSkew4 * (p[0] + p[1] + p[2] + p[3]);
+    float b[4], ds[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float sk = p[k] + skewDelta;
+        b[k] = floorf(sk);
+        ds[k] = sk - b[k];
+    }
+    {
+        const float tu = (float)kTU4 * (ds[0] + ds[1] + ds[2] + ds[3]);
+        float n[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) n[k] = ds[k] + tu;
+        const float xyzwN = -tu;
+        float maxScore = 0.6f - xyzwN;
+        int bits = 0.2f > maxScore ? -1 : 0;
+        maxScore = fmax_(maxScore, 0.2f);
+        ws_consider(maxScore, bits, -n[3], 0x7);
+        ws_consider(maxScore, bits, -n[2], 0xB);
+        ws_consider(maxScore, bits, -n[1], 0xD);
+        ws_consider(maxScore, bits, -n[0], 0xE);
+        maxScore = maxScore + (xyzwN - 0.2f);
+        ws_consider(maxScore, bits, n[0], 0x1);
+        ws_consider(maxScore, bits, n[1], 0x2);
+        ws_consider(maxScore, bits, n[2], 0x4);
+        ws_consider(maxScore, bits, n[3], 0x8);
+        maxScore = maxScore + (0.2f - n[0]);
+        ws_consider(maxScore, bits, n[1], 0x3);
+        ws_consider(maxScore, bits, n[2], 0x5);
+        ws_consider(maxScore, bits, n[3], 0x9);
+        maxScore = maxScore + n[0];
+        ws_consider(maxScore, bits, n[1] + n[2], 0x6);
+        maxScore = maxScore - n[3];
+        ws_consider(maxScore, bits, n[1], 0xA);
+        ws_consider(maxScore, bits, n[2], 0xC);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const bool m = (bits >> k) & 1;
+            b[k] = m ? b[k] + 1.0f : b[k];
+            ds[k] = m ? ds[k] - 1.0f : ds[k];
+        }
+    }
+    int pb[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) pb[k] = imul(cvti(b[k]), kPrimes[k]);
+    const float scs = ds[0] + ds[1] + ds[2] + ds[3];
+    const float tu = (float)kTU4 * scs;
+    float n[4], dB[4];
+    const float ud = (float)kU4 * scs;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) { n[k] = ds[k] + tu; dB[k] = ds[k] + ud; }
+    const float xyzwN = -tu;
+    const float cs = (float)(1 + 4 * kU4) * scs;
+    v[0] = 0.0f; v[1] = 0.0f; v[2] = 0.0f; v[3] = 0.0f;
+    const float fb0 = fmaf(-dB[3], dB[3], fmaf(-dB[2], dB[2], fmaf(-dB[1], dB[1], fmaf(-dB[0], dB[0], (float)kR2)))) * 0.5f;
+    const float stemA = fb0 - (float)(kDA * 0.5), stemB = fb0 - (float)(kDB * 0.5);
+    wvec<4>(gop, hash(seed, pb[0], pb[1], pb[2], pb[3]), dB, fb4(fb0), v);
+    constexpr int order[15] = {0xF, 0x7, 0xB, 0xD, 0xE, 0x1, 0x3, 0x5, 0x9, 0x2, 0x6, 0xA, 0x4, 0xC, 0x8};
+#pragma unroll
+    for (int vi = 0; vi < 15; ++vi) {
+        const int S = order[vi];
+        const int cnt = (S & 1) + ((S >> 1) & 1) + ((S >> 2) & 1) + ((S >> 3) & 1);
+        const int a = (S & 1) ? 0 : (S & 2) ? 1 : (S & 4) ? 2 : 3;             // lowest axis in S
+        const int bb = (S >> (a + 1)) & 1 ? a + 1 : ((S >> (a + 2)) & 1 ? a + 2 : a + 3);   // second axis (pairs)
+        const int missing = !(S & 8) ? 3 : !(S & 4) ? 2 : !(S & 2) ? 1 : 0;    // axis outside S (triples)
+        bool sm;
+        if (cnt == 4) sm = xyzwN < 0.0f;
+        else if (cnt == 3) sm = xyzwN < n[missing];
+        else if (cnt == 1) sm = n[a] < 0.0f;
+        else sm = n[a] < -n[bb & 3];
+        float off1, off0, fb;
+        if (cnt == 4) {
+            off1 = flipm((float)(4 * kU4 + 1), sm);
+            off0 = off1;
+            fb = fmax_(fmaf(off1, cs, stemA), 0.0f);
+        } else if (cnt == 3) {
+            off1 = flipm((float)(3 * kU4 + 1), sm);
+            off0 = flipm((float)(3 * kU4), sm);
+            fb = fmax_(fmaf(off1, cs, stemB) - flipm(dB[missing], sm), 0.0f);
+        } else if (cnt == 1) {
+            off1 = flipm((float)(kU4 + 1), sm);
+            off0 = flipm((float)kU4, sm);
+            fb = fmax_(fmaf(off0, cs, stemA) + flipm(dB[a], sm), 0.0f);
+        } else {
+            off1 = flipm((float)(2 * kU4 + 1), sm);
+            off0 = flipm((float)(2 * kU4), sm);
+            fb = fmax_(fmaf(off0, cs, stemB) + flipm(dB[a] + dB[bb & 3], sm), 0.0f);
+        }
+        int c[4];
+        float d[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const bool in = (S >> k) & 1;
+            c[k] = in ? iadd(pb[k], sm ? -kPrimes[k] : kPrimes[k]) : pb[k];
+            d[k] = dB[k] - (in ? off1 : off0);
+        }
+        wvec<4>(gop, hash(seed, c[0], c[1], c[2], c[3]), d, fb4(fb), v);
+    }
+}
+
+// DomainWarpSimplex / DomainWarpSuperSimplex ::Warp (:729-769, :1092-1129) on
+// frequency-scaled positions `sp`: the vector noise, scaled by the bounding
+// constant x axis scale, added to io with amplitude `amp`; returns |v|^2.
+template <int D>
+FND float warp_simplex(int seed, float amp, const float* sp, const float* axis, float* io, bool super, bool gop)
+{
+    float v[4];
+    float bound;
+    if (D == 2) {
+        if (super) ws_super2(gop, seed, sp, v); else ws_simplex2(gop, seed, sp, v);
+        bound = super ? (gop ? (float)(9.28993664146183 / 2.0) : 12.814453124999995f)
+                      : (gop ? (float)(49.918426513671875 / 2.0) : 70.1480577066486f);
+    } else if (D == 3) {
+        if (super) ws_super3(gop, seed, sp, v); else ws_simplex3(gop, seed, sp, v);
+        bound = super ? (gop ? (float)(144.736422163332608 / 1.4142135623730951) : 37.63698669623629f)
+                      : (gop ? (float)(32.69428253173828125 / 1.4142135623730951) : 16.281631889139874f);
+    } else {
+        if (super) ws_super4(gop, seed, sp, v); else ws_simplex4(gop, seed, sp, v);
+        bound = super ? (gop ? (float)(115.21625311930542 / 1.4142135623730951) : 48.80058117543753f)
+                      : (gop ? (float)(33.653125584827855 / 1.4142135623730951) : 30.88161777516092f);
+    }
+#pragma unroll
+    for (int k = 0; k < D; ++k) v[k] = v[k] * (bound * axis[k]);
+#pragma unroll
+    for (int k = 0; k < D; ++k) io[k] = fmaf(v[k], amp, io[k]);
+    float r = v[0] * v[0];
+#pragma unroll
+    for (int k = 1; k < D; ++k) r = fmaf(v[k], v[k], r);
     return r;
 }
 

@@ -45,6 +45,35 @@ __device__ __forceinline__ void root_position(const fn::PointArgs& a, long long 
     }
 }
 
+// root_position for a known dimensionality and requests below 2^32 points:
+// 32-bit index arithmetic, same positions bit for bit.
+template <int D>
+__device__ __forceinline__ void root_position32(const fn::PointArgs& a, unsigned i, float* R)
+{
+    if (a.src == fn::kSrcGrid) {
+        unsigned r = i;
+#pragma unroll
+        for (int k = 0; k < D - 1; ++k) {
+            const unsigned c = (unsigned)a.count[k];
+            const unsigned ik = r % c;
+            r /= c;
+            R[k] = fmaf(cvtf((int)ik), a.step[k], a.offset[k]);
+        }
+        R[D - 1] = fmaf(cvtf((int)r), a.step[D - 1], a.offset[D - 1]);
+    } else if (D == 4 && a.src == fn::kSrcTileable) {
+        const unsigned c = (unsigned)a.count[0];
+        const float xf = cvtf((int)(i % c)) * a.tmul[0];
+        const float yf = cvtf((int)(i / c)) * a.tmul[1];
+        R[0] = fnd::cos_(xf) * a.tfreq[0];
+        R[1] = fnd::cos_(yf) * a.tfreq[1];
+        R[2 % D] = fnd::sin_(xf) * a.tfreq[0];
+        R[3 % D] = fnd::sin_(yf) * a.tfreq[1];
+    } else {
+#pragma unroll
+        for (int k = 0; k < D; ++k) R[k] = a.offset[k] + __ldg(a.pos[k] + i);
+    }
+}
+
 // OutputMinMax::operator<< (Generator.h:91-96): NaN never replaces.
 __device__ __forceinline__ void fold(float v, float& mn, float& mx)
 {

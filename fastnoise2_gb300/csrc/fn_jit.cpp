@@ -4,12 +4,15 @@
 
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <sstream>
+#include <thread>
 #include <unordered_map>
 
 #include "fn_kernels.cuh"
@@ -55,7 +58,7 @@ void emit_eval(const CompiledProgram& prog, int k, std::ostringstream& o)
     const FnInstr* ins = fn_program_instrs(h);
     const float* P = fn_program_params(h);
     const int nregs = h->n_regs;
-    o << "__device__ __noinline__ float fnjit_eval_" << k << "(int seed, float x, float y, float z, float w)\n{\n";
+    o << "__device__ __forceinline__ float fnjit_eval_" << k << "(int seed, float x, float y, float z, float w)\n{\n";
     o << "    (void)x; (void)y; (void)z; (void)w;\n";
     const char* root[4] = {"x", "y", "z", "w"};
     for (int i = 0; i < nregs; ++i) o << "    float " << r(i) << " = " << (i < h->dim ? root[i] : "0.0f") << ";\n";
@@ -150,13 +153,17 @@ void emit_eval(const CompiledProgram& prog, int k, std::ostringstream& o)
             o << "        float oo[" << D << "]; fnd::cellular_lookup_pos<" << D << ">(" << sd << ", pp, cp, " << p(1) << ", oo);\n";
             for (int j = 0; j < D; ++j) o << "        " << r(I.dst + j) << " = oo[" << j << "];\n";
             break;
-        case FN_OP_WARP_GRAD:
+        case FN_OP_WARP_GRAD: case FN_OP_WARP_SIMPLEX:
             o << "        const float f = " << p(0) << ";\n";
             o << "        float sp[" << D << "], io[" << D << "];\n";
             for (int j = 0; j < D; ++j) o << "        sp[" << j << "] = " << r(I.a + j) << " * f; io[" << j << "] = " << r(I.dst + j) << ";\n";
             o << "        const float axis[" << D << "] = {";
             for (int j = 0; j < D; ++j) o << (j ? ", " : "") << p(1 + j);
-            o << "};\n        const float st = fnd::warp_gradient<" << D << ">(" << sd << ", " << r(I.b) << ", sp, axis, io);\n";
+            if (I.op == FN_OP_WARP_GRAD)
+                o << "};\n        const float st = fnd::warp_gradient<" << D << ">(" << sd << ", " << r(I.b) << ", sp, axis, io);\n";
+            else
+                o << "};\n        const float st = fnd::warp_simplex<" << D << ">(" << sd << ", " << r(I.b) << ", sp, axis, io, "
+                  << ((I.aux & 1) ? "true" : "false") << ", " << ((I.aux & 2) ? "true" : "false") << ");\n";
             for (int j = 0; j < D; ++j) o << "        " << r(I.dst + j) << " = io[" << j << "];\n";
             if (I.c != FN_REG_NONE) o << "        " << r(I.c) << " = st;\n";
             else o << "        (void)st;\n";
@@ -323,13 +330,25 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
     }
 }
 
-void emit_batch(size_t n, std::ostringstream& o)
+// The batch kernel: persistent CTAs pull (request, tile) items; the request's
+// tree slot selects, once per tile, a loop with that tree's code inlined.
+void emit_batch(const std::vector<const CompiledProgram*>& progs, std::ostringstream& o)
 {
-    o << "__device__ __forceinline__ float fnjit_eval_slot(int slot, int seed, const float* p)\n{\n    switch (slot) {\n";
-    for (size_t k = 0; k < n; ++k) o << "    case " << k << ": return fnjit_eval_" << k << "(seed, p[0], p[1], p[2], p[3]);\n";
-    o << "    default: return __int_as_float(0x7fc00000);\n    }\n}\n\n";
-    o << R"(extern "C" __global__ void __launch_bounds__(256) fnjit_batch(fn::BatchHeader* hdr, const fn::BatchRequest* __restrict__ reqs,
-                                                             fn::BatchState* states, const uint2* __restrict__ items)
+    for (size_t k = 0; k < progs.size(); ++k) {
+        const int D = progs[k]->dim;
+        o << "__device__ __forceinline__ void fnjit_tile_" << k
+          << "(const fn::PointArgs& A, float* __restrict__ out, unsigned i, unsigned end, float& mn, float& mx)\n{\n"
+          << "    for (; i < end; i += blockDim.x) {\n"
+          << "        float p[4];\n"
+          << "        fne::root_position32<" << D << ">(A, i, p);\n"
+          << "        const float v = fnjit_eval_" << k << "(A.seed, p[0], p[1], " << (D > 2 ? "p[2]" : "0.0f") << ", "
+          << (D > 3 ? "p[3]" : "0.0f") << ");\n"
+          << "        out[i] = v;\n"
+          << "        fne::fold(v, mn, mx);\n"
+          << "    }\n}\n\n";
+    }
+    o << R"(extern "C" __global__ void __launch_bounds__(256, 2) fnjit_batch(fn::BatchHeader* hdr, const fn::BatchRequest* __restrict__ reqs,
+                                                                fn::BatchState* states, const uint2* __restrict__ items)
 {
     __shared__ unsigned int s_item;
     __shared__ float smn[8], smx[8];
@@ -344,17 +363,15 @@ void emit_batch(size_t n, std::ostringstream& o)
         const uint2 item = items[it];
         const fn::BatchRequest& rq = reqs[item.x];
         const fn::PointArgs args = rq.args;
-        const int slot = rq.jit_slot;
-        const long long begin = (long long)item.y * tile_points;
-        long long end = begin + tile_points;
-        if (end > args.total) end = args.total;
+        const unsigned total = (unsigned)args.total;
+        const unsigned begin = item.y * tile_points;
+        const unsigned end = total - begin < tile_points ? total : begin + tile_points;
         float mn = fne::inf(), mx = -fne::inf();
-        for (long long i = begin + threadIdx.x; i < end; i += blockDim.x) {
-            float pos[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            fne::root_position(args, i, pos);
-            const float v = fnjit_eval_slot(slot, args.seed, pos);
-            rq.out[i] = v;
-            fne::fold(v, mn, mx);
+        switch (rq.jit_slot) {
+)";
+    for (size_t k = 0; k < progs.size(); ++k)
+        o << "        case " << k << ": fnjit_tile_" << k << "(args, rq.out, begin + threadIdx.x, end, mn, mx); break;\n";
+    o << R"(        default: break;
         }
         fne::block_minmax(mn, mx, smn, smx);
         if (threadIdx.x == 0) fne::finish_tile(rq, states + item.x, hdr, mn, mx);
@@ -377,15 +394,47 @@ std::atomic<bool> g_enabled{true};
 
 }  // namespace
 
-std::string jit_module_source(const std::vector<const CompiledProgram*>& progs)
+std::string jit_batch_source(const std::vector<const CompiledProgram*>& progs)
 {
     std::ostringstream o;
-    o << "// generated by fn_jit.cpp\n";
-    o << embedded_device_source() << "\n";
+    o << "// generated by fn_jit.cpp: batch module\n" << embedded_device_source() << "\n";
     for (size_t k = 0; k < progs.size(); ++k) emit_eval(*progs[k], (int)k, o);
-    for (size_t k = 0; k < progs.size(); ++k) emit_percall(*progs[k], (int)k, o);
-    emit_batch(progs.size(), o);
+    emit_batch(progs, o);
     return o.str();
+}
+
+std::string jit_percall_source(const CompiledProgram& prog)
+{
+    std::ostringstream o;
+    o << "// generated by fn_jit.cpp: per-call module\n" << embedded_device_source() << "\n";
+    emit_eval(prog, 0, o);
+    emit_percall(prog, 0, o);
+    return o.str();
+}
+
+bool jit_compile_all(const std::vector<const CompiledProgram*>& progs, std::vector<std::vector<char>>& cubins, std::string& error)
+{
+    // source 0 = the batch module, 1 + k = program k's per-call module; NVRTC
+    // compiles independent programs concurrently, so the sources go to a pool of threads
+    std::vector<std::string> srcs;
+    srcs.push_back(jit_batch_source(progs));
+    for (auto* p : progs) srcs.push_back(jit_percall_source(*p));
+    cubins.assign(srcs.size(), {});
+    std::vector<std::string> logs(srcs.size());
+    std::vector<char> ok(srcs.size(), 0);
+    std::atomic<size_t> next{0};
+    auto worker = [&]() {
+        for (size_t i; (i = next.fetch_add(1)) < srcs.size();) ok[i] = jit_compile_cubin(srcs[i], cubins[i], logs[i]) ? 1 : 0;
+    };
+    unsigned nt = std::thread::hardware_concurrency();
+    nt = std::max(1u, std::min<unsigned>(nt ? nt : 4, (unsigned)srcs.size()));
+    std::vector<std::thread> pool;
+    for (unsigned t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto& t : pool) t.join();
+    for (size_t i = 0; i < srcs.size(); ++i)
+        if (!ok[i]) { error = "NVRTC: " + logs[i].substr(0, 4000); return false; }
+    return true;
 }
 
 bool jit_compile_cubin(const std::string& src, std::vector<char>& cubin, std::string& log)
@@ -395,13 +444,19 @@ bool jit_compile_cubin(const std::string& src, std::vector<char>& cubin, std::st
         log = "nvrtcCreateProgram failed";
         return false;
     }
-    const char* opts[] = {"--gpu-architecture=sm_103a", "-fmad=false", "--std=c++17", "-default-device", "-lineinfo",
-                          "-diag-suppress=177"};
-    nvrtcResult rc = nvrtcCompileProgram(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+    // FASTNOISE_JIT_VERBOSE=1 prints ptxas' register / spill report of every
+    // specialised kernel to stderr (useful when tuning trees).
+    const char* verbose = std::getenv("FASTNOISE_JIT_VERBOSE");
+    const bool v = verbose && verbose[0] == '1';
+    std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "-fmad=false", "--std=c++17", "-default-device",
+                                     "-lineinfo", "-diag-suppress=177"};
+    if (v) opts.push_back("--ptxas-options=-v");
+    nvrtcResult rc = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
     size_t loglen = 0;
     nvrtcGetProgramLogSize(prog, &loglen);
     log.assign(loglen, '\0');
     if (loglen) nvrtcGetProgramLog(prog, &log[0]);
+    if (v) std::fprintf(stderr, "%s\n", log.c_str());
     if (rc != NVRTC_SUCCESS) {
         nvrtcDestroyProgram(&prog);
         return false;
@@ -417,35 +472,42 @@ bool jit_compile_cubin(const std::string& src, std::vector<char>& cubin, std::st
 bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& error)
 {
     if (progs.empty()) return true;
-    const std::string src = jit_module_source(progs);
-    std::vector<char> cubin;
-    std::string log;
-    if (!jit_compile_cubin(src, cubin, log)) { error = "NVRTC: " + log.substr(0, 2000); return false; }
-    auto mod = std::make_unique<Module>();
-    cudaError_t e = cudaLibraryLoadData(&mod->lib, cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
-    if (e != cudaSuccess) { error = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e); return false; }
-    std::unordered_map<uint64_t, JitKernels> found;
-    for (size_t k = 0; k < progs.size(); ++k) {
-        JitKernels jk;
-        jk.slot = (int)k;
-        std::string ks = std::to_string(k);
-        if (cudaLibraryGetKernel(&jk.grid, mod->lib, ("fnjit_grid_" + ks).c_str()) != cudaSuccess ||
-            cudaLibraryGetKernel(&jk.positions, mod->lib, ("fnjit_pos_" + ks).c_str()) != cudaSuccess) {
-            error = "kernel lookup failed";
+    std::vector<std::vector<char>> cubins;
+    if (!jit_compile_all(progs, cubins, error)) return false;
+    std::vector<std::unique_ptr<Module>> mods;
+    for (auto& c : cubins) {
+        auto mod = std::make_unique<Module>();
+        cudaError_t e = cudaLibraryLoadData(&mod->lib, c.data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+        if (e != cudaSuccess) {
+            error = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e);
+            for (auto& m : mods) cudaLibraryUnload(m->lib);
             return false;
         }
-        if (progs[k]->dim == 4) cudaLibraryGetKernel(&jk.tileable, mod->lib, ("fnjit_tile_" + ks).c_str());
-        found[progs[k]->hash] = jk;
-        mod->hashes.push_back(progs[k]->hash);
+        mods.push_back(std::move(mod));
     }
+    std::unordered_map<uint64_t, JitKernels> found;
     cudaKernel_t batch = nullptr;
-    if (cudaLibraryGetKernel(&batch, mod->lib, "fnjit_batch") != cudaSuccess) { error = "batch kernel lookup failed"; return false; }
+    bool ok = cudaLibraryGetKernel(&batch, mods[0]->lib, "fnjit_batch") == cudaSuccess;
+    for (size_t k = 0; ok && k < progs.size(); ++k) {
+        cudaLibrary_t lib = mods[1 + k]->lib;
+        JitKernels jk;
+        jk.slot = (int)k;
+        ok = cudaLibraryGetKernel(&jk.grid, lib, "fnjit_grid_0") == cudaSuccess &&
+             cudaLibraryGetKernel(&jk.positions, lib, "fnjit_pos_0") == cudaSuccess &&
+             (progs[k]->dim != 4 || cudaLibraryGetKernel(&jk.tileable, lib, "fnjit_tile_0") == cudaSuccess);
+        found[progs[k]->hash] = jk;
+    }
+    if (!ok) {
+        error = "kernel lookup failed in a specialised module";
+        for (auto& m : mods) cudaLibraryUnload(m->lib);
+        return false;
+    }
     std::lock_guard<std::mutex> lk(g_jit_mu);
     for (auto& kv : found) g_kernels[kv.first] = kv.second;
     g_batch_kernel = batch;
     g_batch_slots.clear();
     for (auto& kv : found) g_batch_slots[kv.first] = kv.second.slot;
-    g_modules.push_back(std::move(mod));      // modules stay loaded: kernels may still be queued
+    for (auto& m : mods) g_modules.push_back(std::move(m));   // modules stay loaded: kernels may still be queued
     return true;
 }
 

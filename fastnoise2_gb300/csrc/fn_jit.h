@@ -29,8 +29,15 @@ struct JitKernels {
     int slot = -1;                    // index in the module's batch kernel
 };
 
-// Generate the CUDA source of a module for `progs` (exposed for tests/tools).
-std::string jit_module_source(const std::vector<const CompiledProgram*>& progs);
+// CUDA source of the batch module for `progs` (slot k = progs[k]) and of one
+// program's per-call module.
+std::string jit_batch_source(const std::vector<const CompiledProgram*>& progs);
+std::string jit_percall_source(const CompiledProgram& prog);
+
+// NVRTC-compile the batch module and every per-call module (concurrently);
+// cubins[0] = batch, cubins[1 + k] = program k.  Host only, no GPU needed.
+bool jit_compile_all(const std::vector<const CompiledProgram*>& progs, std::vector<std::vector<char>>& cubins,
+                     std::string& error);
 
 // Compile and load a module covering `progs`; on success every program gets
 // per-call kernels and becomes the active batch module.  Thread safe.

@@ -141,6 +141,17 @@ __device__ __forceinline__ void exec_dim(const FnInstr& I, const float* P, float
         if (I.c != FN_REG_NONE) R[I.c] = strength;
         break;
     }
+    case FN_OP_WARP_SIMPLEX: {
+        float sp[4], io[4], axis[4];
+        const float f = P[I.prm];
+#pragma unroll
+        for (int k = 0; k < D; ++k) { sp[k] = R[I.a + k] * f; io[k] = R[I.dst + k]; axis[k] = P[I.prm + 1 + k]; }
+        float strength = warp_simplex<D>(sd, R[I.b], sp, axis, io, I.aux & 1, (I.aux >> 1) & 1);
+#pragma unroll
+        for (int k = 0; k < D; ++k) R[I.dst + k] = io[k];
+        if (I.c != FN_REG_NONE) R[I.c] = strength;
+        break;
+    }
     case FN_OP_SCALE_POS: {
         const float f = P[I.prm];
 #pragma unroll
@@ -284,7 +295,7 @@ __device__ __noinline__ void exec_program(const FnInstr* ins, int n, const float
     }
 }
 
-__global__ void __launch_bounds__(kThreads) interp_kernel(const FnProgramHeader* gprog, uint32_t bytes, PointArgs args,
+__global__ void __launch_bounds__(kThreads, 4) interp_kernel(const FnProgramHeader* gprog, uint32_t bytes, PointArgs args,
                                                           float* __restrict__ out, MinMaxWork* work, float* dminmax)
 {
     extern __shared__ uint4 sprog[];
@@ -315,7 +326,7 @@ int g_num_sms = 0;
 
 constexpr int kBatchThreads = 256;
 
-__global__ void __launch_bounds__(kBatchThreads) batch_kernel(BatchHeader* hdr, const BatchRequest* __restrict__ reqs,
+__global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(BatchHeader* hdr, const BatchRequest* __restrict__ reqs,
                                                               BatchState* states, const uint2* __restrict__ items)
 {
     extern __shared__ uint4 sprog[];

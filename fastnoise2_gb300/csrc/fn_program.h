@@ -52,6 +52,7 @@ enum FnOp : uint8_t {
     FN_OP_RGBA8,       // a = src; P = min, max
     FN_OP_GRADIENT,    // a = pos, b..e = offsets; P[prm..prm+3] = multipliers
     FN_OP_DISTANCE,    // a = offset vector, b = minkowski reg|NONE; aux = df | sqrt<<4
+    FN_OP_WARP_SIMPLEX,// as FN_OP_WARP_GRAD; aux = super (bit 0) | gradient outer product scheme (bit 1)
     FN_OP_COUNT
 };
 

@@ -123,6 +123,56 @@ int Server::submit(const BatchItem& item, uint64_t& ticket)
     return 0;
 }
 
+int Server::submit_many(const BatchItem* items, size_t n, uint64_t* tickets)
+{
+    if (!ok_) { set_error(-6, "server is not running"); return -6; }
+    for (size_t i = 0; i < n; ++i) {        // validate and compile everything before queueing anything
+        const BatchItem& item = items[i];
+        if (!item.node || item.args.total < 0) { set_error(-1, "invalid request " + std::to_string(i)); return -1; }
+        DeviceProgram p;
+        if (!get_program(item.node, item.args.dim, p)) return last_error();
+        const size_t bytes = (size_t)std::max(0ll, item.args.total) * sizeof(float);
+        if (!item.dout && bytes > pool_.capacity()) {
+            set_error(-4, "request " + std::to_string(i) + " output larger than the device pool");
+            return -4;
+        }
+    }
+    const auto now = std::chrono::steady_clock::now();
+    for (size_t i = 0; i < n; ++i) node_ref(const_cast<Node*>(items[i].node));
+    std::lock_guard<std::mutex> lk(mu_);
+    for (size_t i = 0; i < n; ++i) {
+        const uint64_t t = next_ticket_++;
+        Record& r = recs_[t];
+        r.item = items[i];
+        r.t_submit = now;
+        queue_.push_back(t);
+        tickets[i] = t;
+    }
+    submitted_ += n;
+    cv_work_.notify_one();
+    return 0;
+}
+
+int Server::wait_many(const uint64_t* tickets, size_t n, int timeout_ms)
+{
+    std::unique_lock<std::mutex> lk(mu_);
+    for (size_t i = 0; i < n; ++i)
+        if (recs_.find(tickets[i]) == recs_.end()) { set_error(-1, "unknown ticket"); return -1; }
+    auto finished = [&](uint64_t t) { State s = recs_[t].state; return s == kDone || s == kFailed || s == kCancelled; };
+    auto pred = [&] {
+        for (size_t i = 0; i < n; ++i) if (!finished(tickets[i])) return false;
+        return true;
+    };
+    if (timeout_ms < 0) cv_done_.wait(lk, pred);
+    else if (!cv_done_.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) { set_error(-5, "wait timed out"); return -5; }
+    for (size_t i = 0; i < n; ++i) {
+        const State s = recs_[tickets[i]].state;
+        if (s == kFailed) { set_error(-3, "request failed on the device"); return -3; }
+        if (s == kCancelled) { set_error(-6, "request was cancelled"); return -6; }
+    }
+    return 0;
+}
+
 int Server::poll(uint64_t ticket)
 {
     std::lock_guard<std::mutex> lk(mu_);
@@ -214,6 +264,11 @@ void Server::retire()
     std::lock_guard<std::mutex> lk(mu_);
     for (auto& f : flights_) {
         if (!f.busy) continue;
+        // Query the batch's event BEFORE sweeping the done flags: if the event has
+        // completed, every flag the kernel raised is visible to this sweep, so a
+        // request still unmarked afterwards really failed.  (Sweeping first would
+        // race with a kernel that finishes between the sweep and the query.)
+        const cudaError_t q = cudaEventQuery(f.done);
         bool all = true;
         for (uint64_t t : f.tickets) {
             Record& r = recs_[t];
@@ -233,13 +288,13 @@ void Server::retire()
                 all = false;
             }
         }
-        cudaError_t q = cudaEventQuery(f.done);
         if (q == cudaSuccess) {
-            if (!all) {                            // finished without marking: a device-side failure
+            if (!all) {                            // the batch finished without marking these requests
                 for (uint64_t t : f.tickets) {
                     Record& r = recs_[t];
                     if (r.state == kInflight) { r.state = kFailed; free_slots_.push_back(r.slot); ++failed_; any = true; }
                 }
+                set_error(-3, "batch finished without completing every request");
             }
             f.busy = false;
             f.tickets.clear();

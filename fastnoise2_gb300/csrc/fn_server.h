@@ -70,6 +70,11 @@ public:
     bool ok() const { return ok_; }
 
     int submit(const BatchItem& item, uint64_t& ticket);      // item.dout null => pool-allocated output
+    // All-or-nothing submission of n items under one lock (tickets[i] for items[i]).
+    int submit_many(const BatchItem* items, size_t n, uint64_t* tickets);
+    // Wait until every ticket is finished (done, failed or cancelled); FN_ERR_TIMEOUT if
+    // timeout_ms >= 0 runs out first.  Returns 0, or the first failure's status.
+    int wait_many(const uint64_t* tickets, size_t n, int timeout_ms);
     int poll(uint64_t ticket);                                   // 1 done, 0 pending, < 0 error
     int wait(uint64_t ticket, int timeout_ms, float* minmax, float** dout);
     int cancel(uint64_t ticket);                                 // only before admission

@@ -225,6 +225,12 @@ FASTNOISE_API void fnServerDestroy(void* server);
 /* Queue one request.  request->out NULL = the server allocates the output from its pool
  * (admission waits for pool memory).  Tree errors are reported here (FN_ERR_COMPILE). */
 FASTNOISE_API int fnServerSubmit(void* server, const fnGenRequest* request, unsigned long long* ticket);
+/* Queue `count` requests under one lock; all or nothing (nothing is queued if any request is
+ * invalid).  tickets[i] receives the ticket of requests[i]. */
+FASTNOISE_API int fnServerSubmitMany(void* server, const fnGenRequest* requests, int count, unsigned long long* tickets);
+/* Wait until every ticket has finished; FN_ERR_TIMEOUT when timeoutMs (>= 0) runs out first,
+ * else 0 or the status of the first failed / cancelled request. */
+FASTNOISE_API int fnServerWaitMany(void* server, const unsigned long long* tickets, int count, int timeoutMs);
 /* 1 = done, 0 = pending, negative = failed / cancelled / unknown ticket. */
 FASTNOISE_API int fnServerPoll(void* server, unsigned long long ticket);
 /* Wait up to timeoutMs (negative = forever); on success fills minMax (host float[2]) and

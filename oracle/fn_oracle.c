@@ -1537,12 +1537,673 @@ static f32 domain_warp_fractal(const on_node* n, i32 seed, int dim, const f32* p
     return gen_n(warp->lookup[0], seed, dim, warpPos);
 }
 
-/* DomainWarpSimplex / DomainWarpSuperSimplex are declared in the node set but
- * not restated in this oracle; the warp returns zero displacement. */
+/* ---- DomainWarpSimplex / DomainWarpSuperSimplex (DomainWarpSimplex.inl) --
+ * The vector-product helpers follow the portable (non-AVX) branches of
+ * DomainWarpSimplex.inl:40-60, 82-116, 148-191, 221-235, 285-316, 560-695;
+ * FS::Masked*(m, a, b) are written out as selects, FS::SelectHighBit(m, a, b)
+ * as (m < 0 ? a : b). */
+
+static const float kRoot2f = (float)1.4142135623730950488016887242097;
+static const float kRoot3f = (float)1.7320508075688772935274463415059;
+#define WS_SKEW2F ((float)(1.0 / (1.7320508075688772935274463415059 + 1.0)))
+#define WS_SKEW4F ((float)(1.0 / (2.2360679774997896964091736687313 + 1.0)))
+
+static inline f32 ws_selhb(i32 m, f32 a, f32 b) { OC_TICK(1); return (int32_t)m < 0 ? a : b; }
+static inline f32 ws_sel(int m, f32 a, f32 b) { OC_TICK(1); return m ? a : b; }
+
+/* ApplyGradientOuterProductVectorProductSimplex 2D (:7-60) */
+static void ws_gop2(i32 hash31, f32 fX, f32 fY, f32 mul, f32* vX, f32* vY)
+{
+    i32 hs = isrl(hash31, 1);
+    i32 ig = imul(hs, 12 >> 2);
+    i32 io = imul(hs, (int32_t)0xAAAAAAAB) & (int32_t)0xC0000003;
+    {
+        f32 u = ws_selhb(ishl(ig, 2), fY, fX);
+        f32 v = ws_selhb(ishl(ig, 2), fX, fY);
+        f32 a = u * ws_selhb(ig, 2.0f, kRoot3f);
+        f32 b = fs_xor_sign(v, ishl(isra(ig, 30), 31));
+        f32 s = ws_sel((int32_t)ig >= 0, a + b, a);
+        mul = mul * fs_xor_sign(s, ishl(isra(ig, 28) ^ (int32_t)io, 31));
+    }
+    {
+        f32 a = mul * ws_selhb(io, 2.0f, kRoot3f);
+        f32 b = fs_xor_sign(ws_sel((int32_t)io >= 0, mul, 0.0f), ishl(isra(io, 30), 31));
+        *vX = *vX + ws_selhb(ishl(io, 30), b, a);
+        *vY = *vY + ws_selhb(ishl(io, 30), a, b);
+    }
+}
+
+/* ApplyGradientOuterProductVectorProductCommon 3D (:62-116) */
+static void ws_gop3(i32 hash31, f32 fX, f32 fY, f32 fZ, f32 mul, f32* vX, f32* vY, f32* vZ)
+{
+    i32 hs = isrl(hash31, 1);
+    i32 ig = isrl(imul(hs, 12 >> 2), 28);
+    i32 io = imul(hs, (int32_t)0xAAAAAAAB) & (int32_t)0xC0000003;
+    io = (int32_t)io | (int32_t)isra(io, 28);
+    {
+        f32 u = ws_sel((int32_t)ig >= 8, fY, fX);
+        f32 v = ws_sel((int32_t)ig >= 4, fZ, fY);
+        mul = mul * (fs_xor_sign(u, ishl(ig, 31)) + fs_xor_sign(v, ishl(isra(ig, 1), 31)));
+    }
+    {
+        io = (int32_t)io & 0xF;
+        f32 signed0 = fs_xor_sign(mul, ishl(io, 31));
+        f32 signed1 = fs_xor_sign(mul, ishl(isra(io, 1), 31));
+        int notYZ = (int32_t)io < 8;
+        int notXY = (int32_t)io >= 4;
+        *vX = ws_sel(notYZ, *vX + signed0, *vX);
+        *vZ = ws_sel(notXY, *vZ + signed1, *vZ);
+        *vY = ws_sel(notYZ && notXY, *vY, *vY + ws_sel(notXY, signed0, signed1));
+    }
+}
+
+/* one gradient of the 4D outer-product table from a [0,20) << 27 index (:150-171) */
+static void ws_gop4_vector(i32 index, f32* g)
+{
+    i32 iA = (int32_t)index & (0x03 << 27);
+    i32 iB = (int32_t)isra(index, 2) & (0x07 << 27);
+    iB = (int32_t)iB ^ (int32_t)iA;
+    int extra = (int32_t)iB >= (0x04 << 27);
+    int equal = (int32_t)iA == (int32_t)iB;
+    if (equal) iA = -1;
+    f32 neutral = ws_sel(equal || extra, ws_sel(extra, WS_SKEW4F * -1.0f, WS_SKEW4F), 0.0f);
+    for (int k = 0; k < 4; ++k) {
+        f32 t = ws_sel((int32_t)iA == (k << 27), neutral - 1.0f, neutral);
+        g[k] = ws_sel((int32_t)iB == (k << 27), t + 1.0f, t);
+    }
+}
+
+/* ApplyGradientOuterProductVectorProductSimplex 4D (:118-191) */
+static void ws_gop4(i32 hash, f32 fX, f32 fY, f32 fZ, f32 fW, f32 mul, f32* v)
+{
+    i32 hs = isrl(hash, 2);
+    i32 ig = imul(hs, 20 >> 2);
+    i32 io = imul(hs, (int32_t)0xCCCCCCCD);
+    io = imul((int32_t)io & (int32_t)0xE0000003, 3 | (1 << 27));
+    f32 g[4];
+    ws_gop4_vector(ig, g);
+    mul = mul * fs_fma(g[3], fW, fs_fma(g[2], fZ, fs_fma(g[1], fY, g[0] * fX)));
+    ws_gop4_vector(io, g);
+    for (int k = 0; k < 4; ++k) v[k] = fs_fma(mul, g[k], v[k]);
+}
+
+/* ApplyOrthogonalGradientMatrixVectorProductSimplex 2D (:193-235) */
+static void ws_ogm2(i32 hash31, f32 fX, f32 fY, f32 mul, f32* vX, f32* vY)
+{
+    i32 index = imul(isrl(hash31, 1), 12 >> 2);
+    i32 ofThree = isrl(index, 30);
+    i32 signX = ishl(isra(index, 28), 31);
+    i32 signY = ishl(isra(index, 29), 31);
+    f32 masked = ws_sel((int32_t)index >= 0, WS_SKEW2F, 0.0f);
+    f32 gX = fs_xor_sign(ws_sel((int32_t)ofThree != 0, masked + 1.0f, masked), signX);
+    f32 gY = fs_xor_sign(ws_sel((int32_t)ofThree != 1, masked + 1.0f, masked), signY);
+    *vX = fs_fma(mul, fs_fma(fY, gY, fX * gX), *vX);
+    mul = fs_xor_sign(mul, ishl(hash31, 31));
+    *vY = fs_fma(mul, fs_fms(fY, gX, fX * gY), *vY);
+}
+
+/* ApplyOrthogonalGradientMatrixVectorProductCommon 3D (:237-316) */
+static void ws_ogm3(i32 hash31, f32 fX, f32 fY, f32 fZ, f32 mul, f32* vX, f32* vY, f32* vZ)
+{
+    const float cA = 2.224744871391589f, cB = -0.224744871391589f, cC = -1.0f, cDE = 1.0f, cF = 2.0f;
+    i32 hs = isrl(hash31, 1);
+    i32 fb = imul(hs, (int32_t)0xAAAAAAAB);
+    i32 p2hb = ishl(fb, 29);
+    i32 p3 = isrl(imul(hs, 3), 30);
+    i32 finalSign = ishl(hash31, 31);
+    i32 sign0 = ishl(fb, 31);
+    i32 sign1 = (int32_t)ishl(fb, 30) & (int32_t)0x80000000;
+    i32 notYZ = fb;
+    i32 notXY = ishl(fb, 1);
+    i32 either = (int32_t)notYZ | (int32_t)notXY;
+
+    f32 aX = ws_selhb(notYZ, cC, fs_xor_sign(cA, sign0));
+    f32 aY = ws_selhb(either, ws_selhb(notXY, fs_xor_sign(cB, sign1), fs_xor_sign(cA, sign0)), cC);
+    f32 aZ = ws_selhb(notXY, cC, fs_xor_sign(cB, sign1));
+    f32 valA = fs_fma(aZ, fZ, fs_fma(fY, aY, fX * aX));
+
+    f32 bX = ws_selhb(notYZ, cC, fs_xor_sign(cB, sign0));
+    f32 bY = ws_selhb(either, ws_selhb(notXY, fs_xor_sign(cA, sign1), fs_xor_sign(cB, sign0)), cC);
+    f32 bZ = ws_selhb(notXY, cC, fs_xor_sign(cA, sign1));
+    f32 valB = fs_fma(bZ, fZ, fs_fma(fY, bY, fX * bX));
+
+    f32 cX = ws_selhb(notYZ, cF, fs_xor_sign(cDE, sign0));
+    f32 cY = ws_selhb(either, ws_selhb(notXY, fs_xor_sign(cDE, sign1), fs_xor_sign(cDE, sign0)), cF);
+    f32 cZ = ws_selhb(notXY, cF, fs_xor_sign(cDE, sign1));
+    f32 valC = fs_fma(cZ, fZ, fs_fma(fY, cY, fX * cX));
+
+    f32 valAB = ws_selhb(p2hb, valB, valA);
+    f32 valBA = ws_selhb(p2hb, valA, valB);
+
+    mul = fs_xor_sign(mul, finalSign);
+    *vX = fs_fma(mul, ws_sel((int32_t)p3 == 0, valC, valAB), *vX);
+    *vY = fs_fma(mul, ws_sel((int32_t)p3 == 1, valC, ws_sel((int32_t)p3 == 2, valBA, valAB)), *vY);
+    *vZ = fs_fma(mul, ws_sel((int32_t)p3 == 2, valC, valBA), *vZ);
+}
+
+/* ApplyOrthogonalGradientMatrixVectorProductSimplex 4D (:318-695) */
+static void ws_ogm4(i32 hash31, f32 fX, f32 fY, f32 fZ, f32 fW, f32 mul, f32* v)
+{
+    const float kNegAB = -0.375999676691291f;        /* kComponentPairwiseIndexedNegativeAB */
+    const float kFillAB = 0.222726847849776f;        /* kComponentPairwiseUnindexedFillerAB */
+    const float kPosD = -WS_SKEW4F;                  /* kComponentPairwiseIndexedPositiveD */
+    const float kUnD = WS_SKEW4F;                    /* kComponentPairwiseUnindexedD */
+    const float kToSingleAB = -0.124000323308709f;   /* kDeltaPairwiseToSingleAB */
+    const float kToSingleD = 0.190983005625053f;     /* kDeltaPairwiseToSingleD */
+    const float kToExtra = WS_SKEW4F;                /* kDeltaSingleToExtra */
+    const float kABToC = 0.437016024448821f;         /* kDeltaPairwiseABToC */
+    const float kToDiag = -kRoot2f;                  /* kDeltaUnindexedFillerToDiagonal */
+
+    i32 hs = isrl(hash31, 2);
+    i32 indexBasis = imul(hs, 20 >> 2);
+    i32 p3 = isra(imul(hs, (int32_t)0xD5555556), 29);
+    i32 p8 = isra(indexBasis, 24);
+    i32 finalSign = ishl(hash31, 31);
+
+    i32 iPos = (int32_t)indexBasis & (0x03 << 27);
+    i32 iNeg = (int32_t)isra(indexBasis, 2) & (0x03 << 27);
+    iNeg = (int32_t)iNeg ^ (int32_t)iPos;
+
+    /* (0x10 << 27) wraps to INT32_MIN, so with FastSIMD's signed int32 compares
+     * this mask is always set in the portable branch (:567) */
+    int extraCase = (int32_t)indexBasis >= INT32_MIN;
+    int singleCase = (int32_t)iPos == (int32_t)iNeg;
+    int singleNonExtra = (int32_t)indexBasis < (0x04 << 27);
+    if (singleNonExtra) iPos = -1;
+
+    f32 singleOffsetAB = ws_sel(extraCase, kToSingleAB + kToExtra, kToSingleAB);
+    f32 negAB = ws_sel(singleCase, kNegAB + singleOffsetAB, kNegAB);
+    f32 fillAB = ws_sel(singleCase, kFillAB + singleOffsetAB, kFillAB);
+    f32 negC = ws_sel(singleCase, negAB, negAB + kABToC);
+    f32 fillC = ws_sel(singleCase, fillAB, fillAB + kABToC);
+    f32 singleOffsetD = ws_sel(extraCase, kToSingleD + kToExtra, kToSingleD);
+    f32 posD = ws_sel(singleCase, kPosD + singleOffsetD, kPosD);
+    f32 unD = ws_sel(singleCase, kUnD + singleOffsetD, kUnD);
+
+    int counter = -1;
+    f32 valA = 0.0f, valB = 0.0f, valC = 0.0f, valD = 0.0f;
+    const f32 f[4] = {fX, fY, fZ, fW};
+    for (int k = 0; k < 4; ++k) {
+        int idxPos = (int32_t)iPos == (k << 27);
+        int indexed = idxPos || (int32_t)iNeg == (k << 27);
+        f32 icAB = ws_sel(idxPos, negAB + 1.0f, negAB);
+        f32 icC = ws_sel(idxPos, negC + 1.0f, negC);
+        f32 icD = ws_sel(!idxPos, posD - 1.0f, posD);
+        f32 uA, uB, uC;
+        if (k == 0) {
+            uA = fillAB + kToDiag; uB = fillAB; uC = fillC;
+        } else if (k == 1) {
+            uA = ws_sel(counter == -2, fillAB + kToDiag, fillAB);
+            uB = ws_sel(counter == -1, fillAB + kToDiag, fillAB);
+            uC = fillC;
+        } else if (k == 2) {
+            uA = ws_sel(counter == -3, fillAB + kToDiag, fillAB);
+            uB = ws_sel(counter == -2, fillAB + kToDiag, fillAB);
+            uC = ws_sel(counter == -1, fillC + kToDiag, fillC);
+        } else {
+            uA = fillAB;
+            uB = ws_sel(counter == -3, fillAB + kToDiag, fillAB);
+            uC = ws_sel(counter == -2, fillC + kToDiag, fillC);
+        }
+        f32 gA = ws_sel(indexed, icAB, uA);
+        f32 gB = ws_sel(indexed, icAB, uB);
+        f32 gC = ws_sel(indexed, icC, uC);
+        f32 gD = ws_sel(indexed, icD, unD);
+        if (k < 3 && indexed) counter -= 1;
+        if (k == 0) { valA = gA * f[0]; valB = gB * f[0]; valC = gC * f[0]; valD = gD * f[0]; }
+        else { valA = fs_fma(gA, f[k], valA); valB = fs_fma(gB, f[k], valB); valC = fs_fma(gC, f[k], valC); valD = fs_fma(gD, f[k], valD); }
+    }
+
+    i32 ix = isra(p8, 1);
+    i32 iy = iadd(iadd(ix, 1), p3);
+    i32 iz = (int32_t)p8 & 1;
+    iz = iadd(iadd(ix, 1), (int32_t)iz >= (int32_t)p3 ? iadd(iz, 1) : iz);
+    i32 isum = iadd(iadd(ix, iy), iz);
+
+    mul = fs_xor_sign(mul, finalSign);
+#define WS_PICK4(I, A_, B_, C_, D_) ws_selhb(ishl(I, 31), ws_selhb(ishl(I, 30), D_, B_), ws_selhb(ishl(I, 30), C_, A_))
+    v[0] = fs_fma(mul, WS_PICK4(ix, valA, valB, valC, valD), v[0]);
+    v[1] = fs_fma(mul, WS_PICK4(iy, valA, valB, valC, valD), v[1]);
+    v[2] = fs_fma(mul, WS_PICK4(iz, valA, valB, valC, valD), v[2]);
+    v[3] = fs_fma(mul, ws_selhb(ishl(isum, 31), ws_selhb(ishl(isum, 30), valD, valB), ws_selhb(ishl(isum, 30), valA, valC)), v[3]);
+#undef WS_PICK4
+}
+
+static void ws_vec2(int gop, i32 h, f32 fX, f32 fY, f32 mul, f32* v)
+{
+    if (gop) ws_gop2(h, fX, fY, mul, &v[0], &v[1]);
+    else ws_ogm2(h, fX, fY, mul, &v[0], &v[1]);
+}
+static void ws_vec3(int gop, i32 h, f32 fX, f32 fY, f32 fZ, f32 mul, f32* v)
+{
+    if (gop) ws_gop3(h, fX, fY, fZ, mul, &v[0], &v[1], &v[2]);
+    else ws_ogm3(h, fX, fY, fZ, mul, &v[0], &v[1], &v[2]);
+}
+static void ws_vec4(int gop, i32 h, f32 fX, f32 fY, f32 fZ, f32 fW, f32 mul, f32* v)
+{
+    if (gop) ws_gop4(h, fX, fY, fZ, fW, mul, v);
+    else ws_ogm4(h, fX, fY, fZ, fW, mul, v);
+}
+static inline f32 ws_pow4(f32 f) { f = f * f; return f * f; }
+static inline i32 ws_madd(int m, i32 a, i32 b) { OC_TICK(1); return m ? iadd(a, b) : a; }
+
+/* DomainWarpSimplex Warp_2D (:771-833) */
+static void ws_simplex2(int gop, i32 seed, const f32* p, f32* v)
+{
+    const double kSkew2 = 1.0 / (kRoot3 + 1.0), kUnskew2 = -1.0 / (kRoot3 + 3.0), kR2 = 0.5;
+    f32 x = p[0], y = p[1];
+    f32 skewDelta = (float)kSkew2 * (x + y);
+    f32 xs = x + skewDelta, ys = y + skewDelta;
+    f32 xb = fs_floor(xs), yb = fs_floor(ys);
+    f32 dxs = xs - xb, dys = ys - yb;
+    i32 xp = imul(fs_cvt_i(xb), PRIME_X), yp = imul(fs_cvt_i(yb), PRIME_Y);
+    int xGEy = dxs >= dys;
+    f32 unskewDelta = (float)kUnskew2 * (dxs + dys);
+    f32 dx0 = dxs + unskewDelta, dy0 = dys + unskewDelta;
+    f32 dx1 = ws_sel(!xGEy, dx0 + 1.0f, dx0) - (float)(kUnskew2 + 1);
+    f32 dy1 = ws_sel(xGEy, dy0 + 1.0f, dy0) - (float)(kUnskew2 + 1);
+    f32 dx2 = dx0 - (float)(kUnskew2 * 2 + 1);
+    f32 dy2 = dy0 - (float)(kUnskew2 * 2 + 1);
+    f32 f0 = fs_fnma(dx0, dx0, fs_fnma(dy0, dy0, (float)kR2));
+    f32 f1 = fs_fnma(dx1, dx1, fs_fnma(dy1, dy1, (float)kR2));
+    f32 f2 = f0 + fs_fma(unskewDelta, (float)(-4.0 * (kRoot3 + 2.0) / (kRoot3 + 3.0)), (float)(-2.0 / 3.0));
+    f0 = ws_pow4(fs_max(f0, 0.0f)); f1 = ws_pow4(fs_max(f1, 0.0f)); f2 = ws_pow4(fs_max(f2, 0.0f));
+    v[0] = 0.0f; v[1] = 0.0f;
+    ws_vec2(gop, hash2(seed, xp, yp), dx0, dy0, f0, v);
+    ws_vec2(gop, hash2(seed, ws_madd(xGEy, xp, PRIME_X), ws_madd(!xGEy, yp, PRIME_Y)), dx1, dy1, f1, v);
+    ws_vec2(gop, hash2(seed, iadd(xp, PRIME_X), iadd(yp, PRIME_Y)), dx2, dy2, f2, v);
+}
+
+/* DomainWarpSimplex Warp_3D (:835-931) */
+static void ws_simplex3(int gop, i32 seed, const f32* p, f32* v)
+{
+    const double kSkew3 = 1.0 / 3.0, kRU3 = -1.0 / 2.0, kR2 = 0.6;
+    f32 x = p[0], y = p[1], z = p[2];
+    f32 skewDelta = (float)kSkew3 * (x + y + z);
+    f32 xs = x + skewDelta, ys = y + skewDelta, zs = z + skewDelta;
+    f32 xb = fs_floor(xs), yb = fs_floor(ys), zb = fs_floor(zs);
+    f32 dxs = xs - xb, dys = ys - yb, dzs = zs - zb;
+    i32 xp = imul(fs_cvt_i(xb), PRIME_X), yp = imul(fs_cvt_i(yb), PRIME_Y), zp = imul(fs_cvt_i(zb), PRIME_Z);
+    int xGEy = dxs >= dys, yGEz = dys >= dzs, xGEz = dxs >= dzs;
+    f32 unskewDelta = (float)kRU3 * (dxs + dys + dzs);
+    f32 dx0 = dxs + unskewDelta, dy0 = dys + unskewDelta, dz0 = dzs + unskewDelta;
+    int maskX1 = xGEy && xGEz;
+    int maskY1 = yGEz && !xGEy;
+    int maskZ1 = xGEz || yGEz;          /* inverted */
+    int nMaskX2 = xGEy || xGEz;         /* inverted */
+    int nMaskY2 = xGEy && !yGEz;
+    int nMaskZ2 = xGEz && yGEz;
+    f32 dx3 = dx0 - (float)(kRU3 * 3 + 1), dy3 = dy0 - (float)(kRU3 * 3 + 1), dz3 = dz0 - (float)(kRU3 * 3 + 1);
+    f32 dx1 = ws_sel(maskX1, dx3 - 1.0f, dx3);
+    f32 dy1 = ws_sel(maskY1, dy3 - 1.0f, dy3);
+    f32 dz1 = ws_sel(maskZ1, dz3, dz3 - 1.0f);
+    f32 dx2 = ws_sel(!nMaskX2, dx0 + 1.0f, dx0);
+    f32 dy2 = ws_sel(nMaskY2, dy0 + 1.0f, dy0);
+    f32 dz2 = ws_sel(nMaskZ2, dz0 + 1.0f, dz0);
+    f32 f0 = fs_fnma(dz0, dz0, fs_fnma(dy0, dy0, fs_fnma(dx0, dx0, (float)kR2)));
+    f32 f1 = fs_fnma(dz1, dz1, fs_fnma(dy1, dy1, fs_fnma(dx1, dx1, (float)kR2)));
+    f32 f2 = fs_fnma(dz2, dz2, fs_fnma(dy2, dy2, fs_fnma(dx2, dx2, (float)kR2)));
+    f32 f3 = f0 - (unskewDelta + (float)(3.0 / 4.0));
+    f0 = ws_pow4(fs_max(f0, 0.0f)); f1 = ws_pow4(fs_max(f1, 0.0f)); f2 = ws_pow4(fs_max(f2, 0.0f)); f3 = ws_pow4(fs_max(f3, 0.0f));
+    v[0] = 0.0f; v[1] = 0.0f; v[2] = 0.0f;
+    ws_vec3(gop, hash3(seed, xp, yp, zp), dx0, dy0, dz0, f0, v);
+    ws_vec3(gop, hash3(seed, ws_madd(maskX1, xp, PRIME_X), ws_madd(maskY1, yp, PRIME_Y), ws_madd(!maskZ1, zp, PRIME_Z)), dx1, dy1, dz1, f1, v);
+    ws_vec3(gop, hash3(seed, ws_madd(nMaskX2, xp, PRIME_X), ws_madd(!nMaskY2, yp, PRIME_Y), ws_madd(!nMaskZ2, zp, PRIME_Z)), dx2, dy2, dz2, f2, v);
+    ws_vec3(gop, hash3(seed, iadd(xp, PRIME_X), iadd(yp, PRIME_Y), iadd(zp, PRIME_Z)), dx3, dy3, dz3, f3, v);
+    if (gop) {                          /* match gradient orientation (:909-917) */
+        f32 d = (float)(-2.0 / 2.0) * (v[0] + v[1] + v[2]);
+        v[0] = v[0] + d; v[1] = v[1] + d; v[2] = v[2] + d;
+    }
+}
+
+/* DomainWarpSimplex Warp_4D (:933-1089) */
+static void ws_simplex4(int gop, i32 seed, const f32* p, f32* v)
+{
+    const double kSkew4 = 1.0 / (kRoot5 + 1.0), kUnskew4 = -1.0 / (kRoot5 + 5.0), kR2 = 0.6;
+    static const int32_t primes[4] = {PRIME_X, PRIME_Y, PRIME_Z, PRIME_W};
+    f32 skewDelta = (float)kSkew4 * (p[0] + p[1] + p[2] + p[3]);
+    f32 ds[4], d0[4];
+    i32 pb[4];
+    for (int k = 0; k < 4; ++k) {
+        f32 sk = p[k] + skewDelta;
+        f32 b = fs_floor(sk);
+        ds[k] = sk - b;
+        pb[k] = imul(fs_cvt_i(b), primes[k]);
+    }
+    f32 unskewDelta = (float)kUnskew4 * (ds[0] + ds[1] + ds[2] + ds[3]);
+    for (int k = 0; k < 4; ++k) d0[k] = ds[k] + unskewDelta;
+    int rank[4] = {0, 0, 0, 0};
+    for (int a = 0; a < 4; ++a)
+        for (int b = a + 1; b < 4; ++b) {
+            if (d0[a] >= d0[b]) rank[a]++; else rank[b]++;
+        }
+    f32 d[5][4];
+    f32 fo[5];
+    for (int k = 0; k < 4; ++k) {
+        d[0][k] = d0[k];
+        d[1][k] = ws_sel(rank[k] > 2, d0[k] - 1.0f, d0[k]) - (float)kUnskew4;
+        d[2][k] = ws_sel(rank[k] > 1, d0[k] - 1.0f, d0[k]) - (float)(kUnskew4 * 2);
+        d[3][k] = ws_sel(rank[k] > 0, d0[k] - 1.0f, d0[k]) - (float)(kUnskew4 * 3);
+        d[4][k] = d0[k] - (float)(kUnskew4 * 4 + 1);
+    }
+    for (int i = 0; i < 4; ++i)
+        fo[i] = fs_fnma(d[i][3], d[i][3], fs_fnma(d[i][2], d[i][2], fs_fnma(d[i][1], d[i][1], fs_fnma(d[i][0], d[i][0], (float)kR2))));
+    fo[4] = fo[0] + fs_fma(unskewDelta, (float)(-4.0 * (kRoot5 + 3.0) / (kRoot5 + 5.0)), (float)(-4.0 / 5.0));
+    for (int i = 0; i < 5; ++i) fo[i] = ws_pow4(fs_max(fo[i], 0.0f));
+    v[0] = 0.0f; v[1] = 0.0f; v[2] = 0.0f; v[3] = 0.0f;
+    for (int i = 0; i < 5; ++i) {
+        i32 c[4];
+        for (int k = 0; k < 4; ++k) {
+            int m = i == 0 ? 0 : i == 4 ? 1 : rank[k] > 3 - i;
+            c[k] = ws_madd(m, pb[k], primes[k]);
+        }
+        ws_vec4(gop, hash4(seed, c[0], c[1], c[2], c[3]), d[i][0], d[i][1], d[i][2], d[i][3], fo[i], v);
+    }
+}
+
+/* DomainWarpSuperSimplex Warp_2D (:1131-1218) */
+static void ws_super2(int gop, i32 seed, const f32* p, f32* v)
+{
+    const double kSkew2 = 1.0 / (kRoot3 + 1.0), kUnskew2 = -1.0 / (kRoot3 + 3.0), kR2 = 2.0 / 3.0;
+    f32 x = p[0], y = p[1];
+    f32 skewDelta = (float)kSkew2 * (x + y);
+    f32 xs = x + skewDelta, ys = y + skewDelta;
+    f32 xb = fs_floor(xs), yb = fs_floor(ys);
+    f32 dxs = xs - xb, dys = ys - yb;
+    i32 xp = imul(fs_cvt_i(xb), PRIME_X), yp = imul(fs_cvt_i(yb), PRIME_Y);
+    int fXY = dxs + dys > 1.0f;
+    f32 boundaryXY = ws_sel(fXY, -1.0f, 0.0f);
+    int fX = fs_fma(dxs, -2.0f, dys) < boundaryXY;
+    int fY = fs_fma(dys, -2.0f, dxs) < boundaryXY;
+    f32 unskewDelta = (float)kUnskew2 * (dxs + dys);
+    f32 dxB = dxs + unskewDelta, dyB = dys + unskewDelta;
+    v[0] = 0.0f; v[1] = 0.0f;
+    f32 fb0;
+    {   /* <0, 0> */
+        fb0 = fs_fnma(dxB, dxB, fs_fnma(dyB, dyB, (float)kR2));
+        ws_vec2(gop, hash2(seed, xp, yp), dxB, dyB, ws_pow4(fb0), v);
+    }
+    {   /* <1, 1> */
+        f32 f = fs_fma(unskewDelta, (float)(-4.0 * (kRoot3 + 2.0) / (kRoot3 + 3.0)), fb0 - (float)kR2);
+        ws_vec2(gop, hash2(seed, iadd(xp, PRIME_X), iadd(yp, PRIME_Y)),
+                dxB - (float)(2 * kUnskew2 + 1), dyB - (float)(2 * kUnskew2 + 1), ws_pow4(f), v);
+    }
+    f32 xyDelta = ws_sel(fXY, (float)(kUnskew2 + 1), (float)(-kUnskew2));
+    dxB = dxB - xyDelta;
+    dyB = dyB - xyDelta;
+    {   /* <1, 0> or <-1, 0> or <1, 2> */
+        i32 hx = ws_madd(fX, xp, imul(PRIME_X, 2));
+        hx = fXY ? hx : isub(hx, PRIME_X);
+        i32 h = hash2(seed, hx, ws_madd(fXY, yp, PRIME_Y));
+        f32 dx = dxB - ws_sel(fX, (float)(1 + 2 * kUnskew2), -1.0f);
+        f32 dy = ws_sel(fX, dyB - (float)(2 * kUnskew2), dyB);
+        f32 f = fs_max(fs_fnma(dx, dx, fs_fnma(dy, dy, (float)kR2)), 0.0f);
+        ws_vec2(gop, h, dx, dy, ws_pow4(f), v);
+    }
+    {   /* <0, 1> or <0, -1> or <2, 1> */
+        i32 hy = ws_madd(fY, yp, imul(PRIME_Y, 2));
+        hy = fXY ? hy : isub(hy, PRIME_Y);
+        i32 h = hash2(seed, ws_madd(fXY, xp, PRIME_X), hy);
+        f32 dx = ws_sel(fY, dxB - (float)(2 * kUnskew2), dxB);
+        f32 dy = dyB - ws_sel(fY, (float)(1 + 2 * kUnskew2), -1.0f);
+        f32 f = fs_max(fs_fnma(dx, dx, fs_fnma(dy, dy, (float)kR2)), 0.0f);
+        ws_vec2(gop, h, dx, dy, ws_pow4(f), v);
+    }
+}
+
+static inline f32 ws_fb4(f32 fb) { return (fb * fb) * (fb * fb); }
+#define WS_SIGNBIT ((int32_t)0x80000000)
+
+/* DomainWarpSuperSimplex Warp_3D (:1220-1446) */
+static void ws_super3(int gop, i32 seed, const f32* p, f32* v)
+{
+    const double kSkew3 = 1.0 / 3.0, kRU3 = -1.0 / 2.0, kTU3 = -1.0 / 4.0, kDA = 3.0 / 4.0, kDB = 1.0, kR2 = kDA;
+    f32 x = p[0], y = p[1], z = p[2];
+    f32 skewDelta = (float)kSkew3 * (x + y + z);
+    f32 xs = x + skewDelta, ys = y + skewDelta, zs = z + skewDelta;
+    f32 xb = fs_floor(xs), yb = fs_floor(ys), zb = fs_floor(zs);
+    f32 dxs = xs - xb, dys = ys - yb, dzs = zs - zb;
+    {   /* closest vertex of the unit cell */
+        f32 tu = (float)kTU3 * (dxs + dys + dzs);
+        f32 xN = dxs + tu, yN = dys + tu, zN = dzs + tu;
+        f32 xyzN = -tu;
+        f32 maxScore = 0.375f;
+        int32_t bits = xyzN > maxScore ? -1 : 0;
+        maxScore = fs_max(maxScore, xyzN);
+#define WS_CONSIDER(score, b) do { f32 s_ = (score); bits = s_ > maxScore ? (b) : bits; maxScore = fs_max(maxScore, s_); } while (0)
+        WS_CONSIDER(xN, 1);
+        WS_CONSIDER(yN, 2);
+        WS_CONSIDER(zN, 4);
+        maxScore = maxScore + (0.125f - xyzN);
+        WS_CONSIDER(-zN, 3);
+        WS_CONSIDER(-yN, 5);
+        WS_CONSIDER(-xN, 6);
+        int mx = (bits & 1) != 0, my = (bits & 2) != 0, mz = (bits & 4) != 0;
+        xb = ws_sel(mx, xb + 1.0f, xb); yb = ws_sel(my, yb + 1.0f, yb); zb = ws_sel(mz, zb + 1.0f, zb);
+        dxs = ws_sel(mx, dxs - 1.0f, dxs); dys = ws_sel(my, dys - 1.0f, dys); dzs = ws_sel(mz, dzs - 1.0f, dzs);
+    }
+    i32 xp = imul(fs_cvt_i(xb), PRIME_X), yp = imul(fs_cvt_i(yb), PRIME_Y), zp = imul(fs_cvt_i(zb), PRIME_Z);
+    f32 scs = dxs + dys + dzs;
+    f32 tu = (float)kTU3 * scs;
+    f32 xN = dxs + tu, yN = dys + tu, zN = dzs + tu;
+    f32 xyzN = -tu;
+    f32 ud = (float)kRU3 * scs;
+    f32 dxB = dxs + ud, dyB = dys + ud, dzB = dzs + ud;
+    f32 cs = (float)(1 + 3 * kRU3) * scs;
+    v[0] = 0.0f; v[1] = 0.0f; v[2] = 0.0f;
+    f32 stemA, stemB;
+    {   /* <0,0,0> */
+        f32 fb = fs_fnma(dzB, dzB, fs_fnma(dyB, dyB, fs_fnma(dxB, dxB, (float)kR2))) * 0.5f;
+        stemA = fb - (float)(kDA * 0.5);
+        stemB = fb - (float)(kDB * 0.5);
+        ws_vec3(gop, hash3(seed, xp, yp, zp), dxB, dyB, dzB, ws_fb4(fb), v);
+    }
+    {   /* <1,1,1> or <-1,-1,-1> */
+        int sm = xyzN < 0.0f;
+        i32 sign = sm ? WS_SIGNBIT : 0;
+        f32 off = fs_xor_sign((float)(3 * kRU3 + 1), sign);
+        f32 fb = fs_max(fs_fma(off, cs, stemA), 0.0f);
+        ws_vec3(gop, hash3(seed, iadd(xp, sm ? -PRIME_X : PRIME_X), iadd(yp, sm ? -PRIME_Y : PRIME_Y), iadd(zp, sm ? -PRIME_Z : PRIME_Z)),
+                dxB - off, dyB - off, dzB - off, ws_fb4(fb), v);
+    }
+    /* <1,1,0>, <1,0,1>, <0,1,1> or their negatives */
+    {
+        int sm = xyzN < zN;
+        i32 sign = sm ? WS_SIGNBIT : 0;
+        f32 off0 = fs_xor_sign((float)(2 * kRU3), sign);
+        f32 fb = fs_min(fs_xor_sign(dzB, sign) - stemB, 0.0f);
+        ws_vec3(gop, hash3(seed, iadd(xp, sm ? -PRIME_X : PRIME_X), iadd(yp, sm ? -PRIME_Y : PRIME_Y), zp),
+                dxB, dyB, dzB - off0, ws_fb4(fb), v);
+    }
+    {
+        int sm = xyzN < yN;
+        i32 sign = sm ? WS_SIGNBIT : 0;
+        f32 off0 = fs_xor_sign((float)(2 * kRU3), sign);
+        f32 fb = fs_min(fs_xor_sign(dyB, sign) - stemB, 0.0f);
+        ws_vec3(gop, hash3(seed, iadd(xp, sm ? -PRIME_X : PRIME_X), yp, iadd(zp, sm ? -PRIME_Z : PRIME_Z)),
+                dxB, dyB - off0, dzB, ws_fb4(fb), v);
+    }
+    {
+        int sm = xyzN < xN;
+        i32 sign = sm ? WS_SIGNBIT : 0;
+        f32 off0 = fs_xor_sign((float)(2 * kRU3), sign);
+        f32 fb = fs_min(fs_xor_sign(dxB, sign) - stemB, 0.0f);
+        ws_vec3(gop, hash3(seed, xp, iadd(yp, sm ? -PRIME_Y : PRIME_Y), iadd(zp, sm ? -PRIME_Z : PRIME_Z)),
+                dxB - off0, dyB, dzB, ws_fb4(fb), v);
+    }
+    /* <1,0,0>, <0,1,0>, <0,0,1> or their negatives */
+    {
+        int sm = xN < 0.0f;
+        i32 sign = sm ? WS_SIGNBIT : 0;
+        f32 off0 = fs_xor_sign((float)kRU3, sign);
+        f32 fb = fs_max(fs_fma(off0, cs, stemA) + fs_xor_sign(dxB, sign), 0.0f);
+        ws_vec3(gop, hash3(seed, iadd(xp, sm ? -PRIME_X : PRIME_X), yp, zp), dxB + off0, dyB - off0, dzB - off0, ws_fb4(fb), v);
+    }
+    {
+        int sm = yN < 0.0f;
+        i32 sign = sm ? WS_SIGNBIT : 0;
+        f32 off0 = fs_xor_sign((float)kRU3, sign);
+        f32 fb = fs_max(fs_fma(off0, cs, stemA) + fs_xor_sign(dyB, sign), 0.0f);
+        ws_vec3(gop, hash3(seed, xp, iadd(yp, sm ? -PRIME_Y : PRIME_Y), zp), dxB - off0, dyB + off0, dzB - off0, ws_fb4(fb), v);
+    }
+    {
+        int sm = zN < 0.0f;
+        i32 sign = sm ? WS_SIGNBIT : 0;
+        f32 off0 = fs_xor_sign((float)kRU3, sign);
+        f32 fb = fs_max(fs_fma(off0, cs, stemA) + fs_xor_sign(dzB, sign), 0.0f);
+        ws_vec3(gop, hash3(seed, xp, yp, iadd(zp, sm ? -PRIME_Z : PRIME_Z)), dxB - off0, dyB - off0, dzB + off0, ws_fb4(fb), v);
+    }
+    if (gop) {                          /* match gradient orientation (:1424-1432) */
+        f32 d = (float)(-2.0 / 3.0) * (v[0] + v[1] + v[2]);
+        v[0] = v[0] + d; v[1] = v[1] + d; v[2] = v[2] + d;
+    }
+}
+
+/* DomainWarpSuperSimplex Warp_4D (:1448-1835).  The sixteen vertices around
+ * the closest lattice vertex are visited in the reference's order; a vertex is
+ * the set of axes it moves along (bit k = axis k), in the direction given by
+ * the sign test of its group. */
+static void ws_super4(int gop, i32 seed, const f32* p, f32* v)
+{
+    const double kSkew4 = 1.0 / (kRoot5 + 1.0), kU4 = -1.0 / (kRoot5 + 5.0), kTU4 = -1.0 / 5.0;
+    const double kDA = 4.0 / 5.0, kDB = 6.0 / 5.0, kR2 = kDA;
+    static const int32_t primes[4] = {PRIME_X, PRIME_Y, PRIME_Z, PRIME_W};
+    static const int order[16] = {0x0, 0xF, 0x7, 0xB, 0xD, 0xE, 0x1, 0x3, 0x5, 0x9, 0x2, 0x6, 0xA, 0x4, 0xC, 0x8};
+    f32 skewDelta = (float)kSkew4 * (p[0] + p[1] + p[2] + p[3]);
+    f32 b[4], ds[4];
+    for (int k = 0; k < 4; ++k) {
+        f32 sk = p[k] + skewDelta;
+        b[k] = fs_floor(sk);
+        ds[k] = sk - b[k];
+    }
+    {   /* closest vertex of the unit cell */
+        f32 tu = (float)kTU4 * (ds[0] + ds[1] + ds[2] + ds[3]);
+        f32 n[4];
+        for (int k = 0; k < 4; ++k) n[k] = ds[k] + tu;
+        f32 xyzwN = -tu;
+        f32 maxScore = 0.6f - xyzwN;
+        int32_t bits = 0.2f > maxScore ? -1 : 0;
+        maxScore = fs_max(maxScore, 0.2f);
+        WS_CONSIDER(-n[3], 0x7);
+        WS_CONSIDER(-n[2], 0xB);
+        WS_CONSIDER(-n[1], 0xD);
+        WS_CONSIDER(-n[0], 0xE);
+        maxScore = maxScore + (xyzwN - 0.2f);
+        WS_CONSIDER(n[0], 0x1);
+        WS_CONSIDER(n[1], 0x2);
+        WS_CONSIDER(n[2], 0x4);
+        WS_CONSIDER(n[3], 0x8);
+        maxScore = maxScore + (0.2f - n[0]);
+        WS_CONSIDER(n[1], 0x3);
+        WS_CONSIDER(n[2], 0x5);
+        WS_CONSIDER(n[3], 0x9);
+        maxScore = maxScore + n[0];
+        WS_CONSIDER(n[1] + n[2], 0x6);
+        maxScore = maxScore - n[3];
+        WS_CONSIDER(n[1], 0xA);
+        WS_CONSIDER(n[2], 0xC);
+        for (int k = 0; k < 4; ++k) {
+            int m = (bits >> k) & 1;
+            b[k] = ws_sel(m, b[k] + 1.0f, b[k]);
+            ds[k] = ws_sel(m, ds[k] - 1.0f, ds[k]);
+        }
+    }
+    i32 pb[4];
+    for (int k = 0; k < 4; ++k) pb[k] = imul(fs_cvt_i(b[k]), primes[k]);
+    f32 scs = ds[0] + ds[1] + ds[2] + ds[3];
+    f32 tu = (float)kTU4 * scs;
+    f32 n[4], dB[4];
+    for (int k = 0; k < 4; ++k) n[k] = ds[k] + tu;
+    f32 xyzwN = -tu;
+    f32 ud = (float)kU4 * scs;
+    for (int k = 0; k < 4; ++k) dB[k] = ds[k] + ud;
+    f32 cs = (float)(1 + 4 * kU4) * scs;
+    v[0] = 0.0f; v[1] = 0.0f; v[2] = 0.0f; v[3] = 0.0f;
+    f32 stemA = 0.0f, stemB = 0.0f;
+    for (int vi = 0; vi < 16; ++vi) {
+        const int S = order[vi];
+        const int cnt = (S & 1) + ((S >> 1) & 1) + ((S >> 2) & 1) + ((S >> 3) & 1);
+        if (cnt == 0) {
+            f32 fb = fs_fnma(dB[3], dB[3], fs_fnma(dB[2], dB[2], fs_fnma(dB[1], dB[1], fs_fnma(dB[0], dB[0], (float)kR2)))) * 0.5f;
+            stemA = fb - (float)(kDA * 0.5);
+            stemB = fb - (float)(kDB * 0.5);
+            ws_vec4(gop, hash4(seed, pb[0], pb[1], pb[2], pb[3]), dB[0], dB[1], dB[2], dB[3], ws_fb4(fb), v);
+            continue;
+        }
+        int sm;
+        f32 off1, off0, fb;
+        int a = -1, bb = -1;                      /* the one or two axes of single / pair vertices */
+        for (int k = 0; k < 4; ++k) if ((S >> k) & 1) { if (a < 0) a = k; else if (bb < 0) bb = k; }
+        int missing = -1;
+        for (int k = 0; k < 4; ++k) if (!((S >> k) & 1)) missing = k;
+        if (cnt == 4) sm = xyzwN < 0.0f;
+        else if (cnt == 3) sm = xyzwN < n[missing];
+        else if (cnt == 1) sm = n[a] < 0.0f;
+        else sm = n[a] < -n[bb];
+        i32 sign = sm ? WS_SIGNBIT : 0;
+        if (cnt == 4) {
+            off1 = fs_xor_sign((float)(4 * kU4 + 1), sign);
+            off0 = off1;
+            fb = fs_max(fs_fma(off1, cs, stemA), 0.0f);
+        } else if (cnt == 3) {
+            off1 = fs_xor_sign((float)(3 * kU4 + 1), sign);
+            off0 = fs_xor_sign((float)(3 * kU4), sign);
+            fb = fs_max(fs_fma(off1, cs, stemB) - fs_xor_sign(dB[missing], sign), 0.0f);
+        } else if (cnt == 1) {
+            off1 = fs_xor_sign((float)(kU4 + 1), sign);
+            off0 = fs_xor_sign((float)kU4, sign);
+            fb = fs_max(fs_fma(off0, cs, stemA) + fs_xor_sign(dB[a], sign), 0.0f);
+        } else {
+            off1 = fs_xor_sign((float)(2 * kU4 + 1), sign);
+            off0 = fs_xor_sign((float)(2 * kU4), sign);
+            fb = fs_max(fs_fma(off0, cs, stemB) + fs_xor_sign(dB[a] + dB[bb], sign), 0.0f);
+        }
+        i32 c[4];
+        f32 d[4];
+        for (int k = 0; k < 4; ++k) {
+            int in = (S >> k) & 1;
+            c[k] = in ? iadd(pb[k], sm ? -primes[k] : primes[k]) : pb[k];
+            d[k] = dB[k] - (in ? off1 : off0);
+        }
+        ws_vec4(gop, hash4(seed, c[0], c[1], c[2], c[3]), d[0], d[1], d[2], d[3], ws_fb4(fb), v);
+    }
+}
+#undef WS_CONSIDER
+
+/* DomainWarpSimplex / DomainWarpSuperSimplex ::Warp (:729-769, :1092-1129):
+ * seed offset, the vector noise, bounding x axis scale, out += v * amp;
+ * returns |v|^2. */
+static f32 warp_simplex(const on_node* n, i32 seed, f32 warpAmp, int dim, const f32* pin, f32* out)
+{
+    const int super = n->id == N_DOMAINWARPSUPERSIMPLEX;
+    const int gop = n->vec_scheme == 1;
+    seed = iadd(seed, n->seed_offset);
+    f32 v[4];
+    float bound;
+    if (dim == 2) {
+        if (super) ws_super2(gop, seed, pin, v); else ws_simplex2(gop, seed, pin, v);
+        bound = super ? (gop ? (float)(9.28993664146183 / 2.0) : 12.814453124999995f)
+                      : (gop ? (float)(49.918426513671875 / 2.0) : 70.1480577066486f);
+    } else if (dim == 3) {
+        if (super) ws_super3(gop, seed, pin, v); else ws_simplex3(gop, seed, pin, v);
+        bound = super ? (gop ? (float)(144.736422163332608 / 1.4142135623730951) : 37.63698669623629f)
+                      : (gop ? (float)(32.69428253173828125 / 1.4142135623730951) : 16.281631889139874f);
+    } else {
+        if (super) ws_super4(gop, seed, pin, v); else ws_simplex4(gop, seed, pin, v);
+        bound = super ? (gop ? (float)(115.21625311930542 / 1.4142135623730951) : 48.80058117543753f)
+                      : (gop ? (float)(33.653125584827855 / 1.4142135623730951) : 30.88161777516092f);
+    }
+    for (int k = 0; k < dim; ++k) v[k] = v[k] * (float)(bound * n->axis[k]);
+    for (int k = 0; k < dim; ++k) out[k] = fs_fma(v[k], warpAmp, out[k]);
+    f32 r = v[0] * v[0];
+    for (int k = 1; k < dim; ++k) r = fs_fma(v[k], v[k], r);
+    return r;
+}
+
 static f32 warp_any(const on_node* w, i32 seed, f32 amp, int dim, const f32* scaled, f32* out)
 {
     if (w->id == N_DOMAINWARPGRADIENT) return warp_gradient(w, seed, amp, dim, scaled, out);
-    return 0.0f;
+    return warp_simplex(w, seed, amp, dim, scaled, out);
 }
 
 /* ---- Fractal (Fractal.inl:10-67) --------------------------------------- */

@@ -52,6 +52,7 @@ def main():
     cases.append(case("workload1", trees.fbm_perlin_c1(), "grid", [[-128, -128, -128], [24, 24, 24], [1, 1, 1]], 42))
     cases.append(case("workload2-tileable", trees.terrain_c2(), "tile", [48, 40, 1.0, 1.0], 7))
     cases.append(case("demo-caves", decode(trees.DEMO_CAVES), "grid", [[-40, 12, 5], [24, 20, 6], [1, 1, 1]], 1337))
+    cases.append(case("demo-mountain", decode(trees.DEMO_MOUNTAIN), "grid", [[-60, 25], [48, 40], [1, 1]], 1337))
     with open(OUT, "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": cases}, f, indent=1)
     print(f"wrote {len(cases)} cases to {OUT}")

@@ -22,10 +22,18 @@ def test_workload_trees_compile(native):
 
 
 def test_unsupported_nodes_report_compile_error(native):
-    node = native.Node.from_encoded(trees.DEMO_MOUNTAIN)
+    node = trees.to_product(trees.unsupported_tree())
     with pytest.raises(native.FastNoiseError) as e:
         node.compile_info(2)
-    assert e.value.code == -2 and "DomainWarpSimplex" in e.value.message
+    assert e.value.code == -2 and "Minkowski" in e.value.message
+
+
+def test_demo_trees_compile(native):
+    for enc in (trees.DEMO_MOUNTAIN, trees.DEMO_CAVES):
+        node = native.Node.from_encoded(enc)
+        for dim in (2, 3, 4):
+            n_instr, n_regs = node.compile_info(dim)
+            assert 0 < n_instr and 0 < n_regs <= 64
 
 
 def test_missing_source_is_a_compile_error(native):

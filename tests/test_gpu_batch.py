@@ -96,7 +96,7 @@ def test_autotune_and_reuse(gpu, torch_cuda, tmp_path):
 
 def test_bad_request_fails_loudly(gpu, torch_cuda):
     fn = gpu
-    node = fn.Node.from_encoded(trees.DEMO_MOUNTAIN)          # DomainWarpSimplex: no GPU kernel yet
+    node = trees.to_product(trees.unsupported_tree())         # rejected by the GPU compiler
     out = torch_cuda.empty(16, device="cuda")
     with pytest.raises(fn.FastNoiseError):
         fn.gen_batch([fn.make_request(node, fn.KIND_GRID2D, out.data_ptr(), 1, (4, 4))])

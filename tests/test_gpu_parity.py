@@ -30,6 +30,14 @@ def cellular(name, df="Euclidean Squared", **kw):
     return n
 
 
+def warp_simplex(name, scheme):
+    n = N(name, Source=noise("Value", 6.0), Warp_Amplitude=3.5, Feature_Scale=4.5, Seed_Offset=-3)
+    n.set("Vectorization Scheme", scheme)
+    n.set("Warp Amplitude", noise("Simplex", 30.0))          # node-driven amplitude
+    n.set("Amplitude Scaling", 0.75, 0)
+    return n
+
+
 SINGLE = {
     "Constant": lambda: N("Constant", Value=0.625),
     "White": lambda: N("White", Seed_Offset=3),
@@ -64,6 +72,16 @@ COMPOSITE = {
     "WarpProgressive": lambda: N("DomainWarpFractalProgressive",
                                  Domain_Warp_Source=N("DomainWarpGradient", Source=noise("Perlin"), Warp_Amplitude=3.0, Feature_Scale=7.0),
                                  Octaves=3, Weighted_Strength=0.4),
+    "WarpSimplexOGM": lambda: warp_simplex("DomainWarpSimplex", "Orthogonal Gradient Matrix"),
+    "WarpSimplexGOP": lambda: warp_simplex("DomainWarpSimplex", "Gradient Outer Product"),
+    "WarpSuperOGM": lambda: warp_simplex("DomainWarpSuperSimplex", "Orthogonal Gradient Matrix"),
+    "WarpSuperGOP": lambda: warp_simplex("DomainWarpSuperSimplex", "Gradient Outer Product"),
+    "WarpProgressiveSuper": lambda: N("DomainWarpFractalProgressive",
+                                      Domain_Warp_Source=warp_simplex("DomainWarpSuperSimplex", "Gradient Outer Product"),
+                                      Octaves=3, Gain=0.6),
+    "WarpIndependentSimplex": lambda: N("DomainWarpFractalIndependent",
+                                        Domain_Warp_Source=warp_simplex("DomainWarpSimplex", "Orthogonal Gradient Matrix"),
+                                        Octaves=3, Weighted_Strength=0.5),
     "WarpIndependent": lambda: N("DomainWarpFractalIndependent",
                                  Domain_Warp_Source=N("DomainWarpGradient", Source=noise("Value"), Warp_Amplitude=2.0, Feature_Scale=5.0),
                                  Octaves=4, Gain=0.7),
@@ -141,13 +159,12 @@ def test_demo_caves_tree(gpu):
     assert_parity(*run_grid(root, (-40, 12, 5), (48, 40, 12), (1, 1, 1), 1337), label="caves")
 
 
-def test_demo_mountain_tree_needs_domain_warp_simplex(gpu):
-    """DomainWarpSimplex has no GPU kernel yet: the call must fail loudly, never fall back to the CPU."""
-    import fastnoise2_gb300 as fn
-    node = fn.Node.from_encoded(trees.DEMO_MOUNTAIN)
-    with pytest.raises(fn.FastNoiseError) as e:
-        node.gen_uniform_grid((0, 0), (8, 8), (1, 1), 1)
-    assert e.value.code == -2
+@pytest.mark.parametrize("dim", [2, 3])
+def test_demo_mountain_tree(gpu, dim):
+    """The Node Editor's mountain demo (DomainWarpSimplex inside a fractal warp)."""
+    root = decode(trees.DEMO_MOUNTAIN)
+    off, cnt = ((-60, 25), (96, 80)) if dim == 2 else ((-60, 25, 3), (40, 36, 12))
+    assert_parity(*run_grid(root, off, cnt, (1,) * dim, 1337), label=f"mountain {dim}D")
 
 
 @pytest.mark.parametrize("dim", [2, 3, 4])

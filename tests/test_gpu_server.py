@@ -62,6 +62,31 @@ def test_results_same_alone_and_in_the_mix(gpu, torch_cuda):
     srv.close()
 
 
+def test_submit_many_and_wait_many(gpu, torch_cuda):
+    fn = gpu
+    nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
+    chunks = chunkmix.make_mix(64, seed=33, sizes=[(16, 16, 16), (9, 7, 5), (32, 32), (50, 3)])
+    srv = fn.Server(pool_bytes=64 << 20, streams=2, max_batch_requests=24)
+    tickets = srv.submit_many([request(fn, nodes[c.tree], c) for c in chunks])
+    assert len(set(tickets)) == len(chunks)
+    srv.wait_many(tickets, timeout_ms=30000)
+    for t, c in zip(tickets, chunks):
+        assert srv.poll(t) == 1
+        mn, mx, ptr = srv.wait(t, timeout_ms=0)
+        got = device_array(torch_cuda, ptr, c.points)
+        ref, rmm = nodes[c.tree].gen_uniform_grid(c.offset, c.count, (1,) * len(c.count), c.seed)
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), c
+        assert (mn, mx) == rmm
+        assert srv.release(t) == 0
+    # all or nothing: one bad request rejects the whole list
+    bad = [request(fn, nodes[0], chunks[0]), request(fn, trees.to_product(trees.unsupported_tree()), chunks[1])]
+    before = srv.stats()["submitted"]
+    with pytest.raises(fn.FastNoiseError) as e:
+        srv.submit_many(bad)
+    assert e.value.code == -2 and srv.stats()["submitted"] == before
+    srv.close()
+
+
 def test_user_owned_outputs(gpu, torch_cuda):
     fn, torch = gpu, torch_cuda
     node = trees.to_product(trees.fbm_perlin_c1())
@@ -105,7 +130,7 @@ def test_request_larger_than_pool_is_rejected(gpu):
 def test_compile_errors_surface_at_submit(gpu):
     fn = gpu
     srv = fn.Server(pool_bytes=1 << 20)
-    node = fn.Node.from_encoded(trees.DEMO_MOUNTAIN)
+    node = trees.to_product(trees.unsupported_tree())
     with pytest.raises(fn.FastNoiseError) as e:
         srv.submit(fn.make_request(node, fn.KIND_GRID2D, 0, 1, (8, 8)))
     assert e.value.code == -2

@@ -69,6 +69,14 @@ DEMO_CAVES = ("FgIcCS4AAQ@BklCQs@BlRBDNzMw9G@AIMAgAw@ADgC@BCiQIzczMPgkJ@BPkIQH4X
               "JAL/BAAL7FE4PgQKFwkNCQg@CQQQDuB4FPwt7FC4/BAOPwnU8DA==")
 
 
+def unsupported_tree() -> Node:
+    """A tree the GPU compiler rejects: a cellular node whose Minkowski P is driven
+    by another node."""
+    n = N("CellularDistance", Minkowski_P=N("Simplex"))
+    n.set("Distance Function", "Minkowski")
+    return n
+
+
 def to_product(root: Node):
     """Instantiate `root` in the product library through the C-ABI setters."""
     import fastnoise2_gb300 as fn
