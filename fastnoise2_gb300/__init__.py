@@ -170,6 +170,7 @@ def make_request(node: "Node", kind: int, out_ptr: int, seed: int, count=(0, 0, 
                  step=(1, 1, 1, 1), positions=(0, 0, 0, 0), minmax: Optional[np.ndarray] = None) -> GenRequest:
     r = GenRequest()
     r.node = node.handle
+    r._keep = node          # the request holds the Python node, so its native tree outlives the request
     r.kind = kind
     r.seed = int(np.int32(seed))
     for k in range(4):

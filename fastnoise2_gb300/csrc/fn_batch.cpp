@@ -43,6 +43,9 @@ BatchRunner::~BatchRunner()
     if (exec_) cudaGraphExecDestroy(exec_);
     if (graph_) cudaGraphDestroy(graph_);
     if (staged_) cudaEventDestroy(staged_);
+    if (fork_) cudaEventDestroy(fork_);
+    for (auto e : join_) cudaEventDestroy(e);
+    for (auto a : aux_) cudaStreamDestroy(a);
     if (capture_stream_) cudaStreamDestroy(capture_stream_);
     if (d_buf_) cudaFree(d_buf_);
     if (h_buf_) cudaFreeHost(h_buf_);
@@ -55,7 +58,8 @@ bool BatchRunner::reserve(size_t n_req, size_t n_items)
     size_t items = std::max(n_items, std::max<size_t>(cap_items_ * 2, 4096));
     size_t off_req = align_up(sizeof(BatchHeader), 256);
     size_t off_state = align_up(off_req + req * sizeof(BatchRequest), 256);
-    size_t off_items = align_up(off_state + req * sizeof(BatchState), 256);
+    size_t off_groups = align_up(off_state + req * sizeof(BatchState), 256);
+    size_t off_items = align_up(off_groups + req * sizeof(BatchGroup), 256);
     size_t bytes = align_up(off_items + items * sizeof(uint2), 256);
     char* d = nullptr;
     char* h = nullptr;
@@ -65,43 +69,82 @@ bool BatchRunner::reserve(size_t n_req, size_t n_items)
     if (h_buf_) cudaFreeHost(h_buf_);
     d_buf_ = d; h_buf_ = h;
     cap_req_ = req; cap_items_ = items; cap_bytes_ = bytes;
-    off_req_ = off_req; off_state_ = off_state; off_items_ = off_items;
+    off_req_ = off_req; off_state_ = off_state; off_groups_ = off_groups; off_items_ = off_items;
     d_states_ = reinterpret_cast<BatchState*>(d_buf_ + off_state_);
     if (exec_) { cudaGraphExecDestroy(exec_); exec_ = nullptr; }   // kernel arguments changed: recapture
     if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
     return true;
 }
 
-cudaError_t BatchRunner::launch_kernel(cudaKernel_t jit, int grid, uint32_t smem, cudaStream_t stream)
+bool BatchRunner::ensure_aux(size_t n)
+{
+    if (!fork_ && !cuda_ok(cudaEventCreateWithFlags(&fork_, cudaEventDisableTiming), "event")) return false;
+    while (aux_.size() < n) {
+        cudaStream_t st = nullptr;
+        cudaEvent_t ev = nullptr;
+        if (!cuda_ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking), "stream")) return false;
+        if (!cuda_ok(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event")) { cudaStreamDestroy(st); return false; }
+        aux_.push_back(st);
+        join_.push_back(ev);
+    }
+    return true;
+}
+
+cudaError_t BatchRunner::launch_group(size_t g, uint32_t smem, cudaStream_t stream)
 {
     auto* hdr = reinterpret_cast<BatchHeader*>(d_buf_);
     auto* reqs = reinterpret_cast<BatchRequest*>(d_buf_ + off_req_);
     auto* items = reinterpret_cast<uint2*>(d_buf_ + off_items_);
-    if (!jit) return launch_batch(hdr, reqs, d_states_, items, smem, grid, 256, stream);
+    const Group& gr = groups_[g];
+    if (!gr.jit) return launch_batch(hdr, reqs, d_states_, items, smem, gr.grid, 256, stream);
     BatchState* states = d_states_;
-    void* params[] = {&hdr, &reqs, &states, &items};
-    return cudaLaunchKernel((const void*)jit, dim3((unsigned)grid), dim3(256), params, 0, stream);
+    BatchGroup* grp = reinterpret_cast<BatchGroup*>(d_buf_ + off_groups_) + g;
+    void* params[] = {&hdr, &reqs, &states, &items, &grp};
+    return cudaLaunchKernel((const void*)gr.jit, dim3((unsigned)gr.grid), dim3(256), params, 0, stream);
 }
 
-int BatchRunner::launch_graph(cudaStream_t stream, size_t bytes, int grid, uint32_t smem, cudaKernel_t jit)
+// Several group kernels run concurrently: fork from `stream` onto the auxiliary
+// streams (round robin), join back before anything later on `stream`.  Works the
+// same inside a stream capture, where it becomes parallel graph branches.
+bool BatchRunner::launch_groups(cudaStream_t stream, uint32_t smem)
 {
-    // Recapture when the kernel (interpreter <-> specialised module) or its launch
-    // shape changed; otherwise only the upload node is updated.  (Kernel nodes of
-    // library kernels cannot be read back with cudaGraphKernelNodeGetParams.)
-    if (exec_ && (graph_kernel_ != jit || graph_grid_ != grid || graph_smem_ != smem)) {
+    if (groups_.size() == 1) return cuda_ok(launch_group(0, smem, stream), "launch batch");
+    const size_t na = std::min<size_t>(groups_.size(), 8);
+    if (!ensure_aux(na)) return false;
+    if (!cuda_ok(cudaEventRecord(fork_, stream), "fork")) return false;
+    for (size_t a = 0; a < na; ++a)
+        if (!cuda_ok(cudaStreamWaitEvent(aux_[a], fork_, 0), "fork wait")) return false;
+    for (size_t g = 0; g < groups_.size(); ++g)
+        if (!cuda_ok(launch_group(g, smem, aux_[g % na]), "launch batch group")) return false;
+    for (size_t a = 0; a < na; ++a) {
+        if (!cuda_ok(cudaEventRecord(join_[a], aux_[a]), "join")) return false;
+        if (!cuda_ok(cudaStreamWaitEvent(stream, join_[a], 0), "join wait")) return false;
+    }
+    return true;
+}
+
+int BatchRunner::launch_graph(cudaStream_t stream, size_t bytes, uint32_t smem)
+{
+    // Recapture when the launch shape (kernels, grids, dynamic shared memory)
+    // changed; otherwise only the upload node is updated -- the kernel arguments
+    // are the fixed buffer addresses, the work lists travel in the upload.
+    if (exec_ && (graph_groups_ != groups_ || graph_smem_ != smem)) {
         cudaGraphExecDestroy(exec_);
         exec_ = nullptr;
         if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
     }
     if (!exec_) {
-        graph_kernel_ = jit;
-        graph_grid_ = grid;
+        graph_groups_ = groups_;
         graph_smem_ = smem;
+        copy_node_ = nullptr;
         if (!capture_stream_ && !cuda_ok(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking), "stream")) return -3;
         if (!cuda_ok(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal), "begin capture")) return -3;
         cudaMemcpyAsync(d_buf_, h_buf_, bytes, cudaMemcpyHostToDevice, capture_stream_);
-        launch_kernel(jit, grid, smem, capture_stream_);
-        if (!cuda_ok(cudaStreamEndCapture(capture_stream_, &graph_), "end capture")) return -3;
+        const bool queued = launch_groups(capture_stream_, smem);
+        cudaGraph_t g = nullptr;
+        const bool ended = cuda_ok(cudaStreamEndCapture(capture_stream_, &g), "end capture");
+        if (!queued || !ended) { if (g) cudaGraphDestroy(g); return -3; }
+        graph_ = g;
         if (!cuda_ok(cudaGraphInstantiate(&exec_, graph_, 0), "graph instantiate")) return -3;
         size_t n = 0;
         cudaGraphGetNodes(graph_, nullptr, &n);
@@ -111,9 +154,8 @@ int BatchRunner::launch_graph(cudaStream_t stream, size_t bytes, int grid, uint3
             cudaGraphNodeType t;
             cudaGraphNodeGetType(nd, &t);
             if (t == cudaGraphNodeTypeMemcpy) copy_node_ = nd;
-            if (t == cudaGraphNodeTypeKernel) kernel_node_ = nd;
         }
-        if (!copy_node_ || !kernel_node_) { set_error(-3, "unexpected graph shape"); return -3; }
+        if (!copy_node_) { set_error(-3, "unexpected graph shape"); return -3; }
     } else {
         if (!cuda_ok(cudaGraphExecMemcpyNodeSetParams1D(exec_, copy_node_, d_buf_, h_buf_, bytes, cudaMemcpyHostToDevice), "graph memcpy update"))
             return -3;
@@ -138,15 +180,15 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         points_ += (uint64_t)std::max(0ll, items[i].args.total);
     }
     signature_ = batch_signature(items, progs);
-    // Specialised batch kernel when the active module covers every program of the batch.
-    cudaKernel_t jit = nullptr;
-    std::vector<int> slots;
+    // Specialised batch kernels when every program of the batch has one.
+    std::vector<cudaKernel_t> kernels;
+    bool jit = false;
     {
         std::vector<uint64_t> hashes(n);
         for (size_t i = 0; i < n; ++i) hashes[i] = progs[i].hash;
-        bool fits = true;                           // the specialised kernel indexes points with 32 bits
+        bool fits = true;                           // the specialised kernels index points with 32 bits
         for (size_t i = 0; i < n; ++i) fits = fits && items[i].args.total < (1ll << 32);
-        if (!fits || !jit_batch_slots(hashes, slots, jit)) jit = nullptr;
+        jit = fits && jit_batch_kernels(hashes, kernels);
     }
     if (jit) signature_ = signature_ * 0x100000001B3ull + 0x4A17;   // tuned separately from the interpreter
     BatchTuning tuning;
@@ -158,6 +200,27 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
     if (n_items > 0xFFFFFFFFull) { set_error(-4, "batch too large"); return -4; }
     if (!reserve(n, n_items)) return -3;
 
+    // Requests per group: all of them for the interpreter, one group per
+    // distinct specialised kernel (first-appearance order) otherwise.
+    std::vector<std::vector<uint32_t>> members;
+    std::vector<cudaKernel_t> gkernel;
+    if (jit) {
+        std::map<cudaKernel_t, size_t> index;
+        for (size_t i = 0; i < n; ++i) {
+            auto it = index.find(kernels[i]);
+            if (it == index.end()) {
+                it = index.emplace(kernels[i], members.size()).first;
+                members.emplace_back();
+                gkernel.push_back(kernels[i]);
+            }
+            members[it->second].push_back((uint32_t)i);
+        }
+    } else {
+        members.emplace_back();
+        gkernel.push_back(nullptr);
+        for (size_t i = 0; i < n; ++i) members[0].push_back((uint32_t)i);
+    }
+
     // The staging buffer is reused: the previous launch's upload must have been consumed.
     if (!staged_ && !cuda_ok(cudaEventCreateWithFlags(&staged_, cudaEventDisableTiming), "event")) return -3;
     cudaEventSynchronize(staged_);
@@ -165,20 +228,20 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
     auto* hdr = reinterpret_cast<BatchHeader*>(h_buf_);
     auto* reqs = reinterpret_cast<BatchRequest*>(h_buf_ + off_req_);
     auto* states = reinterpret_cast<BatchState*>(h_buf_ + off_state_);
+    auto* grps = reinterpret_cast<BatchGroup*>(h_buf_ + off_groups_);
     auto* its = reinterpret_cast<uint2*>(h_buf_ + off_items_);
     std::memset(hdr, 0, sizeof(BatchHeader));
     hdr->n_req = (unsigned)n;
     hdr->n_items = (unsigned)n_items;
     hdr->tile_points = tp;
     hdr->max_prog_bytes = max_bytes;
-    size_t k = 0;
     last_minmax_.resize(n);
     for (size_t i = 0; i < n; ++i) {
         BatchRequest& r = reqs[i];
         std::memset(&r, 0, sizeof r);
         r.args = items[i].args;
         r.prog = progs[i].dptr;
-        r.jit_slot = jit ? slots[i] : -1;
+        r.jit_slot = -1;
         r.prog_bytes = progs[i].bytes;
         r.out = items[i].dout;
         r.minmax = items[i].dminmax;
@@ -189,25 +252,44 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         states[i].mx_enc = 0u;
         states[i].tiles_done = 0u;
         states[i].pad = 0u;
-        for (uint32_t t = 0; t < r.n_tiles; ++t) its[k++] = make_uint2((unsigned)i, t);
         last_minmax_[i] = items[i].dminmax;
     }
-    const size_t bytes = off_items_ + n_items * sizeof(uint2);
-    int occ = tuning.ctas_per_sm;
-    if (occ <= 0 && jit) {
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)jit, 256, 0) != cudaSuccess || occ < 1) occ = 1;
-    } else if (occ <= 0) {
-        occ = batch_occupancy(256, max_bytes);
+    const int sms = num_sms();
+    groups_.assign(members.size(), Group());
+    size_t k = 0;
+    int total_grid = 0;
+    for (size_t g = 0; g < members.size(); ++g) {
+        Group& gr = groups_[g];
+        gr.jit = gkernel[g];
+        gr.item_begin = (uint32_t)k;
+        for (uint32_t i : members[g])
+            for (uint32_t t = 0; t < reqs[i].n_tiles; ++t) its[k++] = make_uint2(i, t);
+        gr.item_end = (uint32_t)k;
+        grps[g].item_begin = gr.item_begin;
+        grps[g].item_end = gr.item_end;
+        grps[g].head = 0;
+        grps[g].pad = 0;
+        int occ = tuning.ctas_per_sm;
+        if (occ <= 0 && gr.jit) {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)gr.jit, 256, 0) != cudaSuccess || occ < 1) occ = 1;
+        } else if (occ <= 0) {
+            occ = batch_occupancy(256, max_bytes);
+        }
+        long long grid = (long long)sms * occ;
+        const long long group_items = (long long)(gr.item_end - gr.item_begin);
+        if (grid > group_items) grid = group_items;
+        if (grid < 1) grid = 1;
+        gr.grid = (int)grid;
+        total_grid += gr.grid;
     }
-    long long grid = (long long)num_sms() * occ;
-    if (grid > (long long)n_items) grid = (long long)n_items;
-    if (grid < 1) grid = 1;
+    const size_t bytes = off_items_ + n_items * sizeof(uint2);
+    const uint32_t smem = jit ? 0 : max_bytes;
     int rc;
     if (use_graph) {
-        rc = launch_graph(stream, bytes, (int)grid, max_bytes, jit);
+        rc = launch_graph(stream, bytes, smem);
     } else {
         rc = cuda_ok(cudaMemcpyAsync(d_buf_, h_buf_, bytes, cudaMemcpyHostToDevice, stream), "upload batch") &&
-                     cuda_ok(launch_kernel(jit, (int)grid, max_bytes, stream), "launch batch")
+                     launch_groups(stream, smem)
                  ? 0
                  : -3;
     }
@@ -216,8 +298,8 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         items_ = n_items;
         upload_bytes_ = bytes;
         tile_points_ = tp;
-        grid_ = (int)grid;
-        specialised_ = jit != nullptr;
+        grid_ = total_grid;
+        specialised_ = jit;
     }
     return rc;
 }

@@ -54,23 +54,37 @@ public:
     bool last_specialised() const { return specialised_; }
 
 private:
+    // One kernel launch of a batch: the interpreter's batch kernel over all items
+    // (jit null), or one tree's specialised batch kernel over that tree's items.
+    struct Group {
+        cudaKernel_t jit = nullptr;
+        uint32_t item_begin = 0, item_end = 0;
+        int grid = 1;
+        bool operator==(const Group& o) const { return jit == o.jit && grid == o.grid; }
+    };
     bool reserve(size_t n_req, size_t n_items);
-    int launch_graph(cudaStream_t stream, size_t bytes, int grid, uint32_t smem, cudaKernel_t jit);
-    // jit null = the interpreter's batch kernel
-    cudaError_t launch_kernel(cudaKernel_t jit, int grid, uint32_t smem, cudaStream_t stream);
+    int launch_graph(cudaStream_t stream, size_t bytes, uint32_t smem);
+    // Queue the upload-free part: every group's kernel, forked over the auxiliary
+    // streams and joined back into `stream` when there is more than one.
+    bool launch_groups(cudaStream_t stream, uint32_t smem);
+    cudaError_t launch_group(size_t g, uint32_t smem, cudaStream_t stream);
+    bool ensure_aux(size_t n);
 
-    char* d_buf_ = nullptr;            // device: header | reqs | states | items
+    char* d_buf_ = nullptr;            // device: header | reqs | states | groups | items
     char* h_buf_ = nullptr;            // pinned staging with the same layout
     size_t cap_req_ = 0, cap_items_ = 0, cap_bytes_ = 0;
-    size_t off_req_ = 0, off_state_ = 0, off_items_ = 0;
+    size_t off_req_ = 0, off_state_ = 0, off_groups_ = 0, off_items_ = 0;
     BatchState* d_states_ = nullptr;
+    std::vector<Group> groups_;
+    std::vector<cudaStream_t> aux_;     // fork/join streams for concurrent group kernels
+    std::vector<cudaEvent_t> join_;
+    cudaEvent_t fork_ = nullptr;
     cudaStream_t capture_stream_ = nullptr;
     cudaEvent_t staged_ = nullptr;      // recorded after each upload: guards reuse of h_buf_
     cudaGraph_t graph_ = nullptr;
     cudaGraphExec_t exec_ = nullptr;
-    cudaGraphNode_t copy_node_ = nullptr, kernel_node_ = nullptr;
-    cudaKernel_t graph_kernel_ = nullptr;  // kernel the graph was captured with (null = interpreter)
-    int graph_grid_ = 0;                   // and its launch shape
+    cudaGraphNode_t copy_node_ = nullptr;
+    std::vector<Group> graph_groups_;   // launch shape the graph was captured with
     uint32_t graph_smem_ = 0;
     std::vector<float*> last_minmax_;
     uint64_t signature_ = 0;

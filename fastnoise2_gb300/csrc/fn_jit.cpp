@@ -330,8 +330,8 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
     }
 }
 
-// The batch kernel: persistent CTAs pull (request, tile) items; the request's
-// tree slot selects, once per tile, a loop with that tree's code inlined.
+// The batch kernels: persistent CTAs pull (request, tile) items of their tree's
+// group and run a tile loop with that tree's code inlined.
 void emit_batch(const std::vector<const CompiledProgram*>& progs, std::ostringstream& o)
 {
     for (size_t k = 0; k < progs.size(); ++k) {
@@ -347,37 +347,34 @@ void emit_batch(const std::vector<const CompiledProgram*>& progs, std::ostringst
           << "        fne::fold(v, mn, mx);\n"
           << "    }\n}\n\n";
     }
-    o << R"(extern "C" __global__ void __launch_bounds__(256, 2) fnjit_batch(fn::BatchHeader* hdr, const fn::BatchRequest* __restrict__ reqs,
-                                                                fn::BatchState* states, const uint2* __restrict__ items)
-{
-    __shared__ unsigned int s_item;
-    __shared__ float smn[8], smx[8];
-    const unsigned int n_items = hdr->n_items;
-    const unsigned int tile_points = hdr->tile_points;
-    for (;;) {
-        if (threadIdx.x == 0) s_item = atomicAdd(&hdr->head, 1u);
-        __syncthreads();
-        const unsigned int it = s_item;
-        __syncthreads();
-        if (it >= n_items) break;
-        const uint2 item = items[it];
-        const fn::BatchRequest& rq = reqs[item.x];
-        const fn::PointArgs args = rq.args;
-        const unsigned total = (unsigned)args.total;
-        const unsigned begin = item.y * tile_points;
-        const unsigned end = total - begin < tile_points ? total : begin + tile_points;
-        float mn = fne::inf(), mx = -fne::inf();
-        switch (rq.jit_slot) {
-)";
-    for (size_t k = 0; k < progs.size(); ++k)
-        o << "        case " << k << ": fnjit_tile_" << k << "(args, rq.out, begin + threadIdx.x, end, mn, mx); break;\n";
-    o << R"(        default: break;
-        }
-        fne::block_minmax(mn, mx, smn, smx);
-        if (threadIdx.x == 0) fne::finish_tile(rq, states + item.x, hdr, mn, mx);
+    // one persistent kernel per tree: each gets the register allocation its own
+    // code needs, and the trees of a batch run as concurrent kernels
+    for (size_t k = 0; k < progs.size(); ++k) {
+        o << "extern \"C\" __global__ void __launch_bounds__(256, 2) fnjit_batch_" << k
+          << "(fn::BatchHeader* hdr, const fn::BatchRequest* __restrict__ reqs, fn::BatchState* states,\n"
+             "    const uint2* __restrict__ items, fn::BatchGroup* grp)\n{\n"
+             "    __shared__ unsigned int s_item;\n"
+             "    __shared__ float smn[8], smx[8];\n"
+             "    const unsigned int first = grp->item_begin, last = grp->item_end;\n"
+             "    const unsigned int tile_points = hdr->tile_points;\n"
+             "    for (;;) {\n"
+             "        if (threadIdx.x == 0) s_item = first + atomicAdd(&grp->head, 1u);\n"
+             "        __syncthreads();\n"
+             "        const unsigned int it = s_item;\n"
+             "        __syncthreads();\n"
+             "        if (it >= last) break;\n"
+             "        const uint2 item = items[it];\n"
+             "        const fn::BatchRequest& rq = reqs[item.x];\n"
+             "        const fn::PointArgs args = rq.args;\n"
+             "        const unsigned total = (unsigned)args.total;\n"
+             "        const unsigned begin = item.y * tile_points;\n"
+             "        const unsigned end = total - begin < tile_points ? total : begin + tile_points;\n"
+             "        float mn = fne::inf(), mx = -fne::inf();\n"
+             "        fnjit_tile_" << k << "(args, rq.out, begin + threadIdx.x, end, mn, mx);\n"
+             "        fne::block_minmax(mn, mx, smn, smx);\n"
+             "        if (threadIdx.x == 0) fne::finish_tile(rq, states + item.x, hdr, mn, mx);\n"
+             "    }\n}\n\n";
     }
-}
-)";
 }
 
 struct Module {
@@ -388,8 +385,7 @@ struct Module {
 std::mutex g_jit_mu;
 std::unordered_map<uint64_t, JitKernels> g_kernels;
 std::vector<std::unique_ptr<Module>> g_modules;
-cudaKernel_t g_batch_kernel = nullptr;
-std::unordered_map<uint64_t, int> g_batch_slots;
+std::unordered_map<uint64_t, cudaKernel_t> g_batch_kernels;   // per-tree batch kernel
 std::atomic<bool> g_enabled{true};
 
 }  // namespace
@@ -486,16 +482,19 @@ bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& er
         mods.push_back(std::move(mod));
     }
     std::unordered_map<uint64_t, JitKernels> found;
-    cudaKernel_t batch = nullptr;
-    bool ok = cudaLibraryGetKernel(&batch, mods[0]->lib, "fnjit_batch") == cudaSuccess;
+    std::unordered_map<uint64_t, cudaKernel_t> batch;
+    bool ok = true;
     for (size_t k = 0; ok && k < progs.size(); ++k) {
         cudaLibrary_t lib = mods[1 + k]->lib;
         JitKernels jk;
         jk.slot = (int)k;
+        cudaKernel_t bk = nullptr;
         ok = cudaLibraryGetKernel(&jk.grid, lib, "fnjit_grid_0") == cudaSuccess &&
              cudaLibraryGetKernel(&jk.positions, lib, "fnjit_pos_0") == cudaSuccess &&
-             (progs[k]->dim != 4 || cudaLibraryGetKernel(&jk.tileable, lib, "fnjit_tile_0") == cudaSuccess);
+             (progs[k]->dim != 4 || cudaLibraryGetKernel(&jk.tileable, lib, "fnjit_tile_0") == cudaSuccess) &&
+             cudaLibraryGetKernel(&bk, mods[0]->lib, ("fnjit_batch_" + std::to_string(k)).c_str()) == cudaSuccess;
         found[progs[k]->hash] = jk;
+        batch[progs[k]->hash] = bk;
     }
     if (!ok) {
         error = "kernel lookup failed in a specialised module";
@@ -504,9 +503,7 @@ bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& er
     }
     std::lock_guard<std::mutex> lk(g_jit_mu);
     for (auto& kv : found) g_kernels[kv.first] = kv.second;
-    g_batch_kernel = batch;
-    g_batch_slots.clear();
-    for (auto& kv : found) g_batch_slots[kv.first] = kv.second.slot;
+    for (auto& kv : batch) g_batch_kernels[kv.first] = kv.second;
     for (auto& m : mods) g_modules.push_back(std::move(m));   // modules stay loaded: kernels may still be queued
     return true;
 }
@@ -521,34 +518,17 @@ bool jit_lookup(uint64_t hash, JitKernels& out)
     return true;
 }
 
-bool jit_batch_kernel(cudaKernel_t& kernel)
+bool jit_batch_kernels(const std::vector<uint64_t>& hashes, std::vector<cudaKernel_t>& kernels)
 {
     if (!g_enabled.load(std::memory_order_relaxed)) return false;
     std::lock_guard<std::mutex> lk(g_jit_mu);
-    kernel = g_batch_kernel;
-    return kernel != nullptr;
-}
-
-bool jit_batch_slots(const std::vector<uint64_t>& hashes, std::vector<int>& slots, cudaKernel_t& kernel)
-{
-    if (!g_enabled.load(std::memory_order_relaxed)) return false;
-    std::lock_guard<std::mutex> lk(g_jit_mu);
-    if (!g_batch_kernel) return false;
-    slots.resize(hashes.size());
+    kernels.resize(hashes.size());
     for (size_t i = 0; i < hashes.size(); ++i) {
-        auto it = g_batch_slots.find(hashes[i]);
-        if (it == g_batch_slots.end()) return false;
-        slots[i] = it->second;
+        auto it = g_batch_kernels.find(hashes[i]);
+        if (it == g_batch_kernels.end()) return false;
+        kernels[i] = it->second;
     }
-    kernel = g_batch_kernel;
     return true;
-}
-
-int jit_batch_slot(uint64_t hash)
-{
-    std::lock_guard<std::mutex> lk(g_jit_mu);
-    auto it = g_batch_slots.find(hash);
-    return it == g_batch_slots.end() ? -1 : it->second;
 }
 
 void jit_set_enabled(bool on) { g_enabled.store(on); }

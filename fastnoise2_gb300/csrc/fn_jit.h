@@ -6,9 +6,10 @@
 // one call per instruction to the hand-written node functions of
 // fn_device.cuh, positions and values in registers, parameters as literals --
 // and compiled for sm_103a with NVRTC (-fmad=false, so results are identical
-// to the interpreter's).  A module holds, per tree, grid / position-array /
-// tileable per-call kernels, plus one batch kernel that dispatches on the
-// request's tree slot.
+// to the interpreter's).  Each tree gets a module with its grid / position-array
+// / tileable per-call kernels; one batch module holds a persistent batch kernel
+// per tree, so the trees of a batch run as concurrent kernels, each with the
+// register allocation its own code needs.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -40,18 +41,16 @@ bool jit_compile_all(const std::vector<const CompiledProgram*>& progs, std::vect
                      std::string& error);
 
 // Compile and load a module covering `progs`; on success every program gets
-// per-call kernels and becomes the active batch module.  Thread safe.
+// per-call kernels and a batch kernel.  Thread safe.
 bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& error);
 
 // Kernels for a program hash, or false if none have been built.
 bool jit_lookup(uint64_t hash, JitKernels& out);
 
-// Active batch kernel and the slot of each program in it.
-bool jit_batch_kernel(cudaKernel_t& kernel);
-int jit_batch_slot(uint64_t hash);
-// All-or-nothing: the active batch kernel and the slot of every hash, read
-// under one lock (false if JIT is off or any program has no slot).
-bool jit_batch_slots(const std::vector<uint64_t>& hashes, std::vector<int>& slots, cudaKernel_t& kernel);
+// The per-tree batch kernel of every hash, all or nothing (false if JIT is off
+// or any program has none).  Kernel signature: (BatchHeader*, const
+// BatchRequest*, BatchState*, const uint2* items, BatchGroup*).
+bool jit_batch_kernels(const std::vector<uint64_t>& hashes, std::vector<cudaKernel_t>& kernels);
 
 // Launch the specialised per-call kernel for `hash` if one is loaded (and JIT
 // is enabled); returns false when the caller should use the interpreter.

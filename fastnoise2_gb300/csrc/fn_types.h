@@ -68,6 +68,13 @@ struct BatchState {              // per-request mutable state, zeroed by the hos
     unsigned int pad;
 };
 
+struct BatchGroup {               // the work items of one tree (specialised batch kernels)
+    unsigned int item_begin;
+    unsigned int item_end;
+    unsigned int head;           // next item offset (host uploads 0)
+    unsigned int pad;
+};
+
 struct BatchHeader {
     unsigned int n_req;
     unsigned int n_items;

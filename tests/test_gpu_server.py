@@ -79,7 +79,8 @@ def test_submit_many_and_wait_many(gpu, torch_cuda):
         assert (mn, mx) == rmm
         assert srv.release(t) == 0
     # all or nothing: one bad request rejects the whole list
-    bad = [request(fn, nodes[0], chunks[0]), request(fn, trees.to_product(trees.unsupported_tree()), chunks[1])]
+    unsupported = trees.to_product(trees.unsupported_tree())      # keep the node alive while requests point to it
+    bad = [request(fn, nodes[0], chunks[0]), request(fn, unsupported, chunks[1])]
     before = srv.stats()["submitted"]
     with pytest.raises(fn.FastNoiseError) as e:
         srv.submit_many(bad)

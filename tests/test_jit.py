@@ -118,9 +118,13 @@ def test_jit_batch_matches_interpreter(gpu):
         fn.autotune_batch(reqs)                      # several launches of one signature: graph updates
         for _ in range(3):
             fn.gen_batch(reqs, sync=True)
+        fn.gen_batch(reqs, sync=True, graph=False)   # the same work as plain stream launches
         return [o.cpu().numpy()[:c.points] for o, c in zip(outs, chunks)], mms
 
     (ja, jm), (ia, im) = _both(fn, run)
+    run()
+    info = fn.batch_info()
+    assert info["specialised"] == 1 and info["requests"] == len(chunks) and info["ctas"] > 0
     for c, x, y, mx, my in zip(chunks, ja, ia, jm, im):
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), c
         assert np.array_equal(mx.view(np.uint32), my.view(np.uint32)), c

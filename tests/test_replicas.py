@@ -1,0 +1,62 @@
+"""Multi-GPU is replicas only: every rank runs its own copy of the workload and the
+ranks exchange nothing but a barrier and the max-over-ranks step time.  These CPU
+tests run that host logic with two gloo ranks (no GPU)."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank_main(rank, world, port, out):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank),
+                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    sys.path.insert(0, ROOT)
+    import bench
+    r, w, local = bench.dist_setup()
+    bench.barrier(w)
+    out.put((r, w, local, bench.allmax(float(10 + r), w)))
+    import torch.distributed as dist
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_barrier_and_max():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    results = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [r[:3] for r in results] == [(0, 2, 0), (1, 2, 1)]
+    assert all(r[3] == 11.0 for r in results)          # max over ranks seen by every rank
+
+
+def test_reference_arm_under_torchrun_prints_once():
+    """`bench.py --impl reference` launched like the driver's N>1 runs: rank 0 prints the
+    single JSON line, the other rank exits 0 without work."""
+    pytest.importorskip("torch")
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py", "--impl", "reference",
+           "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-seconds", "0.3", "--workload", "simplex-64"]
+    r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+    assert line["cpu_baseline"]["kind"] == "port"
