@@ -176,6 +176,8 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
             return -1;
         }
         if (!get_program(items[i].node, items[i].args.dim, progs[i])) return last_error();
+        std::string err;
+        if (!jit_ensure(progs[i].host, err)) { set_error(-2, "batch request " + std::to_string(i) + ": " + err); return -2; }
         max_bytes = std::max(max_bytes, progs[i].bytes);
         points_ += (uint64_t)std::max(0ll, items[i].args.total);
     }
@@ -190,6 +192,13 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         for (size_t i = 0; i < n; ++i) fits = fits && items[i].args.total < (1ll << 32);
         jit = fits && jit_batch_kernels(hashes, kernels);
     }
+    if (!jit)
+        for (size_t i = 0; i < n; ++i)
+            if (progs[i].host->needs_specialisation() && items[i].args.total > 0) {
+                set_error(-2, "batch request " + std::to_string(i) + ": the tree needs specialised kernels, which this batch "
+                              "cannot use (specialisation disabled or a request of 2^32 points or more)");
+                return -2;
+            }
     if (jit) signature_ = signature_ * 0x100000001B3ull + 0x4A17;   // tuned separately from the interpreter
     BatchTuning tuning;
     if (tuning_in) tuning = *tuning_in;

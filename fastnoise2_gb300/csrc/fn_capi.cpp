@@ -59,7 +59,19 @@ cudaError_t launch_points(const DeviceProgram& prog, const PointArgs& args, floa
 {
     cudaError_t e;
     if (jit_launch(prog.hash, args, out, work, dminmax, stream, e)) return e;
+    // A tree with per-cell sub-programs cannot run on the interpreter; with no
+    // points there is nothing to evaluate and the interpreter only writes min/max.
+    if (prog.host->needs_specialisation() && args.total > 0) return cudaErrorNotSupported;
     return launch_interpreter(prog.dptr, prog.bytes, args, out, work, dminmax, stream);
+}
+
+// Specialise trees the interpreter cannot run before their first launch.
+bool ensure_runnable(const DeviceProgram& prog)
+{
+    std::string err;
+    if (jit_ensure(prog.host, err)) return true;
+    set_error(FN_ERR_COMPILE, err);
+    return false;
 }
 
 // Run one host-memory generation call end to end.
@@ -70,7 +82,7 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
     if (!node || total < 0 || (total > 0 && !out)) { set_error(FN_ERR_ARG, "invalid arguments"); fill_nan(out, total > 0 ? total : 0, minmax); return; }
     ThreadCtx* ctx = thread_ctx();
     DeviceProgram prog;
-    if (!ctx || !get_program(N(node), args.dim, prog)) { fill_nan(out, total, minmax); return; }
+    if (!ctx || !get_program(N(node), args.dim, prog) || !ensure_runnable(prog)) { fill_nan(out, total, minmax); return; }
     MinMaxWork* work = work_for_stream(ctx->stream);
     if (!work || !ensure(ctx->dbuf, ctx->dbuf_cap, (size_t)total)) { fill_nan(out, total, minmax); return; }
     if (args.src == kSrcPositions && total > 0) {
@@ -107,6 +119,7 @@ int gen_device(const void* node, PointArgs args, float* dout, float* dminmax, vo
     if (!thread_ctx()) return FN_ERR_CUDA;
     DeviceProgram prog;
     if (!get_program(N(node), args.dim, prog)) return last_error();
+    if (!ensure_runnable(prog)) return FN_ERR_COMPILE;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     MinMaxWork* work = work_for_stream(s);
     if (!work) return FN_ERR_CUDA;
@@ -935,6 +948,11 @@ int fnGenUniformGrid3DDeviceNoAlloc(const void* node, float* dOut, float xOffset
         if (!compile_program(N(node), 3, cached.prog, err)) { set_error(FN_ERR_COMPILE, err); return FN_ERR_COMPILE; }
         cached.node = N(node);
         cached.epoch = epoch;
+    }
+    if (cached.prog.needs_specialisation()) {
+        set_error(FN_ERR_COMPILE, "the tree evaluates a node per cell (node-driven Minkowski P); the allocation-free "
+                                  "path runs the interpreter only");
+        return FN_ERR_COMPILE;
     }
     const size_t bytes = cached.prog.blob.size();
     if (bytes > kStaticProgramBytes) {

@@ -48,6 +48,7 @@ class Compiler {
 public:
     std::vector<FnInstr> code;
     std::vector<float> params;
+    std::vector<CompiledProgram> subs;   // per-cell sub-programs (node-driven Minkowski P)
     std::string err;
     int max_reg = -1;
     uint64_t used = 0;     // bit r set = register r holds a live value
@@ -133,6 +134,7 @@ public:
     }
 
     int gen(const Node* n, int dim, int32_t seed, int pos);
+    static bool compile_sub(const Node* root, int dim, int32_t seed, CompiledProgram& out, std::string& error);
 };
 
 int Compiler::gen(const Node* n, int dim, int32_t seed, int pos)
@@ -199,13 +201,23 @@ int Compiler::gen(const Node* n, int dim, int32_t seed, int pos)
         int jit = hybrid(n, 1, dim, seed, pos);
         bool size_active = n->hnodes[2] != nullptr || n->hvals[2] != 0.0f;
         int sj = size_active ? hybrid(n, 2, dim, seed, pos) : FN_REG_NONE;
-        if (s.dist_func == 5 && n->hnodes[0]) { fail(std::string(n->meta->name) + ": node-driven Minkowski P is not supported on the GPU path"); return 0; }
         const int32_t cell_seed = sadd(seed, s.seed_offset);
         int df = (s.dist_func < 0 || s.dist_func > 5) ? 0 : s.dist_func;
+        // Minkowski P driven by a node: a sub-program evaluated at every cell's offset
+        // vector with the incoming seed (Cellular.inl:63, Utils.inl:326-331)
+        int sub = FN_REG_NONE;
+        if (df == 5 && n->hnodes[0]) {
+            if (subs.size() >= 255) { fail("too many per-cell sub-programs"); return 0; }
+            CompiledProgram sp;
+            std::string e;
+            if (!compile_sub(n->hnodes[0], dim, seed, sp, e)) { fail(e); return 0; }
+            sub = (int)subs.size();
+            subs.push_back(std::move(sp));
+        }
         if (id == kCellularValue) {
             int r = alloc(1);
             int prm = param_block({s.frequency, range_mul(s, -kValueBounds, kValueBounds), s.range_min, n->hvals[0]});
-            emit(FN_OP_CELL_VALUE, dim, r, pos, jit, sj, FN_REG_NONE, FN_REG_NONE, prm, df | (s.value_index << 4), cell_seed);
+            emit(FN_OP_CELL_VALUE, dim, r, pos, jit, sj, sub, FN_REG_NONE, prm, df | (s.value_index << 4), cell_seed);
             release(jit, 1); if (sj != FN_REG_NONE) release(sj, 1);
             return r;
         }
@@ -217,14 +229,14 @@ int Compiler::gen(const Node* n, int dim, int32_t seed, int pos)
             float nmax = ret == 1 ? maxDist * 2 : ret == 3 ? maxDist * maxDist : maxDist;
             int r = alloc(1);
             int prm = param_block({s.frequency, range_mul(s, 0, nmax), s.range_min, n->hvals[0]});
-            emit(FN_OP_CELL_DIST, dim, r, pos, jit, sj, FN_REG_NONE, FN_REG_NONE, prm,
+            emit(FN_OP_CELL_DIST, dim, r, pos, jit, sj, sub, FN_REG_NONE, prm,
                  df | (s.dist_idx0 << 4) | (s.dist_idx1 << 8) | (ret << 12), cell_seed);
             release(jit, 1); if (sj != FN_REG_NONE) release(sj, 1);
             return r;
         }
         if (lookup(n, 0) < 0) return 0;
         int q = alloc(dim);
-        emit(FN_OP_CELL_LOOKUP, dim, q, pos, jit, sj, FN_REG_NONE, FN_REG_NONE, param_block({s.frequency, s.scale, n->hvals[0]}), df, cell_seed);
+        emit(FN_OP_CELL_LOOKUP, dim, q, pos, jit, sj, sub, FN_REG_NONE, param_block({s.frequency, s.scale, n->hvals[0]}), df, cell_seed);
         release(jit, 1); if (sj != FN_REG_NONE) release(sj, 1);
         int r = gen(n->lookups[0], dim, sadd(seed, 1), q);      // Cellular.inl:633 (sourceSeed - (-1))
         release(q, dim);
@@ -469,6 +481,50 @@ int Compiler::gen(const Node* n, int dim, int32_t seed, int pos)
 
 }  // namespace
 
+namespace {
+
+// Serialise a finished compiler into a program blob (fn_program.h) and hash it.
+bool finalize(Compiler& c, int dim, int out_reg, CompiledProgram& out, std::string& error)
+{
+    FnProgramHeader h;
+    std::memset(&h, 0, sizeof h);
+    h.magic = FN_PROGRAM_MAGIC;
+    h.n_instr = (uint16_t)c.code.size();
+    h.n_regs = (uint16_t)(c.max_reg + 1);
+    h.n_params = (uint16_t)c.params.size();
+    h.dim = (uint8_t)dim;
+    h.out_reg = (uint8_t)out_reg;
+    h.flags = c.subs.empty() ? 0u : 1u;
+    if (c.params.size() > FN_MAX_PARAMS) { error = "program exceeds parameter limit"; return false; }
+    size_t bytes = sizeof(h) + c.code.size() * sizeof(FnInstr) + c.params.size() * sizeof(float);
+    bytes = (bytes + 15) & ~(size_t)15;
+    h.bytes = (uint32_t)bytes;
+    out.blob.assign(bytes, 0);
+    std::memcpy(out.blob.data() + sizeof(h), c.code.data(), c.code.size() * sizeof(FnInstr));
+    std::memcpy(out.blob.data() + sizeof(h) + c.code.size() * sizeof(FnInstr), c.params.data(), c.params.size() * sizeof(float));
+    uint64_t hash = fnv1a64(out.blob.data() + sizeof(h), bytes - sizeof(h), fnv1a64(&h, offsetof(FnProgramHeader, flags)));
+    for (const auto& sp : c.subs) hash = fnv1a64(&sp.hash, sizeof sp.hash, hash);
+    h.hash = hash;
+    std::memcpy(out.blob.data(), &h, sizeof(h));
+    out.hash = h.hash;
+    out.dim = dim;
+    out.n_instr = h.n_instr;
+    out.n_regs = h.n_regs;
+    out.subs = std::move(c.subs);
+    return true;
+}
+
+}  // namespace
+
+bool Compiler::compile_sub(const Node* root, int dim, int32_t seed, CompiledProgram& out, std::string& error)
+{
+    Compiler c;
+    int pos = c.alloc(dim);                 // the cell's offset vector: registers 0 .. dim-1
+    int r = c.gen(root, dim, seed, pos);
+    if (!c.ok()) { error = c.err; return false; }
+    return finalize(c, dim, r, out, error);
+}
+
 bool compile_program(const Node* root, int dim, CompiledProgram& out, std::string& error)
 {
     if (!root) { error = "null node"; return false; }
@@ -477,29 +533,7 @@ bool compile_program(const Node* root, int dim, CompiledProgram& out, std::strin
     int pos = c.alloc(dim);                 // root position: registers 0 .. dim-1
     int r = c.gen(root, dim, 0, pos);
     if (!c.ok()) { error = c.err; return false; }
-    (void)pos;
-    FnProgramHeader h;
-    std::memset(&h, 0, sizeof h);
-    h.magic = FN_PROGRAM_MAGIC;
-    h.n_instr = (uint16_t)c.code.size();
-    h.n_regs = (uint16_t)(c.max_reg + 1);
-    h.n_params = (uint16_t)c.params.size();
-    h.dim = (uint8_t)dim;
-    h.out_reg = (uint8_t)r;
-    if (c.params.size() > FN_MAX_PARAMS) { error = "program exceeds parameter limit"; return false; }
-    size_t bytes = sizeof(h) + c.code.size() * sizeof(FnInstr) + c.params.size() * sizeof(float);
-    bytes = (bytes + 15) & ~(size_t)15;
-    h.bytes = (uint32_t)bytes;
-    out.blob.assign(bytes, 0);
-    std::memcpy(out.blob.data() + sizeof(h), c.code.data(), c.code.size() * sizeof(FnInstr));
-    std::memcpy(out.blob.data() + sizeof(h) + c.code.size() * sizeof(FnInstr), c.params.data(), c.params.size() * sizeof(float));
-    h.hash = fnv1a64(out.blob.data() + sizeof(h), bytes - sizeof(h), fnv1a64(&h, offsetof(FnProgramHeader, flags)));
-    std::memcpy(out.blob.data(), &h, sizeof(h));
-    out.hash = h.hash;
-    out.dim = dim;
-    out.n_instr = h.n_instr;
-    out.n_regs = h.n_regs;
-    return true;
+    return finalize(c, dim, r, out, error);
 }
 
 }  // namespace fn

@@ -11,10 +11,16 @@ namespace fn {
 
 struct CompiledProgram {
     std::vector<uint8_t> blob;   // FnProgramHeader + instrs + params (16-byte multiple)
-    uint64_t hash = 0;
+    uint64_t hash = 0;           // of the blob and of every sub-program
     int dim = 0;
     int n_instr = 0;
     int n_regs = 0;
+    // Sub-programs evaluated per cell by cellular instructions whose Minkowski P is
+    // driven by a node (instruction field d = index here; Utils.inl:326-331 samples
+    // the P node at each cell's offset vector).  Only the specialised kernels run
+    // them, so a program with sub-programs needs fnJitCompile-style kernels.
+    std::vector<CompiledProgram> subs;
+    bool needs_specialisation() const { return !subs.empty(); }
 };
 
 // Compile `root` for a root dimensionality of 2, 3 or 4.  Returns false and

@@ -777,6 +777,14 @@ struct CellParams {
 // fastest): visit(c, cf) gets the primed cell coordinates and the running float
 // cell offsets (cfb[k] + 0, 1, 2).  Nested loops over scalars rather than an
 // odometer over arrays, so the per-cell state stays in registers.
+// Minkowski P of the cellular distance: the node's constant (NoMink), or a
+// functor evaluating the P node at each cell's offset vector (specialised kernels;
+// Cellular.inl:63 passes the offset to CalcDistance, Utils.inl:326-331).
+struct NoMink {
+    static constexpr bool kNode = false;
+    FND float operator()(const float*) const { return 0.0f; }
+};
+
 template <int D, typename F>
 FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
 {
@@ -840,8 +848,8 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
     }
 }
 
-template <int D>
-FND float cellular_value(int seed, const float* pin, const CellParams& cp, int valueIndex)
+template <int D, typename MinkF = NoMink>
+FND float cellular_value(int seed, const float* pin, const CellParams& cp, int valueIndex, const MinkF& mink = MinkF())
 {
     float p[D];
 #pragma unroll
@@ -863,7 +871,8 @@ FND float cellular_value(int seed, const float* pin, const CellParams& cp, int v
         float off[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) off[k] = fmaf(d[k], d[D], cf[k]);
-        float nd = distance<D>(cp.distFunc, D == 2, off, cp.minkowski);
+        const float mk = (MinkF::kNode && cp.distFunc == 5) ? mink(off) : cp.minkowski;
+        float nd = distance<D>(cp.distFunc, D == 2, off, mk);
         if (cp.sizeActive) nd *= size_factor<D>(h, cp.sizeJitter);
         int nh = h;
 #pragma unroll
@@ -884,8 +893,8 @@ FND float cellular_value(int seed, const float* pin, const CellParams& cp, int v
     return cvtf(sel);
 }
 
-template <int D>
-FND void cellular_distances(int seed, const float* pin, const CellParams& cp, float* dist)
+template <int D, typename MinkF = NoMink>
+FND void cellular_distances(int seed, const float* pin, const CellParams& cp, float* dist, const MinkF& mink = MinkF())
 {
     float p[D];
 #pragma unroll
@@ -907,7 +916,8 @@ FND void cellular_distances(int seed, const float* pin, const CellParams& cp, fl
         float off[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) off[k] = fmaf(d[k], d[D], cf[k] - p[k]);
-        float nd = distance<D>(cp.distFunc, false, off, cp.minkowski);
+        const float mk = (MinkF::kNode && cp.distFunc == 5) ? mink(off) : cp.minkowski;
+        float nd = distance<D>(cp.distFunc, false, off, mk);
         if (cp.sizeActive) nd *= size_factor<D>(h, cp.sizeJitter);
 #pragma unroll
         for (int i = 3; i > 0; i--) dist[i] = fmax_(fmin_(dist[i], nd), dist[i - 1]);
@@ -940,8 +950,8 @@ FND float cellular_return(float* dist, int distFunc, int i0, int i1, int ret, fl
     }
 }
 
-template <int D>
-FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, float scale, float* out)
+template <int D, typename MinkF = NoMink>
+FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, float scale, float* out, const MinkF& mink = MinkF())
 {
     float p[D];
 #pragma unroll
@@ -965,7 +975,8 @@ FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, f
         float local[D], off[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) { local[k] = fmaf(d[k], d[D], cf[k]); off[k] = local[k] - p[k]; }
-        float nd = distance<D>(cp.distFunc, false, off, cp.minkowski);
+        const float mk = (MinkF::kNode && cp.distFunc == 5) ? mink(off) : cp.minkowski;
+        float nd = distance<D>(cp.distFunc, false, off, mk);
         if (cp.sizeActive) nd *= size_factor<D>(h, cp.sizeJitter);
         bool closer = nd < best;
         best = fmin_(nd, best);

@@ -51,14 +51,28 @@ const char* noise_fn(int kind)
     }
 }
 
-// One program -> `__device__ float fnjit_eval_<k>(int seed, float x, float y, float z, float w)`.
-void emit_eval(const CompiledProgram& prog, int k, std::ostringstream& o)
+// One program -> `__device__ float <name>(int seed, float x, float y, float z, float w)`.
+// Its per-cell sub-programs (node-driven Minkowski P) come first, each as a
+// function `<name>_s<j>` plus a functor `<name>_s<j>_mk` the cellular walk calls
+// with the cell's offset vector.
+void emit_eval(const CompiledProgram& prog, const std::string& name, std::ostringstream& o)
 {
+    for (size_t j = 0; j < prog.subs.size(); ++j) {
+        const std::string sub = name + "_s" + std::to_string(j);
+        emit_eval(prog.subs[j], sub, o);
+        const int sd = prog.subs[j].dim;
+        o << "struct " << sub << "_mk {\n    int seed;\n    static constexpr bool kNode = true;\n"
+          << "    __device__ __forceinline__ float operator()(const float* v) const { return " << sub << "(seed, v[0], v[1], "
+          << (sd > 2 ? "v[2]" : "0.0f") << ", " << (sd > 3 ? "v[3]" : "0.0f") << "); }\n};\n\n";
+    }
     const FnProgramHeader* h = reinterpret_cast<const FnProgramHeader*>(prog.blob.data());
     const FnInstr* ins = fn_program_instrs(h);
     const float* P = fn_program_params(h);
     const int nregs = h->n_regs;
-    o << "__device__ __forceinline__ float fnjit_eval_" << k << "(int seed, float x, float y, float z, float w)\n{\n";
+    auto mk = [&](const FnInstr& I) {   // trailing functor argument of a cellular call
+        return I.d == FN_REG_NONE ? std::string() : ", " + name + "_s" + std::to_string(I.d) + "_mk{seed}";
+    };
+    o << "__device__ __forceinline__ float " << name << "(int seed, float x, float y, float z, float w)\n{\n";
     o << "    (void)x; (void)y; (void)z; (void)w;\n";
     const char* root[4] = {"x", "y", "z", "w"};
     for (int i = 0; i < nregs; ++i) o << "    float " << r(i) << " = " << (i < h->dim ? root[i] : "0.0f") << ";\n";
@@ -139,18 +153,18 @@ void emit_eval(const CompiledProgram& prog, int k, std::ostringstream& o)
         case FN_OP_CELL_VALUE:
             o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n        " << cellp(3) << "\n";
             o << "        " << r(I.dst) << " = fnd::scale_out(fnd::cellular_value<" << D << ">(" << sd << ", pp, cp, " << ((I.aux >> 4) & 3)
-              << "), -fnd::kValueBounds, " << p(1) << ", " << p(2) << ");\n";
+              << mk(I) << "), -fnd::kValueBounds, " << p(1) << ", " << p(2) << ");\n";
             break;
         case FN_OP_CELL_DIST:
             o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n        " << cellp(3) << "\n";
-            o << "        float dist[4]; fnd::cellular_distances<" << D << ">(" << sd << ", pp, cp, dist);\n";
+            o << "        float dist[4]; fnd::cellular_distances<" << D << ">(" << sd << ", pp, cp, dist" << mk(I) << ");\n";
             o << "        float nmax; const float v = fnd::cellular_return<" << D << ">(dist, cp.distFunc, " << ((I.aux >> 4) & 3) << ", "
               << ((I.aux >> 8) & 3) << ", " << ((I.aux >> 12) & 7) << ", nmax);\n";
             o << "        " << r(I.dst) << " = fnd::scale_out(v, 0.0f, " << p(1) << ", " << p(2) << ");\n";
             break;
         case FN_OP_CELL_LOOKUP:
             o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n        " << cellp(2) << "\n";
-            o << "        float oo[" << D << "]; fnd::cellular_lookup_pos<" << D << ">(" << sd << ", pp, cp, " << p(1) << ", oo);\n";
+            o << "        float oo[" << D << "]; fnd::cellular_lookup_pos<" << D << ">(" << sd << ", pp, cp, " << p(1) << ", oo" << mk(I) << ");\n";
             for (int j = 0; j < D; ++j) o << "        " << r(I.dst + j) << " = oo[" << j << "];\n";
             break;
         case FN_OP_WARP_GRAD: case FN_OP_WARP_SIMPLEX:
@@ -394,7 +408,7 @@ std::string jit_batch_source(const std::vector<const CompiledProgram*>& progs)
 {
     std::ostringstream o;
     o << "// generated by fn_jit.cpp: batch module\n" << embedded_device_source() << "\n";
-    for (size_t k = 0; k < progs.size(); ++k) emit_eval(*progs[k], (int)k, o);
+    for (size_t k = 0; k < progs.size(); ++k) emit_eval(*progs[k], "fnjit_eval_" + std::to_string(k), o);
     emit_batch(progs, o);
     return o.str();
 }
@@ -403,7 +417,7 @@ std::string jit_percall_source(const CompiledProgram& prog)
 {
     std::ostringstream o;
     o << "// generated by fn_jit.cpp: per-call module\n" << embedded_device_source() << "\n";
-    emit_eval(prog, 0, o);
+    emit_eval(prog, "fnjit_eval_0", o);
     emit_percall(prog, 0, o);
     return o.str();
 }
@@ -529,6 +543,23 @@ bool jit_batch_kernels(const std::vector<uint64_t>& hashes, std::vector<cudaKern
         kernels[i] = it->second;
     }
     return true;
+}
+
+bool jit_ensure(const CompiledProgram* prog, std::string& error)
+{
+    if (!prog->needs_specialisation()) return true;
+    if (!g_enabled.load()) {
+        error = "the tree evaluates a node per cell (node-driven Minkowski P), which only specialised kernels "
+                "can do, and specialisation is disabled";
+        return false;
+    }
+    static std::mutex build_mu;                 // one build per program, even with concurrent first calls
+    std::lock_guard<std::mutex> lk(build_mu);
+    {
+        std::lock_guard<std::mutex> rk(g_jit_mu);
+        if (g_kernels.count(prog->hash) && g_batch_kernels.count(prog->hash)) return true;
+    }
+    return jit_build({prog}, error);
 }
 
 void jit_set_enabled(bool on) { g_enabled.store(on); }

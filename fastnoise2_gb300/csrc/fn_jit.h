@@ -58,6 +58,10 @@ bool jit_batch_kernels(const std::vector<uint64_t>& hashes, std::vector<cudaKern
 bool jit_launch(uint64_t hash, const PointArgs& args, float* out, MinMaxWork* work, float* dminmax, cudaStream_t stream,
                 cudaError_t& err);
 
+// Programs the interpreter cannot run (CompiledProgram::needs_specialisation)
+// get their specialised kernels built on first use; true if they exist now.
+bool jit_ensure(const CompiledProgram* prog, std::string& error);
+
 void jit_set_enabled(bool on);
 bool jit_enabled();
 

@@ -1,6 +1,8 @@
 // fn_server.cpp -- continuous-batching request server (see fn_server.h).
 #include "fn_server.h"
 
+#include "fn_jit.h"
+
 #include <algorithm>
 #include <cstring>
 
@@ -109,6 +111,8 @@ int Server::submit(const BatchItem& item, uint64_t& ticket)
     if (!item.node || item.args.total < 0) { set_error(-1, "invalid request"); return -1; }
     DeviceProgram p;                      // compile now so the submitter sees tree errors
     if (!get_program(item.node, item.args.dim, p)) return last_error();
+    std::string jerr;                     // and specialise trees the interpreter cannot run
+    if (!jit_ensure(p.host, jerr)) { set_error(-2, jerr); return -2; }
     const size_t bytes = (size_t)std::max(0ll, item.args.total) * sizeof(float);
     if (!item.dout && bytes > pool_.capacity()) { set_error(-4, "request output larger than the device pool"); return -4; }
     node_ref(const_cast<Node*>(item.node));
@@ -131,6 +135,8 @@ int Server::submit_many(const BatchItem* items, size_t n, uint64_t* tickets)
         if (!item.node || item.args.total < 0) { set_error(-1, "invalid request " + std::to_string(i)); return -1; }
         DeviceProgram p;
         if (!get_program(item.node, item.args.dim, p)) return last_error();
+        std::string jerr;
+        if (!jit_ensure(p.host, jerr)) { set_error(-2, jerr); return -2; }
         const size_t bytes = (size_t)std::max(0ll, item.args.total) * sizeof(float);
         if (!item.dout && bytes > pool_.capacity()) {
             set_error(-4, "request " + std::to_string(i) + " output larger than the device pool");

@@ -53,6 +53,11 @@ def main():
     cases.append(case("workload2-tileable", trees.terrain_c2(), "tile", [48, 40, 1.0, 1.0], 7))
     cases.append(case("demo-caves", decode(trees.DEMO_CAVES), "grid", [[-40, 12, 5], [24, 20, 6], [1, 1, 1]], 1337))
     cases.append(case("demo-mountain", decode(trees.DEMO_MOUNTAIN), "grid", [[-60, 25], [48, 40], [1, 1]], 1337))
+    for name in ("CellularValue", "CellularDistance", "CellularLookup"):
+        for dim in (2, 3, 4):
+            off, cnt, st = GRID[dim]
+            cases.append(case(f"MinkowskiNode-{name}/{dim}D", trees.minkowski_node_tree(name), "grid",
+                              [list(off), list(cnt), list(st)], 1337))
     with open(OUT, "w") as f:
         json.dump({"generator": "tests/golden/make_golden.py", "cases": cases}, f, indent=1)
     print(f"wrote {len(cases)} cases to {OUT}")

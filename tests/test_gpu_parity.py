@@ -217,3 +217,24 @@ def test_unfused_oracle_mode_is_close(gpu):
     a, _ = OracleTree(root).grid((0, 0, 0), (16, 16, 16), (1, 1, 1), 42)
     b, _ = OracleTree(root, unfused=True).grid((0, 0, 0), (16, 16, 16), (1, 1, 1), 42)
     assert np.max(np.abs(a - b)) < 1e-5
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+@pytest.mark.parametrize("name", ["CellularValue", "CellularDistance", "CellularLookup"])
+def test_node_driven_minkowski(gpu, name, dim):
+    """Minkowski P from a node, sampled at each cell's offset vector: the tree is
+    specialised automatically on first use (the interpreter cannot run it)."""
+    off, cnt, st = GRID[dim]
+    assert_parity(*run_grid(trees.minkowski_node_tree(name), off, cnt, st, 1337), label=f"{name} {dim}D")
+
+
+def test_node_driven_minkowski_needs_specialisation(gpu):
+    import fastnoise2_gb300 as fn
+    node = trees.to_product(trees.minkowski_node_tree())
+    was = fn.set_jit_enabled(False)
+    try:
+        with pytest.raises(fn.FastNoiseError) as e:
+            node.gen_uniform_grid((0, 0), (8, 8), (1, 1), 1)
+        assert e.value.code == -2
+    finally:
+        fn.set_jit_enabled(was)

@@ -70,10 +70,21 @@ DEMO_CAVES = ("FgIcCS4AAQ@BklCQs@BlRBDNzMw9G@AIMAgAw@ADgC@BCiQIzczMPgkJ@BPkIQH4X
 
 
 def unsupported_tree() -> Node:
-    """A tree the GPU compiler rejects: a cellular node whose Minkowski P is driven
-    by another node."""
-    n = N("CellularDistance", Minkowski_P=N("Simplex"))
+    """A tree the GPU compiler rejects: a right-deep chain of blends whose pending
+    left operands need more than the program's 64 live registers."""
+    n = N("Simplex")
+    for i in range(70):
+        n = N("Add", LHS=N("Value", Seed_Offset=i), RHS=n)
+    return n
+
+
+def minkowski_node_tree(name: str = "CellularDistance") -> Node:
+    """A cellular node whose Minkowski P is driven by another node (evaluated at
+    every cell's offset vector)."""
+    n = N(name, Feature_Scale=3.3, Minkowski_P=N("Value", Feature_Scale=0.8, Output_Min=0.6, Output_Max=3.0))
     n.set("Distance Function", "Minkowski")
+    if name == "CellularLookup":
+        n.set("Lookup", N("Perlin", Feature_Scale=9.0))
     return n
 
 
