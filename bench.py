@@ -51,7 +51,7 @@ GRID_WORKLOADS = {
     "terrain-tileable-1024": ("terrain_c2", "tile", ((1024, 1024), (1.0, 1.0)), 7),
     "terrain-128": ("terrain_c2", "grid", ((0.0, 0.0, 0.0), (128, 128, 128), (1.0, 1.0, 1.0)), 7),
 }
-WORKLOADS = ["chunk-mix", *GRID_WORKLOADS]
+WORKLOADS = ["chunk-mix", *GRID_WORKLOADS, "mesh-bloxel-128"]
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -457,6 +457,85 @@ def run_served(fn, chunks, nodes, rank, a, dev):
     return result
 
 
+# ---------------------------------------------------------------- GPU: chunk meshing
+
+def mesh_tree():
+    """A terrain surface for the mesher: vertical gradient plus fractal noise."""
+    from oracle.tree import N
+    g = N("Gradient")
+    g.set("Multiplier", 0.02, 1)
+    return N("Add", LHS=N("FractalFBm", Source=N("Simplex", Feature_Scale=60.0), Octaves=4), RHS=g)
+
+
+def run_mesh(a, rank, world, local):
+    """fnBuildChunkMeshBloxel on the Node Editor's chunk size (128^3 voxels, 130^3 densities),
+    a row of 8 chunks across the surface per step."""
+    import torch
+    import fastnoise2_gb300 as fn
+    from tests.trees import to_product
+    size, chunks = 128, 8
+    node = to_product(mesh_tree())
+    if a.kernels == "jit":
+        fn.jit_compile([(node, 3)])
+    else:
+        fn.set_jit_enabled(False)
+    dev = torch.device("cuda", local)
+    vcap, icap = 24 << 20, 36 << 20
+    verts = torch.empty(vcap * 4, dtype=torch.float32, device=dev)
+    idx = torch.empty(icap, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    positions = [(size * (k - chunks // 2), -size // 2, size * (rank % 4)) for k in range(chunks)]
+    faces = []
+
+    def step():
+        for p in positions:
+            r = fn.build_chunk_mesh_bloxel(node, size, p, 1337 + rank, 0.0, False, verts.data_ptr(), vcap, idx.data_ptr(), icap,
+                                           stream.cuda_stream)
+            faces.append(r["indexCount"] // 6)
+
+    for _ in range(max(a.warmup, 3)):
+        step()
+    torch.cuda.synchronize(dev)
+    faces.clear()
+    sampler = ClockSampler(local)
+    with sampler:
+        barrier(world)
+        st = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+        en = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
+        for i in range(a.steps):
+            torch.cuda.nvtx.range_push("timed")
+            st[i].record(stream)
+            step()
+            en[i].record(stream)
+            torch.cuda.nvtx.range_pop()
+        torch.cuda.synchronize(dev)
+        barrier(world)
+    clocks = sampler.summary()
+    ms = statistics.mean(s_.elapsed_time(e_) for s_, e_ in zip(st, en))
+    ms_max = allmax(ms, world)
+    voxels = chunks * size ** 3
+    value = voxels * world / (ms_max * 1e-3) / 1e6
+    if rank != 0:
+        return
+    line = {
+        "metric": "Mpoints/s", "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "mesh-bloxel-128", "chunks_per_step": chunks, "chunk": [size] * 3,
+                   "points_per_step": voxels, "densities_per_chunk": (size + 2) ** 3,
+                   "faces_per_chunk": statistics.mean(faces) if faces else 0,
+                   "path": "fnBuildChunkMeshBloxel: densities (" + ("specialised kernel" if a.kernels == "jit" else "interpreter")
+                           + ") + count/scan/emit mesher, synchronous per chunk",
+                   "l2": "densities of a chunk (8.8 MB) stay in L2 between generation and meshing"},
+        "e2e": {"value": value, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 20 * chunks,
+                "api": "fnBuildChunkMeshBloxel (device mesh buffers; counts, heights and min/max read back per chunk)"},
+        "cpu_baseline": None,
+        "clocks": clocks,
+        "gpu_launches": a.steps * chunks * 6,   # densities, count, 3 scan kernels, emit
+    }
+    print(json.dumps(line))
+
+
 # ---------------------------------------------------------------- GPU: single grids
 
 def run_grid(a, rank, world, local):
@@ -585,6 +664,8 @@ def main():
     torch.cuda.set_device(local)
     if a.workload == "chunk-mix":
         run_chunkmix(a, rank, world, local)
+    elif a.workload == "mesh-bloxel-128":
+        run_mesh(a, rank, world, local)
     else:
         run_grid(a, rank, world, local)
 

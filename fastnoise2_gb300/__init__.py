@@ -100,6 +100,8 @@ def _declare(L):
         "fnGenUniformGrid2DDevice": (c_int, [vp, vp, c_float, c_float, c_int, c_int, c_float, c_float, c_int, vp, vp]),
         "fnGenUniformGrid3DDevice": (c_int, [vp, vp, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, vp, vp]),
         "fnJitCompile": (c_int, [vp, vp, c_int]),
+        "fnBuildChunkMeshBloxel": (c_int, [vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, vp, vp]),
+        "fnBuildChunkMeshHeightmap": (c_int, [vp, c_int, c_int, c_int, c_int, c_float, vp, vp]),
         "fnGetBatchInfo": (c_int, [vp]),
         "fnJitCheck": (c_int, [vp, vp, c_int, ctypes.POINTER(c_int)]),
         "fnSetJitEnabled": (c_int, [c_int]),
@@ -225,6 +227,43 @@ def jit_check(pairs) -> int:
     if lib().fnJitCheck(nodes, dims, len(pairs), ctypes.byref(n)) != 0:
         _check()
     return n.value
+
+
+class ChunkMesh(ctypes.Structure):
+    """fnChunkMesh: device vertex (x, y, z, light) and index buffers plus the results."""
+    _fields_ = [("vertices", ctypes.c_void_p), ("indices", ctypes.c_void_p), ("vertexCapacity", ctypes.c_int),
+                ("indexCapacity", ctypes.c_int), ("vertexCount", ctypes.c_int), ("indexCount", ctypes.c_int),
+                ("minAirY", ctypes.c_float), ("maxSolidY", ctypes.c_float), ("minMax", ctypes.c_float * 2)]
+
+    def result(self) -> dict:
+        return {"vertexCount": self.vertexCount, "indexCount": self.indexCount, "minAirY": self.minAirY,
+                "maxSolidY": self.maxSolidY, "minMax": (self.minMax[0], self.minMax[1])}
+
+
+def _mesh(rc: int, mesh: ChunkMesh) -> dict:
+    if rc != 0 and rc != -4:
+        _check()
+    out = mesh.result()
+    out["fits"] = rc == 0
+    return out
+
+
+def build_chunk_mesh_bloxel(node: "Node", size: int, pos, seed: int, iso: float, up_axis_z: bool, vertices_ptr: int,
+                            vertex_capacity: int, indices_ptr: int, index_capacity: int, stream: int = 0) -> dict:
+    """fnBuildChunkMeshBloxel into device buffers; returns counts, heights, min/max and whether it fit."""
+    m = ChunkMesh(vertices_ptr or None, indices_ptr or None, vertex_capacity, index_capacity, 0, 0, 0.0, 0.0)
+    rc = lib().fnBuildChunkMeshBloxel(node.handle, int(size), int(pos[0]), int(pos[1]), int(pos[2]), int(np.int32(seed)),
+                                      float(iso), 1 if up_axis_z else 0, ctypes.byref(m), stream or None)
+    return _mesh(rc, m)
+
+
+def build_chunk_mesh_heightmap(node: "Node", size: int, pos, seed: int, multiplier: float, vertices_ptr: int,
+                               vertex_capacity: int, indices_ptr: int, index_capacity: int, stream: int = 0) -> dict:
+    """fnBuildChunkMeshHeightmap into device buffers (pos = (x, z))."""
+    m = ChunkMesh(vertices_ptr or None, indices_ptr or None, vertex_capacity, index_capacity, 0, 0, 0.0, 0.0)
+    rc = lib().fnBuildChunkMeshHeightmap(node.handle, int(size), int(pos[0]), int(pos[1]), int(np.int32(seed)),
+                                         float(multiplier), ctypes.byref(m), stream or None)
+    return _mesh(rc, m)
 
 
 class BatchInfo(ctypes.Structure):

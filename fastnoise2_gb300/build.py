@@ -24,7 +24,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["fn_kernels.cu", "fn_static_scratch.cu"]
+CU_SOURCES = ["fn_kernels.cu", "fn_static_scratch.cu", "fn_mesh.cu"]
 CPP_SOURCES = ["fn_node.cpp", "fn_compile.cpp", "fn_runtime.cpp", "fn_batch.cpp", "fn_server.cpp", "fn_capi.cpp",
                "fn_jit.cpp"]
 

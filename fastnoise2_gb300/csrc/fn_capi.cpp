@@ -14,6 +14,7 @@
 #include "../../include/FastNoise/FastNoise_C.h"
 #include "fn_batch.h"
 #include "fn_jit.h"
+#include "fn_mesh.h"
 #include "fn_runtime.h"
 #include "fn_server.h"
 #include "fn_static_scratch.h"
@@ -923,6 +924,155 @@ int fnSetJitEnabled(int enabled)
     const int was = jit_enabled() ? 1 : 0;
     jit_set_enabled(enabled != 0);
     return was;
+}
+
+// ---------------------------------------------------------------- chunk meshing
+namespace {
+
+// Per-thread device scratch of the meshers: densities, their min/max, the bloxel
+// scan buffers and a pinned read-back area.
+struct MeshCtx {
+    float* dens = nullptr;
+    size_t dens_cap = 0;
+    float* dminmax = nullptr;
+    MeshScratch scratch;
+    unsigned* host = nullptr;          // pinned: total, air, solid, minmax[2]
+    ~MeshCtx()
+    {
+        if (dens) cudaFree(dens);
+        if (dminmax) cudaFree(dminmax);
+        if (scratch.counts) cudaFree(scratch.counts);
+        if (host) cudaFreeHost(host);
+    }
+};
+thread_local MeshCtx t_mesh;
+
+bool mesh_reserve(size_t densities, size_t voxels)
+{
+    MeshCtx& m = t_mesh;
+    if (!m.dminmax && !cuda_ok(cudaMalloc(&m.dminmax, 2 * sizeof(float)), "cudaMalloc(mesh minmax)")) return false;
+    if (!m.host && !cuda_ok(cudaMallocHost(&m.host, 8 * sizeof(unsigned)), "cudaMallocHost(mesh read-back)")) return false;
+    if (densities > m.dens_cap) {
+        if (m.dens) cudaFree(m.dens);
+        m.dens = nullptr; m.dens_cap = 0;
+        if (!cuda_ok(cudaMalloc(&m.dens, densities * sizeof(float)), "cudaMalloc(mesh densities)")) return false;
+        m.dens_cap = densities;
+    }
+    if (voxels > m.scratch.cap_voxels) {
+        if (m.scratch.counts) cudaFree(m.scratch.counts);
+        m.scratch = MeshScratch();
+        const size_t nb = (voxels + 1023) / 1024;
+        unsigned* block = nullptr;                  // counts | offsets | block totals | total | air, solid
+        if (!cuda_ok(cudaMalloc(&block, (2 * voxels + nb + 4) * sizeof(unsigned)), "cudaMalloc(mesh scan)")) return false;
+        m.scratch.counts = block;
+        m.scratch.offsets = block + voxels;
+        m.scratch.block_totals = block + 2 * voxels;
+        m.scratch.total = block + 2 * voxels + nb;
+        m.scratch.airsolid = block + 2 * voxels + nb + 1;
+        m.scratch.cap_voxels = voxels;
+    }
+    return true;
+}
+
+float decode_ordered(unsigned u) { return f_of((int32_t)((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u)); }
+
+}  // namespace
+
+int fnBuildChunkMeshBloxel(const void* node, int size, int posX, int posY, int posZ, int seed, float isoSurface, int upAxisZ,
+                           fnChunkMesh* mesh, void* stream)
+{
+    clear_error();
+    if (!node || !mesh || size < 1 || size > 256 || mesh->vertexCapacity < 0 || mesh->indexCapacity < 0) {
+        set_error(FN_ERR_ARG, "invalid arguments");
+        return FN_ERR_ARG;
+    }
+    if (!thread_ctx()) return FN_ERR_CUDA;
+    DeviceProgram prog;
+    if (!get_program(N(node), 3, prog)) return last_error();
+    if (!ensure_runnable(prog)) return FN_ERR_COMPILE;
+    const int sg = size + 2;
+    const size_t voxels = (size_t)size * size * size;
+    if (!mesh_reserve((size_t)sg * sg * sg, voxels)) return FN_ERR_CUDA;
+    MeshCtx& m = t_mesh;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    MinMaxWork* work = work_for_stream(s);
+    if (!work) return FN_ERR_CUDA;
+    // GenPositionArray3D over the editor's grid positions (-1 .. size) offset by the
+    // chunk position (MeshNoisePreview.cpp:447-455), as a grid: the same exact
+    // integer-valued floats; with the z axis up, y and z swap roles.
+    const float off[3] = {(float)(posX - 1), (float)((upAxisZ ? posZ : posY) - 1), (float)((upAxisZ ? posY : posZ) - 1)};
+    const int cnt[3] = {sg, sg, sg};
+    const float step[3] = {1, 1, 1};
+    if (!cuda_ok(launch_points(prog, grid_args(3, off, cnt, step, seed), m.dens, work, m.dminmax, s), "densities")) return FN_ERR_CUDA;
+    if (!cuda_ok(launch_bloxel(m.dens, size, upAxisZ != 0, (float)posX, (float)posY, (float)posZ, isoSurface, m.dminmax, m.scratch,
+                               reinterpret_cast<MeshVertex*>(mesh->vertices), (unsigned)mesh->vertexCapacity, mesh->indices,
+                               (unsigned)mesh->indexCapacity, s),
+                 "bloxel mesher"))
+        return FN_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpyAsync(m.host, m.scratch.total, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read back") ||
+        !cuda_ok(cudaMemcpyAsync(m.host + 4, m.dminmax, 2 * sizeof(float), cudaMemcpyDeviceToHost, s), "read back") ||
+        !cuda_ok(cudaStreamSynchronize(s), "synchronize"))
+        return FN_ERR_CUDA;
+    const unsigned faces = m.host[0];
+    float minAir = m.host[1] == 0xFFFFFFFFu ? INFINITY : decode_ordered(m.host[1]);
+    float maxSolid = m.host[2] == 0u ? -INFINITY : decode_ordered(m.host[2]);
+    std::memcpy(mesh->minMax, m.host + 4, 2 * sizeof(float));
+    if (mesh->minMax[0] > isoSurface) minAir = (float)posY;                                   // all air (:459-461)
+    else if (mesh->minMax[1] < isoSurface) maxSolid = (float)posY - 1.0f + (float)size;       // all solid (:463-465)
+    mesh->minAirY = minAir;
+    mesh->maxSolidY = maxSolid;
+    mesh->vertexCount = (int)(faces * 4u);
+    mesh->indexCount = (int)(faces * 6u);
+    if (mesh->vertexCount > mesh->vertexCapacity || mesh->indexCount > mesh->indexCapacity) {
+        set_error(FN_ERR_CAPACITY, "mesh needs " + std::to_string(mesh->vertexCount) + " vertices and " +
+                                       std::to_string(mesh->indexCount) + " indices");
+        return FN_ERR_CAPACITY;
+    }
+    return FN_OK;
+}
+
+int fnBuildChunkMeshHeightmap(const void* node, int size, int posX, int posZ, int seed, float heightMultiplier, fnChunkMesh* mesh,
+                              void* stream)
+{
+    clear_error();
+    if (!node || !mesh || size < 1 || size > 8192 || mesh->vertexCapacity < 0 || mesh->indexCapacity < 0) {
+        set_error(FN_ERR_ARG, "invalid arguments");
+        return FN_ERR_ARG;
+    }
+    if (!thread_ctx()) return FN_ERR_CUDA;
+    DeviceProgram prog;
+    if (!get_program(N(node), 2, prog)) return last_error();
+    if (!ensure_runnable(prog)) return FN_ERR_COMPILE;
+    const int sg = size + 1;
+    if (!mesh_reserve((size_t)sg * sg, 0)) return FN_ERR_CUDA;
+    MeshCtx& m = t_mesh;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    MinMaxWork* work = work_for_stream(s);
+    if (!work) return FN_ERR_CUDA;
+    // GenPositionArray2D over 0 .. size, offset (pos.x, pos.z) (MeshNoisePreview.cpp:958-962)
+    const float off[2] = {(float)posX, (float)posZ};
+    const int cnt[2] = {sg, sg};
+    const float step[2] = {1, 1};
+    if (!cuda_ok(launch_points(prog, grid_args(2, off, cnt, step, seed), m.dens, work, m.dminmax, s), "densities")) return FN_ERR_CUDA;
+    if (!cuda_ok(launch_heightmap(m.dens, size, (float)posX, (float)posZ, heightMultiplier, reinterpret_cast<MeshVertex*>(mesh->vertices),
+                                  (unsigned)mesh->vertexCapacity, mesh->indices, (unsigned)mesh->indexCapacity, s),
+                 "heightmap mesher"))
+        return FN_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpyAsync(m.host + 4, m.dminmax, 2 * sizeof(float), cudaMemcpyDeviceToHost, s), "read back") ||
+        !cuda_ok(cudaStreamSynchronize(s), "synchronize"))
+        return FN_ERR_CUDA;
+    std::memcpy(mesh->minMax, m.host + 4, 2 * sizeof(float));
+    mesh->minAirY = INFINITY;
+    mesh->maxSolidY = -INFINITY;
+    const long long quads = (long long)size * size;
+    mesh->vertexCount = (int)(quads * 4);
+    mesh->indexCount = (int)(quads * 6);
+    if (mesh->vertexCount > mesh->vertexCapacity || mesh->indexCount > mesh->indexCapacity) {
+        set_error(FN_ERR_CAPACITY, "mesh needs " + std::to_string(mesh->vertexCount) + " vertices and " +
+                                       std::to_string(mesh->indexCount) + " indices");
+        return FN_ERR_CAPACITY;
+    }
+    return FN_OK;
 }
 
 // Allocation-free 3D grid: the program is compiled on the host (cached per

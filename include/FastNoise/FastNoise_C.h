@@ -263,6 +263,32 @@ typedef struct fnBatchInfo {
 } fnBatchInfo;
 FASTNOISE_API int fnGetBatchInfo(fnBatchInfo* info);
 
+/* Chunk meshing after the noise (no counterpart in the reference's library: its Node Editor
+ * meshes preview chunks on the CPU in tools/NodeEditor/MeshNoisePreview.cpp, with a chunk size
+ * of 128).  The chunk's densities are generated on the GPU exactly as the editor's
+ * GenPositionArray3D/2D calls do, then meshed on the GPU; vertices and indices come out in the
+ * editor's order.  vertices / indices are device buffers; the call is synchronous and fills
+ * the counts, heights and OutputMinMax, returning FN_ERR_CAPACITY (counts filled) when the
+ * buffers are too small. */
+typedef struct fnMeshVertex { float x, y, z, light; } fnMeshVertex;   /* the editor's VertexData */
+typedef struct fnChunkMesh {
+    fnMeshVertex* vertices;         /* device, vertexCapacity entries */
+    unsigned int* indices;          /* device, indexCapacity entries (triangle list) */
+    int vertexCapacity, indexCapacity;
+    int vertexCount, indexCount;    /* out: the whole mesh (also when it did not fit) */
+    float minAirY, maxSolidY;       /* out (bloxel): lowest air / highest solid voxel row, +-inf if none */
+    float minMax[2];                /* out: OutputMinMax of the densities */
+} fnChunkMesh;
+/* BuildBloxel3DMesh (MeshNoisePreview.cpp:443-590): block faces between solid (density <=
+ * isoSurface) and air voxels of a size^3 chunk at (posX, posY, posZ), with ambient occlusion
+ * and directional light; size <= 256 (every index fits 32 bits).  upAxisZ swaps the y and z noise axes. */
+FASTNOISE_API int fnBuildChunkMeshBloxel(const void* node, int size, int posX, int posY, int posZ, int seed,
+                                         float isoSurface, int upAxisZ, fnChunkMesh* mesh, void* stream);
+/* BuildHeightMap2DMesh (MeshNoisePreview.cpp:956-1004): size^2 quads of a 2D heightmap at
+ * (posX, posZ), heights = density * heightMultiplier; size <= 8192. */
+FASTNOISE_API int fnBuildChunkMeshHeightmap(const void* node, int size, int posX, int posZ, int seed,
+                                            float heightMultiplier, fnChunkMesh* mesh, void* stream);
+
 /* Run-time specialisation (no counterpart in the reference, whose trees run through
  * virtual calls per SIMD block).  Each (node, dimension) pair is compiled to straight-line
  * CUDA and built for sm_103a with NVRTC into one module: per-tree kernels for the grid,

@@ -1,0 +1,94 @@
+"""Chunk meshing on the GPU (fnBuildChunkMeshBloxel / fnBuildChunkMeshHeightmap)
+against the CPU restatement of the Node Editor's meshers (oracle/mesh.py): the
+same vertices, indices, heights and OutputMinMax, bit for bit."""
+import numpy as np
+import pytest
+
+from oracle import mesh as omesh
+from oracle.tree import N
+from tests import trees
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    assert torch.cuda.is_available()
+    return torch
+
+
+def surface_tree():
+    """Densities that cross 0: a vertical gradient plus fractal noise (a terrain surface)."""
+    g = N("Gradient")
+    g.set("Multiplier", 0.08, 1)
+    return N("Add", LHS=N("FractalFBm", Source=N("Simplex", Feature_Scale=18.0), Octaves=3), RHS=g)
+
+
+def caves_tree():
+    return N("CellularDistance", Feature_Scale=9.0, Return_Type="Index0Sub1")
+
+
+def run_bloxel(fn, torch, root, size, pos, seed, iso, up_z, vcap=None, icap=None):
+    node = trees.to_product(root)
+    vcap = vcap if vcap is not None else size ** 3 * 24
+    icap = icap if icap is not None else size ** 3 * 36
+    v = torch.zeros(max(vcap, 1) * 4, dtype=torch.float32, device="cuda")
+    i = torch.zeros(max(icap, 1), dtype=torch.int32, device="cuda")
+    res = fn.build_chunk_mesh_bloxel(node, size, pos, seed, iso, up_z, v.data_ptr(), vcap, i.data_ptr(), icap)
+    return res, v.cpu().numpy().reshape(-1, 4), i.cpu().numpy().view(np.uint32)
+
+
+def oracle_bloxel(root, size, pos, seed, iso, up_z):
+    d, mm = omesh.bloxel_densities(root, size, pos, seed, up_z)
+    return (*omesh.bloxel_mesh(d, mm, size, pos, iso), mm)
+
+
+@pytest.mark.parametrize("case", [
+    (surface_tree, 16, (32, -8, 16), 1337, 0.0, False),
+    (surface_tree, 20, (-48, 4, -20), 7, 0.1, False),
+    (surface_tree, 16, (16, -16, 0), 42, 0.0, True),
+    (caves_tree, 12, (-12, 24, 36), -5, -0.8, False),
+])
+def test_bloxel_matches_oracle(gpu, torch_cuda, case):
+    make, size, pos, seed, iso, up_z = case
+    res, gv, gi = run_bloxel(gpu, torch_cuda, make(), size, pos, seed, iso, up_z)
+    ov, oi, oair, osolid, omm = oracle_bloxel(make(), size, pos, seed, iso, up_z)
+    assert res["fits"] and res["vertexCount"] == len(ov) and res["indexCount"] == len(oi) > 0
+    assert np.array_equal(gv[:len(ov)].view(np.uint32), ov.view(np.uint32))
+    assert np.array_equal(gi[:len(oi)], oi)
+    assert (res["minAirY"], res["maxSolidY"]) == (float(oair), float(osolid))
+    assert res["minMax"] == (float(omm[0]), float(omm[1]))
+
+
+@pytest.mark.parametrize("value, expect", [(1.0, "air"), (-1.0, "solid")])
+def test_bloxel_early_out(gpu, torch_cuda, value, expect):
+    """OutputMinMax entirely above / below the iso level: no faces, only the height."""
+    res, _, _ = run_bloxel(gpu, torch_cuda, N("Constant", Value=value), 16, (0, 32, 0), 1, 0.0, False)
+    assert res["vertexCount"] == 0 and res["indexCount"] == 0
+    if expect == "air":
+        assert res["minAirY"] == 32.0 and res["maxSolidY"] == float("-inf")
+    else:
+        assert res["maxSolidY"] == 32.0 - 1.0 + 16 and res["minAirY"] == float("inf")
+
+
+def test_bloxel_reports_capacity(gpu, torch_cuda):
+    res, _, _ = run_bloxel(gpu, torch_cuda, surface_tree(), 16, (32, -8, 16), 1337, 0.0, False, vcap=8, icap=12)
+    ov, oi, _, _, _ = oracle_bloxel(surface_tree(), 16, (32, -8, 16), 1337, 0.0, False)
+    assert not res["fits"] and res["vertexCount"] == len(ov) and res["indexCount"] == len(oi)
+
+
+@pytest.mark.parametrize("size, pos, mul", [(16, (32, 16), 100.0), (24, (-40, 8), 37.5)])
+def test_heightmap_matches_oracle(gpu, torch_cuda, size, pos, mul):
+    fn, torch = gpu, torch_cuda
+    root = N("FractalFBm", Source=N("Perlin", Feature_Scale=30.0), Octaves=4)
+    node = trees.to_product(root)
+    v = torch.zeros(size * size * 16, dtype=torch.float32, device="cuda")
+    i = torch.zeros(size * size * 6, dtype=torch.int32, device="cuda")
+    res = fn.build_chunk_mesh_heightmap(node, size, pos, 11, mul, v.data_ptr(), size * size * 4, i.data_ptr(), size * size * 6)
+    d, mm = omesh.heightmap_densities(root, size, (pos[0], 0, pos[1]), 11)
+    ov, oi = omesh.heightmap_mesh(d, size, (pos[0], 0, pos[1]), mul)
+    assert res["fits"] and res["vertexCount"] == len(ov) and res["indexCount"] == len(oi)
+    assert np.array_equal(v.cpu().numpy().reshape(-1, 4).view(np.uint32), ov.view(np.uint32))
+    assert np.array_equal(i.cpu().numpy().view(np.uint32), oi)
+    assert res["minMax"] == (float(mm[0]), float(mm[1]))
