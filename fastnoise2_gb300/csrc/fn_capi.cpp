@@ -128,6 +128,18 @@ int gen_device(const void* node, PointArgs args, float* dout, float* dminmax, vo
     return FN_OK;
 }
 
+// Magic numbers for dividing 32-bit point indices by count (PointArgs::divm/divs):
+// s = ceil(log2 count), m = 2^32 (2^s - count) / count + 1; count 1 gives s = 0.
+void set_divisor(PointArgs& a, int k, int count)
+{
+    const uint64_t d = count > 0 ? (uint64_t)count : 1u;
+    if (d == 1) { a.divm[k] = 0; a.divs[k] = 0; return; }
+    unsigned s = 0;
+    while ((1ull << s) < d) ++s;
+    a.divm[k] = (unsigned)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+    a.divs[k] = s;
+}
+
 PointArgs grid_args(int dim, const float* off, const int* cnt, const float* step, int seed)
 {
     PointArgs a;
@@ -141,6 +153,7 @@ PointArgs grid_args(int dim, const float* off, const int* cnt, const float* step
         a.offset[k] = off[k];
         a.step[k] = step[k];
         total *= cnt[k] > 0 ? cnt[k] : 0;
+        if (k < 3) set_divisor(a, k, cnt[k]);
     }
     a.total = total;
     return a;
@@ -163,6 +176,7 @@ PointArgs tile_args(int xSize, int ySize, float xStep, float yStep, int seed)
     a.tmul[0] = 1 / xSizePi;
     a.tmul[1] = 1 / ySizePi;
     a.total = (long long)(xSize > 0 ? xSize : 0) * (ySize > 0 ? ySize : 0);
+    set_divisor(a, 0, xSize);
     return a;
 }
 

@@ -45,6 +45,15 @@ __device__ __forceinline__ void root_position(const fn::PointArgs& a, long long 
     }
 }
 
+// n / count[k] with the precomputed magic numbers of PointArgs (exact for every
+// 32-bit n): a multiply-high and shifts instead of an integer division.
+__device__ __forceinline__ unsigned fast_div(unsigned n, unsigned m, unsigned s)
+{
+    if (s == 0u) return n;                       // divisor 1
+    const unsigned t = __umulhi(n, m);
+    return (t + ((n - t) >> 1)) >> (s - 1u);
+}
+
 // root_position for a known dimensionality and requests below 2^32 points:
 // 32-bit index arithmetic, same positions bit for bit.
 template <int D>
@@ -54,16 +63,16 @@ __device__ __forceinline__ void root_position32(const fn::PointArgs& a, unsigned
         unsigned r = i;
 #pragma unroll
         for (int k = 0; k < D - 1; ++k) {
-            const unsigned c = (unsigned)a.count[k];
-            const unsigned ik = r % c;
-            r /= c;
+            const unsigned q = fast_div(r, a.divm[k], a.divs[k]);
+            const unsigned ik = r - q * (unsigned)a.count[k];
+            r = q;
             R[k] = fmaf(cvtf((int)ik), a.step[k], a.offset[k]);
         }
         R[D - 1] = fmaf(cvtf((int)r), a.step[D - 1], a.offset[D - 1]);
     } else if (D == 4 && a.src == fn::kSrcTileable) {
-        const unsigned c = (unsigned)a.count[0];
-        const float xf = cvtf((int)(i % c)) * a.tmul[0];
-        const float yf = cvtf((int)(i / c)) * a.tmul[1];
+        const unsigned q = fast_div(i, a.divm[0], a.divs[0]);
+        const float xf = cvtf((int)(i - q * (unsigned)a.count[0])) * a.tmul[0];
+        const float yf = cvtf((int)q) * a.tmul[1];
         R[0] = fnd::cos_(xf) * a.tfreq[0];
         R[1] = fnd::cos_(yf) * a.tfreq[1];
         R[2 % D] = fnd::sin_(xf) * a.tfreq[0];

@@ -318,7 +318,9 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
         pos << "                unsigned r = i;\n";
         const char* ax = "xyzw";
         for (int j = 0; j < D; ++j) {
-            if (j < D - 1) pos << "                const unsigned i" << ax[j] << " = r % A.count[" << j << "]; r /= A.count[" << j << "];\n";
+            if (j < D - 1)
+                pos << "                const unsigned q" << j << " = fne::fast_div(r, A.divm[" << j << "], A.divs[" << j << "]);\n"
+                    << "                const unsigned i" << ax[j] << " = r - q" << j << " * (unsigned)A.count[" << j << "]; r = q" << j << ";\n";
             else pos << "                const unsigned i" << ax[j] << " = r;\n";
             pos << "                const float " << pv[j] << " = fmaf(fnd::cvtf((int)i" << ax[j] << "), A.step[" << j << "], A.offset[" << j << "]);\n";
         }
@@ -333,7 +335,7 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
     // tileable (4D programs): Generator.inl:370-433
     if (D == 4) {
         std::ostringstream pos;
-        pos << "                const unsigned ix = i % A.count[0], iy = i / A.count[0];\n"
+        pos << "                const unsigned iy = fne::fast_div(i, A.divm[0], A.divs[0]), ix = i - iy * (unsigned)A.count[0];\n"
             << "                const float xf = fnd::cvtf((int)ix) * A.tmul[0];\n"
             << "                const float yf = fnd::cvtf((int)iy) * A.tmul[1];\n"
             << "                const float px = fnd::cos_(xf) * A.tfreq[0];\n"

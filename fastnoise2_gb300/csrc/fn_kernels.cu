@@ -11,6 +11,8 @@
 // of a warp executes the same instruction stream (warp-uniform dispatch).
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include "fn_eval.cuh"
 #include "fn_kernels.cuh"
 
@@ -324,6 +326,20 @@ __global__ void __launch_bounds__(kThreads, 4) interp_kernel(const FnProgramHead
 
 int g_num_sms = 0;
 
+// Let a kernel stage up to 96 KB of program in dynamic shared memory, once per
+// device (the attribute is per device; `done` holds one bit per device ordinal).
+cudaError_t allow_program_smem(const void* kernel, std::atomic<unsigned long long>& done)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+    if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
+    return e;
+}
+
 constexpr int kBatchThreads = 256;
 
 __global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(BatchHeader* hdr, const BatchRequest* __restrict__ reqs,
@@ -378,12 +394,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(BatchHeader* hd
 cudaError_t launch_batch(BatchHeader* hdr, const BatchRequest* reqs, BatchState* states, const uint2* items,
                          uint32_t max_prog_bytes, int grid, int block, cudaStream_t stream)
 {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> attr_set{0};      // one bit per device
+    cudaError_t e = allow_program_smem((const void*)batch_kernel, attr_set);
+    if (e != cudaSuccess) return e;
     if (block != kBatchThreads || max_prog_bytes > 96 * 1024) return cudaErrorInvalidValue;
     batch_kernel<<<grid, block, max_prog_bytes, stream>>>(hdr, reqs, states, items);
     return cudaGetLastError();
@@ -412,12 +425,9 @@ int num_sms()
 cudaError_t launch_interpreter(const FnProgramHeader* prog, uint32_t prog_bytes, const PointArgs& args, float* out,
                                MinMaxWork* work, float* dminmax, cudaStream_t stream)
 {
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(interp_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
+    static std::atomic<unsigned long long> attr_set{0};      // one bit per device
+    cudaError_t e = allow_program_smem((const void*)interp_kernel, attr_set);
+    if (e != cudaSuccess) return e;
     if (prog_bytes > 96 * 1024 || (prog_bytes & 15)) return cudaErrorInvalidValue;
     long long blocks = (args.total + kThreads - 1) / kThreads;
     long long cap = (long long)num_sms() * 8;

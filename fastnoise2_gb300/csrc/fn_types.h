@@ -22,6 +22,10 @@ struct PointArgs {
     float step[4];
     float tmul[2], tfreq[2];   // tileable constants
     const float* pos[4];  // position arrays (device)
+    // Division of a point index by count[k] (k < 3) as a multiply-high and shifts:
+    // q = (t + ((n - t) >> 1)) >> (divs[k] - 1), t = umulhi(n, divm[k]); divs = 0 means count 1.
+    unsigned int divm[3];
+    unsigned int divs[3];
 };
 
 // Per-launch reduction workspace.  `counter` must be zero before the first
