@@ -776,7 +776,8 @@ struct CellParams {
 // Visit the 3^D cells around the point in the reference's order (last axis
 // fastest): visit(c, cf) gets the primed cell coordinates and the running float
 // cell offsets (cfb[k] + 0, 1, 2).  Nested loops over scalars rather than an
-// odometer over arrays, so the per-cell state stays in registers.
+// odometer over arrays, so the per-cell state stays in registers; the innermost
+// axis is unrolled so three cells' hashing and distances can overlap.
 // Minkowski P of the cellular distance: the node's constant (NoMink), or a
 // functor evaluating the P node at each cell's offset vector (specialised kernels;
 // Cellular.inl:63 passes the offset to CalcDistance, Utils.inl:326-331).
@@ -795,7 +796,7 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
         for (int xi = 0; xi < 3; ++xi, cx = iadd(cx, kPrimeX), fx += 1.0f) {
             int cy = cb[1];
             float fy = cfb[1];
-#pragma unroll 1
+#pragma unroll
             for (int yi = 0; yi < 3; ++yi, cy = iadd(cy, kPrimeY), fy += 1.0f) {
                 const int c[2] = {cx, cy};
                 const float cf[2] = {fx, fy};
@@ -813,7 +814,7 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
             for (int yi = 0; yi < 3; ++yi, cy = iadd(cy, kPrimeY), fy += 1.0f) {
                 int cz = cb[2];
                 float fz = cfb[2];
-#pragma unroll 1
+#pragma unroll
                 for (int zi = 0; zi < 3; ++zi, cz = iadd(cz, kPrimeZ), fz += 1.0f) {
                     const int c[3] = {cx, cy, cz};
                     const float cf[3] = {fx, fy, fz};
@@ -836,7 +837,7 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
                 for (int zi = 0; zi < 3; ++zi, cz = iadd(cz, kPrimeZ), fz += 1.0f) {
                     int cw = cb[3];
                     float fw = cfb[3];
-#pragma unroll 1
+#pragma unroll
                     for (int wi = 0; wi < 3; ++wi, cw = iadd(cw, kPrimeW), fw += 1.0f) {
                         const int c[4] = {cx, cy, cz, cw};
                         const float cf[4] = {fx, fy, fz, fw};
