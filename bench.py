@@ -51,7 +51,7 @@ GRID_WORKLOADS = {
     "terrain-tileable-1024": ("terrain_c2", "tile", ((1024, 1024), (1.0, 1.0)), 7),
     "terrain-128": ("terrain_c2", "grid", ((0.0, 0.0, 0.0), (128, 128, 128), (1.0, 1.0, 1.0)), 7),
 }
-WORKLOADS = ["chunk-mix", *GRID_WORKLOADS, "mesh-bloxel-128"]
+WORKLOADS = ["chunk-mix", *GRID_WORKLOADS, "mesh-bloxel-128", "mesh-dmc-128"]
 L2_FLUSH_BYTES = 256 << 20
 
 
@@ -468,12 +468,16 @@ def mesh_tree():
 
 
 def run_mesh(a, rank, world, local):
-    """fnBuildChunkMeshBloxel on the Node Editor's chunk size (128^3 voxels, 130^3 densities),
-    a row of 8 chunks across the surface per step."""
+    """fnBuildChunkMeshBloxel (130^3 densities) or fnBuildChunkMeshDmc (132^3 densities) on the
+    Node Editor's chunk size, 128^3 voxels, a row of 8 chunks across the surface per step."""
     import torch
     import fastnoise2_gb300 as fn
     from tests.trees import to_product
     size, chunks = 128, 8
+    dmc = a.workload == "mesh-dmc-128"
+    build = fn.build_chunk_mesh_dmc if dmc else fn.build_chunk_mesh_bloxel
+    api = "fnBuildChunkMeshDmc" if dmc else "fnBuildChunkMeshBloxel"
+    apron = 4 if dmc else 2
     node = to_product(mesh_tree())
     if a.kernels == "jit":
         fn.jit_compile([(node, 3)])
@@ -489,8 +493,9 @@ def run_mesh(a, rank, world, local):
 
     def step():
         for p in positions:
-            r = fn.build_chunk_mesh_bloxel(node, size, p, 1337 + rank, 0.0, False, verts.data_ptr(), vcap, idx.data_ptr(), icap,
-                                           stream.cuda_stream)
+            r = build(node, size, p, 1337 + rank, 0.0, False, verts.data_ptr(), vcap, idx.data_ptr(), icap, stream.cuda_stream)
+            if not r["fits"]:
+                raise RuntimeError(f"{api}: mesh buffers too small ({r['vertexCount']} vertices)")
             faces.append(r["indexCount"] // 6)
 
     for _ in range(max(a.warmup, 3)):
@@ -521,17 +526,19 @@ def run_mesh(a, rank, world, local):
         "metric": "Mpoints/s", "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "mesh-bloxel-128", "chunks_per_step": chunks, "chunk": [size] * 3,
-                   "points_per_step": voxels, "densities_per_chunk": (size + 2) ** 3,
-                   "faces_per_chunk": statistics.mean(faces) if faces else 0,
-                   "path": "fnBuildChunkMeshBloxel: densities (" + ("specialised kernel" if a.kernels == "jit" else "interpreter")
-                           + ") + count/scan/emit mesher, synchronous per chunk",
-                   "l2": "densities of a chunk (8.8 MB) stay in L2 between generation and meshing"},
-        "e2e": {"value": value, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 20 * chunks,
-                "api": "fnBuildChunkMeshBloxel (device mesh buffers; counts, heights and min/max read back per chunk)"},
+        "config": {"workload": a.workload, "chunks_per_step": chunks, "chunk": [size] * 3,
+                   "points_per_step": voxels, "densities_per_chunk": (size + apron) ** 3,
+                   ("quads_per_chunk" if dmc else "faces_per_chunk"): statistics.mean(faces) if faces else 0,
+                   "path": api + ": densities (" + ("specialised kernel" if a.kernels == "jit" else "interpreter")
+                           + (") + count/scan/vertex/quad mesher" if dmc else ") + count/scan/emit mesher")
+                           + ", synchronous per chunk",
+                   "l2": f"densities of a chunk ({(size + apron) ** 3 * 4 / 1e6:.1f} MB) stay in L2 between generation and meshing"},
+        "e2e": {"value": value, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": (24 if dmc else 20) * chunks,
+                "api": api + " (device mesh buffers; counts, heights and min/max read back per chunk)"},
         "cpu_baseline": None,
         "clocks": clocks,
-        "gpu_launches": a.steps * chunks * 6,   # densities, count, 3 scan kernels, emit
+        # densities, count, 3 scan kernels, then emit (bloxel) or vertices + quads (dmc)
+        "gpu_launches": a.steps * chunks * (7 if dmc else 6),
     }
     print(json.dumps(line))
 
@@ -664,7 +671,7 @@ def main():
     torch.cuda.set_device(local)
     if a.workload == "chunk-mix":
         run_chunkmix(a, rank, world, local)
-    elif a.workload == "mesh-bloxel-128":
+    elif a.workload in ("mesh-bloxel-128", "mesh-dmc-128"):
         run_mesh(a, rank, world, local)
     else:
         run_grid(a, rank, world, local)

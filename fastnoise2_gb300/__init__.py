@@ -101,6 +101,7 @@ def _declare(L):
         "fnGenUniformGrid3DDevice": (c_int, [vp, vp, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, vp, vp]),
         "fnJitCompile": (c_int, [vp, vp, c_int]),
         "fnBuildChunkMeshBloxel": (c_int, [vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, vp, vp]),
+        "fnBuildChunkMeshDmc": (c_int, [vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, vp, vp]),
         "fnBuildChunkMeshHeightmap": (c_int, [vp, c_int, c_int, c_int, c_int, c_float, vp, vp]),
         "fnGetBatchInfo": (c_int, [vp]),
         "fnJitCheck": (c_int, [vp, vp, c_int, ctypes.POINTER(c_int)]),
@@ -254,6 +255,15 @@ def build_chunk_mesh_bloxel(node: "Node", size: int, pos, seed: int, iso: float,
     m = ChunkMesh(vertices_ptr or None, indices_ptr or None, vertex_capacity, index_capacity, 0, 0, 0.0, 0.0)
     rc = lib().fnBuildChunkMeshBloxel(node.handle, int(size), int(pos[0]), int(pos[1]), int(pos[2]), int(np.int32(seed)),
                                       float(iso), 1 if up_axis_z else 0, ctypes.byref(m), stream or None)
+    return _mesh(rc, m)
+
+
+def build_chunk_mesh_dmc(node: "Node", size: int, pos, seed: int, iso: float, up_axis_z: bool, vertices_ptr: int,
+                         vertex_capacity: int, indices_ptr: int, index_capacity: int, stream: int = 0) -> dict:
+    """fnBuildChunkMeshDmc (dual marching cubes) into device buffers; same result fields as the bloxel mesher."""
+    m = ChunkMesh(vertices_ptr or None, indices_ptr or None, vertex_capacity, index_capacity, 0, 0, 0.0, 0.0)
+    rc = lib().fnBuildChunkMeshDmc(node.handle, int(size), int(pos[0]), int(pos[1]), int(pos[2]), int(np.int32(seed)),
+                                   float(iso), 1 if up_axis_z else 0, ctypes.byref(m), stream or None)
     return _mesh(rc, m)
 
 

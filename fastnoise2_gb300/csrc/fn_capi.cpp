@@ -950,12 +950,14 @@ struct MeshCtx {
     size_t dens_cap = 0;
     float* dminmax = nullptr;
     MeshScratch scratch;
-    unsigned* host = nullptr;          // pinned: total, air, solid, minmax[2]
+    DmcScratch dmc;
+    unsigned* host = nullptr;          // pinned: total, air, solid, minmax[2]; dmc: vertices, quads, air, solid
     ~MeshCtx()
     {
         if (dens) cudaFree(dens);
         if (dminmax) cudaFree(dminmax);
         if (scratch.counts) cudaFree(scratch.counts);
+        if (dmc.counts) cudaFree(dmc.counts);
         if (host) cudaFreeHost(host);
     }
 };
@@ -985,6 +987,30 @@ bool mesh_reserve(size_t densities, size_t voxels)
         m.scratch.airsolid = block + 2 * voxels + nb + 1;
         m.scratch.cap_voxels = voxels;
     }
+    return true;
+}
+
+bool dmc_reserve(size_t cells)
+{
+    MeshCtx& m = t_mesh;
+    if (cells <= m.dmc.cap_cells) return true;
+    if (m.dmc.counts) cudaFree(m.dmc.counts);
+    m.dmc = DmcScratch();
+    const size_t nb = (cells + 1023) / 1024;
+    // counts | offsets | block totals | total (uint2 each) | air, solid | masks
+    const size_t pairs = 2 * cells + nb + 1;
+    char* block = nullptr;
+    if (!cuda_ok(cudaMalloc(&block, pairs * sizeof(uint2) + 2 * sizeof(unsigned) + cells * sizeof(unsigned short)),
+                 "cudaMalloc(dmc scratch)"))
+        return false;
+    uint2* p = reinterpret_cast<uint2*>(block);
+    m.dmc.counts = p;
+    m.dmc.offsets = p + cells;
+    m.dmc.block_totals = p + 2 * cells;
+    m.dmc.total = p + 2 * cells + nb;
+    m.dmc.airsolid = reinterpret_cast<unsigned*>(p + pairs);
+    m.dmc.masks = reinterpret_cast<unsigned short*>(m.dmc.airsolid + 2);
+    m.dmc.cap_cells = cells;
     return true;
 }
 
@@ -1040,6 +1066,59 @@ int fnBuildChunkMeshBloxel(const void* node, int size, int posX, int posY, int p
     if (mesh->vertexCount > mesh->vertexCapacity || mesh->indexCount > mesh->indexCapacity) {
         set_error(FN_ERR_CAPACITY, "mesh needs " + std::to_string(mesh->vertexCount) + " vertices and " +
                                        std::to_string(mesh->indexCount) + " indices");
+        return FN_ERR_CAPACITY;
+    }
+    return FN_OK;
+}
+
+int fnBuildChunkMeshDmc(const void* node, int size, int posX, int posY, int posZ, int seed, float isoSurface, int upAxisZ,
+                        fnChunkMesh* mesh, void* stream)
+{
+    clear_error();
+    if (!node || !mesh || size < 1 || size > 256 || mesh->vertexCapacity < 0 || mesh->indexCapacity < 0) {
+        set_error(FN_ERR_ARG, "invalid arguments");
+        return FN_ERR_ARG;
+    }
+    if (!thread_ctx()) return FN_ERR_CUDA;
+    DeviceProgram prog;
+    if (!get_program(N(node), 3, prog)) return last_error();
+    if (!ensure_runnable(prog)) return FN_ERR_COMPILE;
+    const int sg = size + 4;
+    if (!mesh_reserve((size_t)sg * sg * sg, 0) || !dmc_reserve((size_t)size * size * size)) return FN_ERR_CUDA;
+    MeshCtx& m = t_mesh;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    MinMaxWork* work = work_for_stream(s);
+    if (!work) return FN_ERR_CUDA;
+    // GenPositionArray3D over the editor's grid positions (-2 .. size+1) offset by the
+    // chunk position (MeshNoisePreview.cpp:594-603), as a grid of the same exact
+    // integer-valued floats; with the z axis up, y and z swap roles.
+    const float off[3] = {(float)(posX - 2), (float)((upAxisZ ? posZ : posY) - 2), (float)((upAxisZ ? posY : posZ) - 2)};
+    const int cnt[3] = {sg, sg, sg};
+    const float step[3] = {1, 1, 1};
+    if (!cuda_ok(launch_points(prog, grid_args(3, off, cnt, step, seed), m.dens, work, m.dminmax, s), "densities")) return FN_ERR_CUDA;
+    if (!cuda_ok(launch_dmc(m.dens, size, upAxisZ != 0, posX, posY, posZ, isoSurface, m.dminmax, m.dmc,
+                            reinterpret_cast<MeshVertex*>(mesh->vertices), (unsigned)mesh->vertexCapacity, mesh->indices,
+                            (unsigned)mesh->indexCapacity, s),
+                 "dual marching cubes mesher"))
+        return FN_ERR_CUDA;
+    if (!cuda_ok(cudaMemcpyAsync(m.host, m.dmc.total, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read back") ||
+        !cuda_ok(cudaMemcpyAsync(m.host + 2, m.dmc.airsolid, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read back") ||
+        !cuda_ok(cudaMemcpyAsync(m.host + 4, m.dminmax, 2 * sizeof(float), cudaMemcpyDeviceToHost, s), "read back") ||
+        !cuda_ok(cudaStreamSynchronize(s), "synchronize"))
+        return FN_ERR_CUDA;
+    const unsigned verts = m.host[0], quads = m.host[1];
+    float minAir = m.host[2] == 0xFFFFFFFFu ? INFINITY : decode_ordered(m.host[2]);
+    float maxSolid = m.host[3] == 0u ? -INFINITY : decode_ordered(m.host[3]);
+    std::memcpy(mesh->minMax, m.host + 4, 2 * sizeof(float));
+    if (mesh->minMax[0] > isoSurface) minAir = (float)posY;                                   // all air (:610-613)
+    else if (mesh->minMax[1] < isoSurface) maxSolid = (float)posY - 1.0f + (float)size;       // all solid (:614-617)
+    mesh->minAirY = minAir;
+    mesh->maxSolidY = maxSolid;
+    const long long nidx = (long long)quads * 6;
+    mesh->vertexCount = (int)verts;
+    mesh->indexCount = nidx > INT32_MAX ? INT32_MAX : (int)nidx;
+    if ((long long)verts > mesh->vertexCapacity || nidx > mesh->indexCapacity) {
+        set_error(FN_ERR_CAPACITY, "mesh needs " + std::to_string(verts) + " vertices and " + std::to_string(nidx) + " indices");
         return FN_ERR_CAPACITY;
     }
     return FN_OK;

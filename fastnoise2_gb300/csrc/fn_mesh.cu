@@ -3,7 +3,8 @@
 // Restates the Node Editor's chunk meshers (reference
 // tools/NodeEditor/MeshNoisePreview.cpp): the bloxel (block) mesher with ambient
 // occlusion (BuildBloxel3DMesh :443-540, BloxelAddQuadAO :542-590) and the
-// heightmap mesher (BuildHeightMap2DMesh :956-1004).  The density array the
+// heightmap mesher (BuildHeightMap2DMesh :956-1004), and the dual marching cubes
+// mesher (BuildDmc3DMesh :592-769, DmcGetVertIndex :771-953).  The density array the
 // reference fills with GenPositionArray3D/2D is produced by the tree's own
 // generation kernel into a scratch buffer that stays in L2 for editor-size
 // chunks; the meshers then run as
@@ -12,7 +13,12 @@
 //   emit   -- 4 vertices + 6 indices per face at the scanned offset,
 // so vertices and indices come out in exactly the reference's sequential order.
 // The OutputMinMax early-out (:457-467) skips all voxels when the chunk is all
-// air or all solid.
+// air or all solid.  Dual marching cubes shares a vertex between the quads of up
+// to twelve cut edges, numbered in the order the reference's hash map first sees
+// it; here every reference to a vertex finds its first use directly (the lowest
+// cell / axis / slot among the quads that use it), so the count pass marks the
+// creating references, a scan numbers them, and the quads look their vertices up
+// without a map.
 #include <cuda_runtime.h>
 
 #include "fn_mesh.h"
@@ -92,65 +98,91 @@ __global__ void bloxel_count(Vox v, int size, float3 pos, float iso, const float
     }
 }
 
-// ---- exclusive scan of n uint32 (1024 per block), block totals scanned by one block
+// ---- exclusive scan of n counts (1024 per block), block totals scanned by one block.
+// T = unsigned (bloxel faces) or uint2 (dual marching cubes: vertices, quads).
+
+__device__ __forceinline__ unsigned shfl_up(unsigned v, int o) { return __shfl_up_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ uint2 shfl_up(uint2 v, int o)
+{
+    return make_uint2(__shfl_up_sync(0xffffffffu, v.x, o), __shfl_up_sync(0xffffffffu, v.y, o));
+}
+__device__ __forceinline__ unsigned plus(unsigned a, unsigned b) { return a + b; }
+__device__ __forceinline__ uint2 plus(uint2 a, uint2 b) { return make_uint2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ unsigned minus(unsigned a, unsigned b) { return a - b; }
+__device__ __forceinline__ uint2 minus(uint2 a, uint2 b) { return make_uint2(a.x - b.x, a.y - b.y); }
+template <class T> __device__ __forceinline__ T zero() { return T{}; }
 
 constexpr int kScanBlock = 1024;
 
-__device__ __forceinline__ unsigned block_exclusive_scan(unsigned v, unsigned* warp_sums, unsigned& total)
+template <class T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* warp_sums, T& total)
 {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    unsigned x = v;
+    T x = v;
     for (int o = 1; o < 32; o <<= 1) {
-        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
+        const T y = shfl_up(x, o);
+        if (lane >= o) x = plus(x, y);
     }
     if (lane == 31) warp_sums[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        unsigned w = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0u;
+        T w = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : zero<T>();
         for (int o = 1; o < 32; o <<= 1) {
-            const unsigned y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
+            const T y = shfl_up(w, o);
+            if (lane >= o) w = plus(w, y);
         }
         warp_sums[lane] = w;                       // inclusive over warps
     }
     __syncthreads();
-    const unsigned before = warp ? warp_sums[warp - 1] : 0u;
+    const T before = warp ? warp_sums[warp - 1] : zero<T>();
     total = warp_sums[(blockDim.x >> 5) - 1];
-    return before + x - v;
+    return plus(before, minus(x, v));
 }
 
-__global__ void __launch_bounds__(kScanBlock) scan_blocks(const unsigned* in, unsigned* out, unsigned* block_totals, unsigned n)
+template <class T>
+__global__ void __launch_bounds__(kScanBlock) scan_blocks(const T* in, T* out, T* block_totals, unsigned n)
 {
-    __shared__ unsigned ws[32];
+    __shared__ T ws[32];
     const unsigned i = blockIdx.x * kScanBlock + threadIdx.x;
-    const unsigned v = i < n ? in[i] : 0u;
-    unsigned total;
-    const unsigned ex = block_exclusive_scan(v, ws, total);
+    const T v = i < n ? in[i] : zero<T>();
+    T total;
+    const T ex = block_exclusive_scan(v, ws, total);
     if (i < n) out[i] = ex;
     if (threadIdx.x == 0) block_totals[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(kScanBlock) scan_totals(unsigned* totals, unsigned nb, unsigned* grand_total)
+template <class T>
+__global__ void __launch_bounds__(kScanBlock) scan_totals(T* totals, unsigned nb, T* grand_total)
 {
-    __shared__ unsigned ws[32];
-    unsigned carry = 0;
+    __shared__ T ws[32];
+    T carry = zero<T>();
     for (unsigned base = 0; base < nb; base += kScanBlock) {
         const unsigned i = base + threadIdx.x;
-        const unsigned v = i < nb ? totals[i] : 0u;
-        unsigned total;
-        const unsigned ex = block_exclusive_scan(v, ws, total);
-        if (i < nb) totals[i] = carry + ex;
-        carry += total;
+        const T v = i < nb ? totals[i] : zero<T>();
+        T total;
+        const T ex = block_exclusive_scan(v, ws, total);
+        if (i < nb) totals[i] = plus(carry, ex);
+        carry = plus(carry, total);
         __syncthreads();
     }
     if (threadIdx.x == 0) *grand_total = carry;
 }
 
-__global__ void __launch_bounds__(kScanBlock) scan_add(unsigned* out, const unsigned* totals, unsigned n)
+template <class T>
+__global__ void __launch_bounds__(kScanBlock) scan_add(T* out, const T* totals, unsigned n)
 {
     const unsigned i = blockIdx.x * kScanBlock + threadIdx.x;
-    if (i < n) out[i] += totals[blockIdx.x];
+    if (i < n) out[i] = plus(out[i], totals[blockIdx.x]);
+}
+
+// Exclusive scan of n counts into `out`; the grand total lands in `total`.
+template <class T>
+void exclusive_scan(const T* in, T* out, T* block_totals, T* total, unsigned n, cudaStream_t stream)
+{
+    const unsigned nb = (n + kScanBlock - 1) / kScanBlock;
+    scan_blocks<T><<<nb, kScanBlock, 0, stream>>>(in, out, block_totals, n);
+    scan_totals<T><<<1, kScanBlock, 0, stream>>>(block_totals, nb, total);
+    scan_add<T><<<nb, kScanBlock, 0, stream>>>(out, block_totals, n);
 }
 
 // ---- bloxel emit: BloxelAddQuadAO for every face of every solid voxel
@@ -288,6 +320,391 @@ __global__ void heightmap_emit(const float* d, int size, float2 pos, float mul, 
     }
 }
 
+// ---- dual marching cubes (BuildDmc3DMesh :592-769, DmcGetVertIndex :771-953)
+//
+// Cell corners are numbered x + 2y + 4z; edge k joins kDmcEdgeCorner[k].  A
+// marching-cubes case (bit k = corner k above the iso level) has one dual point
+// per connected piece of its surface; each piece is the set of cut edges that
+// the face contours join.  On a face with two cut edges they are joined; on an
+// ambiguous face (diagonal corners, four cut edges) each corner above the iso
+// level is cut off on its own.  The table is derived here at compile time from
+// that rule; it equals the reference's kDualPointsList (DmcTable.inl) case for
+// case, piece order aside (the mesher only asks which piece holds an edge).
+
+struct DmcTable {
+    unsigned long long edge_piece[256];   // 4 bits per edge: its piece, 0xF = edge not cut
+    unsigned short code[256][4];          // cut-edge bit set of each piece
+};
+
+constexpr int kDmcEdgeCorner[12][2] = {{0, 1}, {1, 5}, {4, 5}, {0, 4}, {2, 3}, {3, 7},
+                                       {6, 7}, {2, 6}, {0, 2}, {1, 3}, {5, 7}, {4, 6}};
+// the six faces: corners in cyclic order, edge k joins corner k and corner k+1
+constexpr int kDmcFaceCorner[6][4] = {{0, 2, 6, 4}, {1, 3, 7, 5}, {0, 1, 5, 4}, {2, 3, 7, 6}, {0, 1, 3, 2}, {4, 5, 7, 6}};
+constexpr int kDmcFaceEdge[6][4] = {{8, 7, 11, 3}, {9, 5, 10, 1}, {0, 1, 2, 3}, {4, 5, 6, 7}, {0, 9, 4, 8}, {2, 10, 6, 11}};
+
+constexpr int dmc_root(const int* label, int e)
+{
+    while (label[e] != e) e = label[e];
+    return e;
+}
+
+constexpr DmcTable make_dmc_table()
+{
+    DmcTable t{};
+    for (int c = 0; c < 256; ++c) {
+        int label[12] = {};
+        bool cut[12] = {};
+        for (int e = 0; e < 12; ++e) {
+            label[e] = e;
+            cut[e] = ((c >> kDmcEdgeCorner[e][0]) & 1) != ((c >> kDmcEdgeCorner[e][1]) & 1);
+        }
+        for (int f = 0; f < 6; ++f) {
+            int n = 0, first = -1, last = -1;
+            for (int k = 0; k < 4; ++k) {
+                const int e = kDmcFaceEdge[f][k];
+                if (!cut[e]) continue;
+                ++n;
+                if (first < 0) first = e;
+                last = e;
+            }
+            int pairs[2][2] = {{-1, -1}, {-1, -1}};
+            int np = 0;
+            if (n == 2) {
+                pairs[np][0] = first; pairs[np][1] = last; ++np;
+            } else if (n == 4) {
+                for (int k = 0; k < 4; ++k)
+                    if ((c >> kDmcFaceCorner[f][k]) & 1) { pairs[np][0] = kDmcFaceEdge[f][(k + 3) & 3]; pairs[np][1] = kDmcFaceEdge[f][k]; ++np; }
+            }
+            for (int p = 0; p < np; ++p) {
+                const int ra = dmc_root(label, pairs[p][0]), rb = dmc_root(label, pairs[p][1]);
+                if (ra < rb) label[rb] = ra; else label[ra] = rb;
+            }
+        }
+        int piece_of_root[12] = {};
+        for (int e = 0; e < 12; ++e) piece_of_root[e] = -1;
+        int pieces = 0;
+        unsigned long long ep = ~0ull;
+        for (int e = 0; e < 12; ++e) {
+            if (!cut[e]) continue;
+            const int r = dmc_root(label, e);
+            if (piece_of_root[r] < 0) piece_of_root[r] = pieces++;
+            const int p = piece_of_root[r];
+            ep &= ~(0xFull << (4 * e));
+            ep |= (unsigned long long)p << (4 * e);
+            t.code[c][p] = (unsigned short)(t.code[c][p] | (1u << e));
+        }
+        t.edge_piece[c] = ep;
+    }
+    return t;
+}
+
+__device__ const DmcTable kDmc = make_dmc_table();
+
+// Quads: the edge of axis a (x, y, z) from the cell's base corner is cut; its four
+// dual vertices sit in cells base + dmc_slot_off(a, s, .), on edge dmc_slot_edge(a, s).
+__host__ __device__ constexpr int dmc_slot_off(int a, int s, int k)
+{
+    constexpr int t[3][4][3] = {{{0, 0, 0}, {0, 0, -1}, {0, -1, 0}, {0, -1, -1}},
+                                {{0, 0, 0}, {-1, 0, 0}, {0, 0, -1}, {-1, 0, -1}},
+                                {{0, 0, 0}, {0, -1, 0}, {-1, 0, 0}, {-1, -1, 0}}};
+    return t[a][s][k];
+}
+__host__ __device__ constexpr int dmc_slot_edge(int a, int s)
+{
+    constexpr int t[3][4] = {{0, 2, 4, 6}, {8, 9, 11, 10}, {3, 7, 1, 5}};
+    return t[a][s];
+}
+// Inverse: edge e of a vertex cell is used by the quad of cell + dmc_use_off(e, .),
+// at slot dmc_use_slot(e) = axis * 4 + slot.
+__host__ __device__ constexpr int dmc_use_off(int e, int k)
+{
+    constexpr int t[12][3] = {{0, 0, 0}, {1, 0, 0}, {0, 0, 1}, {0, 0, 0}, {0, 1, 0}, {1, 1, 0},
+                              {0, 1, 1}, {0, 1, 0}, {0, 0, 0}, {1, 0, 0}, {1, 0, 1}, {0, 0, 1}};
+    return t[e][k];
+}
+__host__ __device__ constexpr int dmc_use_slot(int e)
+{
+    constexpr int t[12] = {0, 10, 1, 8, 2, 11, 3, 9, 4, 5, 7, 6};
+    return t[e];
+}
+
+struct DmcGrid {
+    const float* d;
+    int sx, sy, sz;     // density strides of the mesher's x / y / z axes
+    int size;           // cells per axis
+};
+
+__device__ __forceinline__ int dmc_index(const DmcGrid& g, int x, int y, int z)
+{
+    return (x + 2) * g.sx + (y + 2) * g.sy + (z + 2) * g.sz;
+}
+
+// DmcGetVertIndex's cell code (:774-790)
+__device__ __forceinline__ unsigned dmc_case(const DmcGrid& g, int i, float iso)
+{
+    const float* d = g.d;
+    unsigned c = 0;
+    c |= d[i] > iso ? 1u : 0u;
+    c |= d[i + g.sx] > iso ? 2u : 0u;
+    c |= d[i + g.sy] > iso ? 4u : 0u;
+    c |= d[i + g.sx + g.sy] > iso ? 8u : 0u;
+    c |= d[i + g.sz] > iso ? 16u : 0u;
+    c |= d[i + g.sx + g.sz] > iso ? 32u : 0u;
+    c |= d[i + g.sy + g.sz] > iso ? 64u : 0u;
+    c |= d[i + g.sx + g.sy + g.sz] > iso ? 128u : 0u;
+    return c;
+}
+
+// the piece (point code) of case `c` that holds edge `e` (:792-800)
+__device__ __forceinline__ unsigned dmc_code(unsigned c, int e)
+{
+    const unsigned p = (unsigned)(__ldg(&kDmc.edge_piece[c]) >> (4 * e)) & 0xFu;
+    return __ldg(&kDmc.code[c][p]);
+}
+
+// The first quad (in the reference's cell / axis / slot order) that uses the
+// dual vertex (cell w, piece `code`): cell index * 12 + axis * 4 + slot.  That
+// quad is the one whose DmcGetVertIndex call creates the vertex in the map.
+__device__ __forceinline__ unsigned dmc_first_use(const DmcGrid& g, int wx, int wy, int wz, unsigned code)
+{
+    unsigned best = 0xFFFFFFFFu;
+#pragma unroll
+    for (int e = 0; e < 12; ++e) {
+        if (!((code >> e) & 1u)) continue;
+        const int cx = wx + dmc_use_off(e, 0), cy = wy + dmc_use_off(e, 1), cz = wz + dmc_use_off(e, 2);
+        if (cx >= g.size || cy >= g.size || cz >= g.size || cx < 0 || cy < 0 || cz < 0) continue;
+        const unsigned key = (((unsigned)cz * g.size + (unsigned)cy) * g.size + (unsigned)cx) * 12u + (unsigned)dmc_use_slot(e);
+        best = key < best ? key : best;
+    }
+    return best;
+}
+
+// mean of the piece's edge crossings, relative to the cell's base corner (:810-890)
+__device__ __forceinline__ float3 dmc_point(const DmcGrid& g, int i, unsigned code, float iso)
+{
+    const float* d = g.d;
+    const int X = g.sx, Y = g.sy, Z = g.sz;
+    auto t = [&](int a, int b) { return (iso - d[a]) / (d[b] - d[a]); };
+    float x = 0.0f, y = 0.0f, z = 0.0f;
+    if (code & 1u) x += t(i, i + X);
+    if (code & 2u) { x += 1.0f; z += t(i + X, i + X + Z); }
+    if (code & 4u) { x += t(i + Z, i + X + Z); z += 1.0f; }
+    if (code & 8u) z += t(i, i + Z);
+    if (code & 16u) { x += t(i + Y, i + X + Y); y += 1.0f; }
+    if (code & 32u) { x += 1.0f; y += 1.0f; z += t(i + X + Y, i + X + Y + Z); }
+    if (code & 64u) { x += t(i + Y + Z, i + X + Y + Z); y += 1.0f; z += 1.0f; }
+    if (code & 128u) { y += 1.0f; z += t(i + Y, i + Y + Z); }
+    if (code & 256u) y += t(i, i + Y);
+    if (code & 512u) { x += 1.0f; y += t(i + X, i + X + Y); }
+    if (code & 1024u) { x += 1.0f; y += t(i + X + Z, i + X + Y + Z); z += 1.0f; }
+    if (code & 2048u) { y += t(i + Z, i + Y + Z); z += 1.0f; }
+    const float n = (float)__popc(code);
+    return make_float3(x / n, y / n, z / n);
+}
+
+// NormaliseConstExpr(-LIGHT_DIR) (:21-30): Newton square root until it repeats
+__device__ __forceinline__ float3 dmc_light_dir()
+{
+    const float x = -kLightX, y = -kLightY, z = -kLightZ;
+    const float len2 = x * x + y * y + z * z;
+    float curr = len2, prev = 0.0f;
+    for (int k = 0; k < 64 && curr != prev; ++k) {
+        const float next = 0.5f * (curr + len2 / curr);
+        prev = curr;
+        curr = next;
+    }
+    return make_float3(x / curr, y / curr, z / curr);
+}
+
+// One coordinate of the vertex offset DmcGetVertIndex receives: the float of the
+// quad's cell coordinate, minus 1 when the vertex cell lies one step back.
+__device__ __forceinline__ float dmc_offset(int pos, int cell, int vcell)
+{
+    const float f = (float)(pos + cell);
+    return vcell != cell ? f - 1.0f : f;
+}
+
+__device__ __forceinline__ float lerp_(float a, float b, float t) { return a + (b - a) * t; }   // ImLerp
+
+// the vertex light: trilinear central-difference gradient at the point (:902-948)
+__device__ __forceinline__ float dmc_light(const DmcGrid& g, int i, float3 v, float3 nl)
+{
+    const float* d = g.d;
+    const int X = g.sx, Y = g.sy, Z = g.sz;
+    // STEP & (int)lroundf(-v): v lies in [0, 1], so lroundf gives -1 (offset one step) or 0
+    const int ox = lroundf(-v.x) == -1 ? X : 0, oy = lroundf(-v.y) == -1 ? Y : 0, oz = lroundf(-v.z) == -1 ? Z : 0;
+    float3 dd = make_float3(v.x + 0.5f, v.y + 0.5f, v.z + 0.5f);
+    dd = make_float3(dd.x - floorf(dd.x), dd.y - floorf(dd.y), dd.z - floorf(dd.z));
+    float3 der = make_float3(0.0f, 0.0f, 0.0f);
+    int cur = i;
+#pragma unroll
+    for (int z = -1; z < 1; ++z) {
+        const float cz = fabsf((float)z + v.z);
+#pragma unroll
+        for (int y = -1; y < 1; ++y) {
+            const float cy = fabsf((float)y + v.y);
+#pragma unroll
+            for (int x = -1; x < 1; ++x) {
+                const float cx = fabsf((float)x + v.x);
+                if (x) {
+                    const int k = cur + ox;
+                    der.x += cy * cz * lerp_(d[k - X] - d[k], d[k] - d[k + X], dd.x);
+                }
+                if (y) {
+                    const int k = cur + oy;
+                    der.y += cx * cz * lerp_(d[k - Y] - d[k], d[k] - d[k + Y], dd.y);
+                }
+                if (z) {
+                    const int k = cur + oz;
+                    der.z += cx * cy * lerp_(d[k - Z] - d[k], d[k] - d[k + Z], dd.z);
+                }
+                cur += X;
+            }
+            cur += Y - X * 2;
+        }
+        cur += Z - Y * 2;
+    }
+    float light = dot3(nl, normalized3(der)) * (0.5f - kAmbient * 0.5f) + (0.5f + kAmbient * 0.5f);
+    light *= light;
+    return light < 1.0f ? light : 1.0f;                        // std::min(1.0f, light): NaN -> 1
+}
+
+// Count pass: per cell, the quads it emits and which of its 12 (axis, slot)
+// references create a vertex (bit axis * 4 + slot of `masks`).
+__global__ void dmc_count(DmcGrid g, float iso, const float* minmax, uint2* counts, unsigned short* masks)
+{
+    const unsigned n = (unsigned)g.size * g.size * g.size;
+    const bool skip = early_out(minmax, iso);
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
+        const int i = dmc_index(g, x, y, z);
+        unsigned nv = 0, nq = 0, mask = 0;
+        if (!skip) {
+            const bool in0 = g.d[i] <= iso;
+            const int step[3] = {g.sx, g.sy, g.sz};
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                if (in0 == (g.d[i + step[a]] <= iso)) continue;
+                ++nq;
+#pragma unroll
+                for (int s = 0; s < 4; ++s) {
+                    const int wx = x + dmc_slot_off(a, s, 0), wy = y + dmc_slot_off(a, s, 1), wz = z + dmc_slot_off(a, s, 2);
+                    const unsigned code = dmc_code(dmc_case(g, dmc_index(g, wx, wy, wz), iso), dmc_slot_edge(a, s));
+                    if (dmc_first_use(g, wx, wy, wz, code) == t * 12u + (unsigned)(a * 4 + s)) {
+                        mask |= 1u << (a * 4 + s);
+                        ++nv;
+                    }
+                }
+            }
+        }
+        counts[t] = make_uint2(nv, nq);
+        masks[t] = (unsigned short)mask;
+    }
+}
+
+// Vertex pass: each cell writes the vertices it creates at its scanned offset.
+__global__ void dmc_vertices(DmcGrid g, int3 pos, float iso, const float* minmax, const unsigned short* masks,
+                             const uint2* offsets, const uint2* total, MeshVertex* verts, unsigned vcap)
+{
+    __shared__ float3 s_nl;
+    if (threadIdx.x == 0) s_nl = dmc_light_dir();
+    __syncthreads();
+    if (early_out(minmax, iso) || total->x > vcap) return;
+    const float3 nl = s_nl;
+    const unsigned n = (unsigned)g.size * g.size * g.size;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+        const unsigned mask = masks[t];
+        if (!mask) continue;
+        const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
+        unsigned out = offsets[t].x;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                if (!((mask >> (a * 4 + s)) & 1u)) continue;
+                const int wx = x + dmc_slot_off(a, s, 0), wy = y + dmc_slot_off(a, s, 1), wz = z + dmc_slot_off(a, s, 2);
+                const int wi = dmc_index(g, wx, wy, wz);
+                const unsigned code = dmc_code(dmc_case(g, wi, iso), dmc_slot_edge(a, s));
+                const float3 p = dmc_point(g, wi, code, iso);
+                const float light = dmc_light(g, wi, p, nl);
+                verts[out++] = MeshVertex{p.x + dmc_offset(pos.x, x, wx), p.y + dmc_offset(pos.y, y, wy), p.z + dmc_offset(pos.z, z, wz),
+                                          light};
+            }
+        }
+    }
+}
+
+// Quad pass: 6 indices per cut edge (:662-674), vertex indices found through the
+// vertex's first use; the y-edge quads also give the min air / max solid heights.
+__global__ void dmc_quads(DmcGrid g, int3 pos, float iso, const float* minmax, const unsigned short* masks, const uint2* offsets,
+                          const uint2* total, const MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap, unsigned* airsolid)
+{
+    const unsigned n = (unsigned)g.size * g.size * g.size;
+    const bool skip = early_out(minmax, iso);
+    const uint2 tot = *total;
+    const bool fits = tot.x <= vcap && (unsigned long long)tot.y * 6ull <= icap;
+    unsigned air = 0xFFFFFFFFu, solid = 0u;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n && !skip; t += gridDim.x * blockDim.x) {
+        const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
+        const int i = dmc_index(g, x, y, z);
+        const float d0 = g.d[i];
+        const bool in0 = d0 <= iso;
+        const int step[3] = {g.sx, g.sy, g.sz};
+        unsigned quad = offsets[t].y;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const float dn = g.d[i + step[a]];
+            if (in0 == (dn <= iso)) continue;
+            unsigned q[4];
+            float qy[4];
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                const int wx = x + dmc_slot_off(a, s, 0), wy = y + dmc_slot_off(a, s, 1), wz = z + dmc_slot_off(a, s, 2);
+                const int wi = dmc_index(g, wx, wy, wz);
+                const unsigned code = dmc_code(dmc_case(g, wi, iso), dmc_slot_edge(a, s));
+                const unsigned first = dmc_first_use(g, wx, wy, wz, code);
+                const unsigned c = first / 12u, bit = first - c * 12u;
+                q[s] = offsets[c].x + __popc(masks[c] & ((1u << bit) - 1u));
+                if (a == 1) {                       // the stored vertex's y: offset of the quad that created it
+                    const int cy = (int)((c / (unsigned)g.size) % (unsigned)g.size);
+                    qy[s] = dmc_point(g, wi, code, iso).y + dmc_offset(pos.y, cy, wy);
+                }
+            }
+            if (fits) {
+                const unsigned rot = fabsf(verts[q[0]].light - verts[q[3]].light) > fabsf(verts[q[1]].light - verts[q[2]].light) ? 2u : 0u;
+                const unsigned flip = d0 < dn ? 2u : 0u;
+                unsigned* o = idx + (size_t)quad * 6u;
+                o[0] = q[flip];
+                o[1] = q[3u - rot];
+                o[2] = q[2u - flip];
+                o[3] = q[3u - flip];
+                o[4] = q[rot];
+                o[5] = q[1u + flip];
+            }
+            if (a == 1) {
+#pragma unroll
+                for (int s = 0; s < 4; ++s) {
+                    if (in0) solid = max(solid, enc(qy[s]));
+                    else air = min(air, enc(qy[s]));
+                }
+            }
+            ++quad;
+        }
+    }
+    __shared__ unsigned s_air[8], s_solid[8];
+    for (int o = 16; o > 0; o >>= 1) {
+        air = min(air, __shfl_xor_sync(0xffffffffu, air, o));
+        solid = max(solid, __shfl_xor_sync(0xffffffffu, solid, o));
+    }
+    if ((threadIdx.x & 31) == 0) { s_air[threadIdx.x >> 5] = air; s_solid[threadIdx.x >> 5] = solid; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { air = min(air, s_air[w]); solid = max(solid, s_solid[w]); }
+        if (air != 0xFFFFFFFFu) atomicMin(&airsolid[0], air);
+        if (solid != 0u) atomicMax(&airsolid[1], solid);
+    }
+}
+
 // Grid-stride launches: one thread per element up to 8 waves of 256-thread blocks per SM.
 int grid_for(unsigned n, int block)
 {
@@ -310,16 +727,13 @@ cudaError_t launch_bloxel(const float* dens, int size, bool up_axis_z, float px,
     const int sg = size + 2;
     Vox v{dens, 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg};
     const unsigned n = (unsigned)size * size * size;
-    const unsigned nb = (n + kScanBlock - 1) / kScanBlock;
     cudaError_t e = cudaMemsetAsync(s.airsolid, 0, 2 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(s.airsolid, 0xFF, sizeof(unsigned), stream);           // min air starts at "none"
     if (e != cudaSuccess) return e;
     const float3 pos = make_float3(px, py, pz);
     bloxel_count<<<grid_for(n, 256), 256, 0, stream>>>(v, size, pos, iso, dminmax, s.counts, s.airsolid);
-    scan_blocks<<<nb, kScanBlock, 0, stream>>>(s.counts, s.offsets, s.block_totals, n);
-    scan_totals<<<1, kScanBlock, 0, stream>>>(s.block_totals, nb, s.total);
-    scan_add<<<nb, kScanBlock, 0, stream>>>(s.offsets, s.block_totals, n);
+    exclusive_scan<unsigned>(s.counts, s.offsets, s.block_totals, s.total, n, stream);
     bloxel_emit<<<grid_for(n, 256), 256, 0, stream>>>(v, size, pos, iso, dminmax, s.offsets, verts, idx, vcap, icap);
     return cudaGetLastError();
 }
@@ -329,6 +743,25 @@ cudaError_t launch_heightmap(const float* dens, int size, float px, float pz, fl
 {
     const unsigned n = (unsigned)size * size;
     heightmap_emit<<<grid_for(n, 256), 256, 0, stream>>>(dens, size, make_float2(px, pz), mul, verts, idx, vcap, icap);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dmc(const float* dens, int size, bool up_axis_z, int px, int py, int pz, float iso, const float* dminmax,
+                       DmcScratch& s, MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap, cudaStream_t stream)
+{
+    const int sg = size + 4;
+    const DmcGrid g{dens, 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg, size};
+    const unsigned n = (unsigned)size * size * size;
+    cudaError_t e = cudaMemsetAsync(s.airsolid, 0, 2 * sizeof(unsigned), stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(s.airsolid, 0xFF, sizeof(unsigned), stream);           // min air starts at "none"
+    if (e != cudaSuccess) return e;
+    const int3 pos = make_int3(px, py, pz);
+    dmc_count<<<grid_for(n, 256), 256, 0, stream>>>(g, iso, dminmax, s.counts, s.masks);
+    exclusive_scan<uint2>(s.counts, s.offsets, s.block_totals, s.total, n, stream);
+    dmc_vertices<<<grid_for(n, 256), 256, 0, stream>>>(g, pos, iso, dminmax, s.masks, s.offsets, s.total, verts, vcap);
+    dmc_quads<<<grid_for(n, 256), 256, 0, stream>>>(g, pos, iso, dminmax, s.masks, s.offsets, s.total, verts, vcap, idx, icap,
+                                                    s.airsolid);
     return cudaGetLastError();
 }
 

@@ -20,6 +20,17 @@ struct MeshScratch {
     size_t cap_voxels = 0;
 };
 
+// Per-thread device scratch of the dual marching cubes mesher.
+struct DmcScratch {
+    uint2* counts = nullptr;           // per cell: vertices it creates, quads it emits
+    uint2* offsets = nullptr;          // exclusive scan of counts
+    uint2* block_totals = nullptr;
+    uint2* total = nullptr;            // vertices, quads in the chunk
+    unsigned short* masks = nullptr;   // per cell: which of its 12 quad slots create a vertex
+    unsigned* airsolid = nullptr;      // order-preserving min air y / max solid y
+    size_t cap_cells = 0;
+};
+
 // Mesh the density array of a bloxel chunk (size^3 voxels, (size+2)^3 densities
 // with a one-voxel apron; `up_axis_z` = the densities were generated with y and z
 // swapped).  Writes at most vcap vertices / icap indices; the face total and the
@@ -31,5 +42,11 @@ cudaError_t launch_bloxel(const float* dens, int size, bool up_axis_z, float px,
 // Heightmap chunk: size^2 quads over (size+1)^2 densities.
 cudaError_t launch_heightmap(const float* dens, int size, float px, float pz, float mul, MeshVertex* verts, unsigned vcap,
                              unsigned* idx, unsigned icap, cudaStream_t stream);
+
+// Dual marching cubes chunk: size^3 cells over (size+4)^3 densities (a two-voxel
+// apron).  Vertices and indices are written only when both fit (vcap / icap);
+// the vertex and quad totals land in s.total either way.
+cudaError_t launch_dmc(const float* dens, int size, bool up_axis_z, int px, int py, int pz, float iso, const float* dminmax,
+                       DmcScratch& s, MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap, cudaStream_t stream);
 
 }  // namespace fn

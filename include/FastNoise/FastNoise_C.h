@@ -276,7 +276,7 @@ typedef struct fnChunkMesh {
     unsigned int* indices;          /* device, indexCapacity entries (triangle list) */
     int vertexCapacity, indexCapacity;
     int vertexCount, indexCount;    /* out: the whole mesh (also when it did not fit) */
-    float minAirY, maxSolidY;       /* out (bloxel): lowest air / highest solid voxel row, +-inf if none */
+    float minAirY, maxSolidY;       /* out (bloxel, dmc): lowest air / highest solid height, +-inf if none */
     float minMax[2];                /* out: OutputMinMax of the densities */
 } fnChunkMesh;
 /* BuildBloxel3DMesh (MeshNoisePreview.cpp:443-590): block faces between solid (density <=
@@ -284,6 +284,13 @@ typedef struct fnChunkMesh {
  * and directional light; size <= 256 (every index fits 32 bits).  upAxisZ swaps the y and z noise axes. */
 FASTNOISE_API int fnBuildChunkMeshBloxel(const void* node, int size, int posX, int posY, int posZ, int seed,
                                          float isoSurface, int upAxisZ, fnChunkMesh* mesh, void* stream);
+/* BuildDmc3DMesh / DmcGetVertIndex (MeshNoisePreview.cpp:592-953), the editor's default mesh:
+ * dual marching cubes over a size^3 chunk at (posX, posY, posZ) with a two-voxel apron, one
+ * vertex per surface piece of each cell (the mean of its edge crossings, lit by the density
+ * gradient), one quad per cut grid edge, vertices shared and numbered in the editor's first-use
+ * order; size <= 256.  Vertices and indices are written only when both fit. */
+FASTNOISE_API int fnBuildChunkMeshDmc(const void* node, int size, int posX, int posY, int posZ, int seed,
+                                      float isoSurface, int upAxisZ, fnChunkMesh* mesh, void* stream);
 /* BuildHeightMap2DMesh (MeshNoisePreview.cpp:956-1004): size^2 quads of a 2D heightmap at
  * (posX, posZ), heights = density * heightMultiplier; size <= 8192. */
 FASTNOISE_API int fnBuildChunkMeshHeightmap(const void* node, int size, int posX, int posZ, int seed,

@@ -92,3 +92,59 @@ def test_heightmap_matches_oracle(gpu, torch_cuda, size, pos, mul):
     assert np.array_equal(v.cpu().numpy().reshape(-1, 4).view(np.uint32), ov.view(np.uint32))
     assert np.array_equal(i.cpu().numpy().view(np.uint32), oi)
     assert res["minMax"] == (float(mm[0]), float(mm[1]))
+
+
+def white_tree():
+    """Independent random densities per voxel: every marching-cubes case, ambiguous faces included."""
+    return N("White", Seed_Offset=5)
+
+
+def run_dmc(fn, torch, root, size, pos, seed, iso, up_z, vcap=None, icap=None):
+    node = trees.to_product(root)
+    vcap = vcap if vcap is not None else (size + 1) ** 3 * 4
+    icap = icap if icap is not None else size ** 3 * 18
+    v = torch.zeros(max(vcap, 1) * 4, dtype=torch.float32, device="cuda")
+    i = torch.zeros(max(icap, 1), dtype=torch.int32, device="cuda")
+    res = fn.build_chunk_mesh_dmc(node, size, pos, seed, iso, up_z, v.data_ptr(), vcap, i.data_ptr(), icap)
+    return res, v.cpu().numpy().reshape(-1, 4), i.cpu().numpy().view(np.uint32)
+
+
+def oracle_dmc(root, size, pos, seed, iso, up_z):
+    d, mm = omesh.dmc_densities(root, size, pos, seed, up_z)
+    return (*omesh.dmc_mesh(d, mm, size, pos, iso), mm)
+
+
+@pytest.mark.parametrize("case", [
+    (surface_tree, 16, (32, -8, 16), 1337, 0.0, False),
+    (surface_tree, 20, (-48, 4, -20), 7, 0.1, False),
+    (surface_tree, 16, (16, -16, 0), 42, 0.0, True),
+    (caves_tree, 12, (-12, 24, 36), -5, -0.8, False),
+    (white_tree, 10, (100, -3, 7), 99, 0.0, False),
+    (white_tree, 9, (0, 0, 0), -1234, 0.3, True),
+])
+def test_dmc_matches_oracle(gpu, torch_cuda, case):
+    make, size, pos, seed, iso, up_z = case
+    res, gv, gi = run_dmc(gpu, torch_cuda, make(), size, pos, seed, iso, up_z)
+    ov, oi, oair, osolid, omm = oracle_dmc(make(), size, pos, seed, iso, up_z)
+    assert res["fits"] and res["vertexCount"] == len(ov) and res["indexCount"] == len(oi) > 0
+    assert np.array_equal(gv[:len(ov)].view(np.uint32), ov.view(np.uint32))
+    assert np.array_equal(gi[:len(oi)], oi)
+    assert (res["minAirY"], res["maxSolidY"]) == (float(oair), float(osolid))
+    assert res["minMax"] == (float(omm[0]), float(omm[1]))
+
+
+@pytest.mark.parametrize("value, expect", [(1.0, "air"), (-1.0, "solid")])
+def test_dmc_early_out(gpu, torch_cuda, value, expect):
+    res, _, _ = run_dmc(gpu, torch_cuda, N("Constant", Value=value), 16, (0, 32, 0), 1, 0.0, False)
+    assert res["vertexCount"] == 0 and res["indexCount"] == 0
+    if expect == "air":
+        assert res["minAirY"] == 32.0 and res["maxSolidY"] == float("-inf")
+    else:
+        assert res["maxSolidY"] == 32.0 - 1.0 + 16 and res["minAirY"] == float("inf")
+
+
+def test_dmc_reports_capacity(gpu, torch_cuda):
+    res, _, _ = run_dmc(gpu, torch_cuda, surface_tree(), 16, (32, -8, 16), 1337, 0.0, False, vcap=8, icap=12)
+    ov, oi, oair, osolid, _ = oracle_dmc(surface_tree(), 16, (32, -8, 16), 1337, 0.0, False)
+    assert not res["fits"] and res["vertexCount"] == len(ov) and res["indexCount"] == len(oi)
+    assert (res["minAirY"], res["maxSolidY"]) == (float(oair), float(osolid))
