@@ -990,17 +990,19 @@ bool mesh_reserve(size_t densities, size_t voxels)
     return true;
 }
 
-bool dmc_reserve(size_t cells)
+bool dmc_reserve(int size)
 {
     MeshCtx& m = t_mesh;
+    const size_t cells = (size_t)size * size * size, vcells = (size_t)(size + 1) * (size + 1) * (size + 1);
     if (cells <= m.dmc.cap_cells) return true;
     if (m.dmc.counts) cudaFree(m.dmc.counts);
     m.dmc = DmcScratch();
     const size_t nb = (cells + 1023) / 1024;
-    // counts | offsets | block totals | total (uint2 each) | air, solid | masks
-    const size_t pairs = 2 * cells + nb + 1;
+    // uint2: counts | offsets | block totals | total; uint32: air, solid | list counters |
+    // vertex items | quad items; then masks (uint16) and cases (uint8)
+    const size_t pairs = 2 * cells + nb + 1, words = 4 + 4 * vcells + 3 * cells;
     char* block = nullptr;
-    if (!cuda_ok(cudaMalloc(&block, pairs * sizeof(uint2) + 2 * sizeof(unsigned) + cells * sizeof(unsigned short)),
+    if (!cuda_ok(cudaMalloc(&block, pairs * sizeof(uint2) + words * sizeof(unsigned) + cells * sizeof(unsigned short) + vcells),
                  "cudaMalloc(dmc scratch)"))
         return false;
     uint2* p = reinterpret_cast<uint2*>(block);
@@ -1008,8 +1010,13 @@ bool dmc_reserve(size_t cells)
     m.dmc.offsets = p + cells;
     m.dmc.block_totals = p + 2 * cells;
     m.dmc.total = p + 2 * cells + nb;
-    m.dmc.airsolid = reinterpret_cast<unsigned*>(p + pairs);
-    m.dmc.masks = reinterpret_cast<unsigned short*>(m.dmc.airsolid + 2);
+    unsigned* w = reinterpret_cast<unsigned*>(p + pairs);
+    m.dmc.airsolid = w;
+    m.dmc.counters = w + 2;
+    m.dmc.vert_items = w + 4;
+    m.dmc.quad_items = w + 4 + 4 * vcells;
+    m.dmc.masks = reinterpret_cast<unsigned short*>(w + words);
+    m.dmc.cases = reinterpret_cast<unsigned char*>(m.dmc.masks + cells);
     m.dmc.cap_cells = cells;
     return true;
 }
@@ -1084,7 +1091,7 @@ int fnBuildChunkMeshDmc(const void* node, int size, int posX, int posY, int posZ
     if (!get_program(N(node), 3, prog)) return last_error();
     if (!ensure_runnable(prog)) return FN_ERR_COMPILE;
     const int sg = size + 4;
-    if (!mesh_reserve((size_t)sg * sg * sg, 0) || !dmc_reserve((size_t)size * size * size)) return FN_ERR_CUDA;
+    if (!mesh_reserve((size_t)sg * sg * sg, 0) || !dmc_reserve(size)) return FN_ERR_CUDA;
     MeshCtx& m = t_mesh;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     MinMaxWork* work = work_for_stream(s);

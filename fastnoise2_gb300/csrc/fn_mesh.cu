@@ -400,14 +400,13 @@ constexpr DmcTable make_dmc_table()
 
 __device__ const DmcTable kDmc = make_dmc_table();
 
-// Quads: the edge of axis a (x, y, z) from the cell's base corner is cut; its four
-// dual vertices sit in cells base + dmc_slot_off(a, s, .), on edge dmc_slot_edge(a, s).
+// Quads: the edge of axis a (x, y, z) from a cell's base corner is cut; its four
+// dual vertices sit in cells base + dmc_slot_off(a, s, .), on edge dmc_slot_edge(a, s)
+// (s = 0..3).  Per axis, slot bit 0 steps back along axis (a + 2) % 3 and slot
+// bit 1 along axis (a + 1) % 3.
 __host__ __device__ constexpr int dmc_slot_off(int a, int s, int k)
 {
-    constexpr int t[3][4][3] = {{{0, 0, 0}, {0, 0, -1}, {0, -1, 0}, {0, -1, -1}},
-                                {{0, 0, 0}, {-1, 0, 0}, {0, 0, -1}, {-1, 0, -1}},
-                                {{0, 0, 0}, {0, -1, 0}, {-1, 0, 0}, {-1, -1, 0}}};
-    return t[a][s][k];
+    return -((k == (a + 2) % 3 ? (s & 1) : 0) + (k == (a + 1) % 3 ? (s >> 1) & 1 : 0));
 }
 __host__ __device__ constexpr int dmc_slot_edge(int a, int s)
 {
@@ -418,25 +417,61 @@ __host__ __device__ constexpr int dmc_slot_edge(int a, int s)
 // at slot dmc_use_slot(e) = axis * 4 + slot.
 __host__ __device__ constexpr int dmc_use_off(int e, int k)
 {
-    constexpr int t[12][3] = {{0, 0, 0}, {1, 0, 0}, {0, 0, 1}, {0, 0, 0}, {0, 1, 0}, {1, 1, 0},
-                              {0, 1, 1}, {0, 1, 0}, {0, 0, 0}, {1, 0, 0}, {1, 0, 1}, {0, 0, 1}};
-    return t[e][k];
+    for (int a = 0; a < 3; ++a)
+        for (int s = 0; s < 4; ++s)
+            if (dmc_slot_edge(a, s) == e) return -dmc_slot_off(a, s, k);
+    return 0;
 }
 __host__ __device__ constexpr int dmc_use_slot(int e)
 {
-    constexpr int t[12] = {0, 10, 1, 8, 2, 11, 3, 9, 4, 5, 7, 6};
-    return t[e];
+    for (int a = 0; a < 3; ++a)
+        for (int s = 0; s < 4; ++s)
+            if (dmc_slot_edge(a, s) == e) return a * 4 + s;
+    return 0;
 }
+// The same tables packed into integers for run-time lookup: 4 bits per slot for the
+// slot edges, 4 bits per edge for the use slot, 3 bits (x, y, z) per edge for the use offset.
+constexpr unsigned long long pack_slot_edges()
+{
+    unsigned long long v = 0;
+    for (int b = 0; b < 12; ++b) v |= (unsigned long long)dmc_slot_edge(b / 4, b % 4) << (4 * b);
+    return v;
+}
+constexpr unsigned long long pack_use_slots()
+{
+    unsigned long long v = 0;
+    for (int e = 0; e < 12; ++e) v |= (unsigned long long)dmc_use_slot(e) << (4 * e);
+    return v;
+}
+constexpr unsigned long long pack_use_offs()
+{
+    unsigned long long v = 0;
+    for (int e = 0; e < 12; ++e)
+        v |= (unsigned long long)(dmc_use_off(e, 0) | dmc_use_off(e, 1) << 1 | dmc_use_off(e, 2) << 2) << (3 * e);
+    return v;
+}
+constexpr unsigned long long kDmcSlotEdges = pack_slot_edges();
+constexpr unsigned long long kDmcUseSlots = pack_use_slots();
+constexpr unsigned long long kDmcUseOffs = pack_use_offs();
+static_assert(dmc_use_slot(1) == 10 && dmc_use_off(10, 0) == 1 && dmc_use_off(10, 2) == 1 && dmc_use_off(6, 1) == 1,
+              "quad slot tables");
 
 struct DmcGrid {
     const float* d;
-    int sx, sy, sz;     // density strides of the mesher's x / y / z axes
-    int size;           // cells per axis
+    int sx, sy, sz;               // density strides of the mesher's x / y / z axes
+    int size;                     // cells per axis
+    unsigned char* cases;         // marching-cubes case of each vertex cell, (size + 1)^3, from -1
 };
 
 __device__ __forceinline__ int dmc_index(const DmcGrid& g, int x, int y, int z)
 {
     return (x + 2) * g.sx + (y + 2) * g.sy + (z + 2) * g.sz;
+}
+
+__device__ __forceinline__ unsigned dmc_case_at(const DmcGrid& g, int x, int y, int z)
+{
+    const unsigned s1 = (unsigned)g.size + 1u;
+    return g.cases[((unsigned)(z + 1) * s1 + (unsigned)(y + 1)) * s1 + (unsigned)(x + 1)];
 }
 
 // DmcGetVertIndex's cell code (:774-790)
@@ -462,21 +497,36 @@ __device__ __forceinline__ unsigned dmc_code(unsigned c, int e)
     return __ldg(&kDmc.code[c][p]);
 }
 
-// The first quad (in the reference's cell / axis / slot order) that uses the
-// dual vertex (cell w, piece `code`): cell index * 12 + axis * 4 + slot.  That
-// quad is the one whose DmcGetVertIndex call creates the vertex in the map.
+__device__ __forceinline__ int dmc_slot_offset(int a, int s, int k)
+{
+    return -((k == (a + 2) % 3 ? (s & 1) : 0) + (k == (a + 1) % 3 ? (s >> 1) & 1 : 0));
+}
+
+// The first quad (in the reference's cell / axis / slot order) that uses the dual
+// vertex (cell w, piece `code`), as cell index * 12 + axis * 4 + slot: that quad's
+// DmcGetVertIndex call is the one that creates the vertex in the reference's map.
 __device__ __forceinline__ unsigned dmc_first_use(const DmcGrid& g, int wx, int wy, int wz, unsigned code)
 {
     unsigned best = 0xFFFFFFFFu;
-#pragma unroll
-    for (int e = 0; e < 12; ++e) {
-        if (!((code >> e) & 1u)) continue;
-        const int cx = wx + dmc_use_off(e, 0), cy = wy + dmc_use_off(e, 1), cz = wz + dmc_use_off(e, 2);
-        if (cx >= g.size || cy >= g.size || cz >= g.size || cx < 0 || cy < 0 || cz < 0) continue;
-        const unsigned key = (((unsigned)cz * g.size + (unsigned)cy) * g.size + (unsigned)cx) * 12u + (unsigned)dmc_use_slot(e);
+    const unsigned n = (unsigned)g.size;
+    for (unsigned m = code; m; m &= m - 1u) {
+        const int e = __ffs(m) - 1;
+        const unsigned off = (unsigned)(kDmcUseOffs >> (3 * e)) & 7u;
+        const unsigned cx = (unsigned)(wx + (int)(off & 1u)), cy = (unsigned)(wy + (int)((off >> 1) & 1u)),
+                       cz = (unsigned)(wz + (int)(off >> 2));
+        if (cx >= n || cy >= n || cz >= n) continue;                // also catches -1
+        const unsigned key = ((cz * n + cy) * n + cx) * 12u + ((unsigned)(kDmcUseSlots >> (4 * e)) & 0xFu);
         best = key < best ? key : best;
     }
     return best;
+}
+
+// Index of the dual vertex whose first use is `first`: the creating cell's offset plus
+// the vertices that cell creates at earlier slots.
+__device__ __forceinline__ unsigned dmc_vertex_index(const uint2* offsets, const unsigned short* masks, unsigned first)
+{
+    const unsigned c = first / 12u, bit = first - c * 12u;
+    return offsets[c].x + __popc((unsigned)masks[c] & ((1u << bit) - 1u));
 }
 
 // mean of the piece's edge crossings, relative to the cell's base corner (:810-890)
@@ -569,126 +619,144 @@ __device__ __forceinline__ float dmc_light(const DmcGrid& g, int i, float3 v, fl
     return light < 1.0f ? light : 1.0f;                        // std::min(1.0f, light): NaN -> 1
 }
 
-// Count pass: per cell, the quads it emits and which of its 12 (axis, slot)
-// references create a vertex (bit axis * 4 + slot of `masks`).
-__global__ void dmc_count(DmcGrid g, float iso, const float* minmax, uint2* counts, unsigned short* masks)
+// Case pass: the marching-cubes case of every vertex cell, -1 .. size-1 per axis.
+__global__ void dmc_cases(DmcGrid g, float iso, const float* minmax)
 {
-    const unsigned n = (unsigned)g.size * g.size * g.size;
-    const bool skip = early_out(minmax, iso);
+    if (early_out(minmax, iso)) return;
+    const unsigned s1 = (unsigned)g.size + 1u, n = s1 * s1 * s1;
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
-        const int i = dmc_index(g, x, y, z);
-        unsigned nv = 0, nq = 0, mask = 0;
-        if (!skip) {
-            const bool in0 = g.d[i] <= iso;
-            const int step[3] = {g.sx, g.sy, g.sz};
-#pragma unroll
-            for (int a = 0; a < 3; ++a) {
-                if (in0 == (g.d[i + step[a]] <= iso)) continue;
-                ++nq;
-#pragma unroll
-                for (int s = 0; s < 4; ++s) {
-                    const int wx = x + dmc_slot_off(a, s, 0), wy = y + dmc_slot_off(a, s, 1), wz = z + dmc_slot_off(a, s, 2);
-                    const unsigned code = dmc_code(dmc_case(g, dmc_index(g, wx, wy, wz), iso), dmc_slot_edge(a, s));
-                    if (dmc_first_use(g, wx, wy, wz, code) == t * 12u + (unsigned)(a * 4 + s)) {
-                        mask |= 1u << (a * 4 + s);
-                        ++nv;
-                    }
-                }
-            }
-        }
-        counts[t] = make_uint2(nv, nq);
-        masks[t] = (unsigned short)mask;
+        const int x = (int)(t % s1) - 1, y = (int)((t / s1) % s1) - 1, z = (int)(t / (s1 * s1)) - 1;
+        g.cases[t] = (unsigned char)dmc_case(g, dmc_index(g, x, y, z), iso);
     }
 }
 
-// Vertex pass: each cell writes the vertices it creates at its scanned offset.
-__global__ void dmc_vertices(DmcGrid g, int3 pos, float iso, const float* minmax, const unsigned short* masks,
-                             const uint2* offsets, const uint2* total, MeshVertex* verts, unsigned vcap)
+// Work lists of the vertex and quad passes, appended warp by warp.
+struct DmcLists {
+    unsigned* vert_items;   // cell << 4 | slot bit, one per vertex
+    unsigned* quad_items;   // cell << 2 | axis, one per quad
+    unsigned* counters;     // [0] vertex items, [1] quad items
+};
+
+__device__ __forceinline__ unsigned warp_append(unsigned* counter, unsigned n, unsigned& total)
+{
+    const int lane = threadIdx.x & 31;
+    unsigned x = n;
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    total = __shfl_sync(0xffffffffu, x, 31);
+    unsigned base = 0;
+    if (lane == 31 && total) base = atomicAdd(counter, total);
+    return __shfl_sync(0xffffffffu, base, 31) + x - n;
+}
+
+// Count pass: per cell, the quads it emits and which of its 12 (axis, slot)
+// references create a vertex (bit axis * 4 + slot of `masks`); both listed as work items.
+__global__ void dmc_count(DmcGrid g, float iso, const float* minmax, uint2* counts, unsigned short* masks, DmcLists lists)
+{
+    const unsigned n = (unsigned)g.size * g.size * g.size;
+    const bool skip = early_out(minmax, iso);
+    const unsigned lane = threadIdx.x & 31u;
+    for (unsigned t0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); t0 < n; t0 += gridDim.x * blockDim.x) {
+        const unsigned t = t0 + lane;
+        unsigned mask = 0, axes = 0;
+        if (t < n && !skip) {
+            const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
+            const unsigned own = dmc_case_at(g, x, y, z);
+            // cut edges from the cell's base corner: x (corners 0-1), y (0-2), z (0-4)
+            axes = ((own ^ (own >> 1)) & 1u) | (((own ^ (own >> 2)) & 1u) << 1) | (((own ^ (own >> 4)) & 1u) << 2);
+            for (unsigned am = axes; am; am &= am - 1u) {
+                const int a = __ffs(am) - 1;
+                for (int s = 0; s < 4; ++s) {
+                    const int wx = x + dmc_slot_offset(a, s, 0), wy = y + dmc_slot_offset(a, s, 1), wz = z + dmc_slot_offset(a, s, 2);
+                    const int bit = a * 4 + s;
+                    const unsigned code = dmc_code(dmc_case_at(g, wx, wy, wz), (int)((kDmcSlotEdges >> (4 * bit)) & 0xFu));
+                    if (dmc_first_use(g, wx, wy, wz, code) == t * 12u + (unsigned)bit) mask |= 1u << bit;
+                }
+            }
+        }
+        if (t < n) {
+            counts[t] = make_uint2(__popc(mask), __popc(axes));
+            masks[t] = (unsigned short)mask;
+        }
+        unsigned total;
+        unsigned vbase = warp_append(&lists.counters[0], __popc(mask), total);
+        for (unsigned m = mask; m; m &= m - 1u) lists.vert_items[vbase++] = t << 4 | (unsigned)(__ffs(m) - 1);
+        unsigned qbase = warp_append(&lists.counters[1], __popc(axes), total);
+        for (unsigned m = axes; m; m &= m - 1u) lists.quad_items[qbase++] = t << 2 | (unsigned)(__ffs(m) - 1);
+    }
+}
+
+// Vertex pass: one thread per created vertex, written at its cell's scanned offset.
+__global__ void dmc_vertices(DmcGrid g, int3 pos, float iso, const unsigned short* masks, const uint2* offsets,
+                             const uint2* total, DmcLists lists, MeshVertex* verts, unsigned vcap)
 {
     __shared__ float3 s_nl;
     if (threadIdx.x == 0) s_nl = dmc_light_dir();
     __syncthreads();
-    if (early_out(minmax, iso) || total->x > vcap) return;
+    if (total->x > vcap) return;
     const float3 nl = s_nl;
-    const unsigned n = (unsigned)g.size * g.size * g.size;
-    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const unsigned mask = masks[t];
-        if (!mask) continue;
+    const unsigned items = lists.counters[0];
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < items; j += gridDim.x * blockDim.x) {
+        const unsigned it = lists.vert_items[j];
+        const unsigned t = it >> 4, bit = it & 15u;
+        const int a = (int)(bit >> 2), s = (int)(bit & 3u);
         const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
-        unsigned out = offsets[t].x;
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-#pragma unroll
-            for (int s = 0; s < 4; ++s) {
-                if (!((mask >> (a * 4 + s)) & 1u)) continue;
-                const int wx = x + dmc_slot_off(a, s, 0), wy = y + dmc_slot_off(a, s, 1), wz = z + dmc_slot_off(a, s, 2);
-                const int wi = dmc_index(g, wx, wy, wz);
-                const unsigned code = dmc_code(dmc_case(g, wi, iso), dmc_slot_edge(a, s));
-                const float3 p = dmc_point(g, wi, code, iso);
-                const float light = dmc_light(g, wi, p, nl);
-                verts[out++] = MeshVertex{p.x + dmc_offset(pos.x, x, wx), p.y + dmc_offset(pos.y, y, wy), p.z + dmc_offset(pos.z, z, wz),
-                                          light};
-            }
-        }
+        const int wx = x + dmc_slot_offset(a, s, 0), wy = y + dmc_slot_offset(a, s, 1), wz = z + dmc_slot_offset(a, s, 2);
+        const int wi = dmc_index(g, wx, wy, wz);
+        const unsigned code = dmc_code(dmc_case_at(g, wx, wy, wz), (int)((kDmcSlotEdges >> (4 * bit)) & 0xFu));
+        const float3 p = dmc_point(g, wi, code, iso);
+        const float light = dmc_light(g, wi, p, nl);
+        const unsigned out = offsets[t].x + __popc((unsigned)masks[t] & ((1u << bit) - 1u));
+        verts[out] = MeshVertex{p.x + dmc_offset(pos.x, x, wx), p.y + dmc_offset(pos.y, y, wy), p.z + dmc_offset(pos.z, z, wz), light};
     }
 }
 
-// Quad pass: 6 indices per cut edge (:662-674), vertex indices found through the
-// vertex's first use; the y-edge quads also give the min air / max solid heights.
-__global__ void dmc_quads(DmcGrid g, int3 pos, float iso, const float* minmax, const unsigned short* masks, const uint2* offsets,
-                          const uint2* total, const MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap, unsigned* airsolid)
+// Quad pass: one thread per cut edge, 6 indices (:662-674) with the vertex indices
+// found through each vertex's first use; the y-edge quads also give the min air /
+// max solid heights (:706-724).
+__global__ void dmc_quads(DmcGrid g, int3 pos, float iso, const unsigned short* masks, const uint2* offsets, const uint2* total,
+                          DmcLists lists, const MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap, unsigned* airsolid)
 {
-    const unsigned n = (unsigned)g.size * g.size * g.size;
-    const bool skip = early_out(minmax, iso);
     const uint2 tot = *total;
     const bool fits = tot.x <= vcap && (unsigned long long)tot.y * 6ull <= icap;
+    const unsigned items = lists.counters[1];
     unsigned air = 0xFFFFFFFFu, solid = 0u;
-    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n && !skip; t += gridDim.x * blockDim.x) {
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < items; j += gridDim.x * blockDim.x) {
+        const unsigned it = lists.quad_items[j];
+        const unsigned t = it >> 2;
+        const int a = (int)(it & 3u);
         const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
-        const int i = dmc_index(g, x, y, z);
-        const float d0 = g.d[i];
-        const bool in0 = d0 <= iso;
-        const int step[3] = {g.sx, g.sy, g.sz};
-        unsigned quad = offsets[t].y;
+        const unsigned own = dmc_case_at(g, x, y, z);
+        const bool inside = !(own & 1u);                      // density <= iso; cut, so also density < neighbour
+        const unsigned axes = ((own ^ (own >> 1)) & 1u) | (((own ^ (own >> 2)) & 1u) << 1) | (((own ^ (own >> 4)) & 1u) << 2);
+        const unsigned quad = offsets[t].y + __popc(axes & ((1u << a) - 1u));
+        unsigned q[4];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const float dn = g.d[i + step[a]];
-            if (in0 == (dn <= iso)) continue;
-            unsigned q[4];
-            float qy[4];
-#pragma unroll
-            for (int s = 0; s < 4; ++s) {
-                const int wx = x + dmc_slot_off(a, s, 0), wy = y + dmc_slot_off(a, s, 1), wz = z + dmc_slot_off(a, s, 2);
-                const int wi = dmc_index(g, wx, wy, wz);
-                const unsigned code = dmc_code(dmc_case(g, wi, iso), dmc_slot_edge(a, s));
-                const unsigned first = dmc_first_use(g, wx, wy, wz, code);
-                const unsigned c = first / 12u, bit = first - c * 12u;
-                q[s] = offsets[c].x + __popc(masks[c] & ((1u << bit) - 1u));
-                if (a == 1) {                       // the stored vertex's y: offset of the quad that created it
-                    const int cy = (int)((c / (unsigned)g.size) % (unsigned)g.size);
-                    qy[s] = dmc_point(g, wi, code, iso).y + dmc_offset(pos.y, cy, wy);
-                }
+        for (int s = 0; s < 4; ++s) {
+            const int wx = x + dmc_slot_offset(a, s, 0), wy = y + dmc_slot_offset(a, s, 1), wz = z + dmc_slot_offset(a, s, 2);
+            const int bit = a * 4 + s;
+            const unsigned code = dmc_code(dmc_case_at(g, wx, wy, wz), (int)((kDmcSlotEdges >> (4 * bit)) & 0xFu));
+            const unsigned first = dmc_first_use(g, wx, wy, wz, code);
+            q[s] = dmc_vertex_index(offsets, masks, first);
+            if (a == 1) {                       // the stored vertex's y: offset of the quad that created it
+                const int cy = (int)((first / 12u / (unsigned)g.size) % (unsigned)g.size);
+                const float vy = dmc_point(g, dmc_index(g, wx, wy, wz), code, iso).y + dmc_offset(pos.y, cy, wy);
+                if (inside) solid = max(solid, enc(vy));
+                else air = min(air, enc(vy));
             }
-            if (fits) {
-                const unsigned rot = fabsf(verts[q[0]].light - verts[q[3]].light) > fabsf(verts[q[1]].light - verts[q[2]].light) ? 2u : 0u;
-                const unsigned flip = d0 < dn ? 2u : 0u;
-                unsigned* o = idx + (size_t)quad * 6u;
-                o[0] = q[flip];
-                o[1] = q[3u - rot];
-                o[2] = q[2u - flip];
-                o[3] = q[3u - flip];
-                o[4] = q[rot];
-                o[5] = q[1u + flip];
-            }
-            if (a == 1) {
-#pragma unroll
-                for (int s = 0; s < 4; ++s) {
-                    if (in0) solid = max(solid, enc(qy[s]));
-                    else air = min(air, enc(qy[s]));
-                }
-            }
-            ++quad;
+        }
+        if (fits) {
+            const unsigned rot = fabsf(verts[q[0]].light - verts[q[3]].light) > fabsf(verts[q[1]].light - verts[q[2]].light) ? 2u : 0u;
+            const unsigned flip = inside ? 2u : 0u;
+            unsigned* o = idx + (size_t)quad * 6u;
+            o[0] = q[flip];
+            o[1] = q[3u - rot];
+            o[2] = q[2u - flip];
+            o[3] = q[3u - flip];
+            o[4] = q[rot];
+            o[5] = q[1u + flip];
         }
     }
     __shared__ unsigned s_air[8], s_solid[8];
@@ -750,18 +818,24 @@ cudaError_t launch_dmc(const float* dens, int size, bool up_axis_z, int px, int 
                        DmcScratch& s, MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap, cudaStream_t stream)
 {
     const int sg = size + 4;
-    const DmcGrid g{dens, 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg, size};
-    const unsigned n = (unsigned)size * size * size;
+    const DmcGrid g{dens, 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg, size, s.cases};
+    const DmcLists lists{s.vert_items, s.quad_items, s.counters};
+    const unsigned n = (unsigned)size * size * size, s1 = (unsigned)size + 1u;
+    // air = "none" (all ones), solid = 0, then the two list counters = 0
     cudaError_t e = cudaMemsetAsync(s.airsolid, 0, 2 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(s.airsolid, 0xFF, sizeof(unsigned), stream);           // min air starts at "none"
+    e = cudaMemsetAsync(s.airsolid, 0xFF, sizeof(unsigned), stream);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(s.counters, 0, 2 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     const int3 pos = make_int3(px, py, pz);
-    dmc_count<<<grid_for(n, 256), 256, 0, stream>>>(g, iso, dminmax, s.counts, s.masks);
+    dmc_cases<<<grid_for(s1 * s1 * s1, 256), 256, 0, stream>>>(g, iso, dminmax);
+    dmc_count<<<grid_for(n, 256), 256, 0, stream>>>(g, iso, dminmax, s.counts, s.masks, lists);
     exclusive_scan<uint2>(s.counts, s.offsets, s.block_totals, s.total, n, stream);
-    dmc_vertices<<<grid_for(n, 256), 256, 0, stream>>>(g, pos, iso, dminmax, s.masks, s.offsets, s.total, verts, vcap);
-    dmc_quads<<<grid_for(n, 256), 256, 0, stream>>>(g, pos, iso, dminmax, s.masks, s.offsets, s.total, verts, vcap, idx, icap,
-                                                    s.airsolid);
+    // one thread per vertex / quad: the lists hold at most a few per surface cell
+    dmc_vertices<<<grid_for(n / 4, 256), 256, 0, stream>>>(g, pos, iso, s.masks, s.offsets, s.total, lists, verts, vcap);
+    dmc_quads<<<grid_for(n / 4, 256), 256, 0, stream>>>(g, pos, iso, s.masks, s.offsets, s.total, lists, verts, vcap, idx, icap,
+                                                        s.airsolid);
     return cudaGetLastError();
 }
 

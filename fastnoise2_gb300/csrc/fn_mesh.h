@@ -28,6 +28,10 @@ struct DmcScratch {
     uint2* total = nullptr;            // vertices, quads in the chunk
     unsigned short* masks = nullptr;   // per cell: which of its 12 quad slots create a vertex
     unsigned* airsolid = nullptr;      // order-preserving min air y / max solid y
+    unsigned* counters = nullptr;      // work items listed: vertices, quads
+    unsigned* vert_items = nullptr;    // 4 (size+1)^3: every (vertex cell, piece) at most once
+    unsigned* quad_items = nullptr;    // 3 size^3: every cut edge at most once
+    unsigned char* cases = nullptr;    // (size+1)^3 marching-cubes cases
     size_t cap_cells = 0;
 };
 
