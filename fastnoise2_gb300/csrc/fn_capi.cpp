@@ -957,7 +957,7 @@ struct MeshCtx {
         if (dens) cudaFree(dens);
         if (dminmax) cudaFree(dminmax);
         if (scratch.counts) cudaFree(scratch.counts);
-        if (dmc.counts) cudaFree(dmc.counts);
+        if (dmc.offsets) cudaFree(dmc.offsets);
         if (host) cudaFreeHost(host);
     }
 };
@@ -995,28 +995,26 @@ bool dmc_reserve(int size)
     MeshCtx& m = t_mesh;
     const size_t cells = (size_t)size * size * size, vcells = (size_t)(size + 1) * (size + 1) * (size + 1);
     if (cells <= m.dmc.cap_cells) return true;
-    if (m.dmc.counts) cudaFree(m.dmc.counts);
+    if (m.dmc.offsets) cudaFree(m.dmc.offsets);
     m.dmc = DmcScratch();
-    const size_t nb = (cells + 1023) / 1024;
-    // uint2: counts | offsets | block totals | total; uint32: air, solid | list counters |
-    // vertex items | quad items; then masks (uint16) and cases (uint8)
-    const size_t pairs = 2 * cells + nb + 1, words = 4 + 4 * vcells + 3 * cells;
+    const size_t tiles = (cells + 2047) / 2048;
+    // uint2: offsets | tile sums | total; uint32: masks | air, solid | list counters |
+    // vertex items | quad items; then cases (uint8)
+    const size_t pairs = cells + tiles + 1, words = cells + 4 + 4 * vcells + 3 * cells;
     char* block = nullptr;
-    if (!cuda_ok(cudaMalloc(&block, pairs * sizeof(uint2) + words * sizeof(unsigned) + cells * sizeof(unsigned short) + vcells),
-                 "cudaMalloc(dmc scratch)"))
+    if (!cuda_ok(cudaMalloc(&block, pairs * sizeof(uint2) + words * sizeof(unsigned) + vcells), "cudaMalloc(dmc scratch)"))
         return false;
     uint2* p = reinterpret_cast<uint2*>(block);
-    m.dmc.counts = p;
-    m.dmc.offsets = p + cells;
-    m.dmc.block_totals = p + 2 * cells;
-    m.dmc.total = p + 2 * cells + nb;
+    m.dmc.offsets = p;
+    m.dmc.tile_sums = p + cells;
+    m.dmc.total = p + cells + tiles;
     unsigned* w = reinterpret_cast<unsigned*>(p + pairs);
-    m.dmc.airsolid = w;
-    m.dmc.counters = w + 2;
-    m.dmc.vert_items = w + 4;
-    m.dmc.quad_items = w + 4 + 4 * vcells;
-    m.dmc.masks = reinterpret_cast<unsigned short*>(w + words);
-    m.dmc.cases = reinterpret_cast<unsigned char*>(m.dmc.masks + cells);
+    m.dmc.masks = w;
+    m.dmc.airsolid = w + cells;
+    m.dmc.counters = w + cells + 2;
+    m.dmc.vert_items = w + cells + 4;
+    m.dmc.quad_items = w + cells + 4 + 4 * vcells;
+    m.dmc.cases = reinterpret_cast<unsigned char*>(w + words);
     m.dmc.cap_cells = cells;
     return true;
 }

@@ -330,10 +330,49 @@ __global__ void heightmap_emit(const float* d, int size, float2 pos, float mul, 
 // level is cut off on its own.  The table is derived here at compile time from
 // that rule; it equals the reference's kDualPointsList (DmcTable.inl) case for
 // case, piece order aside (the mesher only asks which piece holds an edge).
+//
+// Quads: the edge of axis a (x, y, z) from a cell's base corner is cut; its four
+// dual vertices sit in cells base + dmc_slot_off(a, s, .), on edge dmc_slot_edge(a, s)
+// (slot s = 0..3; slot bit 0 steps back along axis (a + 2) % 3, bit 1 along (a + 1) % 3).
+// The reference numbers a vertex when its first quad (cell-major, then axis, then
+// slot) asks for it; `dmc_first_use` finds that quad from the vertex's side.
+
+__host__ __device__ constexpr int dmc_slot_off(int a, int s, int k)
+{
+    return -((k == (a + 2) % 3 ? (s & 1) : 0) + (k == (a + 1) % 3 ? (s >> 1) & 1 : 0));
+}
+__host__ __device__ constexpr int dmc_slot_edge(int a, int s)
+{
+    constexpr int t[3][4] = {{0, 2, 4, 6}, {8, 9, 11, 10}, {3, 7, 1, 5}};
+    return t[a][s];
+}
+// Inverse: edge e of a vertex cell is used by the quad of cell + dmc_use_off(e, .),
+// at slot dmc_use_slot(e) = axis * 4 + slot.
+__host__ __device__ constexpr int dmc_use_off(int e, int k)
+{
+    for (int a = 0; a < 3; ++a)
+        for (int s = 0; s < 4; ++s)
+            if (dmc_slot_edge(a, s) == e) return -dmc_slot_off(a, s, k);
+    return 0;
+}
+__host__ __device__ constexpr int dmc_use_slot(int e)
+{
+    for (int a = 0; a < 3; ++a)
+        for (int s = 0; s < 4; ++s)
+            if (dmc_slot_edge(a, s) == e) return a * 4 + s;
+    return 0;
+}
+// Order of edge e's quad among the quads around one vertex cell when all of them lie
+// inside the chunk: cell-major (z, y, x of the using cell), then slot.
+__host__ __device__ constexpr int dmc_use_rank(int e)
+{
+    return ((dmc_use_off(e, 2) * 2 + dmc_use_off(e, 1)) * 2 + dmc_use_off(e, 0)) * 12 + dmc_use_slot(e);
+}
 
 struct DmcTable {
     unsigned long long edge_piece[256];   // 4 bits per edge: its piece, 0xF = edge not cut
     unsigned short code[256][4];          // cut-edge bit set of each piece
+    unsigned char first[256][4];          // each piece's edge whose quad comes first (all quads in the chunk)
 };
 
 constexpr int kDmcEdgeCorner[12][2] = {{0, 1}, {1, 5}, {4, 5}, {0, 4}, {2, 3}, {3, 7},
@@ -392,6 +431,7 @@ constexpr DmcTable make_dmc_table()
             ep &= ~(0xFull << (4 * e));
             ep |= (unsigned long long)p << (4 * e);
             t.code[c][p] = (unsigned short)(t.code[c][p] | (1u << e));
+            if (t.code[c][p] == (1u << e) || dmc_use_rank(e) < dmc_use_rank(t.first[c][p])) t.first[c][p] = (unsigned char)e;
         }
         t.edge_piece[c] = ep;
     }
@@ -400,36 +440,7 @@ constexpr DmcTable make_dmc_table()
 
 __device__ const DmcTable kDmc = make_dmc_table();
 
-// Quads: the edge of axis a (x, y, z) from a cell's base corner is cut; its four
-// dual vertices sit in cells base + dmc_slot_off(a, s, .), on edge dmc_slot_edge(a, s)
-// (s = 0..3).  Per axis, slot bit 0 steps back along axis (a + 2) % 3 and slot
-// bit 1 along axis (a + 1) % 3.
-__host__ __device__ constexpr int dmc_slot_off(int a, int s, int k)
-{
-    return -((k == (a + 2) % 3 ? (s & 1) : 0) + (k == (a + 1) % 3 ? (s >> 1) & 1 : 0));
-}
-__host__ __device__ constexpr int dmc_slot_edge(int a, int s)
-{
-    constexpr int t[3][4] = {{0, 2, 4, 6}, {8, 9, 11, 10}, {3, 7, 1, 5}};
-    return t[a][s];
-}
-// Inverse: edge e of a vertex cell is used by the quad of cell + dmc_use_off(e, .),
-// at slot dmc_use_slot(e) = axis * 4 + slot.
-__host__ __device__ constexpr int dmc_use_off(int e, int k)
-{
-    for (int a = 0; a < 3; ++a)
-        for (int s = 0; s < 4; ++s)
-            if (dmc_slot_edge(a, s) == e) return -dmc_slot_off(a, s, k);
-    return 0;
-}
-__host__ __device__ constexpr int dmc_use_slot(int e)
-{
-    for (int a = 0; a < 3; ++a)
-        for (int s = 0; s < 4; ++s)
-            if (dmc_slot_edge(a, s) == e) return a * 4 + s;
-    return 0;
-}
-// The same tables packed into integers for run-time lookup: 4 bits per slot for the
+// The slot tables packed into integers for run-time lookup: 4 bits per slot for the
 // slot edges, 4 bits per edge for the use slot, 3 bits (x, y, z) per edge for the use offset.
 constexpr unsigned long long pack_slot_edges()
 {
@@ -455,6 +466,7 @@ constexpr unsigned long long kDmcUseSlots = pack_use_slots();
 constexpr unsigned long long kDmcUseOffs = pack_use_offs();
 static_assert(dmc_use_slot(1) == 10 && dmc_use_off(10, 0) == 1 && dmc_use_off(10, 2) == 1 && dmc_use_off(6, 1) == 1,
               "quad slot tables");
+static_assert(make_dmc_table().first[1][0] == 0 && make_dmc_table().first[255 - 64][0] == 7, "first-use edges");
 
 struct DmcGrid {
     const float* d;
@@ -490,11 +502,10 @@ __device__ __forceinline__ unsigned dmc_case(const DmcGrid& g, int i, float iso)
     return c;
 }
 
-// the piece (point code) of case `c` that holds edge `e` (:792-800)
-__device__ __forceinline__ unsigned dmc_code(unsigned c, int e)
+// cut edges from a cell's base corner: bit 0 x (corners 0-1), bit 1 y (0-2), bit 2 z (0-4)
+__device__ __forceinline__ unsigned dmc_axes(unsigned c)
 {
-    const unsigned p = (unsigned)(__ldg(&kDmc.edge_piece[c]) >> (4 * e)) & 0xFu;
-    return __ldg(&kDmc.code[c][p]);
+    return ((c ^ (c >> 1)) & 1u) | (((c ^ (c >> 2)) & 1u) << 1) | (((c ^ (c >> 4)) & 1u) << 2);
 }
 
 __device__ __forceinline__ int dmc_slot_offset(int a, int s, int k)
@@ -502,31 +513,55 @@ __device__ __forceinline__ int dmc_slot_offset(int a, int s, int k)
     return -((k == (a + 2) % 3 ? (s & 1) : 0) + (k == (a + 1) % 3 ? (s >> 1) & 1 : 0));
 }
 
-// The first quad (in the reference's cell / axis / slot order) that uses the dual
-// vertex (cell w, piece `code`), as cell index * 12 + axis * 4 + slot: that quad's
-// DmcGetVertIndex call is the one that creates the vertex in the reference's map.
-__device__ __forceinline__ unsigned dmc_first_use(const DmcGrid& g, int wx, int wy, int wz, unsigned code)
+__device__ __forceinline__ unsigned dmc_key(const DmcGrid& g, unsigned cx, unsigned cy, unsigned cz, unsigned slot)
 {
-    unsigned best = 0xFFFFFFFFu;
     const unsigned n = (unsigned)g.size;
-    for (unsigned m = code; m; m &= m - 1u) {
+    return ((cz * n + cy) * n + cx) * 12u + slot;
+}
+
+// The first quad (in the reference's cell / axis / slot order) that uses the dual vertex
+// (cell w, piece p of case c), as cell index * 12 + axis * 4 + slot: that quad's
+// DmcGetVertIndex call is the one that creates the vertex in the reference's map.  Away
+// from the chunk's faces every quad around w lies in the chunk and the table knows the
+// first; next to them the quads that fall outside are skipped.
+__device__ __forceinline__ unsigned dmc_first_use(const DmcGrid& g, int wx, int wy, int wz, unsigned c, unsigned p)
+{
+    const unsigned n = (unsigned)g.size;
+    if ((unsigned)wx < n - 1u && (unsigned)wy < n - 1u && (unsigned)wz < n - 1u) {
+        const int e = __ldg(&kDmc.first[c][p]);
+        const unsigned off = (unsigned)(kDmcUseOffs >> (3 * e)) & 7u;
+        return dmc_key(g, (unsigned)wx + (off & 1u), (unsigned)wy + ((off >> 1) & 1u), (unsigned)wz + (off >> 2),
+                       (unsigned)(kDmcUseSlots >> (4 * e)) & 0xFu);
+    }
+    unsigned best = 0xFFFFFFFFu;
+    for (unsigned m = __ldg(&kDmc.code[c][p]); m; m &= m - 1u) {
         const int e = __ffs(m) - 1;
         const unsigned off = (unsigned)(kDmcUseOffs >> (3 * e)) & 7u;
         const unsigned cx = (unsigned)(wx + (int)(off & 1u)), cy = (unsigned)(wy + (int)((off >> 1) & 1u)),
                        cz = (unsigned)(wz + (int)(off >> 2));
         if (cx >= n || cy >= n || cz >= n) continue;                // also catches -1
-        const unsigned key = ((cz * n + cy) * n + cx) * 12u + ((unsigned)(kDmcUseSlots >> (4 * e)) & 0xFu);
+        const unsigned key = dmc_key(g, cx, cy, cz, (unsigned)(kDmcUseSlots >> (4 * e)) & 0xFu);
         best = key < best ? key : best;
     }
     return best;
 }
 
-// Index of the dual vertex whose first use is `first`: the creating cell's offset plus
-// the vertices that cell creates at earlier slots.
-__device__ __forceinline__ unsigned dmc_vertex_index(const uint2* offsets, const unsigned short* masks, unsigned first)
+// One quad reference: vertex cell w of slot (a, s) of cell (x, y, z), its case and piece.
+struct DmcRef {
+    int wx, wy, wz;
+    unsigned c, p;
+};
+
+__device__ __forceinline__ DmcRef dmc_ref(const DmcGrid& g, int x, int y, int z, int a, int s)
 {
-    const unsigned c = first / 12u, bit = first - c * 12u;
-    return offsets[c].x + __popc((unsigned)masks[c] & ((1u << bit) - 1u));
+    DmcRef r;
+    r.wx = x + dmc_slot_offset(a, s, 0);
+    r.wy = y + dmc_slot_offset(a, s, 1);
+    r.wz = z + dmc_slot_offset(a, s, 2);
+    r.c = dmc_case_at(g, r.wx, r.wy, r.wz);
+    const int e = (int)((kDmcSlotEdges >> (4 * (a * 4 + s))) & 0xFu);
+    r.p = (unsigned)(__ldg(&kDmc.edge_piece[r.c]) >> (4 * e)) & 0xFu;    // the piece holding e (:792-800)
+    return r;
 }
 
 // mean of the piece's edge crossings, relative to the cell's base corner (:810-890)
@@ -619,25 +654,27 @@ __device__ __forceinline__ float dmc_light(const DmcGrid& g, int i, float3 v, fl
     return light < 1.0f ? light : 1.0f;                        // std::min(1.0f, light): NaN -> 1
 }
 
-// Case pass: the marching-cubes case of every vertex cell, -1 .. size-1 per axis.
-__global__ void dmc_cases(DmcGrid g, float iso, const float* minmax)
-{
-    if (early_out(minmax, iso)) return;
-    const unsigned s1 = (unsigned)g.size + 1u, n = s1 * s1 * s1;
-    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
-        const int x = (int)(t % s1) - 1, y = (int)((t / s1) % s1) - 1, z = (int)(t / (s1 * s1)) - 1;
-        g.cases[t] = (unsigned char)dmc_case(g, dmc_index(g, x, y, z), iso);
-    }
-}
+// Cell counts are scanned in tiles of 2048 cells; the tile sums are accumulated with
+// atomics by the passes that produce the counts, so the scan reads each count once.
+constexpr int kDmcTile = 2048;
 
-// Work lists of the vertex and quad passes, appended warp by warp.
+// Work lists, appended warp by warp.
 struct DmcLists {
     unsigned* vert_items;   // cell << 4 | slot bit, one per vertex
     unsigned* quad_items;   // cell << 2 | axis, one per quad
     unsigned* counters;     // [0] vertex items, [1] quad items
+    uint2* tile_sums;       // per 2048 cells: vertices, quads; then scanned in place
 };
 
-__device__ __forceinline__ unsigned warp_append(unsigned* counter, unsigned n, unsigned& total)
+// Add v to sums[tile] with one atomic per distinct tile among the warp's lanes.
+__device__ __forceinline__ void warp_tile_add(unsigned* sums, unsigned tile, unsigned v)
+{
+    const unsigned group = __match_any_sync(0xffffffffu, tile);
+    const unsigned sum = __reduce_add_sync(group, v);
+    if ((threadIdx.x & 31u) == (unsigned)(__ffs(group) - 1) && sum) atomicAdd(&sums[2 * tile], sum);
+}
+
+__device__ __forceinline__ unsigned warp_append(unsigned* counter, unsigned n)
 {
     const int lane = threadIdx.x & 31;
     unsigned x = n;
@@ -645,52 +682,125 @@ __device__ __forceinline__ unsigned warp_append(unsigned* counter, unsigned n, u
         const unsigned y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= o) x += y;
     }
-    total = __shfl_sync(0xffffffffu, x, 31);
+    const unsigned total = __shfl_sync(0xffffffffu, x, 31);
     unsigned base = 0;
     if (lane == 31 && total) base = atomicAdd(counter, total);
     return __shfl_sync(0xffffffffu, base, 31) + x - n;
 }
 
-// Count pass: per cell, the quads it emits and which of its 12 (axis, slot)
-// references create a vertex (bit axis * 4 + slot of `masks`); both listed as work items.
-__global__ void dmc_count(DmcGrid g, float iso, const float* minmax, uint2* counts, unsigned short* masks, DmcLists lists)
+// Case pass: the marching-cubes case of every vertex cell (-1 .. size-1 per axis); for the
+// chunk's own cells also their quads (one per cut axis): tile sums and work items.
+__global__ void dmc_cases(DmcGrid g, float iso, const float* minmax, unsigned* masks, DmcLists lists)
 {
-    const unsigned n = (unsigned)g.size * g.size * g.size;
-    const bool skip = early_out(minmax, iso);
-    const unsigned lane = threadIdx.x & 31u;
+    if (early_out(minmax, iso)) return;
+    const unsigned s1 = (unsigned)g.size + 1u, n = s1 * s1 * s1, lane = threadIdx.x & 31u;
+    unsigned* quad_sums = &lists.tile_sums[0].y;
     for (unsigned t0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); t0 < n; t0 += gridDim.x * blockDim.x) {
         const unsigned t = t0 + lane;
-        unsigned mask = 0, axes = 0;
-        if (t < n && !skip) {
-            const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
-            const unsigned own = dmc_case_at(g, x, y, z);
-            // cut edges from the cell's base corner: x (corners 0-1), y (0-2), z (0-4)
-            axes = ((own ^ (own >> 1)) & 1u) | (((own ^ (own >> 2)) & 1u) << 1) | (((own ^ (own >> 4)) & 1u) << 2);
-            for (unsigned am = axes; am; am &= am - 1u) {
-                const int a = __ffs(am) - 1;
-                for (int s = 0; s < 4; ++s) {
-                    const int wx = x + dmc_slot_offset(a, s, 0), wy = y + dmc_slot_offset(a, s, 1), wz = z + dmc_slot_offset(a, s, 2);
-                    const int bit = a * 4 + s;
-                    const unsigned code = dmc_code(dmc_case_at(g, wx, wy, wz), (int)((kDmcSlotEdges >> (4 * bit)) & 0xFu));
-                    if (dmc_first_use(g, wx, wy, wz, code) == t * 12u + (unsigned)bit) mask |= 1u << bit;
-                }
+        unsigned axes = 0, cell = 0;
+        if (t < n) {
+            const int x = (int)(t % s1) - 1, y = (int)((t / s1) % s1) - 1, z = (int)(t / (s1 * s1)) - 1;
+            const unsigned c = dmc_case(g, dmc_index(g, x, y, z), iso);
+            g.cases[t] = (unsigned char)c;
+            if (x >= 0 && y >= 0 && z >= 0) {
+                cell = ((unsigned)z * g.size + (unsigned)y) * g.size + (unsigned)x;
+                axes = dmc_axes(c);
+                if (axes) masks[cell] = 0u;
             }
         }
-        if (t < n) {
-            counts[t] = make_uint2(__popc(mask), __popc(axes));
-            masks[t] = (unsigned short)mask;
-        }
-        unsigned total;
-        unsigned vbase = warp_append(&lists.counters[0], __popc(mask), total);
-        for (unsigned m = mask; m; m &= m - 1u) lists.vert_items[vbase++] = t << 4 | (unsigned)(__ffs(m) - 1);
-        unsigned qbase = warp_append(&lists.counters[1], __popc(axes), total);
-        for (unsigned m = axes; m; m &= m - 1u) lists.quad_items[qbase++] = t << 2 | (unsigned)(__ffs(m) - 1);
+        warp_tile_add(quad_sums, cell / kDmcTile, __popc(axes));
+        unsigned q = warp_append(&lists.counters[1], __popc(axes));
+        for (unsigned m = axes; m; m &= m - 1u) lists.quad_items[q++] = cell << 2 | (unsigned)(__ffs(m) - 1);
     }
 }
 
+// Count pass: one thread per quad; each of its 4 references that is the vertex's first
+// use creates the vertex (bit axis * 4 + slot of the cell's mask) and becomes a vertex item.
+__global__ void dmc_count(DmcGrid g, unsigned* masks, DmcLists lists)
+{
+    const unsigned items = lists.counters[1];
+    unsigned* vert_sums = &lists.tile_sums[0].x;
+    for (unsigned j0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); j0 < items; j0 += gridDim.x * blockDim.x) {
+        const unsigned j = j0 + (threadIdx.x & 31u);
+        unsigned bits = 0, t = 0;
+        if (j < items) {
+            const unsigned it = lists.quad_items[j];
+            t = it >> 2;
+            const int a = (int)(it & 3u);
+            const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
+#pragma unroll
+            for (int s = 0; s < 4; ++s) {
+                const DmcRef r = dmc_ref(g, x, y, z, a, s);
+                if (dmc_first_use(g, r.wx, r.wy, r.wz, r.c, r.p) == t * 12u + (unsigned)(a * 4 + s)) bits |= 1u << (a * 4 + s);
+            }
+            if (bits) atomicOr(&masks[t], bits);
+        }
+        warp_tile_add(vert_sums, t / kDmcTile, __popc(bits));
+        unsigned v = warp_append(&lists.counters[0], __popc(bits));
+        for (unsigned m = bits; m; m &= m - 1u) lists.vert_items[v++] = t << 4 | (unsigned)(__ffs(m) - 1);
+    }
+}
+
+// Tile offsets: exclusive scan of the tile sums (one block); the grand total lands in `total`.
+__global__ void __launch_bounds__(kScanBlock) dmc_scan_tiles(uint2* tile_sums, unsigned tiles, uint2* total)
+{
+    __shared__ uint2 ws[32];
+    uint2 carry = make_uint2(0u, 0u);
+    for (unsigned base = 0; base < tiles; base += kScanBlock) {
+        const unsigned i = base + threadIdx.x;
+        const uint2 v = i < tiles ? tile_sums[i] : make_uint2(0u, 0u);
+        uint2 sum;
+        const uint2 ex = block_exclusive_scan(v, ws, sum);
+        if (i < tiles) tile_sums[i] = plus(carry, ex);
+        carry = plus(carry, sum);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total = carry;
+}
+
+// Cell offsets within each tile that holds quads (256 threads x 8 cells, staged through
+// shared memory so that global loads and stores stay coalesced).  A cell's counts come from
+// its case (one quad per cut axis) and its mask (the vertices it creates).
+__global__ void __launch_bounds__(256) dmc_scan_cells(DmcGrid g, const unsigned* masks, uint2* offsets, const uint2* tile_offsets,
+                                                      const uint2* total)
+{
+    __shared__ uint2 tile[kDmcTile];
+    __shared__ uint2 ws[32];
+    const unsigned n = (unsigned)g.size * g.size * g.size;
+    const unsigned base = blockIdx.x * kDmcTile;
+    const unsigned next = blockIdx.x + 1u < gridDim.x ? tile_offsets[blockIdx.x + 1].y : total->y;
+    if (next == tile_offsets[blockIdx.x].y) return;             // no quads: nobody reads these offsets
+    for (int k = threadIdx.x; k < kDmcTile; k += 256) {
+        const unsigned t = base + k;
+        uint2 c = make_uint2(0u, 0u);
+        if (t < n) {
+            const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
+            const unsigned axes = dmc_axes(dmc_case_at(g, x, y, z));
+            if (axes) c = make_uint2(__popc(masks[t]), __popc(axes));
+        }
+        tile[k] = c;
+    }
+    __syncthreads();
+    uint2 local[8];
+    uint2 run = make_uint2(0u, 0u);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        local[k] = run;
+        run = plus(run, tile[threadIdx.x * 8 + k]);
+    }
+    uint2 sum;
+    const uint2 before = plus(tile_offsets[blockIdx.x], block_exclusive_scan(run, ws, sum));
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 8; ++k) tile[threadIdx.x * 8 + k] = plus(before, local[k]);
+    __syncthreads();
+    for (int k = threadIdx.x; k < kDmcTile; k += 256)
+        if (base + k < n) offsets[base + k] = tile[k];
+}
+
 // Vertex pass: one thread per created vertex, written at its cell's scanned offset.
-__global__ void dmc_vertices(DmcGrid g, int3 pos, float iso, const unsigned short* masks, const uint2* offsets,
-                             const uint2* total, DmcLists lists, MeshVertex* verts, unsigned vcap)
+__global__ void dmc_vertices(DmcGrid g, int3 pos, float iso, const unsigned* masks, const uint2* offsets, const uint2* total,
+                             DmcLists lists, MeshVertex* verts, unsigned vcap)
 {
     __shared__ float3 s_nl;
     if (threadIdx.x == 0) s_nl = dmc_light_dir();
@@ -703,20 +813,20 @@ __global__ void dmc_vertices(DmcGrid g, int3 pos, float iso, const unsigned shor
         const unsigned t = it >> 4, bit = it & 15u;
         const int a = (int)(bit >> 2), s = (int)(bit & 3u);
         const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
-        const int wx = x + dmc_slot_offset(a, s, 0), wy = y + dmc_slot_offset(a, s, 1), wz = z + dmc_slot_offset(a, s, 2);
-        const int wi = dmc_index(g, wx, wy, wz);
-        const unsigned code = dmc_code(dmc_case_at(g, wx, wy, wz), (int)((kDmcSlotEdges >> (4 * bit)) & 0xFu));
-        const float3 p = dmc_point(g, wi, code, iso);
+        const DmcRef r = dmc_ref(g, x, y, z, a, s);
+        const int wi = dmc_index(g, r.wx, r.wy, r.wz);
+        const float3 p = dmc_point(g, wi, __ldg(&kDmc.code[r.c][r.p]), iso);
         const float light = dmc_light(g, wi, p, nl);
-        const unsigned out = offsets[t].x + __popc((unsigned)masks[t] & ((1u << bit) - 1u));
-        verts[out] = MeshVertex{p.x + dmc_offset(pos.x, x, wx), p.y + dmc_offset(pos.y, y, wy), p.z + dmc_offset(pos.z, z, wz), light};
+        const unsigned out = offsets[t].x + __popc(masks[t] & ((1u << bit) - 1u));
+        verts[out] = MeshVertex{p.x + dmc_offset(pos.x, x, r.wx), p.y + dmc_offset(pos.y, y, r.wy),
+                                p.z + dmc_offset(pos.z, z, r.wz), light};
     }
 }
 
-// Quad pass: one thread per cut edge, 6 indices (:662-674) with the vertex indices
-// found through each vertex's first use; the y-edge quads also give the min air /
-// max solid heights (:706-724).
-__global__ void dmc_quads(DmcGrid g, int3 pos, float iso, const unsigned short* masks, const uint2* offsets, const uint2* total,
+// Quad pass: one thread per cut edge, 6 indices (:662-674) with the vertex indices found
+// through each vertex's first use; the y-edge quads also give the min air / max solid
+// heights (:706-724).
+__global__ void dmc_quads(DmcGrid g, int3 pos, float iso, const unsigned* masks, const uint2* offsets, const uint2* total,
                           DmcLists lists, const MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap, unsigned* airsolid)
 {
     const uint2 tot = *total;
@@ -730,19 +840,18 @@ __global__ void dmc_quads(DmcGrid g, int3 pos, float iso, const unsigned short* 
         const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
         const unsigned own = dmc_case_at(g, x, y, z);
         const bool inside = !(own & 1u);                      // density <= iso; cut, so also density < neighbour
-        const unsigned axes = ((own ^ (own >> 1)) & 1u) | (((own ^ (own >> 2)) & 1u) << 1) | (((own ^ (own >> 4)) & 1u) << 2);
-        const unsigned quad = offsets[t].y + __popc(axes & ((1u << a) - 1u));
+        const unsigned quad = offsets[t].y + __popc(dmc_axes(own) & ((1u << a) - 1u));
         unsigned q[4];
 #pragma unroll
         for (int s = 0; s < 4; ++s) {
-            const int wx = x + dmc_slot_offset(a, s, 0), wy = y + dmc_slot_offset(a, s, 1), wz = z + dmc_slot_offset(a, s, 2);
-            const int bit = a * 4 + s;
-            const unsigned code = dmc_code(dmc_case_at(g, wx, wy, wz), (int)((kDmcSlotEdges >> (4 * bit)) & 0xFu));
-            const unsigned first = dmc_first_use(g, wx, wy, wz, code);
-            q[s] = dmc_vertex_index(offsets, masks, first);
+            const DmcRef r = dmc_ref(g, x, y, z, a, s);
+            const unsigned first = dmc_first_use(g, r.wx, r.wy, r.wz, r.c, r.p);
+            const unsigned c = first / 12u, bit = first - c * 12u;
+            q[s] = offsets[c].x + __popc(masks[c] & ((1u << bit) - 1u));
             if (a == 1) {                       // the stored vertex's y: offset of the quad that created it
-                const int cy = (int)((first / 12u / (unsigned)g.size) % (unsigned)g.size);
-                const float vy = dmc_point(g, dmc_index(g, wx, wy, wz), code, iso).y + dmc_offset(pos.y, cy, wy);
+                const int cy = (int)((c / (unsigned)g.size) % (unsigned)g.size);
+                const float vy = dmc_point(g, dmc_index(g, r.wx, r.wy, r.wz), __ldg(&kDmc.code[r.c][r.p]), iso).y +
+                                 dmc_offset(pos.y, cy, r.wy);
                 if (inside) solid = max(solid, enc(vy));
                 else air = min(air, enc(vy));
             }
@@ -819,22 +928,26 @@ cudaError_t launch_dmc(const float* dens, int size, bool up_axis_z, int px, int 
 {
     const int sg = size + 4;
     const DmcGrid g{dens, 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg, size, s.cases};
-    const DmcLists lists{s.vert_items, s.quad_items, s.counters};
+    const DmcLists lists{s.vert_items, s.quad_items, s.counters, s.tile_sums};
     const unsigned n = (unsigned)size * size * size, s1 = (unsigned)size + 1u;
-    // air = "none" (all ones), solid = 0, then the two list counters = 0
+    const unsigned tiles = (n + kDmcTile - 1) / kDmcTile;
+    // air = "none" (all ones), solid = 0; list counters and tile sums = 0 (one contiguous block)
     cudaError_t e = cudaMemsetAsync(s.airsolid, 0, 2 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(s.airsolid, 0xFF, sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(s.counters, 0, 2 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(s.tile_sums, 0, tiles * sizeof(uint2), stream);
+    if (e != cudaSuccess) return e;
     const int3 pos = make_int3(px, py, pz);
-    dmc_cases<<<grid_for(s1 * s1 * s1, 256), 256, 0, stream>>>(g, iso, dminmax);
-    dmc_count<<<grid_for(n, 256), 256, 0, stream>>>(g, iso, dminmax, s.counts, s.masks, lists);
-    exclusive_scan<uint2>(s.counts, s.offsets, s.block_totals, s.total, n, stream);
-    // one thread per vertex / quad: the lists hold at most a few per surface cell
-    dmc_vertices<<<grid_for(n / 4, 256), 256, 0, stream>>>(g, pos, iso, s.masks, s.offsets, s.total, lists, verts, vcap);
-    dmc_quads<<<grid_for(n / 4, 256), 256, 0, stream>>>(g, pos, iso, s.masks, s.offsets, s.total, lists, verts, vcap, idx, icap,
+    dmc_cases<<<grid_for(s1 * s1 * s1, 256), 256, 0, stream>>>(g, iso, dminmax, s.masks, lists);
+    // one thread per quad / vertex: the lists hold a few items per surface cell
+    dmc_count<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, s.masks, lists);
+    dmc_scan_tiles<<<1, kScanBlock, 0, stream>>>(s.tile_sums, tiles, s.total);
+    dmc_scan_cells<<<tiles, 256, 0, stream>>>(g, s.masks, s.offsets, s.tile_sums, s.total);
+    dmc_vertices<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, pos, iso, s.masks, s.offsets, s.total, lists, verts, vcap);
+    dmc_quads<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, pos, iso, s.masks, s.offsets, s.total, lists, verts, vcap, idx, icap,
                                                         s.airsolid);
     return cudaGetLastError();
 }

@@ -22,11 +22,10 @@ struct MeshScratch {
 
 // Per-thread device scratch of the dual marching cubes mesher.
 struct DmcScratch {
-    uint2* counts = nullptr;           // per cell: vertices it creates, quads it emits
-    uint2* offsets = nullptr;          // exclusive scan of counts
-    uint2* block_totals = nullptr;
+    uint2* offsets = nullptr;          // per cell: first vertex it creates, first quad it emits (tiles that hold quads)
+    uint2* tile_sums = nullptr;        // per 2048 cells: vertices, quads; then scanned into tile offsets
     uint2* total = nullptr;            // vertices, quads in the chunk
-    unsigned short* masks = nullptr;   // per cell: which of its 12 quad slots create a vertex
+    unsigned* masks = nullptr;         // per cell: which of its 12 quad slots create a vertex
     unsigned* airsolid = nullptr;      // order-preserving min air y / max solid y
     unsigned* counters = nullptr;      // work items listed: vertices, quads
     unsigned* vert_items = nullptr;    // 4 (size+1)^3: every (vertex cell, piece) at most once
