@@ -126,6 +126,18 @@ def _declare(L):
         "fnServerRelease": (c_int, [vp, ctypes.c_ulonglong]),
         "fnServerGetStats": (c_int, [vp, vp]),
         "fnServerResetStats": (c_int, [vp]),
+        "fnEditorIpcSetup": (vp, [ctypes.c_bool]),
+        "fnEditorIpcRelease": (None, [vp]),
+        "fnEditorIpcSendSelectedNode": (ctypes.c_bool, [vp, cp]),
+        "fnEditorIpcSendImportRequest": (ctypes.c_bool, [vp, cp]),
+        "fnEditorIpcPollMessage": (c_int, [vp, vp, c_int]),
+        "fnEditorIpcSetNodeEditorPath": (None, [cp]),
+        "fnEditorIpcStartNodeEditor": (ctypes.c_bool, [cp, ctypes.c_bool, ctypes.c_bool]),
+        "fnLiveTreeCreate": (vp, [vp, cp, vp, c_int, c_int]),
+        "fnLiveTreeUpdate": (c_int, [vp]),
+        "fnLiveTreeAcquire": (vp, [vp, vp]),
+        "fnLiveTreeGetInfo": (c_int, [vp, vp]),
+        "fnLiveTreeDelete": (None, [vp]),
         "fnAutotuneLoad": (c_int, [cp]),
         "fnAutotuneSave": (c_int, [cp]),
     }
@@ -274,6 +286,93 @@ def build_chunk_mesh_heightmap(node: "Node", size: int, pos, seed: int, multipli
     rc = lib().fnBuildChunkMeshHeightmap(node.handle, int(size), int(pos[0]), int(pos[1]), int(np.int32(seed)),
                                          float(multiplier), ctypes.byref(m), stream or None)
     return _mesh(rc, m)
+
+
+class EditorChannel:
+    """The Node Editor's shared-memory channel (NodeEditorIpc_C.h): send and poll encoded trees."""
+
+    SELECTED_NODE, IMPORT_REQUEST = 1, 2
+
+    def __init__(self, read_previous: bool = False):
+        self._h = lib().fnEditorIpcSetup(bool(read_previous))
+        if not self._h:
+            raise OSError("fnEditorIpcSetup failed (no POSIX shared memory?)")
+
+    @property
+    def handle(self) -> int:
+        return self._h
+
+    def send_selected(self, encoded: str) -> bool:
+        return bool(lib().fnEditorIpcSendSelectedNode(self._h, encoded.encode()))
+
+    def send_import(self, encoded: str) -> bool:
+        return bool(lib().fnEditorIpcSendImportRequest(self._h, encoded.encode()))
+
+    def poll(self, size: int = 65536):
+        """(message type, tree) of the newest unseen message; type 0 = none, negative = error."""
+        buf = ctypes.create_string_buffer(max(size, 1))
+        t = lib().fnEditorIpcPollMessage(self._h, buf if size > 0 else None, size)
+        return t, (buf.value.decode() if t > 0 else None)
+
+    def close(self):
+        if self._h:
+            lib().fnEditorIpcRelease(self._h)
+            self._h = None
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.fnEditorIpcRelease(self._h)
+            self._h = None
+
+
+def set_node_editor_path(path: Optional[str]) -> None:
+    lib().fnEditorIpcSetNodeEditorPath(path.encode() if path else None)
+
+
+def start_node_editor(encoded: Optional[str] = None, detached: bool = False, child: bool = True) -> bool:
+    return bool(lib().fnEditorIpcStartNodeEditor(encoded.encode() if encoded else None, detached, child))
+
+
+class LiveTreeInfo(ctypes.Structure):
+    _fields_ = [("version", ctypes.c_ulonglong), ("rejected", ctypes.c_ulonglong), ("lastStatus", ctypes.c_int),
+                ("lastError", ctypes.c_char * 256)]
+
+
+class LiveTree:
+    """fnLiveTree*: a tree that follows a Node Editor channel (hot swap of the selected tree)."""
+
+    def __init__(self, channel: Optional[EditorChannel], initial: Optional[str], dims=(3,), poll_ms: int = 0):
+        self._channel = channel                       # keeps the channel open while the tree lives
+        arr = (ctypes.c_int * len(dims))(*dims)
+        self._h = lib().fnLiveTreeCreate(channel.handle if channel else None, initial.encode() if initial else None,
+                                          arr, len(dims), int(poll_ms))
+        if not self._h:
+            _check()
+            raise FastNoiseError(-1, "fnLiveTreeCreate failed")
+
+    def update(self) -> int:
+        return lib().fnLiveTreeUpdate(self._h)
+
+    def acquire(self):
+        """(Node or None, version) of the current tree."""
+        v = ctypes.c_ulonglong(0)
+        h = lib().fnLiveTreeAcquire(self._h, ctypes.byref(v))
+        return (Node(h) if h else None), v.value
+
+    def info(self) -> dict:
+        i = LiveTreeInfo()
+        lib().fnLiveTreeGetInfo(self._h, ctypes.byref(i))
+        return {"version": i.version, "rejected": i.rejected, "lastStatus": i.lastStatus, "lastError": i.lastError.decode()}
+
+    def close(self):
+        if self._h:
+            lib().fnLiveTreeDelete(self._h)
+            self._h = None
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.fnLiveTreeDelete(self._h)
+            self._h = None
 
 
 class BatchInfo(ctypes.Structure):

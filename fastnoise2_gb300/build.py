@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["fn_kernels.cu", "fn_static_scratch.cu", "fn_mesh.cu"]
 CPP_SOURCES = ["fn_node.cpp", "fn_compile.cpp", "fn_runtime.cpp", "fn_batch.cpp", "fn_server.cpp", "fn_capi.cpp",
-               "fn_jit.cpp"]
+               "fn_jit.cpp", "fn_ipc.cpp", "fn_live.cpp"]
 
 # Headers handed to NVRTC at run time (in this order), embedded into the library.
 JIT_HEADERS = ["fn_types.h", "fn_device.cuh", "fn_eval.cuh"]
@@ -113,7 +113,7 @@ def build(verbose: bool = False) -> str:
         objs = list(ex.map(_compile, sources))
     if os.path.exists(LIB) and all(os.path.getmtime(o) <= os.path.getmtime(LIB) for o in objs):
         return LIB
-    cmd = ["g++", "-shared", "-o", LIB + ".tmp", *objs, f"-L{CUDA_HOME}/lib64", "-lcudart", "-lnvrtc", "-lpthread",
+    cmd = ["g++", "-shared", "-o", LIB + ".tmp", *objs, f"-L{CUDA_HOME}/lib64", "-lcudart", "-lnvrtc", "-lpthread", "-lrt", "-ldl",
            f"-Wl,-rpath,{CUDA_HOME}/lib64"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -296,14 +296,38 @@ FASTNOISE_API int fnBuildChunkMeshDmc(const void* node, int size, int posX, int 
 FASTNOISE_API int fnBuildChunkMeshHeightmap(const void* node, int size, int posX, int posZ, int seed,
                                             float heightMultiplier, fnChunkMesh* mesh, void* stream);
 
+/* Live trees (no counterpart in the reference, whose consumers poll the Node Editor's channel,
+ * tools/NodeEditorIpc, and rebuild their generator themselves).  A live tree follows a channel
+ * from fnEditorIpcSetup (NodeEditorIpc_C.h): fnLiveTreeUpdate polls it and, for each tree the
+ * editor sends as its selected node, decodes it, compiles it for the listed dimensionalities
+ * (and specialises it with NVRTC when specialisation is enabled), and only then makes it
+ * current, so callers never wait on or see a half-built tree.  A tree that fails to decode or
+ * compile is rejected and the current one stays.  With pollMs > 0 a background thread updates
+ * every pollMs milliseconds (the live tree then owns polling of that channel).  ipc may be NULL
+ * (the initial tree only).  fnLiveTreeUpdate returns 1 when a new tree became current, 0 when
+ * nothing new arrived, FN_ERR_* when the newest tree was rejected.  fnLiveTreeAcquire returns
+ * the current tree with a reference the caller drops with fnDeleteNodeRef (NULL before the
+ * first tree); requests already submitted keep the tree they were submitted with. */
+typedef struct fnLiveTreeInfo {
+    unsigned long long version;     /* trees made current so far */
+    unsigned long long rejected;    /* trees that failed to decode or compile */
+    int lastStatus;                 /* FN_OK, or the FN_ERR_* of the last rejected tree */
+    char lastError[256];
+} fnLiveTreeInfo;
+FASTNOISE_API void* fnLiveTreeCreate(void* ipc, const char* initialEncodedTree, const int* dimensions, int count, int pollMs);
+FASTNOISE_API int fnLiveTreeUpdate(void* live);
+FASTNOISE_API void* fnLiveTreeAcquire(void* live, unsigned long long* version);
+FASTNOISE_API int fnLiveTreeGetInfo(void* live, fnLiveTreeInfo* info);
+FASTNOISE_API void fnLiveTreeDelete(void* live);
+
 /* Run-time specialisation (no counterpart in the reference, whose trees run through
  * virtual calls per SIMD block).  Each (node, dimension) pair is compiled to straight-line
- * CUDA and built for sm_103a with NVRTC into one module: per-tree kernels for the grid,
- * position-array and tileable calls, and one batch kernel covering all the listed trees.
- * Later generation calls on these trees (host, device, batch and server paths) use the
- * specialised kernels; results are bit-identical to the interpreter's.  Building takes
- * seconds, so do it once at start-up.  A later call replaces the active batch module;
- * per-tree kernels of earlier calls stay loaded.  Returns FN_OK or FN_ERR_*. */
+ * CUDA and built for sm_103a with NVRTC: per-tree kernels for the grid, position-array and
+ * tileable calls, and a persistent batch kernel per tree.  Later generation calls on these
+ * trees (host, device, batch and server paths) use the specialised kernels; results are
+ * bit-identical to the interpreter's.  Building takes seconds, so do it once at start-up.
+ * Kernels of earlier calls stay loaded (a tree specialised again gets its new kernels).
+ * Returns FN_OK or FN_ERR_*. */
 FASTNOISE_API int fnJitCompile(const void* const* nodes, const int* dimensions, int count);
 /* Generate and compile the module source with NVRTC without loading it (no GPU needed);
  * *cubinBytes (may be NULL) receives the size of the compiled code. */
