@@ -126,6 +126,7 @@ def _declare(L):
         "fnServerRelease": (c_int, [vp, ctypes.c_ulonglong]),
         "fnServerGetStats": (c_int, [vp, vp]),
         "fnServerResetStats": (c_int, [vp]),
+        "fnGenPreviewTextureDevice": (c_int, [vp, c_int, c_int, c_int, vp, c_float, c_int, vp, vp, vp]),
         "fnEditorIpcSetup": (vp, [ctypes.c_bool]),
         "fnEditorIpcRelease": (None, [vp]),
         "fnEditorIpcSendSelectedNode": (ctypes.c_bool, [vp, cp]),
@@ -286,6 +287,17 @@ def build_chunk_mesh_heightmap(node: "Node", size: int, pos, seed: int, multipli
     rc = lib().fnBuildChunkMeshHeightmap(node.handle, int(size), int(pos[0]), int(pos[1]), int(np.int32(seed)),
                                          float(multiplier), ctypes.byref(m), stream or None)
     return _mesh(rc, m)
+
+
+def gen_preview_texture(node: "Node", gen_type: int, size, offset, scale: float, seed: int, pixels_ptr: int,
+                        minmax_ptr: int = 0, stream: int = 0) -> None:
+    """fnGenPreviewTextureDevice: the Node Editor's RGBA8 preview image into device uint32 pixels."""
+    off = (ctypes.c_float * 4)(*[float(v) for v in (list(offset) + [0.0] * 4)[:4]])
+    rc = lib().fnGenPreviewTextureDevice(node.handle, int(gen_type), int(size[0]), int(size[1]), off, float(scale),
+                                         int(np.int32(seed)), pixels_ptr or None, minmax_ptr or None, stream or None)
+    if rc != 0:
+        _check()
+        raise FastNoiseError(rc, "fnGenPreviewTextureDevice failed")
 
 
 class EditorChannel:

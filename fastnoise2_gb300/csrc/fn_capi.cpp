@@ -862,6 +862,46 @@ int fnGenTileable2DDevice(const void* node, float* dOut, int xSize, int ySize, f
     return gen_device(node, tile_args(xSize, ySize, xStepSize, yStepSize, seed), dOut, dMinMax, stream);
 }
 
+int fnGenPreviewTextureDevice(const void* node, int genType, int sizeX, int sizeY, const float* offset, float scale, int seed,
+                              unsigned int* dPixels, float* dMinMax, void* stream)
+{
+    clear_error();
+    if (!node || !offset || genType < 0 || genType > 3 || sizeX < 0 || sizeY < 0) {
+        set_error(FN_ERR_ARG, "invalid arguments");
+        return FN_ERR_ARG;
+    }
+    // the editor wraps its tree in a default ConvertRGBA8 (range -1..1) (NoiseTexture.cpp:503-504)
+    const NodeMeta* meta = meta_by_name("ConvertRGBA8");
+    Node* wrap = meta ? node_new(meta->id) : nullptr;
+    if (!wrap || !wrap->set_lookup(0, const_cast<Node*>(N(node)))) {
+        if (wrap) node_unref(wrap);
+        set_error(FN_ERR_ARG, "cannot wrap the tree in ConvertRGBA8");
+        return FN_ERR_ARG;
+    }
+    // image centred on (offset.x, offset.y) (:508-509)
+    const float x0 = offset[0] - ((float)sizeX / 2.0f) * scale;
+    const float y0 = offset[1] - ((float)sizeY / 2.0f) * scale;
+    float* out = reinterpret_cast<float*>(dPixels);      // packed RGBA8 bits, stored as the node returns them
+    int rc;
+    switch (genType) {
+    case 0:
+        rc = fnGenUniformGrid2DDevice(wrap, out, x0, y0, sizeX, sizeY, scale, scale, seed, dMinMax, stream);
+        break;
+    case 1:
+        rc = fnGenTileable2DDevice(wrap, out, sizeX, sizeY, scale, scale, seed, dMinMax, stream);
+        break;
+    case 2:
+        rc = fnGenUniformGrid3DDevice(wrap, out, x0, y0, offset[2], sizeX, sizeY, 1, scale, scale, scale, seed, dMinMax, stream);
+        break;
+    default:
+        rc = fnGenUniformGrid4DDevice(wrap, out, x0, y0, offset[2], offset[3], sizeX, sizeY, 1, 1, scale, scale, scale, scale,
+                                      seed, dMinMax, stream);
+        break;
+    }
+    node_unref(wrap);
+    return rc;
+}
+
 // ---------------------------------------------------------------- run-time specialisation
 namespace {
 int jit_programs(const void* const* nodes, const int* dims, int count, std::vector<CompiledProgram>& store,

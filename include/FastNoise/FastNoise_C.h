@@ -263,6 +263,17 @@ typedef struct fnBatchInfo {
 } fnBatchInfo;
 FASTNOISE_API int fnGetBatchInfo(fnBatchInfo* info);
 
+/* NoiseTexture::BuildTexture (no counterpart in the reference's library: its Node Editor builds
+ * preview images in tools/NodeEditor/NoiseTexture.cpp:499-540).  The tree is wrapped in a
+ * default ConvertRGBA8 (range -1..1 to grey 0..255, alpha 255) and generated over sizeX x sizeY
+ * pixels centred on (offset[0], offset[1]), `scale` apart: genType 0 = 2D grid, 1 = 2D
+ * tileable, 2 = 3D slice at z = offset[2], 3 = 4D slice at (offset[2], offset[3]).  dPixels:
+ * device uint32[sizeX * sizeY], row-major, written by the generation kernel itself (4 bytes per
+ * pixel, no float image in between); dMinMax (device float[2] or NULL) receives the
+ * OutputMinMax of the packed values, as the editor's call returns it.  Asynchronous. */
+FASTNOISE_API int fnGenPreviewTextureDevice(const void* node, int genType, int sizeX, int sizeY, const float* offset,
+                                            float scale, int seed, unsigned int* dPixels, float* dMinMax, void* stream);
+
 /* Chunk meshing after the noise (no counterpart in the reference's library: its Node Editor
  * meshes preview chunks on the CPU in tools/NodeEditor/MeshNoisePreview.cpp, with a chunk size
  * of 128).  The chunk's densities are generated on the GPU exactly as the editor's
