@@ -115,6 +115,7 @@ def _declare(L):
         "fnGenBatchDevice": (c_int, [vp, c_int, vp, c_int]),
         "fnAutotuneBatch": (c_int, [vp, c_int, vp]),
         "fnGenEachDevice": (c_int, [vp, c_int, vp, c_int]),
+        "fnGenBatchHost": (c_int, [vp, c_int, c_int]),
         "fnServerCreate": (vp, [vp]),
         "fnServerDestroy": (None, [vp]),
         "fnServerSubmit": (c_int, [vp, vp, vp]),
@@ -205,6 +206,18 @@ def gen_batch(requests, stream: int = 0, sync: bool = True, graph: bool = True) 
     arr = (GenRequest * len(requests))(*requests)
     flags = (BATCH_SYNC if sync else 0) | (0 if graph else BATCH_NO_GRAPH)
     if lib().fnGenBatchDevice(arr, len(requests), stream or None, flags) != 0:
+        _check()
+
+
+def request_array(requests):
+    """A ctypes array of GenRequest (build it once for request lists that are launched repeatedly)."""
+    return requests if isinstance(requests, ctypes.Array) else (GenRequest * len(requests))(*requests)
+
+
+def gen_batch_host(requests, graph: bool = True) -> None:
+    """fnGenBatchHost: requests whose `out` is host memory; returns when every output is on the host."""
+    arr = request_array(requests)
+    if lib().fnGenBatchHost(arr, len(arr), 0 if graph else BATCH_NO_GRAPH) != 0:
         _check()
 
 

@@ -297,6 +297,77 @@ int run_batch(const fnGenRequest* reqs, int n, void* stream, int flags, const Ba
     return FN_OK;
 }
 
+// Host-output batches: two device staging buffers, the requests cut into slices that fit one;
+// slice k is generated on `gen` into buffer k % 2 while slice k - 1 is copied to the host on
+// `copy`, so the copy engine and the SMs work at the same time.  Slices start small (the first
+// copy starts early) and shrink again at the end (little is left to copy after the last
+// generation).  Slices are launched without graphs: each has its own shape.
+constexpr size_t kHostSlicePoints = size_t(1) << 25;       // 128 MB of output per staging buffer
+constexpr size_t kHostSliceMin = size_t(1) << 23;
+
+size_t host_slice_cap(int k, size_t remaining)
+{
+    size_t cap = std::min(kHostSlicePoints, kHostSliceMin << std::min(k, 8));
+    if (remaining <= 2 * kHostSlicePoints) cap = std::min(cap, std::max(kHostSliceMin, remaining / 2));
+    return cap;
+}
+
+struct HostBatchCtx {
+    cudaStream_t gen = nullptr, copy = nullptr;
+    cudaEvent_t gen_done[2] = {}, copy_done[2] = {};
+    float* stage[2] = {};
+    size_t stage_cap = 0;                  // floats per staging buffer
+    float* hmm = nullptr;                  // pinned: min/max of every request
+    size_t hmm_cap = 0;
+    fnBatchInfo info{};                    // summed over the slices of the last call
+    bool info_valid = false;
+    ~HostBatchCtx()
+    {
+        for (int k = 0; k < 2; ++k) {
+            if (stage[k]) cudaFree(stage[k]);
+            if (gen_done[k]) cudaEventDestroy(gen_done[k]);
+            if (copy_done[k]) cudaEventDestroy(copy_done[k]);
+        }
+        if (hmm) cudaFreeHost(hmm);
+        if (gen) cudaStreamDestroy(gen);
+        if (copy) cudaStreamDestroy(copy);
+    }
+};
+thread_local HostBatchCtx* t_hbatch = nullptr;
+
+HostBatchCtx* host_batch_ctx(size_t stage_floats, size_t requests)
+{
+    if (!t_hbatch) {
+        HostBatchCtx* h = new HostBatchCtx();
+        bool ok = cuda_ok(cudaStreamCreateWithFlags(&h->gen, cudaStreamNonBlocking), "stream") &&
+                  cuda_ok(cudaStreamCreateWithFlags(&h->copy, cudaStreamNonBlocking), "stream");
+        for (int k = 0; ok && k < 2; ++k)
+            ok = cuda_ok(cudaEventCreateWithFlags(&h->gen_done[k], cudaEventDisableTiming), "event") &&
+                 cuda_ok(cudaEventCreateWithFlags(&h->copy_done[k], cudaEventDisableTiming), "event");
+        if (!ok) { delete h; return nullptr; }
+        t_hbatch = h;
+    }
+    HostBatchCtx* h = t_hbatch;
+    if (stage_floats > h->stage_cap) {
+        for (int k = 0; k < 2; ++k) {
+            if (h->stage[k]) cudaFree(h->stage[k]);
+            h->stage[k] = nullptr;
+        }
+        h->stage_cap = 0;
+        for (int k = 0; k < 2; ++k)
+            if (!cuda_ok(cudaMalloc(&h->stage[k], stage_floats * sizeof(float)), "cudaMalloc(host batch staging)")) return nullptr;
+        h->stage_cap = stage_floats;
+    }
+    if (2 * requests > h->hmm_cap) {
+        if (h->hmm) cudaFreeHost(h->hmm);
+        h->hmm = nullptr;
+        h->hmm_cap = 0;
+        if (!cuda_ok(cudaMallocHost(&h->hmm, 2 * requests * sizeof(float)), "cudaMallocHost(host batch minmax)")) return nullptr;
+        h->hmm_cap = 2 * requests;
+    }
+    return h;
+}
+
 }  // namespace
 
 extern "C" {
@@ -603,7 +674,90 @@ int fnSerialiseNodeTree(const void* node, char* buffer, int bufferSize)
 int fnGenBatchDevice(const fnGenRequest* requests, int count, void* stream, int flags)
 {
     clear_error();
+    if (t_hbatch) t_hbatch->info_valid = false;
     return run_batch(requests, count, stream, flags, nullptr);
+}
+
+int fnGenBatchHost(const fnGenRequest* requests, int count, int flags)
+{
+    (void)flags;
+    clear_error();
+    if (count < 0 || (count > 0 && !requests)) { set_error(FN_ERR_ARG, "invalid request list"); return FN_ERR_ARG; }
+    if (count == 0) return FN_OK;
+    if (!thread_ctx()) return FN_ERR_CUDA;
+    std::vector<size_t> points((size_t)count);
+    size_t largest = 0;
+    for (int i = 0; i < count; ++i) {
+        PointArgs a;
+        if (!requests[i].node || !request_args(requests[i], a) || a.total < 0 || (a.total > 0 && !requests[i].out)) {
+            set_error(FN_ERR_ARG, "invalid request " + std::to_string(i));
+            return FN_ERR_ARG;
+        }
+        points[(size_t)i] = (size_t)a.total;
+        largest = std::max(largest, points[(size_t)i]);
+    }
+    const size_t cap = std::max(kHostSlicePoints, largest);
+    HostBatchCtx* h = host_batch_ctx(cap, (size_t)count);
+    if (!h) return FN_ERR_CUDA;
+    h->info = fnBatchInfo{};
+    h->info_valid = false;
+    std::vector<fnGenRequest> slice;
+    size_t remaining = 0;
+    for (size_t p : points) remaining += p;
+    int k = 0;
+    for (int i0 = 0; i0 < count; ++k) {
+        const int buf = k & 1;
+        const size_t want = host_slice_cap(k, remaining);
+        size_t used = 0;
+        int i1 = i0;
+        while (i1 < count && (i1 == i0 || used + points[(size_t)i1] <= want)) used += points[(size_t)i1++];
+        remaining -= used;
+        slice.assign(requests + i0, requests + i1);
+        size_t off = 0;
+        for (size_t j = 0; j < slice.size(); ++j) {
+            slice[j].out = h->stage[buf] + off;
+            slice[j].minMax = nullptr;
+            off += points[(size_t)i0 + j];
+        }
+        // buffer `buf` is free once the copy of slice k - 2 is done
+        if (!cuda_ok(cudaStreamWaitEvent(h->gen, h->copy_done[buf], 0), "wait")) return FN_ERR_CUDA;
+        const int rc = run_batch(slice.data(), (int)slice.size(), h->gen, FN_BATCH_NO_GRAPH, nullptr);
+        if (rc) return rc;
+        const BatchRunner& r = t_batch->runner;
+        h->info.requests += (int)slice.size();
+        h->info.specialised = r.last_specialised() ? 1 : 0;
+        h->info.tilePoints = (int)r.last_tile_points();
+        h->info.ctas = r.last_grid();
+        h->info.workItems += r.last_items();
+        h->info.points += r.last_points();
+        h->info.uploadBytes += r.last_upload_bytes();
+        if (!cuda_ok(cudaMemcpyAsync(h->hmm + 2 * (size_t)i0, t_batch->dminmax, slice.size() * 2 * sizeof(float),
+                                     cudaMemcpyDeviceToHost, h->gen), "copy minmax") ||
+            !cuda_ok(cudaEventRecord(h->gen_done[buf], h->gen), "record") ||
+            !cuda_ok(cudaStreamWaitEvent(h->copy, h->gen_done[buf], 0), "wait"))
+            return FN_ERR_CUDA;
+        // one copy per run of requests whose host outputs are contiguous
+        size_t src = 0;
+        for (int j = i0; j < i1;) {
+            float* dst = requests[j].out;
+            size_t n = points[(size_t)j];
+            int e = j + 1;
+            while (e < i1 && points[(size_t)e] && requests[e].out == dst + n) n += points[(size_t)e++];
+            if (n && !cuda_ok(cudaMemcpyAsync(dst, h->stage[buf] + src, n * sizeof(float), cudaMemcpyDeviceToHost, h->copy),
+                              "copy output"))
+                return FN_ERR_CUDA;
+            src += n;
+            j = e;
+        }
+        if (!cuda_ok(cudaEventRecord(h->copy_done[buf], h->copy), "record")) return FN_ERR_CUDA;
+        i0 = i1;
+    }
+    if (!cuda_ok(cudaStreamSynchronize(h->copy), "synchronize") || !cuda_ok(cudaStreamSynchronize(h->gen), "synchronize"))
+        return FN_ERR_CUDA;
+    for (int i = 0; i < count; ++i)
+        if (requests[i].minMax) { requests[i].minMax[0] = h->hmm[2 * i]; requests[i].minMax[1] = h->hmm[2 * i + 1]; }
+    h->info_valid = true;
+    return FN_OK;
 }
 
 int fnGenEachDevice(const fnGenRequest* requests, int count, void* stream, int flags)
@@ -928,6 +1082,10 @@ int fnGetBatchInfo(fnBatchInfo* info)
     clear_error();
     if (!info) { set_error(FN_ERR_ARG, "null info"); return FN_ERR_ARG; }
     std::memset(info, 0, sizeof *info);
+    if (t_hbatch && t_hbatch->info_valid) {          // the last call was fnGenBatchHost: its slices summed
+        *info = t_hbatch->info;
+        return FN_OK;
+    }
     if (!t_batch) return FN_OK;
     const BatchRunner& r = t_batch->runner;
     info->requests = (int)r.last_device_minmax().size();

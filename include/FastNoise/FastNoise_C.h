@@ -192,6 +192,14 @@ typedef struct fnGenRequest {
  * Tile size and CTAs per SM come from the autotuner's entry for this batch's signature
  * (set by fnAutotuneBatch), else defaults. */
 FASTNOISE_API int fnGenBatchDevice(const fnGenRequest* requests, int count, void* stream, int flags);
+/* The same requests with HOST outputs (pinned memory gives full copy speed; any host memory
+ * works): request.out points to host memory, minMax (host float[2] or NULL) is filled, and the
+ * call returns when every output is on the host.  The requests are generated in slices of at
+ * most 2^25 points (smaller at the start and the end) through two device staging buffers, each
+ * slice's copy to the host overlapping the next slice's generation; requests whose outputs are
+ * adjacent in host memory are copied together.  fnGetBatchInfo then reports the slices summed.
+ * flags: reserved, pass 0. */
+FASTNOISE_API int fnGenBatchHost(const fnGenRequest* requests, int count, int flags);
 /* The per-call path for the same request list: one plain launch per request, queued in
  * order on `stream` (what a caller looping over fnGen*Device would do), for comparison
  * with fnGenBatchDevice.  minMax pointers are filled when FN_BATCH_SYNC is set. */

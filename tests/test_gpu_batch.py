@@ -100,3 +100,33 @@ def test_bad_request_fails_loudly(gpu, torch_cuda):
     out = torch_cuda.empty(16, device="cuda")
     with pytest.raises(fn.FastNoiseError):
         fn.gen_batch([fn.make_request(node, fn.KIND_GRID2D, out.data_ptr(), 1, (4, 4))])
+
+
+@pytest.mark.parametrize("contiguous", [True, False])
+def test_batch_host_outputs_match_device_batch(gpu, torch_cuda, contiguous):
+    """fnGenBatchHost: host outputs (contiguous runs copied together, or separate arrays), slices
+    across both staging buffers (the mix is larger than one 2^25-point slice), a request larger
+    than a slice, and empty requests; outputs and min/max equal the device batch's."""
+    fn, torch = gpu, torch_cuda
+    chunks = chunkmix.make_mix(40, seed=19, sizes=[(128, 128, 64), (96, 80, 70), (0, 5, 5), (17, 3)])
+    chunks.append(chunkmix.Chunk(tree=1, count=(384, 320, 300), offset=(-5.0, 7.0, 3.0), seed=77))   # 36.9 M points
+    nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
+    dreqs, douts, dmms = requests_for(fn, torch, chunks, nodes)
+    fn.gen_batch(dreqs, sync=True)
+    total = sum(c.points for c in chunks)
+    block = torch.empty(max(total, 1), dtype=torch.float32, pin_memory=True).numpy()
+    hreqs, houts, hmms, off = [], [], [], 0
+    for c in chunks:
+        out = block[off:off + c.points] if contiguous else np.empty(c.points, np.float32)
+        off += c.points
+        mm = np.zeros(2, np.float32)
+        kind = fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D
+        hreqs.append(fn.make_request(nodes[c.tree], kind, out.ctypes.data, c.seed, c.count, c.offset, (1, 1, 1, 1), minmax=mm))
+        houts.append(out)
+        hmms.append(mm)
+    fn.gen_batch_host(hreqs)
+    info = fn.batch_info()
+    assert info["requests"] == len(chunks) and info["points"] == total
+    for c, dout, dmm, hout, hmm in zip(chunks, douts, dmms, houts, hmms):
+        assert np.array_equal(hout.view(np.uint32), dout.cpu().numpy().view(np.uint32)), c
+        assert (hmm[0], hmm[1]) == (dmm[0], dmm[1]), c
