@@ -4,6 +4,7 @@
 // argument meaning, sentinel return values).  Generation runs on the GPU
 // through the program interpreter; host output arrays are filled by a
 // device->host copy on this thread's stream.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -76,6 +77,80 @@ bool ensure_runnable(const DeviceProgram& prog)
 }
 
 // Run one host-memory generation call end to end.
+// Large grids into host memory are generated in slabs along the outermost axis: every slab is
+// launched at once, and slab s is copied to the host as soon as it is done, while later slabs
+// are still being generated.  Positions come from the point's index in the whole grid (the
+// slab's `base`), so the output is the same as one launch's; the slabs' min/max are combined
+// in slab order with the same comparisons the kernels' own block reduction uses.
+constexpr long long kSlabMinPoints = 1ll << 22;
+constexpr int kMaxSlabs = 8;
+
+struct SlabCtx {
+    cudaStream_t copy = nullptr;
+    cudaEvent_t done[kMaxSlabs] = {};
+    float* dmm = nullptr;                  // device: min/max per slab
+    float* hmm = nullptr;                  // pinned copy
+    ~SlabCtx()
+    {
+        for (cudaEvent_t& e : done) if (e) cudaEventDestroy(e);
+        if (dmm) cudaFree(dmm);
+        if (hmm) cudaFreeHost(hmm);
+        if (copy) cudaStreamDestroy(copy);
+    }
+};
+thread_local SlabCtx* t_slab = nullptr;
+
+SlabCtx* slab_ctx()
+{
+    if (t_slab) return t_slab;
+    SlabCtx* c = new SlabCtx();
+    bool ok = cuda_ok(cudaStreamCreateWithFlags(&c->copy, cudaStreamNonBlocking), "stream") &&
+              cuda_ok(cudaMalloc(&c->dmm, 2 * kMaxSlabs * sizeof(float)), "cudaMalloc(slab minmax)") &&
+              cuda_ok(cudaMallocHost(&c->hmm, 2 * kMaxSlabs * sizeof(float)), "cudaMallocHost(slab minmax)");
+    for (int k = 0; ok && k < kMaxSlabs; ++k) ok = cuda_ok(cudaEventCreateWithFlags(&c->done[k], cudaEventDisableTiming), "event");
+    if (!ok) { delete c; return nullptr; }
+    return t_slab = c;
+}
+
+// Generate a grid in slabs into host memory; false on a CUDA error (already reported).
+bool gen_host_slabs(const DeviceProgram& prog, const PointArgs& args, ThreadCtx* ctx, MinMaxWork* work, float* out, float* minmax)
+{
+    SlabCtx* sc = slab_ctx();
+    if (!sc) return false;
+    const int k = args.dim - 1;
+    const int rows = args.count[k];
+    const long long row = args.total / rows;                   // points per index of the outermost axis
+    int slabs = (int)std::min<long long>(std::min<long long>(kMaxSlabs, args.total / kSlabMinPoints), rows);
+    const int per = (rows + slabs - 1) / slabs;
+    slabs = (rows + per - 1) / per;
+    for (int s = 0; s < slabs; ++s) {
+        PointArgs a = args;
+        const long long r0 = (long long)s * per, r1 = std::min<long long>(rows, r0 + per);
+        a.base = (unsigned)(r0 * row);
+        a.total = (r1 - r0) * row;
+        if (!cuda_ok(launch_points(prog, a, ctx->dbuf + a.base, work, sc->dmm + 2 * s, ctx->stream), "launch") ||
+            !cuda_ok(cudaEventRecord(sc->done[s], ctx->stream), "record"))
+            return false;
+    }
+    for (int s = 0; s < slabs; ++s) {
+        const long long r0 = (long long)s * per, r1 = std::min<long long>(rows, r0 + per);
+        if (!cuda_ok(cudaStreamWaitEvent(sc->copy, sc->done[s], 0), "wait") ||
+            !cuda_ok(cudaMemcpyAsync(out + r0 * row, ctx->dbuf + r0 * row, (size_t)((r1 - r0) * row) * 4, cudaMemcpyDeviceToHost,
+                                     sc->copy), "copy output"))
+            return false;
+    }
+    if (!cuda_ok(cudaMemcpyAsync(sc->hmm, sc->dmm, 2 * slabs * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream), "copy minmax") ||
+        !cuda_ok(cudaStreamSynchronize(sc->copy), "synchronize") || !cuda_ok(cudaStreamSynchronize(ctx->stream), "synchronize"))
+        return false;
+    float mn = std::numeric_limits<float>::infinity(), mx = -mn;
+    for (int s = 0; s < slabs; ++s) {
+        mn = mn < sc->hmm[2 * s] ? mn : sc->hmm[2 * s];
+        mx = mx > sc->hmm[2 * s + 1] ? mx : sc->hmm[2 * s + 1];
+    }
+    store_minmax(minmax, mn, mx);
+    return true;
+}
+
 void gen_host(const void* node, PointArgs args, float* out, float* minmax, const float* const* hpos)
 {
     clear_error();
@@ -102,6 +177,10 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
             }
             args.pos[k] = ctx->dpos[k];
         }
+    }
+    if (args.src == kSrcGrid && total >= 2 * kSlabMinPoints && total < (1ll << 32)) {
+        if (!gen_host_slabs(prog, args, ctx, work, out, minmax)) fill_nan(out, total, minmax);
+        return;
     }
     if (!cuda_ok(launch_points(prog, args, ctx->dbuf, work, nullptr, ctx->stream), "launch")) { fill_nan(out, total, minmax); return; }
     if (total > 0 && !cuda_ok(cudaMemcpyAsync(out, ctx->dbuf, (size_t)total * 4, cudaMemcpyDeviceToHost, ctx->stream), "copy output")) { fill_nan(out, total, minmax); return; }

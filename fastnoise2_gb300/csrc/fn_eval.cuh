@@ -19,6 +19,7 @@ __device__ __forceinline__ float inf() { return __int_as_float(0x7f800000); }
 // Root position of point i (Generator.inl:104-105, 160-162, 225-228, 295-297, 400-406).
 __device__ __forceinline__ void root_position(const fn::PointArgs& a, long long i, float* R)
 {
+    i += a.base;
     if (a.src == fn::kSrcGrid) {
         long long r = i;
 #pragma unroll
@@ -59,6 +60,7 @@ __device__ __forceinline__ unsigned fast_div(unsigned n, unsigned m, unsigned s)
 template <int D>
 __device__ __forceinline__ void root_position32(const fn::PointArgs& a, unsigned i, float* R)
 {
+    i += a.base;
     if (a.src == fn::kSrcGrid) {
         unsigned r = i;
 #pragma unroll

@@ -315,7 +315,7 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
     // grid: Generator.inl:79-254, pos_k = fma(float(i_k), step_k, offset_k), x fastest
     {
         std::ostringstream pos;
-        pos << "                unsigned r = i;\n";
+        pos << "                unsigned r = i + A.base;\n";          // index in the whole request
         const char* ax = "xyzw";
         for (int j = 0; j < D; ++j) {
             if (j < D - 1)
@@ -329,13 +329,15 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
     // position arrays: Generator.inl:256-350, pos_k = offset_k + array_k[i]
     {
         std::ostringstream pos;
-        for (int j = 0; j < D; ++j) pos << "                const float " << pv[j] << " = A.offset[" << j << "] + __ldg(A.pos[" << j << "] + i);\n";
+        for (int j = 0; j < D; ++j)
+            pos << "                const float " << pv[j] << " = A.offset[" << j << "] + __ldg(A.pos[" << j << "] + i + A.base);\n";
         kernel("fnjit_pos", "", pos.str());
     }
     // tileable (4D programs): Generator.inl:370-433
     if (D == 4) {
         std::ostringstream pos;
-        pos << "                const unsigned iy = fne::fast_div(i, A.divm[0], A.divs[0]), ix = i - iy * (unsigned)A.count[0];\n"
+        pos << "                const unsigned g = i + A.base;\n"
+            << "                const unsigned iy = fne::fast_div(g, A.divm[0], A.divs[0]), ix = g - iy * (unsigned)A.count[0];\n"
             << "                const float xf = fnd::cvtf((int)ix) * A.tmul[0];\n"
             << "                const float yf = fnd::cvtf((int)iy) * A.tmul[1];\n"
             << "                const float px = fnd::cos_(xf) * A.tfreq[0];\n"

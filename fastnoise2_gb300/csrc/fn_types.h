@@ -26,6 +26,9 @@ struct PointArgs {
     // q = (t + ((n - t) >> 1)) >> (divs[k] - 1), t = umulhi(n, divm[k]); divs = 0 means count 1.
     unsigned int divm[3];
     unsigned int divs[3];
+    // Index of this launch's first point in the whole request (0 unless a large grid is
+    // generated slab by slab): positions come from base + i, output and min/max cover i only.
+    unsigned int base;
 };
 
 // Per-launch reduction workspace.  `counter` must be zero before the first

@@ -1,0 +1,54 @@
+"""Large grids into host memory are generated slab by slab along the outermost axis (each slab's
+copy to the host overlapping the next slab's generation).  The output and OutputMinMax must be
+those of one launch over the whole grid: positions come from each point's index in the whole
+grid, and the slabs' min/max are combined in slab order."""
+import numpy as np
+import pytest
+
+from oracle.oracle import OracleTree
+from tests import trees
+
+pytestmark = pytest.mark.gpu
+
+
+def device_grid(fn, torch, node, offset, count, step, seed):
+    L = fn.lib()
+    n = int(np.prod(count))
+    out = torch.empty(n, dtype=torch.float32, device="cuda")
+    mm = torch.empty(2, dtype=torch.float32, device="cuda")
+    f = {3: L.fnGenUniformGrid3DDevice, 4: L.fnGenUniformGrid4DDevice}[len(count)]
+    rc = f(node.handle, out.data_ptr(), *map(float, offset), *map(int, count), *map(float, step), int(seed), mm.data_ptr(), None)
+    assert rc == 0
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), tuple(float(v) for v in mm.cpu().numpy())
+
+
+@pytest.mark.parametrize("jit", [True, False])
+@pytest.mark.parametrize("case", [
+    ((-100.0, 20.5, -7.0), (200, 160, 300), (1.0, 0.5, 2.0)),           # 9.6 M points, two slabs
+    ((3.0, -2.0, 11.0), (257, 129, 300), (0.75, 1.25, 1.0)),            # odd row length: slabs start unaligned
+    ((0.0, 0.0, 0.0, 5.0), (64, 48, 40, 70), (1.0, 1.0, 1.0, 1.0)),     # 4D, 8.6 M points
+])
+def test_slabbed_host_grid_equals_one_launch(gpu, case, jit):
+    torch = pytest.importorskip("torch")
+    fn = gpu
+    offset, count, step = case
+    root = trees.fbm_perlin_c1()
+    node = trees.to_product(root)
+    if jit:
+        fn.jit_compile([(node, len(count))])
+    old = fn.set_jit_enabled(jit)
+    try:
+        host, hmm = node.gen_uniform_grid(offset, count, step, 42)
+        dev, dmm = device_grid(fn, torch, node, offset, count, step, 42)
+    finally:
+        fn.set_jit_enabled(old)
+    assert np.array_equal(host.view(np.uint32), dev.view(np.uint32))
+    assert hmm == dmm
+    # spot check against the oracle: the first and last planes of the outermost axis, as
+    # one-plane grids at that plane's position (fma(r, step, offset), exact in float64 here)
+    plane = int(np.prod(count[:-1]))
+    for r in (0, count[-1] - 1):
+        pos = float(np.float32(float(r) * float(np.float32(step[-1])) + float(np.float32(offset[-1]))))
+        o, _ = OracleTree(root).grid(tuple(offset[:-1]) + (pos,), tuple(count[:-1]) + (1,), step, 42)
+        assert np.array_equal(host[r * plane:(r + 1) * plane].view(np.uint32), np.asarray(o, np.float32).view(np.uint32)), r
