@@ -385,7 +385,7 @@ def run_chunkmix(a, rank, world, local):
         "batch": binfo,
         "cpu_baseline": cpu,
         "clocks": clocks,
-        "gpu_launches": a.steps,
+        "gpu_launches": a.steps * binfo["kernels"],          # one persistent kernel per tree and dimensionality
     }
     print(json.dumps(line))
 

@@ -403,7 +403,7 @@ class LiveTree:
 class BatchInfo(ctypes.Structure):
     _fields_ = [("requests", ctypes.c_int), ("specialised", ctypes.c_int), ("tilePoints", ctypes.c_int),
                 ("ctas", ctypes.c_int), ("workItems", ctypes.c_ulonglong), ("points", ctypes.c_ulonglong),
-                ("uploadBytes", ctypes.c_ulonglong)]
+                ("uploadBytes", ctypes.c_ulonglong), ("kernels", ctypes.c_int)]
 
 
 def batch_info() -> dict:

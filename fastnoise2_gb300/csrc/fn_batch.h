@@ -52,6 +52,7 @@ public:
     uint32_t last_tile_points() const { return tile_points_; }
     int last_grid() const { return grid_; }
     bool last_specialised() const { return specialised_; }
+    int last_kernels() const { return (int)groups_.size(); }
 
 private:
     // One kernel launch of a batch: the interpreter's batch kernel over all items

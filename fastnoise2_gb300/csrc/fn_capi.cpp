@@ -810,6 +810,7 @@ int fnGenBatchHost(const fnGenRequest* requests, int count, int flags)
         h->info.workItems += r.last_items();
         h->info.points += r.last_points();
         h->info.uploadBytes += r.last_upload_bytes();
+        h->info.kernels += r.last_kernels();
         if (!cuda_ok(cudaMemcpyAsync(h->hmm + 2 * (size_t)i0, t_batch->dminmax, slice.size() * 2 * sizeof(float),
                                      cudaMemcpyDeviceToHost, h->gen), "copy minmax") ||
             !cuda_ok(cudaEventRecord(h->gen_done[buf], h->gen), "record") ||
@@ -1174,6 +1175,7 @@ int fnGetBatchInfo(fnBatchInfo* info)
     info->workItems = r.last_items();
     info->points = r.last_points();
     info->uploadBytes = r.last_upload_bytes();
+    info->kernels = r.last_kernels();
     return FN_OK;
 }
 

@@ -268,6 +268,7 @@ typedef struct fnBatchInfo {
     unsigned long long workItems;   /* (request, tile) items in the device queue */
     unsigned long long points;
     unsigned long long uploadBytes; /* descriptor bytes copied host -> device for the launch */
+    int kernels;                    /* kernels launched (one per tree and dimensionality when specialised) */
 } fnBatchInfo;
 FASTNOISE_API int fnGetBatchInfo(fnBatchInfo* info);
 
