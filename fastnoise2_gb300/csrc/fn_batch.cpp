@@ -293,8 +293,15 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
     }
     const size_t bytes = off_items_ + n_items * sizeof(uint2);
     const uint32_t smem = jit ? 0 : max_bytes;
+    // A graph pays off for a launch shape that repeats (the same batch every frame); batches
+    // whose shape keeps changing (a server's admissions) would pay a capture each time, so a
+    // new shape is captured only when it comes twice in a row and runs as plain launches until then.
+    const bool same_as_graph = exec_ && graph_groups_ == groups_ && graph_smem_ == smem;
+    const bool repeated = last_groups_ == groups_ && last_smem_ == smem;
+    last_groups_ = groups_;
+    last_smem_ = smem;
     int rc;
-    if (use_graph) {
+    if (use_graph && (same_as_graph || repeated)) {
         rc = launch_graph(stream, bytes, smem);
     } else {
         rc = cuda_ok(cudaMemcpyAsync(d_buf_, h_buf_, bytes, cudaMemcpyHostToDevice, stream), "upload batch") &&
