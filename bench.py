@@ -31,6 +31,7 @@ per GPU, no collective on the data path); value = all points / max rank time.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -441,14 +442,13 @@ def run_served(fn, chunks, nodes, rank, a, dev):
         gaps = rng.exponential(1.0 / rate, n)
         t_start = time.perf_counter()
         due = t_start
-        tickets = []
+        tickets = (ctypes.c_ulonglong * n)()
         for k in range(n):
             due += gaps[k]
             while time.perf_counter() < due:
                 pass
-            tickets.append(srv.submit(serve[k % len(serve)]))
-        for t in tickets:
-            srv.wait(t)
+            tickets[k] = srv.submit(serve[k % len(serve)])
+        srv.wait_many(tickets, timeout_ms=60000)         # one native wait: the last completion ends the run
         wall = time.perf_counter() - t_start
         st = srv.stats()
         for t in tickets:

@@ -473,7 +473,7 @@ class Server:
     def wait_many(self, tickets, timeout_ms: int = -1) -> None:
         """Wait until every ticket has finished; raises FastNoiseError on failure or timeout."""
         n = len(tickets)
-        t = (ctypes.c_ulonglong * n)(*tickets)
+        t = tickets if isinstance(tickets, ctypes.Array) else (ctypes.c_ulonglong * n)(*tickets)
         rc = lib().fnServerWaitMany(self._h, t, n, timeout_ms)
         if rc != 0:
             raise FastNoiseError(rc, lib().fnGetLastErrorString().decode())
