@@ -53,6 +53,7 @@ FND int imul(int a, int b) { return (int)((unsigned)a * (unsigned)b); }
 FND int iadd(int a, int b) { return (int)((unsigned)a + (unsigned)b); }
 FND float invsqrt(float x) { return 1.0f / sqrtf(x); }
 
+FND int hash_mix(int v) { int h = imul(v, kHashA); return (h >> 15) ^ h; }
 FND int hash(int seed, int a, int b) { int h = imul(seed ^ a ^ b, kHashA); return (h >> 15) ^ h; }
 FND int hash(int seed, int a, int b, int c) { int h = imul(seed ^ a ^ b ^ c, kHashA); return (h >> 15) ^ h; }
 FND int hash(int seed, int a, int b, int c, int d) { int h = imul(seed ^ a ^ b ^ c ^ d, kHashA); return (h >> 15) ^ h; }
@@ -608,10 +609,12 @@ FND float perlin3(int seed, float x, float y, float z)
     float xf0 = x - xs, yf0 = y - ys, zf0 = z - zs;
     float xf1 = xf0 - 1.0f, yf1 = yf0 - 1.0f, zf1 = zf0 - 1.0f;
     float u = quintic(xf0), v = quintic(yf0), s = quintic(zf0);
-    return lerp(lerp(lerp(grad3(hash(seed, x0, y0, z0), xf0, yf0, zf0), grad3(hash(seed, x1, y0, z0), xf1, yf0, zf0), u),
-                     lerp(grad3(hash(seed, x0, y1, z0), xf0, yf1, zf0), grad3(hash(seed, x1, y1, z0), xf1, yf1, zf0), u), v),
-                lerp(lerp(grad3(hash(seed, x0, y0, z1), xf0, yf0, zf1), grad3(hash(seed, x1, y0, z1), xf1, yf0, zf1), u),
-                     lerp(grad3(hash(seed, x0, y1, z1), xf0, yf1, zf1), grad3(hash(seed, x1, y1, z1), xf1, yf1, zf1), u), v), s);
+    // seed ^ y ^ z shared by each x pair of corners (xor reassociated: the same hashes)
+    const int a00 = seed ^ y0 ^ z0, a10 = seed ^ y1 ^ z0, a01 = seed ^ y0 ^ z1, a11 = seed ^ y1 ^ z1;
+    return lerp(lerp(lerp(grad3(hash_mix(a00 ^ x0), xf0, yf0, zf0), grad3(hash_mix(a00 ^ x1), xf1, yf0, zf0), u),
+                     lerp(grad3(hash_mix(a10 ^ x0), xf0, yf1, zf0), grad3(hash_mix(a10 ^ x1), xf1, yf1, zf0), u), v),
+                lerp(lerp(grad3(hash_mix(a01 ^ x0), xf0, yf0, zf1), grad3(hash_mix(a01 ^ x1), xf1, yf0, zf1), u),
+                     lerp(grad3(hash_mix(a11 ^ x0), xf0, yf1, zf1), grad3(hash_mix(a11 ^ x1), xf1, yf1, zf1), u), v), s);
 }
 
 FND float perlin4(int seed, float x, float y, float z, float w)
@@ -622,7 +625,7 @@ FND float perlin4(int seed, float x, float y, float z, float w)
     float xf0 = x - xs, yf0 = y - ys, zf0 = z - zs, wf0 = w - ws;
     float xf1 = xf0 - 1.0f, yf1 = yf0 - 1.0f, zf1 = zf0 - 1.0f, wf1 = wf0 - 1.0f;
     float u = quintic(xf0), v = quintic(yf0), s = quintic(zf0), q = quintic(wf0);
-#define G(a, b, c, d, fa, fb, fc, fd) grad4(hash(seed, a, b, c, d), fa, fb, fc, fd)
+#define G(a, b, c, d, fa, fb, fc, fd) grad4(hash_mix((seed ^ b ^ c ^ d) ^ a), fa, fb, fc, fd)
     return lerp(
         lerp(lerp(lerp(G(x0, y0, z0, w0, xf0, yf0, zf0, wf0), G(x1, y0, z0, w0, xf1, yf0, zf0, wf0), u),
                   lerp(G(x0, y1, z0, w0, xf0, yf1, zf0, wf0), G(x1, y1, z0, w0, xf1, yf1, zf0, wf0), u), v),
@@ -651,10 +654,9 @@ FND float value3(int seed, float x, float y, float z)
     int x0 = imul(cvti(xs), kPrimeX), y0 = imul(cvti(ys), kPrimeY), z0 = imul(cvti(zs), kPrimeZ);
     int x1 = iadd(x0, kPrimeX), y1 = iadd(y0, kPrimeY), z1 = iadd(z0, kPrimeZ);
     float u = hermite(x - xs), v = hermite(y - ys), s = hermite(z - zs);
-    return lerp(lerp(lerp(valcoord(seed ^ x0 ^ y0 ^ z0), valcoord(seed ^ x1 ^ y0 ^ z0), u),
-                     lerp(valcoord(seed ^ x0 ^ y1 ^ z0), valcoord(seed ^ x1 ^ y1 ^ z0), u), v),
-                lerp(lerp(valcoord(seed ^ x0 ^ y0 ^ z1), valcoord(seed ^ x1 ^ y0 ^ z1), u),
-                     lerp(valcoord(seed ^ x0 ^ y1 ^ z1), valcoord(seed ^ x1 ^ y1 ^ z1), u), v), s);
+    const int a00 = seed ^ y0 ^ z0, a10 = seed ^ y1 ^ z0, a01 = seed ^ y0 ^ z1, a11 = seed ^ y1 ^ z1;   // shared by x pairs
+    return lerp(lerp(lerp(valcoord(a00 ^ x0), valcoord(a00 ^ x1), u), lerp(valcoord(a10 ^ x0), valcoord(a10 ^ x1), u), v),
+                lerp(lerp(valcoord(a01 ^ x0), valcoord(a01 ^ x1), u), lerp(valcoord(a11 ^ x0), valcoord(a11 ^ x1), u), v), s);
 }
 
 FND float value4(int seed, float x, float y, float z, float w)
@@ -663,7 +665,7 @@ FND float value4(int seed, float x, float y, float z, float w)
     int x0 = imul(cvti(xs), kPrimeX), y0 = imul(cvti(ys), kPrimeY), z0 = imul(cvti(zs), kPrimeZ), w0 = imul(cvti(ws), kPrimeW);
     int x1 = iadd(x0, kPrimeX), y1 = iadd(y0, kPrimeY), z1 = iadd(z0, kPrimeZ), w1 = iadd(w0, kPrimeW);
     float u = hermite(x - xs), v = hermite(y - ys), s = hermite(z - zs), q = hermite(w - ws);
-#define V(a, b, c, d) valcoord(seed ^ a ^ b ^ c ^ d)
+#define V(a, b, c, d) valcoord((seed ^ b ^ c ^ d) ^ a)
     return lerp(
         lerp(lerp(lerp(V(x0, y0, z0, w0), V(x1, y0, z0, w0), u), lerp(V(x0, y1, z0, w0), V(x1, y1, z0, w0), u), v),
              lerp(lerp(V(x0, y0, z1, w0), V(x1, y0, z1, w0), u), lerp(V(x0, y1, z1, w0), V(x1, y1, z1, w0), u), v), s),
