@@ -69,10 +69,10 @@ FND float quintic(float t) { return t * t * t * fmaf(t, fmaf(t, 6.0f, -15.0f), 1
 // GetGradientDotCommon, portable branch (Utils.inl:132-158)
 FND float grad3(int h, float x, float y, float z)
 {
-    int h13 = h & 13;
-    float u = h13 > 7 ? y : x;
-    float v = h13 == 12 ? x : z;
-    v = h13 < 2 ? y : v;
+    // h & 13 > 7: bit 3;  h & 13 == 12: bits 3, 2 set, bit 0 clear;  h & 13 < 2: bits 3, 2 clear
+    const bool b3 = (h & 8) != 0, b2 = (h & 4) != 0, x_case = (h & 9) == 8;
+    const float u = b3 ? y : x;
+    const float v = b2 ? (x_case ? x : z) : (b3 ? z : y);
     return flip(u, h << 31) + flip(v, (h >> 1) << 31);
 }
 // GetGradientDotPerlin 2D, portable branch (Utils.inl:181-190)
