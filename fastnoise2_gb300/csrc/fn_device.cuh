@@ -44,8 +44,10 @@ FND float flip(float v, int s) { return __int_as_float(__float_as_int(v) ^ (s & 
 FND float flipm(float v, bool m) { return m ? __int_as_float(__float_as_int(v) ^ (int)0x80000000) : v; }
 FND int cvti(float x)
 {
+    // cvt.rni saturates: below -2^31 (and -inf) it already gives INT_MIN, as x86 does; at or
+    // above 2^31 and for NaN the comparison fails and INT_MIN is substituted.
     int r = __float2int_rn(x);
-    return (x >= -2147483648.0f && x < 2147483648.0f) ? r : (int)0x80000000;
+    return x < 2147483648.0f ? r : (int)0x80000000;
 }
 FND float cvtf(int i) { return __int2float_rn(i); }
 FND unsigned srl(int a, int s) { return (unsigned)a >> s; }

@@ -238,3 +238,17 @@ def test_node_driven_minkowski_needs_specialisation(gpu):
         assert e.value.code == -2
     finally:
         fn.set_jit_enabled(was)
+
+
+@pytest.mark.parametrize("name", ["Perlin", "Value", "Simplex", "SuperSimplex", "CellularDistance", "CellularValue"])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_out_of_range_lattice_coordinates(gpu, name, dim):
+    """Coordinates at and beyond +-2^31: the lattice index conversion must give INT_MIN out of
+    range (x86 cvtps2dq) exactly as the oracle does."""
+    vals = np.array([0.5, 1e10, -1e10, 2147483648.0, -2147483904.0, 2147483520.0, -2147483648.0,
+                     3.0e9, -3.0e9, 123.25], np.float32)
+    rng = np.random.default_rng(3)
+    pos = [rng.permutation(np.tile(vals, 4)).astype(np.float32) for _ in range(dim)]
+    root = N(name, Feature_Scale=1.0)
+    g, gmm, o, omm = run_positions(root, pos, (0.0,) * dim, 1337)
+    assert_parity(g, gmm, o, omm, label=f"{name} {dim}D out of range")
