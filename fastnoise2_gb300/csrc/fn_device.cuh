@@ -39,6 +39,10 @@ constexpr float kValueBounds = 2147483648.f;
 
 FND float fmin_(float a, float b) { return a < b ? a : b; }
 FND float fmax_(float a, float b) { return a > b ? a : b; }
+// The simplex-family falloffs clamp with fmaxf(v, 0.0f) / fminf(v, 0.0f) (one min/max
+// instruction): there the clamped value is only ever raised to an even power, so the one case
+// where these differ from FS::Max / FS::Min against 0 (the sign of a zero) cannot show, and a
+// NaN becomes 0 in both.
 FND float fabs_(float a) { return __int_as_float(__float_as_int(a) & 0x7FFFFFFF); }
 FND float flip(float v, int s) { return __int_as_float(__float_as_int(v) ^ (s & (int)0x80000000)); }
 FND float flipm(float v, bool m) { return m ? __int_as_float(__float_as_int(v) ^ (int)0x80000000) : v; }
@@ -213,7 +217,7 @@ FND float simplex2(int seed, float x, float y)
     float f0 = fmaf(-dx0, dx0, fmaf(-dy0, dy0, 0.5f));
     float f1 = fmaf(-dx1, dx1, fmaf(-dy1, dy1, 0.5f));
     float f2 = f0 + fmaf(unskew, (float)(-4.0 * (kRoot3 + 2.0) / (kRoot3 + 3.0)), (float)(-2.0 / 3.0));
-    f0 = fmax_(f0, 0.0f); f1 = fmax_(f1, 0.0f); f2 = fmax_(f2, 0.0f);
+    f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); f2 = fmaxf(f2, 0.0f);
     f0 *= f0; f0 *= f0; f1 *= f1; f1 *= f1; f2 *= f2; f2 *= f2;
     float g0 = grad2(hash(seed, xp, yp), dx0, dy0);
     float g1 = grad2(hash(seed, xgey ? iadd(xp, kPrimeX) : xp, xgey ? yp : iadd(yp, kPrimeY)), dx1, dy1);
@@ -247,7 +251,7 @@ FND float simplex3(int seed, float x, float y, float z)
     float f1 = fmaf(-dz1, dz1, fmaf(-dy1, dy1, fmaf(-dx1, dx1, R)));
     float f2 = fmaf(-dz2, dz2, fmaf(-dy2, dy2, fmaf(-dx2, dx2, R)));
     float f3 = f0 - (unskew + (float)(3.0 / 4.0));
-    f0 = fmax_(f0, 0.0f); f1 = fmax_(f1, 0.0f); f2 = fmax_(f2, 0.0f); f3 = fmax_(f3, 0.0f);
+    f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); f2 = fmaxf(f2, 0.0f); f3 = fmaxf(f3, 0.0f);
     f0 *= f0; f0 *= f0; f1 *= f1; f1 *= f1; f2 *= f2; f2 *= f2; f3 *= f3; f3 *= f3;
     float g0 = grad3(hash(seed, xp, yp, zp), dx0, dy0, dz0);
     float g1 = grad3(hash(seed, mx1 ? iadd(xp, kPrimeX) : xp, my1 ? iadd(yp, kPrimeY) : yp, mz1 ? zp : iadd(zp, kPrimeZ)), dx1, dy1, dz1);
@@ -288,7 +292,7 @@ FND float simplex4(int seed, float x, float y, float z, float w)
     float f2 = fmaf(-dw2, dw2, fmaf(-dz2, dz2, fmaf(-dy2, dy2, fmaf(-dx2, dx2, R))));
     float f3 = fmaf(-dw3, dw3, fmaf(-dz3, dz3, fmaf(-dy3, dy3, fmaf(-dx3, dx3, R))));
     float f4 = f0 + fmaf(unskew, (float)(-4.0 * (kRoot5 + 3.0) / (kRoot5 + 5.0)), (float)(-4.0 / 5.0));
-    f0 = fmax_(f0, 0.0f); f1 = fmax_(f1, 0.0f); f2 = fmax_(f2, 0.0f); f3 = fmax_(f3, 0.0f); f4 = fmax_(f4, 0.0f);
+    f0 = fmaxf(f0, 0.0f); f1 = fmaxf(f1, 0.0f); f2 = fmaxf(f2, 0.0f); f3 = fmaxf(f3, 0.0f); f4 = fmaxf(f4, 0.0f);
     f0 *= f0; f0 *= f0; f1 *= f1; f1 *= f1; f2 *= f2; f2 *= f2; f3 *= f3; f3 *= f3; f4 *= f4; f4 *= f4;
     float g0 = grad4(hash(seed, xp, yp, zp, wp), dx0, dy0, dz0, dw0);
     float g1 = grad4(hash(seed, rx > 2 ? iadd(xp, kPrimeX) : xp, ry > 2 ? iadd(yp, kPrimeY) : yp, rz > 2 ? iadd(zp, kPrimeZ) : zp, rw > 2 ? iadd(wp, kPrimeW) : wp), dx1, dy1, dz1, dw1);
@@ -338,7 +342,7 @@ FND float supersimplex2(int seed, float x, float y)
         float dx = dxb - (fx ? (float)(1 + 2 * kUnskew2) : -1.0f);
         float dy = fx ? dyb - (float)(2 * kUnskew2) : dyb;
         float g = grad2(h, dx, dy);
-        float f = fmax_(fmaf(-dx, dx, fmaf(-dy, dy, R)), 0.0f);
+        float f = fmaxf(fmaf(-dx, dx, fmaf(-dy, dy, R)), 0.0f);
         f *= f; f *= f;
         value = fmaf(f, g, value);
     }
@@ -348,7 +352,7 @@ FND float supersimplex2(int seed, float x, float y)
         float dx = fy ? dxb - (float)(2 * kUnskew2) : dxb;
         float dy = dyb - (fy ? (float)(1 + 2 * kUnskew2) : -1.0f);
         float g = grad2(h, dx, dy);
-        float f = fmax_(fmaf(-dx, dx, fmaf(-dy, dy, R)), 0.0f);
+        float f = fmaxf(fmaf(-dx, dx, fmaf(-dy, dy, R)), 0.0f);
         f *= f; f *= f;
         value = fmaf(f, g, value);
     }
@@ -406,49 +410,49 @@ FND float supersimplex3(int seed, float x, float y, float z)
         bool m = xyzn < 0.0f;
         float off = flipm((float)(3 * kReflect + 1), m);
         float g = grad3(hash(seed, iadd(xp, m ? -kPrimeX : kPrimeX), iadd(yp, m ? -kPrimeY : kPrimeY), iadd(zp, m ? -kPrimeZ : kPrimeZ)), dx - off, dy - off, dz - off);
-        float fb = fmax_(fmaf(off, cs, stemA), 0.0f);
+        float fb = fmaxf(fmaf(off, cs, stemA), 0.0f);
         value = fmaf((fb * fb) * (fb * fb), g, value);
     }
     {
         bool m = xyzn < zn;
         float o0 = flipm((float)(2 * kReflect), m);
         float g = grad3(hash(seed, iadd(xp, m ? -kPrimeX : kPrimeX), iadd(yp, m ? -kPrimeY : kPrimeY), zp), dx, dy, dz - o0);
-        float fb = fmin_(flipm(dz, m) - stemB, 0.0f);
+        float fb = fminf(flipm(dz, m) - stemB, 0.0f);
         value = fmaf((fb * fb) * (fb * fb), g, value);
     }
     {
         bool m = xyzn < yn;
         float o0 = flipm((float)(2 * kReflect), m);
         float g = grad3(hash(seed, iadd(xp, m ? -kPrimeX : kPrimeX), yp, iadd(zp, m ? -kPrimeZ : kPrimeZ)), dx, dy - o0, dz);
-        float fb = fmin_(flipm(dy, m) - stemB, 0.0f);
+        float fb = fminf(flipm(dy, m) - stemB, 0.0f);
         value = fmaf((fb * fb) * (fb * fb), g, value);
     }
     {
         bool m = xyzn < xn;
         float o0 = flipm((float)(2 * kReflect), m);
         float g = grad3(hash(seed, xp, iadd(yp, m ? -kPrimeY : kPrimeY), iadd(zp, m ? -kPrimeZ : kPrimeZ)), dx - o0, dy, dz);
-        float fb = fmin_(flipm(dx, m) - stemB, 0.0f);
+        float fb = fminf(flipm(dx, m) - stemB, 0.0f);
         value = fmaf((fb * fb) * (fb * fb), g, value);
     }
     {
         bool m = xn < 0.0f;
         float o0 = flipm((float)kReflect, m);
         float g = grad3(hash(seed, iadd(xp, m ? -kPrimeX : kPrimeX), yp, zp), dx + o0, dy - o0, dz - o0);
-        float fb = fmax_(fmaf(o0, cs, stemA) + flipm(dx, m), 0.0f);
+        float fb = fmaxf(fmaf(o0, cs, stemA) + flipm(dx, m), 0.0f);
         value = fmaf((fb * fb) * (fb * fb), g, value);
     }
     {
         bool m = yn < 0.0f;
         float o0 = flipm((float)kReflect, m);
         float g = grad3(hash(seed, xp, iadd(yp, m ? -kPrimeY : kPrimeY), zp), dx - o0, dy + o0, dz - o0);
-        float fb = fmax_(fmaf(o0, cs, stemA) + flipm(dy, m), 0.0f);
+        float fb = fmaxf(fmaf(o0, cs, stemA) + flipm(dy, m), 0.0f);
         value = fmaf((fb * fb) * (fb * fb), g, value);
     }
     {
         bool m = zn < 0.0f;
         float o0 = flipm((float)kReflect, m);
         float g = grad3(hash(seed, xp, yp, iadd(zp, m ? -kPrimeZ : kPrimeZ)), dx - o0, dy - o0, dz + o0);
-        float fb = fmax_(fmaf(o0, cs, stemA) + flipm(dz, m), 0.0f);
+        float fb = fmaxf(fmaf(o0, cs, stemA) + flipm(dz, m), 0.0f);
         value = fmaf((fb * fb) * (fb * fb), g, value);
     }
     return value;
@@ -509,7 +513,7 @@ FND float supersimplex4(int seed, float x, float y, float z, float w)
         value = (fb * fb) * (fb * fb) * g;
     }
 #define FND_P(m, base, P) iadd(base, (m) ? -(P) : (P))
-#define FND_ACC(fbexpr, gexpr) { float g_ = (gexpr); float fb_ = fmax_((fbexpr), 0.0f); value = fmaf((fb_ * fb_) * (fb_ * fb_), g_, value); }
+#define FND_ACC(fbexpr, gexpr) { float g_ = (gexpr); float fb_ = fmaxf((fbexpr), 0.0f); value = fmaf((fb_ * fb_) * (fb_ * fb_), g_, value); }
     {
         bool m = xyzwn < 0.0f;
         float o = flipm((float)(4 * kU + 1), m);
@@ -1287,7 +1291,7 @@ FND void ws_simplex2(bool gop, int seed, const float* p, float* v)
     float f0 = fmaf(-dx0, dx0, fmaf(-dy0, dy0, (float)kR2));
     float f1 = fmaf(-dx1, dx1, fmaf(-dy1, dy1, (float)kR2));
     float f2 = f0 + fmaf(ud, (float)(-4.0 * (kRoot3 + 2.0) / (kRoot3 + 3.0)), (float)(-2.0 / 3.0));
-    f0 = pow4(fmax_(f0, 0.0f)); f1 = pow4(fmax_(f1, 0.0f)); f2 = pow4(fmax_(f2, 0.0f));
+    f0 = pow4(fmaxf(f0, 0.0f)); f1 = pow4(fmaxf(f1, 0.0f)); f2 = pow4(fmaxf(f2, 0.0f));
     v[0] = 0.0f; v[1] = 0.0f;
     { const float d[2] = {dx0, dy0}; wvec<2>(gop, hash(seed, xp, yp), d, f0, v); }
     { const float d[2] = {dx1, dy1}; wvec<2>(gop, hash(seed, xGEy ? iadd(xp, kPrimeX) : xp, !xGEy ? iadd(yp, kPrimeY) : yp), d, f1, v); }
@@ -1315,7 +1319,7 @@ FND void ws_simplex3(bool gop, int seed, const float* p, float* v)
     float f1 = fmaf(-dz1, dz1, fmaf(-dy1, dy1, fmaf(-dx1, dx1, (float)kR2)));
     float f2 = fmaf(-dz2, dz2, fmaf(-dy2, dy2, fmaf(-dx2, dx2, (float)kR2)));
     float f3 = f0 - (ud + (float)(3.0 / 4.0));
-    f0 = pow4(fmax_(f0, 0.0f)); f1 = pow4(fmax_(f1, 0.0f)); f2 = pow4(fmax_(f2, 0.0f)); f3 = pow4(fmax_(f3, 0.0f));
+    f0 = pow4(fmaxf(f0, 0.0f)); f1 = pow4(fmaxf(f1, 0.0f)); f2 = pow4(fmaxf(f2, 0.0f)); f3 = pow4(fmaxf(f3, 0.0f));
     v[0] = 0.0f; v[1] = 0.0f; v[2] = 0.0f;
     { const float d[3] = {dx0, dy0, dz0}; wvec<3>(gop, hash(seed, xp, yp, zp), d, f0, v); }
     { const float d[3] = {dx1, dy1, dz1};
@@ -1370,7 +1374,7 @@ FND void ws_simplex4(bool gop, int seed, const float* p, float* v)
         if (i < 4) f = fmaf(-d[3], d[3], fmaf(-d[2], d[2], fmaf(-d[1], d[1], fmaf(-d[0], d[0], (float)kR2))));
         else f = f0 + fmaf(ud, (float)(-4.0 * (kRoot5 + 3.0) / (kRoot5 + 5.0)), (float)(-4.0 / 5.0));
         if (i == 0) f0 = f;
-        wvec<4>(gop, hash(seed, c[0], c[1], c[2], c[3]), d, pow4(fmax_(f, 0.0f)), v);
+        wvec<4>(gop, hash(seed, c[0], c[1], c[2], c[3]), d, pow4(fmaxf(f, 0.0f)), v);
     }
 }
 
@@ -1406,7 +1410,7 @@ FND void ws_super2(bool gop, int seed, const float* p, float* v)
         hx = fXY ? hx : iadd(hx, -kPrimeX);
         const float dx = dxB - (fX ? (float)(1 + 2 * kUnskew2) : -1.0f);
         const float dy = fX ? dyB - (float)(2 * kUnskew2) : dyB;
-        const float f = fmax_(fmaf(-dx, dx, fmaf(-dy, dy, (float)kR2)), 0.0f);
+        const float f = fmaxf(fmaf(-dx, dx, fmaf(-dy, dy, (float)kR2)), 0.0f);
         const float d[2] = {dx, dy};
         wvec<2>(gop, hash(seed, hx, fXY ? iadd(yp, kPrimeY) : yp), d, pow4(f), v);
     }
@@ -1415,7 +1419,7 @@ FND void ws_super2(bool gop, int seed, const float* p, float* v)
         hy = fXY ? hy : iadd(hy, -kPrimeY);
         const float dx = fY ? dxB - (float)(2 * kUnskew2) : dxB;
         const float dy = dyB - (fY ? (float)(1 + 2 * kUnskew2) : -1.0f);
-        const float f = fmax_(fmaf(-dx, dx, fmaf(-dy, dy, (float)kR2)), 0.0f);
+        const float f = fmaxf(fmaf(-dx, dx, fmaf(-dy, dy, (float)kR2)), 0.0f);
         const float d[2] = {dx, dy};
         wvec<2>(gop, hash(seed, fXY ? iadd(xp, kPrimeX) : xp, hy), d, pow4(f), v);
     }
@@ -1474,7 +1478,7 @@ FND void ws_super3(bool gop, int seed, const float* p, float* v)
     {   // <1,1,1> or <-1,-1,-1>
         const bool sm = xyzN < 0.0f;
         const float off = flipm((float)(3 * kRU3 + 1), sm);
-        const float fb = fmax_(fmaf(off, cs, stemA), 0.0f);
+        const float fb = fmaxf(fmaf(off, cs, stemA), 0.0f);
         int c[3];
         float d[3];
 #pragma unroll
@@ -1486,7 +1490,7 @@ FND void ws_super3(bool gop, int seed, const float* p, float* v)
     for (int m = 2; m >= 0; --m) {
         const bool sm = xyzN < n[m];
         const float off0 = flipm((float)(2 * kRU3), sm);
-        const float fb = fmin_(flipm(dB[m], sm) - stemB, 0.0f);
+        const float fb = fminf(flipm(dB[m], sm) - stemB, 0.0f);
         int c[3];
         float d[3];
 #pragma unroll
@@ -1501,7 +1505,7 @@ FND void ws_super3(bool gop, int seed, const float* p, float* v)
     for (int a = 0; a < 3; ++a) {
         const bool sm = n[a] < 0.0f;
         const float off0 = flipm((float)kRU3, sm);
-        const float fb = fmax_(fmaf(off0, cs, stemA) + flipm(dB[a], sm), 0.0f);
+        const float fb = fmaxf(fmaf(off0, cs, stemA) + flipm(dB[a], sm), 0.0f);
         int c[3];
         float d[3];
 #pragma unroll
@@ -1598,19 +1602,19 @@ FND void ws_super4(bool gop, int seed, const float* p, float* v)
         if (cnt == 4) {
             off1 = flipm((float)(4 * kU4 + 1), sm);
             off0 = off1;
-            fb = fmax_(fmaf(off1, cs, stemA), 0.0f);
+            fb = fmaxf(fmaf(off1, cs, stemA), 0.0f);
         } else if (cnt == 3) {
             off1 = flipm((float)(3 * kU4 + 1), sm);
             off0 = flipm((float)(3 * kU4), sm);
-            fb = fmax_(fmaf(off1, cs, stemB) - flipm(dB[missing], sm), 0.0f);
+            fb = fmaxf(fmaf(off1, cs, stemB) - flipm(dB[missing], sm), 0.0f);
         } else if (cnt == 1) {
             off1 = flipm((float)(kU4 + 1), sm);
             off0 = flipm((float)kU4, sm);
-            fb = fmax_(fmaf(off0, cs, stemA) + flipm(dB[a], sm), 0.0f);
+            fb = fmaxf(fmaf(off0, cs, stemA) + flipm(dB[a], sm), 0.0f);
         } else {
             off1 = flipm((float)(2 * kU4 + 1), sm);
             off0 = flipm((float)(2 * kU4), sm);
-            fb = fmax_(fmaf(off0, cs, stemB) + flipm(dB[a] + dB[bb & 3], sm), 0.0f);
+            fb = fmaxf(fmaf(off0, cs, stemB) + flipm(dB[a] + dB[bb & 3], sm), 0.0f);
         }
         int c[4];
         float d[4];
