@@ -902,7 +902,10 @@ FND float cellular_value(int seed, const float* pin, const CellParams& cp, int v
     return cvtf(sel);
 }
 
-template <int D, typename MinkF = NoMink>
+// NS = sorted distance slots kept (the reference keeps 4).  Slot i only ever depends on
+// slots i and i - 1, so a caller that reads slots below NS alone may keep fewer: the
+// specialised kernels pass max(index0, index1) + 1; the other slots stay +inf.
+template <int D, int NS = 4, typename MinkF = NoMink>
 FND void cellular_distances(int seed, const float* pin, const CellParams& cp, float* dist, const MinkF& mink = MinkF())
 {
     float p[D];
@@ -929,7 +932,7 @@ FND void cellular_distances(int seed, const float* pin, const CellParams& cp, fl
         float nd = distance<D>(cp.distFunc, false, off, mk);
         if (cp.sizeActive) nd *= size_factor<D>(h, cp.sizeJitter);
 #pragma unroll
-        for (int i = 3; i > 0; i--) dist[i] = fmax_(fmin_(dist[i], nd), dist[i - 1]);
+        for (int i = NS - 1; i > 0; i--) dist[i] = fmax_(fmin_(dist[i], nd), dist[i - 1]);
         dist[0] = fmin_(dist[0], nd);
     });
 }

@@ -157,7 +157,8 @@ void emit_eval(const CompiledProgram& prog, const std::string& name, std::ostrin
             break;
         case FN_OP_CELL_DIST:
             o << "        const float pp[" << D << "] = " << pos(I.a) << ";\n        " << cellp(3) << "\n";
-            o << "        float dist[4]; fnd::cellular_distances<" << D << ">(" << sd << ", pp, cp, dist" << mk(I) << ");\n";
+            o << "        float dist[4]; fnd::cellular_distances<" << D << ", "
+              << std::max((I.aux >> 4) & 3, (I.aux >> 8) & 3) + 1 << ">(" << sd << ", pp, cp, dist" << mk(I) << ");\n";
             o << "        float nmax; const float v = fnd::cellular_return<" << D << ">(dist, cp.distFunc, " << ((I.aux >> 4) & 3) << ", "
               << ((I.aux >> 8) & 3) << ", " << ((I.aux >> 12) & 7) << ", nmax);\n";
             o << "        " << r(I.dst) << " = fnd::scale_out(v, 0.0f, " << p(1) << ", " << p(2) << ");\n";

@@ -5,6 +5,8 @@ for bit on every driver, alone and in batches."""
 import numpy as np
 import pytest
 
+from oracle.oracle import OracleTree
+from oracle.tree import N
 from tests import chunkmix, trees
 from tests.parity import assert_parity
 from tests.test_gpu_parity import COMPOSITE, GRID, SINGLE
@@ -128,3 +130,23 @@ def test_jit_batch_matches_interpreter(gpu):
     for c, x, y, mx, my in zip(chunks, ja, ia, jm, im):
         assert np.array_equal(x.view(np.uint32), y.view(np.uint32)), c
         assert np.array_equal(mx.view(np.uint32), my.view(np.uint32)), c
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("i0, i1", [(0, 0), (0, 3), (2, 1), (3, 3), (1, 2)])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_specialised_cellular_distance_slots(gpu, i0, i1, dim):
+    """The specialised kernels keep only the sorted distance slots up to max(i0, i1); every
+    index pair must still match the oracle."""
+    fn = gpu
+    root = N("CellularDistance", Feature_Scale=7.0, Return_Type="Index0Sub1")
+    root.set("Distance Index 0", i0)
+    root.set("Distance Index 1", i1)
+    root.set("Distance Function", "Euclidean Squared")
+    node = trees.to_product(root)
+    fn.jit_compile([(node, dim)])
+    count = (40, 24, 9)[:dim]
+    offset = (-13.0, 5.5, 2.0)[:dim]
+    g, gmm = node.gen_uniform_grid(offset, count, (1.0,) * dim, 99)
+    o, omm = OracleTree(root).grid(offset, count, (1.0,) * dim, 99)
+    assert_parity(g, gmm, o, omm, label=f"{dim}D indices {i0},{i1}")
