@@ -79,24 +79,25 @@ FND float grad3(int h, float x, float y, float z)
     const bool b3 = (h & 8) != 0, b2 = (h & 4) != 0, x_case = (h & 9) == 8;
     const float u = b3 ? y : x;
     const float v = b2 ? (x_case ? x : z) : (b3 ? z : y);
-    return flip(u, h << 31) + flip(v, (h >> 1) << 31);
+    return flip(u, h << 31) + flip(v, h << 30);
 }
 // GetGradientDotPerlin 2D, portable branch (Utils.inl:181-190)
 FND float grad2(int h, float x, float y)
 {
     x = flip(x, h << 31);
-    y = flip(y, (h >> 1) << 31);
+    y = flip(y, h << 30);
     bool s = (h << 29) < 0;
     return fmaf(1.0f + (float)kRoot2, s ? y : x, s ? x : y);
 }
 // GetGradientDotPerlin 4D, portable branch (Utils.inl:205-218)
 FND float grad4(int h, float x, float y, float z, float w)
 {
-    int p = h & (3 << 3);
-    float a = p > 0 ? x : y;
-    float b = (h << 27) < 0 ? y : z;
-    float c = p > (2 << 3) ? z : w;
-    return (flip(a, h << 31) + flip(b, (h >> 1) << 31)) + flip(c, (h >> 2) << 31);
+    // h & 24 > 0: bit 3 or 4;  (h << 27) < 0: bit 4;  h & 24 > 16: bits 3 and 4
+    const bool any34 = (h & 24) != 0, b4 = (h & 16) != 0, both34 = (h & 24) == 24;
+    const float a = any34 ? x : y;
+    const float b = b4 ? y : z;
+    const float c = both34 ? z : w;
+    return (flip(a, h << 31) + flip(b, h << 30)) + flip(c, h << 29);
 }
 
 // Sin / Cos: Cody-Waite reduction by pi/2 (three-part constant), Taylor
