@@ -9,6 +9,8 @@
 // and only then swaps it in under a lock, so a generation or serving thread that acquires the
 // tree always gets a fully built one.  The swapped-out tree is released by reference count:
 // requests already submitted with it (the server holds a reference per request) finish with it.
+#include <cuda_runtime.h>
+
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -36,6 +38,7 @@ struct LiveTree {
     std::mutex update_mu;                 // one update at a time
     std::vector<char> buf = std::vector<char>(64 * 1024);
     std::thread poller;
+    int device = 0;                       // the creating thread's device, used by the poller
     std::mutex stop_mu;
     std::condition_variable stop_cv;
     bool stop = false;
@@ -110,6 +113,7 @@ int update(LiveTree* lt)
 
 void poll_loop(LiveTree* lt, int period_ms)
 {
+    cudaSetDevice(lt->device);
     std::unique_lock<std::mutex> lk(lt->stop_mu);
     while (!lt->stop) {
         lk.unlock();
@@ -132,6 +136,7 @@ void* fnLiveTreeCreate(void* ipc, const char* initialEncodedTree, const int* dim
     }
     LiveTree* lt = new LiveTree();
     lt->ipc = ipc;
+    cudaGetDevice(&lt->device);
     for (int i = 0; i < count; ++i) {
         if (dimensions[i] < 2 || dimensions[i] > 4) {
             delete lt;
