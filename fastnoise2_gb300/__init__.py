@@ -106,6 +106,9 @@ def _declare(L):
         "fnGetBatchInfo": (c_int, [vp]),
         "fnJitCheck": (c_int, [vp, vp, c_int, ctypes.POINTER(c_int)]),
         "fnSetJitEnabled": (c_int, [c_int]),
+        "fnSetAutoSpecialise": (c_int, [c_int]),
+        "fnAutoSpecialiseWait": (c_int, [c_int]),
+        "fnJitIsSpecialised": (c_int, [vp, c_int]),
         "fnGenUniformGrid3DDeviceNoAlloc": (c_int, [vp, vp, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, vp, vp]),
         "fnGenUniformGrid4DDevice": (c_int, [vp, vp] + [c_float] * 4 + [c_int] * 4 + [c_float] * 4 + [c_int, vp, vp]),
         "fnGenPositionArray2DDevice": (c_int, [vp, vp, c_int, vp, vp, c_float, c_float, c_int, vp, vp]),
@@ -412,6 +415,23 @@ def batch_info() -> dict:
     if lib().fnGetBatchInfo(ctypes.byref(info)) != 0:
         _check()
     return {k: getattr(info, k) for k, _ in info._fields_}
+
+
+def set_auto_specialise(uses: int) -> int:
+    """Interpreter runs after which a tree is specialised in the background (0 = off); returns the old value."""
+    return lib().fnSetAutoSpecialise(int(uses))
+
+
+def auto_specialise_wait(timeout_ms: int = -1) -> bool:
+    """True once no background specialisation is queued or running."""
+    return lib().fnAutoSpecialiseWait(int(timeout_ms)) == 0
+
+
+def is_specialised(node: "Node", dim: int) -> bool:
+    rc = lib().fnJitIsSpecialised(node.handle, int(dim))
+    if rc < 0:
+        _check()
+    return rc == 1
 
 
 def set_jit_enabled(on: bool) -> bool:

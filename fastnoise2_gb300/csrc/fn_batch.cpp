@@ -192,6 +192,14 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         for (size_t i = 0; i < n; ++i) fits = fits && items[i].args.total < (1ll << 32);
         jit = fits && jit_batch_kernels(hashes, kernels);
     }
+    if (!jit) {                                     // interpreter batch: count a use of each program
+        std::vector<uint64_t> seen;
+        for (size_t i = 0; i < n; ++i)
+            if (std::find(seen.begin(), seen.end(), progs[i].hash) == seen.end()) {
+                seen.push_back(progs[i].hash);
+                jit_note_interpreted(progs[i].host);
+            }
+    }
     if (!jit)
         for (size_t i = 0; i < n; ++i)
             if (progs[i].host->needs_specialisation() && items[i].args.total > 0) {

@@ -64,6 +64,7 @@ cudaError_t launch_points(const DeviceProgram& prog, const PointArgs& args, floa
     // A tree with per-cell sub-programs cannot run on the interpreter; with no
     // points there is nothing to evaluate and the interpreter only writes min/max.
     if (prog.host->needs_specialisation() && args.total > 0) return cudaErrorNotSupported;
+    if (args.total > 0) jit_note_interpreted(prog.host);      // may queue a background specialisation
     return launch_interpreter(prog.dptr, prog.bytes, args, out, work, dminmax, stream);
 }
 
@@ -1194,6 +1195,26 @@ int fnJitCompile(const void* const* nodes, const int* dims, int count)
     std::string err;
     if (!jit_build(progs, err)) { set_error(FN_ERR_COMPILE, err); return FN_ERR_COMPILE; }
     return FN_OK;
+}
+
+int fnSetAutoSpecialise(int uses) { return jit_set_auto_threshold(uses); }
+
+int fnAutoSpecialiseWait(int timeoutMs)
+{
+    clear_error();
+    if (jit_auto_wait(timeoutMs)) return FN_OK;
+    set_error(FN_ERR_TIMEOUT, "background specialisation still running");
+    return FN_ERR_TIMEOUT;
+}
+
+int fnJitIsSpecialised(const void* node, int dimension)
+{
+    clear_error();
+    if (!node || dimension < 2 || dimension > 4) { set_error(FN_ERR_ARG, "invalid node or dimension"); return FN_ERR_ARG; }
+    CompiledProgram prog;
+    std::string err;
+    if (!compile_program(N(node), dimension, prog, err)) { set_error(FN_ERR_COMPILE, err); return FN_ERR_COMPILE; }
+    return jit_is_specialised(prog.hash) ? 1 : 0;
 }
 
 int fnJitCheck(const void* const* nodes, const int* dims, int count, int* cubinBytes)

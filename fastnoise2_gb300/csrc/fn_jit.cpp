@@ -6,6 +6,9 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <deque>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -14,6 +17,7 @@
 #include <sstream>
 #include <thread>
 #include <unordered_map>
+#include <unordered_set>
 
 #include "fn_kernels.cuh"
 #include "fn_runtime.h"
@@ -550,6 +554,14 @@ bool jit_batch_kernels(const std::vector<uint64_t>& hashes, std::vector<cudaKern
     return true;
 }
 
+namespace {
+bool is_built(uint64_t hash)
+{
+    std::lock_guard<std::mutex> lk(g_jit_mu);
+    return g_kernels.count(hash) && g_batch_kernels.count(hash);
+}
+}  // namespace
+
 bool jit_ensure(const CompiledProgram* prog, std::string& error)
 {
     if (!prog->needs_specialisation()) return true;
@@ -569,6 +581,112 @@ bool jit_ensure(const CompiledProgram* prog, std::string& error)
 
 void jit_set_enabled(bool on) { g_enabled.store(on); }
 bool jit_enabled() { return g_enabled.load(); }
+
+// ---------------------------------------------------------------- automatic specialisation
+namespace {
+
+struct AutoJit {
+    std::mutex mu;
+    std::condition_variable cv, idle_cv;
+    std::unordered_map<uint64_t, int> uses;        // interpreter launches per program hash
+    std::unordered_set<uint64_t> queued;           // handed to the worker once, whatever the outcome
+    std::deque<std::pair<CompiledProgram, int>> work;   // program copy, device
+    int running = 0;
+    int threshold = -1;                            // -1 = not read from the environment yet
+    bool stop = false;
+    std::thread worker;
+    ~AutoJit()
+    {
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            stop = true;
+            work.clear();
+        }
+        cv.notify_all();
+        if (worker.joinable()) worker.join();
+    }
+};
+
+AutoJit& auto_jit()
+{
+    static AutoJit a;
+    return a;
+}
+
+int threshold_locked(AutoJit& a)
+{
+    if (a.threshold < 0) {
+        const char* env = std::getenv("FASTNOISE_AUTO_SPECIALISE");
+        a.threshold = env && *env ? std::max(0, std::atoi(env)) : 4;
+    }
+    return a.threshold;
+}
+
+void auto_worker()
+{
+    AutoJit& a = auto_jit();
+    std::unique_lock<std::mutex> lk(a.mu);
+    for (;;) {
+        a.cv.wait(lk, [&] { return a.stop || !a.work.empty(); });
+        if (a.stop) return;
+        std::pair<CompiledProgram, int> job = std::move(a.work.front());
+        a.work.pop_front();
+        ++a.running;
+        lk.unlock();
+        cudaSetDevice(job.second);
+        std::string err;
+        if (!is_built(job.first.hash)) jit_build({&job.first}, err);   // a failure leaves the interpreter in use
+        lk.lock();
+        --a.running;
+        if (a.work.empty() && a.running == 0) a.idle_cv.notify_all();
+    }
+}
+
+}  // namespace
+
+bool jit_is_specialised(uint64_t hash)
+{
+    std::lock_guard<std::mutex> lk(g_jit_mu);
+    return g_kernels.count(hash) && g_batch_kernels.count(hash);
+}
+
+void jit_note_interpreted(const CompiledProgram* prog)
+{
+    if (!prog || !g_enabled.load(std::memory_order_relaxed)) return;
+    AutoJit& a = auto_jit();
+    std::lock_guard<std::mutex> lk(a.mu);
+    const int t = threshold_locked(a);
+    if (t == 0 || a.stop || a.queued.count(prog->hash)) return;
+    if (++a.uses[prog->hash] < t) return;
+    a.queued.insert(prog->hash);
+    a.uses.erase(prog->hash);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    a.work.emplace_back(*prog, dev);
+    if (!a.worker.joinable()) a.worker = std::thread(auto_worker);
+    a.cv.notify_one();
+}
+
+int jit_set_auto_threshold(int uses)
+{
+    AutoJit& a = auto_jit();
+    std::lock_guard<std::mutex> lk(a.mu);
+    const int was = threshold_locked(a);
+    a.threshold = std::max(0, uses);
+    return was;
+}
+
+bool jit_auto_wait(int timeout_ms)
+{
+    AutoJit& a = auto_jit();
+    std::unique_lock<std::mutex> lk(a.mu);
+    auto idle = [&] { return a.work.empty() && a.running == 0; };
+    if (timeout_ms < 0) {
+        a.idle_cv.wait(lk, idle);
+        return true;
+    }
+    return a.idle_cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), idle);
+}
 
 bool jit_launch(uint64_t hash, const PointArgs& args, float* out, MinMaxWork* work, float* dminmax, cudaStream_t stream,
                 cudaError_t& err)

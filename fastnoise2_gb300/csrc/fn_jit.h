@@ -65,6 +65,16 @@ bool jit_ensure(const CompiledProgram* prog, std::string& error);
 void jit_set_enabled(bool on);
 bool jit_enabled();
 
+// Automatic specialisation: the interpreter paths report each launch of a program
+// here; once a program has run `threshold` times on the interpreter it is queued
+// for a background NVRTC build (one worker thread), and later launches find its
+// specialised kernels.  threshold 0 = off; the default comes from the environment
+// variable FASTNOISE_AUTO_SPECIALISE (a number, 0 = off), else 4.
+void jit_note_interpreted(const CompiledProgram* prog);
+int jit_set_auto_threshold(int uses);              // returns the previous threshold
+bool jit_auto_wait(int timeout_ms);                // true when no build is queued or running
+bool jit_is_specialised(uint64_t hash);
+
 // Compile NVRTC source for sm_103a to a cubin (host only; used by tests).
 bool jit_compile_cubin(const std::string& src, std::vector<char>& cubin, std::string& log);
 

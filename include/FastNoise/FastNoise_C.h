@@ -349,6 +349,18 @@ FASTNOISE_API void fnLiveTreeDelete(void* live);
  * Kernels of earlier calls stay loaded (a tree specialised again gets its new kernels).
  * Returns FN_OK or FN_ERR_*. */
 FASTNOISE_API int fnJitCompile(const void* const* nodes, const int* dimensions, int count);
+/* Automatic specialisation: a tree that has run `uses` times on the program interpreter (per
+ * dimensionality; host, device, batch and server calls all count) is specialised on a
+ * background thread, and its later calls use the specialised kernels -- the same results,
+ * without a call to fnJitCompile.  0 turns it off; the default is 4, or the number in the
+ * environment variable FASTNOISE_AUTO_SPECIALISE.  Returns the previous setting. */
+FASTNOISE_API int fnSetAutoSpecialise(int uses);
+/* Wait until no background specialisation is queued or running (timeoutMs < 0: no limit);
+ * FN_OK, or FN_ERR_TIMEOUT. */
+FASTNOISE_API int fnAutoSpecialiseWait(int timeoutMs);
+/* 1 when the tree's specialised kernels for `dimension` are loaded, 0 when calls run on the
+ * interpreter, FN_ERR_* on error. */
+FASTNOISE_API int fnJitIsSpecialised(const void* node, int dimension);
 /* Generate and compile the module source with NVRTC without loading it (no GPU needed);
  * *cubinBytes (may be NULL) receives the size of the compiled code. */
 FASTNOISE_API int fnJitCheck(const void* const* nodes, const int* dimensions, int count, int* cubinBytes);

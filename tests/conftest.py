@@ -7,6 +7,10 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+# Tests choose the kernel tier they exercise (fnJitCompile / fnSetJitEnabled); automatic
+# background specialisation stays off unless a test turns it on (tests/test_jit.py does).
+os.environ.setdefault("FASTNOISE_AUTO_SPECIALISE", "0")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA device (runs on the GB300 box)")

@@ -150,3 +150,35 @@ def test_specialised_cellular_distance_slots(gpu, i0, i1, dim):
     g, gmm = node.gen_uniform_grid(offset, count, (1.0,) * dim, 99)
     o, omm = OracleTree(root).grid(offset, count, (1.0,) * dim, 99)
     assert_parity(g, gmm, o, omm, label=f"{dim}D indices {i0},{i1}")
+
+
+@pytest.mark.gpu
+def test_automatic_specialisation(gpu):
+    """A tree used repeatedly on the interpreter is specialised in the background; its calls
+    then run the specialised kernels with the same results."""
+    fn = gpu
+    root = N("FractalRidged", Source=N("Value", Feature_Scale=23.0), Octaves=3)   # a tree no other test specialises
+    node = trees.to_product(root)
+    off, cnt, st = (3.0, -7.0, 11.0), (48, 40, 36), (1.0, 1.0, 1.0)
+    old = fn.set_auto_specialise(3)
+    try:
+        assert not fn.is_specialised(node, 3)
+        first, fmm = node.gen_uniform_grid(off, cnt, st, 5)
+        for _ in range(3):
+            node.gen_uniform_grid(off, cnt, st, 5)
+        assert fn.auto_specialise_wait(120000)
+        assert fn.is_specialised(node, 3)
+        again, amm = node.gen_uniform_grid(off, cnt, st, 5)
+        assert np.array_equal(first.view(np.uint32), again.view(np.uint32)) and fmm == amm
+        o, omm = OracleTree(root).grid(off, cnt, st, 5)
+        assert_parity(again, amm, o, omm, label="auto-specialised")
+    finally:
+        fn.set_auto_specialise(old)
+
+
+def test_automatic_specialisation_controls(native):
+    fn = native
+    old = fn.set_auto_specialise(0)
+    assert fn.set_auto_specialise(7) == 0
+    assert fn.set_auto_specialise(old) == 7
+    assert fn.auto_specialise_wait(0)
