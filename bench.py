@@ -476,15 +476,16 @@ def mesh_tree():
 
 
 def run_mesh(a, rank, world, local):
-    """fnBuildChunkMeshBloxel (130^3 densities) or fnBuildChunkMeshDmc (132^3 densities) on the
-    Node Editor's chunk size, 128^3 voxels, a row of 8 chunks across the surface per step."""
+    """fnBuildChunkMeshesBloxel (130^3 densities per chunk) or fnBuildChunkMeshesDmc (132^3) on
+    the Node Editor's chunk size, 128^3 voxels: a row of 8 chunks across the surface per step, in
+    one multi-chunk call; the same chunks one synchronous call each are reported beside it."""
     import torch
     import fastnoise2_gb300 as fn
     from tests.trees import to_product
     size, chunks = 128, 8
     dmc = a.workload == "mesh-dmc-128"
     build = fn.build_chunk_mesh_dmc if dmc else fn.build_chunk_mesh_bloxel
-    api = "fnBuildChunkMeshDmc" if dmc else "fnBuildChunkMeshBloxel"
+    api = "fnBuildChunkMeshesDmc" if dmc else "fnBuildChunkMeshesBloxel"
     apron = 4 if dmc else 2
     node = to_product(mesh_tree())
     if a.kernels == "jit":
@@ -492,19 +493,25 @@ def run_mesh(a, rank, world, local):
     else:
         fn.set_jit_enabled(False)
     dev = torch.device("cuda", local)
-    vcap, icap = 24 << 20, 36 << 20
-    verts = torch.empty(vcap * 4, dtype=torch.float32, device=dev)
-    idx = torch.empty(icap, dtype=torch.int32, device=dev)
+    vcap, icap = 2 << 20, 4 << 20                       # per chunk: a 128^3 surface chunk needs ~0.5 M / 0.7 M
+    bufs = [(torch.empty(vcap * 4, dtype=torch.float32, device=dev), torch.empty(icap, dtype=torch.int32, device=dev))
+            for _ in range(chunks)]
+    ptrs = [(v.data_ptr(), vcap, i.data_ptr(), icap) for v, i in bufs]
     stream = torch.cuda.current_stream(dev)
     positions = [(size * (k - chunks // 2), -size // 2, size * (rank % 4)) for k in range(chunks)]
     faces = []
 
     def step():
-        for p in positions:
-            r = build(node, size, p, 1337 + rank, 0.0, False, verts.data_ptr(), vcap, idx.data_ptr(), icap, stream.cuda_stream)
+        res = fn.build_chunk_meshes("dmc" if dmc else "bloxel", node, size, positions, 1337 + rank, 0.0, False, ptrs,
+                                    stream.cuda_stream)
+        for r in res:
             if not r["fits"]:
                 raise RuntimeError(f"{api}: mesh buffers too small ({r['vertexCount']} vertices)")
             faces.append(r["indexCount"] // 6)
+
+    def step_single():
+        for p, (vp, vc, ip, ic) in zip(positions, ptrs):
+            build(node, size, p, 1337 + rank, 0.0, False, vp, vc, ip, ic, stream.cuda_stream)
 
     for _ in range(max(a.warmup, 3)):
         step()
@@ -528,6 +535,16 @@ def run_mesh(a, rank, world, local):
     ms_max = allmax(ms, world)
     voxels = chunks * size ** 3
     value = voxels * world / (ms_max * 1e-3) / 1e6
+    # the same chunks, one synchronous single-chunk call each (for comparison)
+    step_single()
+    torch.cuda.synchronize(dev)
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for _ in range(a.steps):
+        step_single()
+    s1.record(stream)
+    torch.cuda.synchronize(dev)
+    single_ms = s0.elapsed_time(s1) / a.steps
     if rank != 0:
         return
     line = {
@@ -538,14 +555,16 @@ def run_mesh(a, rank, world, local):
                    "points_per_step": voxels, "densities_per_chunk": (size + apron) ** 3,
                    ("quads_per_chunk" if dmc else "faces_per_chunk"): statistics.mean(faces) if faces else 0,
                    "path": api + ": densities (" + ("specialised kernel" if a.kernels == "jit" else "interpreter")
-                           + (") + count/scan/vertex/quad mesher" if dmc else ") + count/scan/emit mesher")
-                           + ", synchronous per chunk",
+                           + (") + cases/count/scan/vertex/quad mesher" if dmc else ") + count/scan/emit mesher")
+                           + f", {chunks} chunks per call over 4 internal streams",
                    "l2": f"densities of a chunk ({(size + apron) ** 3 * 4 / 1e6:.1f} MB) stay in L2 between generation and meshing"},
         "e2e": {"value": value, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": (24 if dmc else 20) * chunks,
                 "api": api + " (device mesh buffers; counts, heights and min/max read back per chunk)"},
+        "single_chunk_calls": {"value": voxels / (single_ms * 1e-3) / 1e6, "unit": "Mpoints/s", "ms_per_step": single_ms,
+                               "api": api.replace("Meshes", "Mesh") + ", one synchronous call per chunk"},
         "cpu_baseline": None,
         "clocks": clocks,
-        # densities, count, 3 scan kernels, then emit (bloxel) or vertices + quads (dmc)
+        # densities, then cases, count, 2 scan kernels, vertices, quads (dmc) or count, 3 scan kernels, emit (bloxel)
         "gpu_launches": a.steps * chunks * (7 if dmc else 6),
     }
     print(json.dumps(line))

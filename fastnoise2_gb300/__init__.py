@@ -102,6 +102,8 @@ def _declare(L):
         "fnJitCompile": (c_int, [vp, vp, c_int]),
         "fnBuildChunkMeshBloxel": (c_int, [vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, vp, vp]),
         "fnBuildChunkMeshDmc": (c_int, [vp, c_int, c_int, c_int, c_int, c_int, c_float, c_int, vp, vp]),
+        "fnBuildChunkMeshesDmc": (c_int, [vp, c_int, c_int, vp, c_int, c_float, c_int, vp, vp]),
+        "fnBuildChunkMeshesBloxel": (c_int, [vp, c_int, c_int, vp, c_int, c_float, c_int, vp, vp]),
         "fnBuildChunkMeshHeightmap": (c_int, [vp, c_int, c_int, c_int, c_int, c_float, vp, vp]),
         "fnGetBatchInfo": (c_int, [vp]),
         "fnJitCheck": (c_int, [vp, vp, c_int, ctypes.POINTER(c_int)]),
@@ -294,6 +296,25 @@ def build_chunk_mesh_dmc(node: "Node", size: int, pos, seed: int, iso: float, up
     rc = lib().fnBuildChunkMeshDmc(node.handle, int(size), int(pos[0]), int(pos[1]), int(pos[2]), int(np.int32(seed)),
                                    float(iso), 1 if up_axis_z else 0, ctypes.byref(m), stream or None)
     return _mesh(rc, m)
+
+
+def build_chunk_meshes(kind: str, node: "Node", size: int, positions, seed: int, iso: float, up_axis_z: bool, buffers,
+                       stream: int = 0) -> list:
+    """fnBuildChunkMeshesDmc / fnBuildChunkMeshesBloxel (kind "dmc" / "bloxel"): many chunks in one call.
+    buffers: one (vertices_ptr, vertex_capacity, indices_ptr, index_capacity) per chunk."""
+    n = len(positions)
+    pos = (ctypes.c_int * (3 * n))(*[int(v) for p in positions for v in p])
+    meshes = (ChunkMesh * n)(*[ChunkMesh(b[0] or None, b[2] or None, b[1], b[3], 0, 0, 0.0, 0.0) for b in buffers])
+    fnc = lib().fnBuildChunkMeshesDmc if kind == "dmc" else lib().fnBuildChunkMeshesBloxel
+    rc = fnc(node.handle, int(size), n, pos, int(np.int32(seed)), float(iso), 1 if up_axis_z else 0, meshes, stream or None)
+    if rc != 0 and rc != -4:
+        _check()
+    out = []
+    for m in meshes:
+        r = m.result()
+        r["fits"] = m.vertexCount <= m.vertexCapacity and m.indexCount <= m.indexCapacity
+        out.append(r)
+    return out
 
 
 def build_chunk_mesh_heightmap(node: "Node", size: int, pos, seed: int, multiplier: float, vertices_ptr: int,

@@ -311,6 +311,15 @@ FASTNOISE_API int fnBuildChunkMeshBloxel(const void* node, int size, int posX, i
  * order; size <= 256.  Vertices and indices are written only when both fit. */
 FASTNOISE_API int fnBuildChunkMeshDmc(const void* node, int size, int posX, int posY, int posZ, int seed,
                                       float isoSurface, int upAxisZ, fnChunkMesh* mesh, void* stream);
+/* Many chunks of one tree in one call (what the editor's mesh worker threads do chunk by
+ * chunk): positions holds (x, y, z) per chunk, meshes one fnChunkMesh per chunk, each with its
+ * own buffers.  The chunks run on several internal streams, ordered after earlier work on
+ * `stream`; the call returns when every chunk is done.  FN_ERR_CAPACITY when any chunk's
+ * buffers were too small (that chunk's counts are filled; the others are complete). */
+FASTNOISE_API int fnBuildChunkMeshesBloxel(const void* node, int size, int count, const int* positions, int seed,
+                                           float isoSurface, int upAxisZ, fnChunkMesh* meshes, void* stream);
+FASTNOISE_API int fnBuildChunkMeshesDmc(const void* node, int size, int count, const int* positions, int seed,
+                                        float isoSurface, int upAxisZ, fnChunkMesh* meshes, void* stream);
 /* BuildHeightMap2DMesh (MeshNoisePreview.cpp:956-1004): size^2 quads of a 2D heightmap at
  * (posX, posZ), heights = density * heightMultiplier; size <= 8192. */
 FASTNOISE_API int fnBuildChunkMeshHeightmap(const void* node, int size, int posX, int posZ, int seed,

@@ -148,3 +148,37 @@ def test_dmc_reports_capacity(gpu, torch_cuda):
     ov, oi, oair, osolid, _ = oracle_dmc(surface_tree(), 16, (32, -8, 16), 1337, 0.0, False)
     assert not res["fits"] and res["vertexCount"] == len(ov) and res["indexCount"] == len(oi)
     assert (res["minAirY"], res["maxSolidY"]) == (float(oair), float(osolid))
+
+
+@pytest.mark.parametrize("kind", ["dmc", "bloxel"])
+def test_many_chunks_match_single_calls(gpu, torch_cuda, kind):
+    """fnBuildChunkMeshes*: chunks spread over internal streams give each chunk exactly the
+    single-call mesh; a chunk with too small buffers reports its counts, the others complete."""
+    fn, torch = gpu, torch_cuda
+    size = 16
+    positions = [(16 * k - 40, -8 + 4 * (k % 3), 16 * (k % 2)) for k in range(7)]
+    node = trees.to_product(surface_tree())
+    vcap, icap = (size + 1) ** 3 * 4, size ** 3 * 18
+    single = {"dmc": fn.build_chunk_mesh_dmc, "bloxel": fn.build_chunk_mesh_bloxel}[kind]
+    bufs, tensors = [], []
+    for k in range(len(positions)):
+        v = torch.zeros(vcap * 4, dtype=torch.float32, device="cuda")
+        i = torch.zeros(icap, dtype=torch.int32, device="cuda")
+        small = k == 3
+        bufs.append((v.data_ptr(), 8 if small else vcap, i.data_ptr(), 12 if small else icap))
+        tensors.append((v, i))
+    res = fn.build_chunk_meshes(kind, node, size, positions, 1337, 0.0, False, bufs)
+    for k, p in enumerate(positions):
+        v1 = torch.zeros(vcap * 4, dtype=torch.float32, device="cuda")
+        i1 = torch.zeros(icap, dtype=torch.int32, device="cuda")
+        ref = single(node, size, p, 1337, 0.0, False, v1.data_ptr(), vcap, i1.data_ptr(), icap)
+        r = res[k]
+        assert (r["vertexCount"], r["indexCount"], r["minAirY"], r["maxSolidY"], r["minMax"]) == \
+               (ref["vertexCount"], ref["indexCount"], ref["minAirY"], ref["maxSolidY"], ref["minMax"]), k
+        if k == 3:
+            assert not r["fits"]
+            continue
+        nv, ni = ref["vertexCount"], ref["indexCount"]
+        v, i = tensors[k]
+        assert torch.equal(v[:nv * 4].view(torch.int32), v1[:nv * 4].view(torch.int32)), k
+        assert torch.equal(i[:ni], i1[:ni]), k
