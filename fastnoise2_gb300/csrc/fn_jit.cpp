@@ -278,7 +278,7 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
     call += ")";
 
     auto kernel = [&](const char* name, const std::string& prologue, const std::string& position) {
-        o << "extern \"C\" __global__ void __launch_bounds__(256, 2) " << name << "_" << k
+        o << "extern \"C\" __global__ void __launch_bounds__(256, 4) " << name << "_" << k
           << "(fn::PointArgs A, float* __restrict__ out, fn::MinMaxWork* work, float* dminmax, unsigned ppl)\n{\n"
           << "    __shared__ float4 stage[8][32];\n"
           << "    __shared__ float smn[8], smx[8];\n"
@@ -373,7 +373,7 @@ void emit_batch(const std::vector<const CompiledProgram*>& progs, std::ostringst
     // one persistent kernel per tree: each gets the register allocation its own
     // code needs, and the trees of a batch run as concurrent kernels
     for (size_t k = 0; k < progs.size(); ++k) {
-        o << "extern \"C\" __global__ void __launch_bounds__(256, 2) fnjit_batch_" << k
+        o << "extern \"C\" __global__ void __launch_bounds__(256, 4) fnjit_batch_" << k
           << "(fn::BatchHeader* hdr, const fn::BatchRequest* __restrict__ reqs, fn::BatchState* states,\n"
              "    const uint2* __restrict__ items, fn::BatchGroup* grp)\n{\n"
              "    __shared__ unsigned int s_item;\n"
