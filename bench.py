@@ -251,6 +251,7 @@ def run_reference(a):
 def run_chunkmix(a, rank, world, local):
     import torch
     import fastnoise2_gb300 as fn
+    fn.set_auto_specialise(0)              # the kernel tier is chosen explicitly (--kernels)
     from tests import chunkmix, trees
 
     dev = torch.device("cuda", local)
@@ -481,6 +482,7 @@ def run_mesh(a, rank, world, local):
     one multi-chunk call; the same chunks one synchronous call each are reported beside it."""
     import torch
     import fastnoise2_gb300 as fn
+    fn.set_auto_specialise(0)              # the kernel tier is chosen explicitly (--kernels)
     from tests.trees import to_product
     size, chunks = 128, 8
     dmc = a.workload == "mesh-dmc-128"
@@ -581,6 +583,7 @@ def run_grid(a, rank, world, local):
     node = to_product(root)
     node.prepare(4 if kind == "tile" else len(args[1]))
     import fastnoise2_gb300 as fn
+    fn.set_auto_specialise(0)              # the kernel tier is chosen explicitly (--kernels)
     if a.kernels == "jit":
         fn.jit_compile([(node, 4 if kind == "tile" else len(args[1]))])
     else:
