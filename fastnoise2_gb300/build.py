@@ -26,7 +26,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["fn_kernels.cu", "fn_static_scratch.cu", "fn_mesh.cu"]
 CPP_SOURCES = ["fn_node.cpp", "fn_compile.cpp", "fn_runtime.cpp", "fn_batch.cpp", "fn_server.cpp", "fn_capi.cpp",
-               "fn_jit.cpp", "fn_ipc.cpp", "fn_live.cpp"]
+               "fn_jit.cpp", "fn_ipc.cpp", "fn_live.cpp", "fn_capi_mesh.cpp"]
 
 # Headers handed to NVRTC at run time (in this order), embedded into the library.
 JIT_HEADERS = ["fn_types.h", "fn_device.cuh", "fn_eval.cuh"]
