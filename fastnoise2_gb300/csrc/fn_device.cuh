@@ -725,9 +725,9 @@ FND float distance(int df, bool sqrt_euclid, const float* p, float mp)
 constexpr float kJitter2D = 0.437016f, kJitter3D = 0.396144f, kJitter4D = 0.366025f;
 
 template <int D> struct CellConst;
-template <> struct CellConst<2> { static constexpr float jitter = kJitter2D; static constexpr float size = -1.f / 0x3ff; };
-template <> struct CellConst<3> { static constexpr float jitter = kJitter3D; static constexpr float size = -1.f / 0xffff; };
-template <> struct CellConst<4> { static constexpr float jitter = kJitter4D; static constexpr float size = -1.f / 0xfffff; };
+template <> struct CellConst<2> { static constexpr float jitter = kJitter2D; static constexpr float size = -1.f / 0x3ff; static constexpr float sizeMax = 0x3ff; };
+template <> struct CellConst<3> { static constexpr float jitter = kJitter3D; static constexpr float size = -1.f / 0xffff; static constexpr float sizeMax = 0xffff; };
+template <> struct CellConst<4> { static constexpr float jitter = kJitter4D; static constexpr float size = -1.f / 0xfffff; static constexpr float sizeMax = 0xfffff; };
 
 __device__ constexpr int kPrimes[4] = {kPrimeX, kPrimeY, kPrimeZ, kPrimeW};
 
@@ -783,8 +783,9 @@ struct CellParams {
 };
 
 // Visit the 3^D cells around the point in the reference's order (last axis
-// fastest): visit(c, cf) gets the primed cell coordinates and the running float
-// cell offsets (cfb[k] + 0, 1, 2).  Nested loops over scalars rather than an
+// fastest): visit(c, cf, kRefOrder) gets the primed cell coordinates and the running
+// float cell offsets (cfb[k] + 0, 1, 2); kRefOrder tells the visitor that cells arrive in
+// the reference's order, so its ties need no order index.  Nested loops over scalars rather than an
 // odometer over arrays, so the per-cell state stays in registers; the innermost
 // axis is unrolled so three cells' hashing and distances can overlap.
 // Minkowski P of the cellular distance: the node's constant (NoMink), or a
@@ -794,6 +795,8 @@ struct NoMink {
     static constexpr bool kNode = false;
     FND float operator()(const float*) const { return 0.0f; }
 };
+
+constexpr int kRefOrder = 0x7fffffff;
 
 template <int D, typename F>
 FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
@@ -809,7 +812,7 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
             for (int yi = 0; yi < 3; ++yi, cy = iadd(cy, kPrimeY), fy += 1.0f) {
                 const int c[2] = {cx, cy};
                 const float cf[2] = {fx, fy};
-                visit(c, cf);
+                visit(c, cf, kRefOrder);
             }
         }
     } else if constexpr (D == 3) {
@@ -827,7 +830,7 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
                 for (int zi = 0; zi < 3; ++zi, cz = iadd(cz, kPrimeZ), fz += 1.0f) {
                     const int c[3] = {cx, cy, cz};
                     const float cf[3] = {fx, fy, fz};
-                    visit(c, cf);
+                    visit(c, cf, kRefOrder);
                 }
             }
         }
@@ -850,12 +853,123 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
                     for (int wi = 0; wi < 3; ++wi, cw = iadd(cw, kPrimeW), fw += 1.0f) {
                         const int c[4] = {cx, cy, cz, cw};
                         const float cf[4] = {fx, fy, fz, fw};
-                        visit(c, cf);
+                        visit(c, cf, kRefOrder);
                     }
                 }
             }
         }
     }
+}
+
+// Skipping cells that cannot change the result.  A cell's point is its lattice point plus
+// the jitter vector d * (jitter / |d|): |d|^2 is exact (half-integer components below 2^11),
+// so the vector's length is |jitter| within three roundings, below J = |jitter| (1 + 2^-16),
+// and so is each of its components.  The cell's fma adds that component to an offset t_k
+// (cell - position, as the walk computes it), and since rounding is monotone
+// |offset_k| >= lb_k = max(0, RN(|t_k| - J)).  The distance formula evaluated on lb, with
+// the axes not yet fixed at 0, uses the same monotone operations as the cell's own distance
+// (sums of squares / absolute values, max, square root, the size-jitter factor >= fmin > 0),
+// so it bounds that distance from below.  A plane, row or cell whose bound is above the
+// current threshold (the last distance slot the walk keeps) cannot enter the kept slots and
+// is skipped.
+//
+// Pruned walks visit each axis middle-first (reference index 1, 0, 2), which finds the near
+// cells early (3D: ~12 of 27 cells left per warp for one slot, ~35 of 81 in 4D for two).
+// Kept distances do not depend on the visiting order; where the walk keeps one cell's hash or
+// point, ties are broken on the reference's visiting index `o`, which makes the result the
+// one the reference's strictly-closer rule gives in its own order.  CellularValue with a
+// value index above 0 keeps several hashes, and the reference's insertion moves a displaced
+// hash past equal distances only when strictly closer, so which of two tied hashes ends in
+// which slot depends on the visiting order: that walk prunes in the reference's order.  Pruning and the order
+// change are used only where no NaN can reach a distance unless every cell's is NaN: a
+// finite jitter, a finite size jitter whose factor stays positive, and not Minkowski (whose
+// power functions are not shown monotone here); otherwise the reference-order walk runs.
+struct CellBound {
+    int df;
+    bool sq;       // the walk takes the square root of Euclidean distances
+    bool size;     // distances are multiplied by a size-jitter factor >= fmin
+    float fmin;
+    float J;       // bound on each jitter component
+    bool on;       // pruned, middle-first walk
+};
+
+template <int D>
+FND CellBound cell_bound_params(const CellParams& cp, bool sq)
+{
+    CellBound B;
+    B.df = cp.distFunc;
+    B.sq = sq && cp.distFunc != kEuclideanSq;
+    B.size = cp.sizeActive;
+    B.J = fabs_(cp.jitter) * 1.00001526f;                      // 1 + 2^-16
+    const bool sizeFinite = fabs_(cp.sizeJitter) <= 3.40282347e38f;
+    B.fmin = cp.sizeJitter > 0.0f ? fmaf(-cp.sizeJitter, CellConst<D>::sizeMax, 1.0f) : 1.0f;
+    B.on = B.J <= 3.40282347e38f && cp.distFunc >= kEuclidean && cp.distFunc <= kMaxAxis &&
+           (!cp.sizeActive || (sizeFinite && B.fmin > 0.0f));
+    return B;
+}
+
+// Lower bound of the distance with axes 0..K at lb and the others at 0 (same operation
+// order as distance<D>).
+template <int K>
+FND float cell_bound(const CellBound& B, const float* lb)
+{
+    float b;
+    if (B.df == kManhattan) {
+        float t = lb[K];
+#pragma unroll
+        for (int k = K - 1; k >= 1; --k) t = lb[k] + t;
+        b = K == 0 ? lb[0] : lb[0] + t;
+    } else if (B.df == kHybrid) {
+        b = fmaf(lb[0], lb[0], lb[0]);
+#pragma unroll
+        for (int k = 1; k <= K; ++k) b = b + fmaf(lb[k], lb[k], lb[k]);
+    } else if (B.df == kMaxAxis) {
+        b = lb[0];
+#pragma unroll
+        for (int k = 1; k <= K; ++k) b = fmax_(lb[k], b);
+    } else {
+        b = lb[0] * lb[0];
+#pragma unroll
+        for (int k = 1; k <= K; ++k) b = fmaf(lb[k], lb[k], b);
+        if (B.sq) b = sqrtf(b);
+    }
+    return B.size ? b * B.fmin : b;
+}
+
+// Pruned walk over axis K and the axes after it, middle-first (Mid) or in the reference's
+// order.  axis_lb(k, cf) gives lb_k for the cell offset cf on axis k; thr() the current
+// threshold; visit(c, cf, o) as above with the cell's index in the reference's order
+// (kRefOrder when the walk keeps the reference's order).
+template <bool Mid, int D, int K, typename LbF, typename ThrF, typename F>
+FND void walk_mid(const int* cb, const float* cfb, int* c, float* cf, float* lb, int o, const CellBound& B,
+                  LbF& axis_lb, ThrF& thr, F& visit)
+{
+    const int c1 = iadd(cb[K], kPrimes[K]), c2 = iadd(c1, kPrimes[K]);
+    const float f1 = cfb[K] + 1.0f, f2 = f1 + 1.0f;
+    auto step = [&](int m) {
+        const int j = Mid ? (m == 0 ? 1 : (m == 1 ? 0 : 2)) : m;
+        c[K] = j == 0 ? cb[K] : (j == 1 ? c1 : c2);
+        cf[K] = j == 0 ? cfb[K] : (j == 1 ? f1 : f2);
+        lb[K] = axis_lb(K, cf[K]);
+        if (cell_bound<K>(B, lb) > thr()) return;
+        if constexpr (K + 1 < D) walk_mid<Mid, D, K + 1>(cb, cfb, c, cf, lb, o * 3 + j, B, axis_lb, thr, visit);
+        else visit(c, cf, Mid ? o * 3 + j : kRefOrder);
+    };
+    if constexpr (K == D - 1) {
+#pragma unroll
+        for (int m = 0; m < 3; ++m) step(m);
+    } else {
+#pragma unroll 1
+        for (int m = 0; m < 3; ++m) step(m);
+    }
+}
+
+template <int D, bool Mid = true, typename LbF, typename ThrF, typename F>
+FND void for_each_cell_pruned(const int* cb, const float* cfb, const CellBound& B, LbF&& axis_lb, ThrF&& thr, F&& visit)
+{
+    int c[D];
+    float cf[D], lb[D];
+    walk_mid<Mid, D, 0>(cb, cfb, c, cf, lb, 0, B, axis_lb, thr, visit);
 }
 
 template <int D, typename MinkF = NoMink>
@@ -866,6 +980,7 @@ FND float cellular_value(int seed, const float* pin, const CellParams& cp, int v
     for (int k = 0; k < D; ++k) p[k] = pin[k] * cp.freq;
     float dist[4] = {__int_as_float(0x7F800000), __int_as_float(0x7F800000), __int_as_float(0x7F800000), __int_as_float(0x7F800000)};
     int vh[4] = {0, 0, 0, 0};
+    int ord[4] = {-1, -1, -1, -1};   // the initial slots precede every cell
     int cb[D];
     float cfb[D];
 #pragma unroll
@@ -874,7 +989,7 @@ FND float cellular_value(int seed, const float* pin, const CellParams& cp, int v
         cfb[k] = cvtf(cb[k]) - p[k];
         cb[k] = imul(cb[k], kPrimes[k]);
     }
-    for_each_cell<D>(cb, cfb, [&](const int* c, const float* cf) {
+    auto visit = [&](const int* c, const float* cf, int o) {
         int h = cell_hash<D>(seed, c);
         float d[D + 1];
         cell_dir<D>(h, cp.jitter, d);
@@ -884,19 +999,37 @@ FND float cellular_value(int seed, const float* pin, const CellParams& cp, int v
         const float mk = (MinkF::kNode && cp.distFunc == 5) ? mink(off) : cp.minkowski;
         float nd = distance<D>(cp.distFunc, D == 2, off, mk);
         if (cp.sizeActive) nd *= size_factor<D>(h, cp.sizeJitter);
-        int nh = h;
+        int nh = h, no = o;
 #pragma unroll
         for (int i = 0; i < 4; i++) {
-            bool closer = nd < dist[i];
+            bool closer = nd < dist[i] || (nd == dist[i] && no < ord[i]);
             float ld = dist[i];
-            int lh = vh[i];
+            int lh = vh[i], lo = ord[i];
             dist[i] = closer ? nd : dist[i];
             vh[i] = closer ? nh : vh[i];
+            ord[i] = closer ? no : ord[i];
             if (i >= valueIndex) break;
             nd = closer ? ld : nd;
             nh = closer ? lh : nh;
+            no = closer ? lo : no;
         }
-    });
+    };
+    const CellBound B = cell_bound_params<D>(cp, D == 2);
+    auto axis_lb = [&](int, float cf) { return fmaxf(0.0f, fabs_(cf) - B.J); };
+    if (B.on && valueIndex == 0) {
+        for_each_cell_pruned<D>(cb, cfb, B, axis_lb, [&]() { return dist[0]; }, visit);
+    } else if (B.on) {
+        for_each_cell_pruned<D, false>(cb, cfb, B, axis_lb,
+            [&]() {
+                float t = dist[1];
+#pragma unroll
+                for (int i = 2; i < 4; ++i) t = valueIndex == i ? dist[i] : t;
+                return t;
+            },
+            visit);
+    } else {
+        for_each_cell<D>(cb, cfb, visit);
+    }
     int sel = vh[0];
 #pragma unroll
     for (int i = 1; i < 4; ++i) sel = valueIndex == i ? vh[i] : sel;
@@ -922,7 +1055,7 @@ FND void cellular_distances(int seed, const float* pin, const CellParams& cp, fl
         cfb[k] = cvtf(cb[k]);
         cb[k] = imul(cb[k], kPrimes[k]);
     }
-    for_each_cell<D>(cb, cfb, [&](const int* c, const float* cf) {
+    auto visit = [&](const int* c, const float* cf, int) {
         int h = cell_hash<D>(seed, c);
         float d[D + 1];
         cell_dir<D>(h, cp.jitter, d);
@@ -935,7 +1068,16 @@ FND void cellular_distances(int seed, const float* pin, const CellParams& cp, fl
 #pragma unroll
         for (int i = NS - 1; i > 0; i--) dist[i] = fmax_(fmin_(dist[i], nd), dist[i - 1]);
         dist[0] = fmin_(dist[0], nd);
-    });
+    };
+    const CellBound B = cell_bound_params<D>(cp, false);
+    if (B.on) {
+        for_each_cell_pruned<D>(cb, cfb, B,
+            [&](int k, float cf) { return fmaxf(0.0f, fabs_(cf - p[k]) - B.J); },
+            [&]() { return dist[NS - 1]; },
+            visit);
+    } else {
+        for_each_cell<D>(cb, cfb, visit);
+    }
 }
 
 // CellularDistance::GetReturn (Cellular.inl:531-565) without the final ScaleOutput;
@@ -970,6 +1112,7 @@ FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, f
 #pragma unroll
     for (int k = 0; k < D; ++k) p[k] = pin[k] * cp.freq;
     float best = 3.40282347e+38f;
+    int bo = -1;
     float cell[D];
 #pragma unroll
     for (int k = 0; k < D; ++k) cell[k] = 0.0f;
@@ -981,7 +1124,7 @@ FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, f
         cfb[k] = cvtf(cb[k]);
         cb[k] = imul(cb[k], kPrimes[k]);
     }
-    for_each_cell<D>(cb, cfb, [&](const int* c, const float* cf) {
+    auto visit = [&](const int* c, const float* cf, int o) {
         int h = cell_hash<D>(seed, c);
         float d[D + 1];
         cell_dir<D>(h, cp.jitter, d);
@@ -991,11 +1134,26 @@ FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, f
         const float mk = (MinkF::kNode && cp.distFunc == 5) ? mink(off) : cp.minkowski;
         float nd = distance<D>(cp.distFunc, false, off, mk);
         if (cp.sizeActive) nd *= size_factor<D>(h, cp.sizeJitter);
-        bool closer = nd < best;
+        const bool closer = nd < best || (nd == best && o < bo);
         best = fmin_(nd, best);
+        bo = closer ? o : bo;
 #pragma unroll
         for (int k = 0; k < D; ++k) cell[k] = closer ? local[k] : cell[k];
-    });
+    };
+    const CellBound B = cell_bound_params<D>(cp, false);
+    if (B.on) {
+        // the cell point is rounded before the position is subtracted: widen J by the
+        // rounding of the cell point and of cf - p (2^-22 covers both with room)
+        for_each_cell_pruned<D>(cb, cfb, B,
+            [&](int k, float cf) {
+                const float t = fabs_(cf - p[k]);
+                return fmaxf(0.0f, t - fmaf(t + fabs_(cf) + B.J, 2.38418579e-7f, B.J));
+            },
+            [&]() { return best; },
+            visit);
+    } else {
+        for_each_cell<D>(cb, cfb, visit);
+    }
 #pragma unroll
     for (int k = 0; k < D; ++k) out[k] = cell[k] * scale;
 }

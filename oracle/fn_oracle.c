@@ -2577,11 +2577,13 @@ static void run_jobs(job_t* proto, int64_t total, int threads, float* minmax)
         for (int t = 0; t < threads; ++t) pthread_create(&tid[t], NULL, run_range_thread, &jobs[t]);
         for (int t = 0; t < threads; ++t) pthread_join(tid[t], NULL);
     }
+    /* OutputMinMax << OutputMinMax (Generator.h:99-104): min with min, max with max, so a
+       range whose values were all NaN (still +inf, -inf) leaves the result unchanged. */
     float mn = INFINITY, mx = -INFINITY;
     for (int t = 0; t < threads; ++t) {
         if (jobs[t].begin >= jobs[t].end) continue;
-        minmax_acc(jobs[t].mn, &mn, &mx);
-        minmax_acc(jobs[t].mx, &mn, &mx);
+        if (jobs[t].mn < mn) mn = jobs[t].mn;
+        if (mx < jobs[t].mx) mx = jobs[t].mx;
     }
     if (minmax) { minmax[0] = mn; minmax[1] = mx; }
 }

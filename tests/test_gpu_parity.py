@@ -61,6 +61,15 @@ SINGLE = {
     "CellularDistanceMinkowski": lambda: cellular("CellularDistance", "Minkowski", Minkowski_P=1.7),
     "CellularJitter": lambda: cellular("CellularDistance", Grid_Jitter=0.6, Size_Jitter=0.4),
     "CellularLookup": lambda: N("CellularLookup", Feature_Scale=4.0, Lookup=noise("Perlin", 9.0)),
+    # parameters that change which cells the walk may skip
+    "CellularNegJitter": lambda: cellular("CellularValue", "Euclidean", Grid_Jitter=-0.8),
+    "CellularSizeShrink": lambda: cellular("CellularValue", "Manhattan", Size_Jitter=-0.5),
+    "CellularSizeNegative": lambda: cellular("CellularDistance", "Euclidean", Size_Jitter=-1.5, Return_Type="Index0Add1"),
+    "CellularValueHybrid": lambda: cellular("CellularValue", "Hybrid", Value_Index=1, Grid_Jitter=1.3),
+    "CellularLookupManhattan": lambda: N("CellularLookup", Feature_Scale=2.9, Lookup=noise("Simplex", 9.0))
+                                       .set("Distance Function", "Manhattan").set("Size Jitter", 0.3),
+    "CellularJitterNode": lambda: N("CellularLookup", Feature_Scale=3.3, Lookup=noise("Value", 5.0),
+                                    Grid_Jitter=noise("Simplex", 9.0)),
 }
 
 COMPOSITE = {
@@ -129,7 +138,35 @@ def test_single_node_grid(gpu, name, dim):
 @pytest.mark.parametrize("name", sorted(COMPOSITE))
 def test_composite_grid(gpu, name, dim):
     off, cnt, st = GRID[dim]
-    assert_parity(*run_grid(COMPOSITE[name](), off, cnt, st, -42), label=f"{name}/{dim}D")
+    assert_parity(*run_grid(COMPOSITE[name](), off, cnt, st, -42), label=f"{name}/{dim}D",
+                  nan_equal=name != "ConvertRGBA8")
+
+
+TIE_GRID = {2: ((-3.0, -2.5), (29, 27), (0.25, 0.25)),
+            3: ((-3.0, -2.5, -1.75), (15, 13, 11), (0.25, 0.25, 0.25)),
+            4: ((-3.0, -2.5, -1.75, -1.0), (9, 7, 7, 5), (0.25, 0.25, 0.25, 0.25))}
+
+
+@pytest.mark.parametrize("dim", [2, 3, 4])
+@pytest.mark.parametrize("kind,df,extra", [
+    ("CellularValue", "Euclidean Squared", {}),
+    ("CellularValue", "Manhattan", {"Value Index": 1}),
+    ("CellularValue", "Max Axis", {}),
+    ("CellularLookup", "Euclidean", {}),
+    ("CellularLookup", "Max Axis", {}),
+    ("CellularDistance", "Manhattan", {"Return Type": "Index0Sub1"}),
+])
+def test_cellular_ties(gpu, kind, df, extra, dim):
+    """Grid jitter 0 puts every cell point on its lattice point; positions on a quarter grid at
+    frequency 1 are then often equidistant from several cells, and the cell the reference visits
+    first must win the tie whatever order the walk visits them in."""
+    n = N(kind, Feature_Scale=1.0, Grid_Jitter=0.0) if kind != "CellularLookup" else \
+        N(kind, Feature_Scale=1.0, Grid_Jitter=0.0, Lookup=noise("Value", 0.7))
+    n.set("Distance Function", df)
+    for k, v in extra.items():
+        n.set(k, v)
+    off, cnt, st = TIE_GRID[dim]
+    assert_parity(*run_grid(n, off, cnt, st, 77), label=f"{kind}/{df}/{dim}D ties")
 
 
 @pytest.mark.parametrize("seed", [0, 1337, -1, 2**31 - 1, -(2**31)])
