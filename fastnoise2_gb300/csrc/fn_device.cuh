@@ -884,6 +884,8 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
 // change are used only where no NaN can reach a distance unless every cell's is NaN: a
 // finite jitter, a finite size jitter whose factor stays positive, and not Minkowski (whose
 // power functions are not shown monotone here); otherwise the reference-order walk runs.
+// 2D walks (9 cells, few to skip) also run in the reference's order: the checks cost there
+// about what the skipped cells save (CellularLookup 2D measured 1.6 % faster without).
 struct CellBound {
     int df;
     bool sq;       // the walk takes the square root of Euclidean distances
@@ -903,7 +905,7 @@ FND CellBound cell_bound_params(const CellParams& cp, bool sq)
     B.J = fabs_(cp.jitter) * 1.00001526f;                      // 1 + 2^-16
     const bool sizeFinite = fabs_(cp.sizeJitter) <= 3.40282347e38f;
     B.fmin = cp.sizeJitter > 0.0f ? fmaf(-cp.sizeJitter, CellConst<D>::sizeMax, 1.0f) : 1.0f;
-    B.on = B.J <= 3.40282347e38f && cp.distFunc >= kEuclidean && cp.distFunc <= kMaxAxis &&
+    B.on = D > 2 && B.J <= 3.40282347e38f && cp.distFunc >= kEuclidean && cp.distFunc <= kMaxAxis &&
            (!cp.sizeActive || (sizeFinite && B.fmin > 0.0f));
     return B;
 }
