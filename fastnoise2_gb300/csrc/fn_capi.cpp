@@ -323,10 +323,9 @@ struct BatchCtx {
 };
 thread_local BatchCtx* t_batch = nullptr;
 
-BatchCtx* batch_ctx(size_t n)
+// Size `b`'s min/max buffers for n requests.
+bool reserve_batch(BatchCtx* b, size_t n)
 {
-    if (!t_batch) t_batch = new BatchCtx();
-    BatchCtx* b = t_batch;
     if (n > b->cap) {
         if (b->dminmax) cudaFree(b->dminmax);
         if (b->hminmax) cudaFreeHost(b->hminmax);
@@ -334,10 +333,16 @@ BatchCtx* batch_ctx(size_t n)
         size_t want = n < 256 ? 256 : n;
         if (!cuda_ok(cudaMalloc(&b->dminmax, want * 2 * sizeof(float)), "cudaMalloc(batch minmax)") ||
             !cuda_ok(cudaMallocHost(&b->hminmax, want * 2 * sizeof(float)), "cudaMallocHost(batch minmax)"))
-            return nullptr;
+            return false;
         b->cap = want;
     }
-    return b;
+    return true;
+}
+
+BatchCtx* batch_ctx(size_t n)
+{
+    if (!t_batch) t_batch = new BatchCtx();
+    return reserve_batch(t_batch, n) ? t_batch : nullptr;
 }
 
 int build_items(const fnGenRequest* reqs, int n, BatchCtx* b, std::vector<BatchItem>& items)
@@ -356,13 +361,14 @@ int build_items(const fnGenRequest* reqs, int n, BatchCtx* b, std::vector<BatchI
     return FN_OK;
 }
 
-int run_batch(const fnGenRequest* reqs, int n, void* stream, int flags, const BatchTuning* tuning)
+// One batch launch on `stream` with the runner and buffers of `b` (b == nullptr: this
+// thread's context).
+int run_batch(const fnGenRequest* reqs, int n, void* stream, int flags, const BatchTuning* tuning, BatchCtx* b = nullptr)
 {
     if (n < 0 || (n > 0 && !reqs)) { set_error(FN_ERR_ARG, "invalid request list"); return FN_ERR_ARG; }
     if (n == 0) return FN_OK;
     if (!thread_ctx()) return FN_ERR_CUDA;
-    BatchCtx* b = batch_ctx((size_t)n);
-    if (!b) return FN_ERR_CUDA;
+    if (b ? !reserve_batch(b, (size_t)n) : !(b = batch_ctx((size_t)n))) return FN_ERR_CUDA;
     std::vector<BatchItem> items;
     int rc = build_items(reqs, n, b, items);
     if (rc) return rc;
@@ -380,10 +386,12 @@ int run_batch(const fnGenRequest* reqs, int n, void* stream, int flags, const Ba
 }
 
 // Host-output batches: two device staging buffers, the requests cut into slices that fit one;
-// slice k is generated on `gen` into buffer k % 2 while slice k - 1 is copied to the host on
-// `copy`, so the copy engine and the SMs work at the same time.  Slices start small (the first
-// copy starts early) and shrink again at the end (little is left to copy after the last
-// generation).  Slices are launched without graphs: each has its own shape.
+// slice k is generated on gen[k % 2] into buffer k % 2 while slice k - 1 is copied to the host
+// on `copy`, so the copy engine and the SMs work at the same time.  The two generation streams
+// have their own batch runners, so consecutive slices also overlap each other's kernel tails.
+// Slices start small (the first copy starts early) and shrink again at the end (little is left
+// to copy after the last generation).  Slices are launched without graphs: each has its own
+// shape.
 constexpr size_t kHostSlicePoints = size_t(1) << 25;       // 128 MB of output per staging buffer
 constexpr size_t kHostSliceMin = size_t(1) << 23;
 
@@ -395,7 +403,8 @@ size_t host_slice_cap(int k, size_t remaining)
 }
 
 struct HostBatchCtx {
-    cudaStream_t gen = nullptr, copy = nullptr;
+    cudaStream_t gen[2] = {}, copy = nullptr;   // slice k is generated on gen[k % 2]
+    BatchCtx lane[2];                            // with its own batch runner and buffers
     cudaEvent_t gen_done[2] = {}, copy_done[2] = {};
     float* stage[2] = {};
     size_t stage_cap = 0;                  // floats per staging buffer
@@ -411,7 +420,8 @@ struct HostBatchCtx {
             if (copy_done[k]) cudaEventDestroy(copy_done[k]);
         }
         if (hmm) cudaFreeHost(hmm);
-        if (gen) cudaStreamDestroy(gen);
+        for (int k = 0; k < 2; ++k)
+            if (gen[k]) cudaStreamDestroy(gen[k]);
         if (copy) cudaStreamDestroy(copy);
     }
 };
@@ -421,7 +431,8 @@ HostBatchCtx* host_batch_ctx(size_t stage_floats, size_t requests)
 {
     if (!t_hbatch) {
         HostBatchCtx* h = new HostBatchCtx();
-        bool ok = cuda_ok(cudaStreamCreateWithFlags(&h->gen, cudaStreamNonBlocking), "stream") &&
+        bool ok = cuda_ok(cudaStreamCreateWithFlags(&h->gen[0], cudaStreamNonBlocking), "stream") &&
+                  cuda_ok(cudaStreamCreateWithFlags(&h->gen[1], cudaStreamNonBlocking), "stream") &&
                   cuda_ok(cudaStreamCreateWithFlags(&h->copy, cudaStreamNonBlocking), "stream");
         for (int k = 0; ok && k < 2; ++k)
             ok = cuda_ok(cudaEventCreateWithFlags(&h->gen_done[k], cudaEventDisableTiming), "event") &&
@@ -804,11 +815,14 @@ int fnGenBatchHost(const fnGenRequest* requests, int count, int flags)
             slice[j].minMax = nullptr;
             off += points[(size_t)i0 + j];
         }
-        // buffer `buf` is free once the copy of slice k - 2 is done
-        if (!cuda_ok(cudaStreamWaitEvent(h->gen, h->copy_done[buf], 0), "wait")) return FN_ERR_CUDA;
-        const int rc = run_batch(slice.data(), (int)slice.size(), h->gen, FN_BATCH_NO_GRAPH, nullptr);
+        // buffer `buf` is free once the copy of slice k - 2 is done; slices k and k + 1 run on
+        // different streams with their own runners, so one slice's kernel tails overlap the next
+        cudaStream_t gen = h->gen[buf];
+        BatchCtx* lane = &h->lane[buf];
+        if (!cuda_ok(cudaStreamWaitEvent(gen, h->copy_done[buf], 0), "wait")) return FN_ERR_CUDA;
+        const int rc = run_batch(slice.data(), (int)slice.size(), gen, FN_BATCH_NO_GRAPH, nullptr, lane);
         if (rc) return rc;
-        const BatchRunner& r = t_batch->runner;
+        const BatchRunner& r = lane->runner;
         h->info.requests += (int)slice.size();
         h->info.specialised = r.last_specialised() ? 1 : 0;
         h->info.tilePoints = (int)r.last_tile_points();
@@ -817,9 +831,9 @@ int fnGenBatchHost(const fnGenRequest* requests, int count, int flags)
         h->info.points += r.last_points();
         h->info.uploadBytes += r.last_upload_bytes();
         h->info.kernels += r.last_kernels();
-        if (!cuda_ok(cudaMemcpyAsync(h->hmm + 2 * (size_t)i0, t_batch->dminmax, slice.size() * 2 * sizeof(float),
-                                     cudaMemcpyDeviceToHost, h->gen), "copy minmax") ||
-            !cuda_ok(cudaEventRecord(h->gen_done[buf], h->gen), "record") ||
+        if (!cuda_ok(cudaMemcpyAsync(h->hmm + 2 * (size_t)i0, lane->dminmax, slice.size() * 2 * sizeof(float),
+                                     cudaMemcpyDeviceToHost, gen), "copy minmax") ||
+            !cuda_ok(cudaEventRecord(h->gen_done[buf], gen), "record") ||
             !cuda_ok(cudaStreamWaitEvent(h->copy, h->gen_done[buf], 0), "wait"))
             return FN_ERR_CUDA;
         // one copy per run of requests whose host outputs are contiguous
@@ -838,7 +852,8 @@ int fnGenBatchHost(const fnGenRequest* requests, int count, int flags)
         if (!cuda_ok(cudaEventRecord(h->copy_done[buf], h->copy), "record")) return FN_ERR_CUDA;
         i0 = i1;
     }
-    if (!cuda_ok(cudaStreamSynchronize(h->copy), "synchronize") || !cuda_ok(cudaStreamSynchronize(h->gen), "synchronize"))
+    if (!cuda_ok(cudaStreamSynchronize(h->copy), "synchronize") || !cuda_ok(cudaStreamSynchronize(h->gen[0]), "synchronize") ||
+        !cuda_ok(cudaStreamSynchronize(h->gen[1]), "synchronize"))
         return FN_ERR_CUDA;
     for (int i = 0; i < count; ++i)
         if (requests[i].minMax) { requests[i].minMax[0] = h->hmm[2 * i]; requests[i].minMax[1] = h->hmm[2 * i + 1]; }
