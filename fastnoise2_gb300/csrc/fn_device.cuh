@@ -739,27 +739,33 @@ FND int cell_hash(int seed, const int* c)
     return hashhb(seed, c[0], c[1], c[2], c[3]);
 }
 
-// Jittered cell-point direction scaled by jitter/|dir| (Cellular.inl:55-58, 141-145, 239-244)
+// Jittered cell-point direction scaled by jitter/|dir| (Cellular.inl:55-58, 141-145, 239-244):
+// cell_dir_raw gives the D direction components (half-integers, exact), cell_dir_scale the
+// factor jitter / |dir| in d[D].
 template <int D>
-FND void cell_dir(int h, float jitter, float* d)
+FND void cell_dir_raw(int h, float* d)
 {
     if (D == 2) {
         d[0] = cvtf(h & 0x7ff) - (0x7ff / 2.0f);
         d[1] = cvtf((int)srl(h, 21)) - (0x7ff / 2.0f);
-        float inv = jitter * invsqrt(fmaf(d[0], d[0], d[1] * d[1]));
-        d[2] = inv;
     } else if (D == 3) {
         d[0] = cvtf(h & 0x3ff) - (0x3ff / 2.0f);
         d[1] = cvtf((h >> 11) & 0x3ff) - (0x3ff / 2.0f);
         d[2] = cvtf((int)srl(h, 22)) - (0x3ff / 2.0f);
-        d[3] = jitter * invsqrt(fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2])));
     } else {
         d[0] = cvtf(h & 0xff) - (0xff / 2.0f);
         d[1] = cvtf((h >> 8) & 0xff) - (0xff / 2.0f);
         d[2] = cvtf((h >> 16) & 0xff) - (0xff / 2.0f);
         d[3] = cvtf((int)srl(h, 24)) - (0xff / 2.0f);
-        d[4] = jitter * invsqrt(fmaf(d[0], d[0], fmaf(d[1], d[1], fmaf(d[2], d[2], d[3] * d[3]))));
     }
+}
+
+template <int D>
+FND void cell_dir_scale(float jitter, float* d)
+{
+    if (D == 2) d[2] = jitter * invsqrt(fmaf(d[0], d[0], d[1] * d[1]));
+    else if (D == 3) d[3] = jitter * invsqrt(fmaf(d[0], d[0], fmaf(d[1], d[1], d[2] * d[2])));
+    else d[4] = jitter * invsqrt(fmaf(d[0], d[0], fmaf(d[1], d[1], fmaf(d[2], d[2], d[3] * d[3]))));
 }
 
 template <int D>
@@ -783,9 +789,10 @@ struct CellParams {
 };
 
 // Visit the 3^D cells around the point in the reference's order (last axis
-// fastest): visit(c, cf, kRefOrder) gets the primed cell coordinates and the running
-// float cell offsets (cfb[k] + 0, 1, 2); kRefOrder tells the visitor that cells arrive in
-// the reference's order, so its ties need no order index.  Nested loops over scalars rather than an
+// fastest): visit(c, cf, kRefOrder, nullptr) gets the primed cell coordinates and the
+// running float cell offsets (cfb[k] + 0, 1, 2); kRefOrder tells the visitor that cells
+// arrive in the reference's order, so its ties need no order index, and the null bound
+// array that the cell is not to be skipped.  Nested loops over scalars rather than an
 // odometer over arrays, so the per-cell state stays in registers; the innermost
 // axis is unrolled so three cells' hashing and distances can overlap.
 // Minkowski P of the cellular distance: the node's constant (NoMink), or a
@@ -812,7 +819,7 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
             for (int yi = 0; yi < 3; ++yi, cy = iadd(cy, kPrimeY), fy += 1.0f) {
                 const int c[2] = {cx, cy};
                 const float cf[2] = {fx, fy};
-                visit(c, cf, kRefOrder);
+                visit(c, cf, kRefOrder, nullptr);
             }
         }
     } else if constexpr (D == 3) {
@@ -830,7 +837,7 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
                 for (int zi = 0; zi < 3; ++zi, cz = iadd(cz, kPrimeZ), fz += 1.0f) {
                     const int c[3] = {cx, cy, cz};
                     const float cf[3] = {fx, fy, fz};
-                    visit(c, cf, kRefOrder);
+                    visit(c, cf, kRefOrder, nullptr);
                 }
             }
         }
@@ -853,7 +860,7 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
                     for (int wi = 0; wi < 3; ++wi, cw = iadd(cw, kPrimeW), fw += 1.0f) {
                         const int c[4] = {cx, cy, cz, cw};
                         const float cf[4] = {fx, fy, fz, fw};
-                        visit(c, cf, kRefOrder);
+                        visit(c, cf, kRefOrder, nullptr);
                     }
                 }
             }
@@ -938,6 +945,23 @@ FND float cell_bound(const CellBound& B, const float* lb)
     return B.size ? b * B.fmin : b;
 }
 
+// Second bound, once the cell's hash gives its jitter direction d (before the normalisation
+// and distance): on an axis where the jitter component d_k * jitter has the sign of the
+// offset t_k it is added to, the cell point lies beyond t_k, so |offset_k| >= |t_k| (rounding
+// is monotone; for CellularLookup, whose cell point is rounded before the position is
+// subtracted, the rounded point lies beyond cf as well); elsewhere lb_k stands.  Used by the
+// 81-cell 4D walks only: terrain tileable (4D) measured 3.51 -> 3.65 Gpts/s with it, while in
+// 3D the per-lane test after the hash cost more than it saved (chunk mix 47.6 -> 46.8).
+template <int D>
+FND float cell_bound_dir(const CellBound& B, const float* lb, const float* t, const float* d, float jitter)
+{
+    float l2[D];
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+        l2[k] = ((__float_as_uint(d[k]) ^ __float_as_uint(jitter) ^ __float_as_uint(t[k])) >> 31) ? lb[k] : fabs_(t[k]);
+    return cell_bound<D - 1>(B, l2);
+}
+
 // Pruned walk over axis K and the axes after it, middle-first (Mid) or in the reference's
 // order.  axis_lb(k, cf) gives lb_k for the cell offset cf on axis k; thr() the current
 // threshold; visit(c, cf, o) as above with the cell's index in the reference's order
@@ -955,7 +979,7 @@ FND void walk_mid(const int* cb, const float* cfb, int* c, float* cf, float* lb,
         lb[K] = axis_lb(K, cf[K]);
         if (cell_bound<K>(B, lb) > thr()) return;
         if constexpr (K + 1 < D) walk_mid<Mid, D, K + 1>(cb, cfb, c, cf, lb, o * 3 + j, B, axis_lb, thr, visit);
-        else visit(c, cf, Mid ? o * 3 + j : kRefOrder);
+        else visit(c, cf, Mid ? o * 3 + j : kRefOrder, static_cast<const float*>(lb));
     };
     if constexpr (K == D - 1) {
 #pragma unroll
@@ -991,10 +1015,19 @@ FND float cellular_value(int seed, const float* pin, const CellParams& cp, int v
         cfb[k] = cvtf(cb[k]) - p[k];
         cb[k] = imul(cb[k], kPrimes[k]);
     }
-    auto visit = [&](const int* c, const float* cf, int o) {
+    const CellBound B = cell_bound_params<D>(cp, D == 2);
+    auto thr = [&]() {
+        float t = dist[0];
+#pragma unroll
+        for (int i = 1; i < 4; ++i) t = valueIndex == i ? dist[i] : t;
+        return t;
+    };
+    auto visit = [&](const int* c, const float* cf, int o, const float* lb) {
         int h = cell_hash<D>(seed, c);
         float d[D + 1];
-        cell_dir<D>(h, cp.jitter, d);
+        cell_dir_raw<D>(h, d);
+        if (D == 4 && lb && cell_bound_dir<D>(B, lb, cf, d, cp.jitter) > thr()) return;
+        cell_dir_scale<D>(cp.jitter, d);
         float off[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) off[k] = fmaf(d[k], d[D], cf[k]);
@@ -1016,19 +1049,11 @@ FND float cellular_value(int seed, const float* pin, const CellParams& cp, int v
             no = closer ? lo : no;
         }
     };
-    const CellBound B = cell_bound_params<D>(cp, D == 2);
     auto axis_lb = [&](int, float cf) { return fmaxf(0.0f, fabs_(cf) - B.J); };
     if (B.on && valueIndex == 0) {
-        for_each_cell_pruned<D>(cb, cfb, B, axis_lb, [&]() { return dist[0]; }, visit);
+        for_each_cell_pruned<D>(cb, cfb, B, axis_lb, thr, visit);
     } else if (B.on) {
-        for_each_cell_pruned<D, false>(cb, cfb, B, axis_lb,
-            [&]() {
-                float t = dist[1];
-#pragma unroll
-                for (int i = 2; i < 4; ++i) t = valueIndex == i ? dist[i] : t;
-                return t;
-            },
-            visit);
+        for_each_cell_pruned<D, false>(cb, cfb, B, axis_lb, thr, visit);
     } else {
         for_each_cell<D>(cb, cfb, visit);
     }
@@ -1057,13 +1082,19 @@ FND void cellular_distances(int seed, const float* pin, const CellParams& cp, fl
         cfb[k] = cvtf(cb[k]);
         cb[k] = imul(cb[k], kPrimes[k]);
     }
-    auto visit = [&](const int* c, const float* cf, int) {
+    const CellBound B = cell_bound_params<D>(cp, false);
+    auto thr = [&]() { return dist[NS - 1]; };
+    auto visit = [&](const int* c, const float* cf, int, const float* lb) {
         int h = cell_hash<D>(seed, c);
-        float d[D + 1];
-        cell_dir<D>(h, cp.jitter, d);
+        float d[D + 1], t[D];
+        cell_dir_raw<D>(h, d);
+#pragma unroll
+        for (int k = 0; k < D; ++k) t[k] = cf[k] - p[k];
+        if (D == 4 && lb && cell_bound_dir<D>(B, lb, t, d, cp.jitter) > thr()) return;
+        cell_dir_scale<D>(cp.jitter, d);
         float off[D];
 #pragma unroll
-        for (int k = 0; k < D; ++k) off[k] = fmaf(d[k], d[D], cf[k] - p[k]);
+        for (int k = 0; k < D; ++k) off[k] = fmaf(d[k], d[D], t[k]);
         const float mk = (MinkF::kNode && cp.distFunc == 5) ? mink(off) : cp.minkowski;
         float nd = distance<D>(cp.distFunc, false, off, mk);
         if (cp.sizeActive) nd *= size_factor<D>(h, cp.sizeJitter);
@@ -1071,12 +1102,10 @@ FND void cellular_distances(int seed, const float* pin, const CellParams& cp, fl
         for (int i = NS - 1; i > 0; i--) dist[i] = fmax_(fmin_(dist[i], nd), dist[i - 1]);
         dist[0] = fmin_(dist[0], nd);
     };
-    const CellBound B = cell_bound_params<D>(cp, false);
     if (B.on) {
         for_each_cell_pruned<D>(cb, cfb, B,
             [&](int k, float cf) { return fmaxf(0.0f, fabs_(cf - p[k]) - B.J); },
-            [&]() { return dist[NS - 1]; },
-            visit);
+            thr, visit);
     } else {
         for_each_cell<D>(cb, cfb, visit);
     }
@@ -1126,10 +1155,19 @@ FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, f
         cfb[k] = cvtf(cb[k]);
         cb[k] = imul(cb[k], kPrimes[k]);
     }
-    auto visit = [&](const int* c, const float* cf, int o) {
+    const CellBound B = cell_bound_params<D>(cp, false);
+    auto thr = [&]() { return best; };
+    auto visit = [&](const int* c, const float* cf, int o, const float* lb) {
         int h = cell_hash<D>(seed, c);
         float d[D + 1];
-        cell_dir<D>(h, cp.jitter, d);
+        cell_dir_raw<D>(h, d);
+        if (D == 4 && lb) {
+            float t[D];
+#pragma unroll
+            for (int k = 0; k < D; ++k) t[k] = cf[k] - p[k];
+            if (cell_bound_dir<D>(B, lb, t, d, cp.jitter) > thr()) return;
+        }
+        cell_dir_scale<D>(cp.jitter, d);
         float local[D], off[D];
 #pragma unroll
         for (int k = 0; k < D; ++k) { local[k] = fmaf(d[k], d[D], cf[k]); off[k] = local[k] - p[k]; }
@@ -1142,7 +1180,6 @@ FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, f
 #pragma unroll
         for (int k = 0; k < D; ++k) cell[k] = closer ? local[k] : cell[k];
     };
-    const CellBound B = cell_bound_params<D>(cp, false);
     if (B.on) {
         // the cell point is rounded before the position is subtracted: widen J by the
         // rounding of the cell point and of cf - p (2^-22 covers both with room)
@@ -1151,8 +1188,7 @@ FND void cellular_lookup_pos(int seed, const float* pin, const CellParams& cp, f
                 const float t = fabs_(cf - p[k]);
                 return fmaxf(0.0f, t - fmaf(t + fabs_(cf) + B.J, 2.38418579e-7f, B.J));
             },
-            [&]() { return best; },
-            visit);
+            thr, visit);
     } else {
         for_each_cell<D>(cb, cfb, visit);
     }
