@@ -502,14 +502,15 @@ class Server:
             _check()
         return t.value
 
-    def submit_many(self, requests) -> list:
-        """Queue many requests at once (all or nothing); returns their tickets."""
+    def submit_many(self, requests, as_array: bool = False):
+        """Queue many requests at once (all or nothing); returns their tickets (a list, or the
+        ctypes array itself with `as_array`).  `requests` may be a prebuilt request_array()."""
         n = len(requests)
-        arr = (GenRequest * n)(*requests)
+        arr = requests if isinstance(requests, ctypes.Array) else (GenRequest * n)(*requests)
         t = (ctypes.c_ulonglong * n)()
         if lib().fnServerSubmitMany(self._h, arr, n, t) != 0:
             _check()
-        return list(t)
+        return t if as_array else list(t)
 
     def wait_many(self, tickets, timeout_ms: int = -1) -> None:
         """Wait until every ticket has finished; raises FastNoiseError on failure or timeout."""

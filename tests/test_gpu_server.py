@@ -78,6 +78,16 @@ def test_submit_many_and_wait_many(gpu, torch_cuda):
         assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), c
         assert (mn, mx) == rmm
         assert srv.release(t) == 0
+    # a prebuilt request array and the tickets as a ctypes array (no per-call list conversion)
+    arr = fn.request_array([request(fn, nodes[c.tree], c) for c in chunks])
+    tarr = srv.submit_many(arr, as_array=True)
+    srv.wait_many(tarr, timeout_ms=30000)
+    for t, c in zip(tarr, chunks):
+        mn, mx, ptr = srv.wait(t, timeout_ms=0)
+        got = device_array(torch_cuda, ptr, c.points)
+        ref, rmm = nodes[c.tree].gen_uniform_grid(c.offset, c.count, (1,) * len(c.count), c.seed)
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), c
+        assert srv.release(t) == 0
     # all or nothing: one bad request rejects the whole list
     unsupported = trees.to_product(trees.unsupported_tree())      # keep the node alive while requests point to it
     bad = [request(fn, nodes[0], chunks[0]), request(fn, unsupported, chunks[1])]
