@@ -207,8 +207,8 @@ def make_request(node: "Node", kind: int, out_ptr: int, seed: int, count=(0, 0, 
 
 
 def gen_batch(requests, stream: int = 0, sync: bool = True, graph: bool = True) -> None:
-    """fnGenBatchDevice over a sequence of GenRequest."""
-    arr = (GenRequest * len(requests))(*requests)
+    """fnGenBatchDevice over a sequence of GenRequest (or a prebuilt request_array())."""
+    arr = request_array(requests)
     flags = (BATCH_SYNC if sync else 0) | (0 if graph else BATCH_NO_GRAPH)
     if lib().fnGenBatchDevice(arr, len(requests), stream or None, flags) != 0:
         _check()
@@ -228,7 +228,7 @@ def gen_batch_host(requests, graph: bool = True) -> None:
 
 def gen_each(requests, stream: int = 0, sync: bool = True) -> None:
     """fnGenEachDevice: one plain launch per request (the per-call path)."""
-    arr = (GenRequest * len(requests))(*requests)
+    arr = request_array(requests)
     if lib().fnGenEachDevice(arr, len(requests), stream or None, BATCH_SYNC if sync else 0) != 0:
         _check()
 
