@@ -887,10 +887,11 @@ FND void for_each_cell(const int* cb, const float* cfb, F&& visit)
 // one the reference's strictly-closer rule gives in its own order.  CellularValue with a
 // value index above 0 keeps several hashes, and the reference's insertion moves a displaced
 // hash past equal distances only when strictly closer, so which of two tied hashes ends in
-// which slot depends on the visiting order: that walk prunes in the reference's order.  Pruning and the order
-// change are used only where no NaN can reach a distance unless every cell's is NaN: a
-// finite jitter, a finite size jitter whose factor stays positive, and not Minkowski (whose
-// power functions are not shown monotone here); otherwise the reference-order walk runs.
+// which slot depends on the visiting order: that walk prunes in the reference's order.
+// Pruning and the order change are used only where no NaN can reach a distance unless every
+// cell's is NaN: a finite jitter, a finite size jitter whose factor stays positive, and not
+// Minkowski (whose power functions are not shown monotone here); otherwise the unpruned
+// reference-order walk runs.
 // 2D walks (9 cells, few to skip) also run in the reference's order: the checks cost there
 // about what the skipped cells save (CellularLookup 2D measured 1.6 % faster without).
 struct CellBound {
@@ -899,7 +900,7 @@ struct CellBound {
     bool size;     // distances are multiplied by a size-jitter factor >= fmin
     float fmin;
     float J;       // bound on each jitter component
-    bool on;       // pruned, middle-first walk
+    bool on;       // pruned walk (middle-first unless the walk must keep the reference's order)
 };
 
 template <int D>
