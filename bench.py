@@ -22,8 +22,9 @@ reference's configs[1]), simplex-64, terrain-tileable-1024, terrain-128.
 
 --impl reference times the CPU restatement of the reference's algorithm
 (oracle/, "port": the reference binary cannot be built here because its
-FastSIMD dependency is not vendored) with every host thread on a bounded
-sample of the same workload.
+FastSIMD dependency is not vendored): every step is one whole pass over the
+same workload on a persistent pool of all host threads (whole requests per
+thread for the chunk mix), plus a one-thread figure on a bounded sample.
 
 Multi-GPU: requests are independent, so --gpus N runs N replicas (one process
 per GPU, no collective on the data path); value = all points / max rank time.
@@ -171,50 +172,99 @@ def ops_per_point(tree, dim, seed):
 
 # ---------------------------------------------------------------- CPU side
 
-def cpu_sample(workload, seconds):
-    """The CPU restatement (all host threads) on a bounded sample of the workload."""
-    from oracle.oracle import OracleTree
-    from tests import chunkmix, trees
-    threads = os.cpu_count()
-    t0 = time.perf_counter()
-    done = 0
-    if workload == "chunk-mix":
-        chunks = chunkmix.make_mix(4096)
-        otrees = [OracleTree(m()) for m in trees.MIX_TREES]
-        n = 0
-        while time.perf_counter() - t0 < seconds and n < len(chunks):
-            c = chunks[n]
-            otrees[c.tree].grid(c.offset, c.count, (1.0,) * len(c.count), c.seed, threads=threads)
-            done += c.points
-            n += 1
-        sample = f"first {n} requests of the 4096-request chunk mix ({done} points)"
-    else:
-        tname, kind, args, seed = GRID_WORKLOADS[workload]
-        t = OracleTree(tree_named(tname))
-        slab = 0
-        if kind == "grid":
-            off, cnt, st = args
+class CpuWorkload:
+    """One step of a workload on the CPU restatement (oracle/): the whole chunk mix as one
+    batch on the oracle's persistent worker pool (whole requests per thread, largest first),
+    or the whole grid / tileable image cut into contiguous slabs, one per thread."""
+
+    def __init__(self, workload, rank=0):
+        from oracle import oracle
+        from tests import chunkmix, trees
+        self.workload = workload
+        self.oracle = oracle
+        if workload == "chunk-mix":
+            chunks = chunkmix.make_mix(4096)
+            otrees = [oracle.OracleTree(m()) for m in trees.MIX_TREES]
+            self.points = sum(c.points for c in chunks)
+            self.out = np.empty(self.points, np.float32)
+            self.mm = np.zeros((len(chunks), 2), np.float32)
+            self.reqs, off = [], 0
+            for k, c in enumerate(chunks):
+                kind = oracle.KIND_GRID3D if len(c.count) == 3 else oracle.KIND_GRID2D
+                self.reqs.append(oracle.request(otrees[c.tree], kind, self.out[off:off + c.points], self.mm[k],
+                                                c.seed + rank, c.count, c.offset, (1.0,) * len(c.count)))
+                off += c.points
+            self.trees = otrees
+            self.chunk_points = [c.points for c in chunks]
+        else:
+            tname, kind, args, seed = GRID_WORKLOADS[workload]
+            self.tree = oracle.OracleTree(tree_named(tname))
+            self.kind, self.args, self.seed = kind, args, seed + rank
+            self.points = int(np.prod(args[1])) if kind == "grid" else int(args[0][0] * args[0][1])
+
+    def step(self, threads):
+        """One whole pass; returns seconds."""
+        t0 = time.perf_counter()
+        if self.workload == "chunk-mix":
+            self.oracle.gen_requests(self.reqs, threads=threads)
+        elif self.kind == "grid":
+            self.tree.grid(*self.args, self.seed, threads=threads)
+        else:
+            (xs, ys), (sx, sy) = self.args
+            self.tree.tileable(xs, ys, sx, sy, self.seed, threads=threads)
+        return time.perf_counter() - t0
+
+    def single_thread(self, seconds):
+        """Mpoints/s of one thread on a bounded leading part of the workload: the first requests
+        of the mix, or the first z-slabs / rows of the grid, about `seconds` of work."""
+        t0 = time.perf_counter()
+        done = 0
+        if self.workload == "chunk-mix":
+            n = 0
+            while time.perf_counter() - t0 < seconds and n < len(self.reqs):
+                self.oracle.gen_requests(self.reqs[n:n + 16], threads=1)
+                done += sum(self.chunk_points[n:n + 16])
+                n += 16
+            what = f"first {min(n, len(self.reqs))} requests"
+        elif self.kind == "grid":
+            off, cnt, st = self.args
             plane = int(np.prod(cnt[:-1]))
-            zs = max(1, min(cnt[-1], 8))
-            while time.perf_counter() - t0 < seconds:
-                z0 = (slab * zs) % cnt[-1]
-                z = min(zs, cnt[-1] - z0)
+            z0 = 0
+            while time.perf_counter() - t0 < seconds and z0 < cnt[-1]:
                 o = list(off)
                 o[-1] = float(np.float32(off[-1]) + np.float32(z0) * np.float32(st[-1]))
-                t.grid(o, list(cnt[:-1]) + [z], st, seed, threads=threads)
-                done += plane * z
-                slab += 1
-            sample = f"{slab} z-slabs of {zs} planes ({done} points) of the {'x'.join(map(str, cnt))} grid"
+                self.tree.grid(o, list(cnt[:-1]) + [1], st, self.seed, threads=1)
+                done += plane
+                z0 += 1
+            what = f"first {z0} z-planes"
         else:
-            (xs, ys), (sx, sy) = args
+            (xs, ys), (sx, sy) = self.args
+            reps = 0
             while time.perf_counter() - t0 < seconds:
-                t.tileable(xs, ys, sx, sy, seed, threads=threads)
+                self.tree.tileable(xs, ys, sx, sy, self.seed, threads=1)
                 done += xs * ys
-                slab += 1
-            sample = f"{slab} full {xs}x{ys} tileable passes ({done} points)"
-    dt = time.perf_counter() - t0
-    return {"value": done / dt / 1e6, "unit": "Mpoints/s", "cores": threads, "kind": "port",
-            "sample": sample + "; CPU restatement of FastNoise2 (oracle/), the reference binary needs the unvendored FastSIMD"}
+                reps += 1
+            what = f"{reps} whole images"
+        return done / (time.perf_counter() - t0) / 1e6, f"{what} ({done} points)"
+
+
+def cpu_baseline(workload, passes, single_seconds, rank=0):
+    """The CPU restatement on the host cores: `passes` whole passes over the workload with every
+    host thread (the median pass is reported), and one thread on a bounded sample."""
+    from oracle import oracle
+    w = CpuWorkload(workload, rank)
+    threads = os.cpu_count()
+    w.step(threads)                                      # warm: page in outputs, start the pool
+    times = [w.step(threads) for _ in range(max(passes, 1))]
+    t = statistics.median(times)
+    one, one_sample = w.single_thread(single_seconds)
+    return {"value": w.points / t / 1e6, "unit": "Mpoints/s", "cores": threads, "kind": "port",
+            "sample": (f"{len(times)} whole passes over the workload ({w.points} points each, median {t * 1e3:.0f} ms); "
+                       "CPU restatement of FastNoise2 (oracle/) on a persistent pool of all host threads, "
+                       + ("whole requests per thread, largest first" if workload == "chunk-mix" else "one contiguous slab per thread")
+                       + "; the reference binary needs the unvendored FastSIMD"),
+            "single_thread": {"value": one, "unit": "Mpoints/s", "sample": one_sample},
+            "host": oracle.cpu_description()}
 
 
 def points_per_step(workload):
@@ -226,21 +276,35 @@ def points_per_step(workload):
 
 
 def run_reference(a):
+    """The CPU restatement of the reference's path, every step one whole pass over the same
+    workload (no sampling), on all host threads; rank 0 only."""
     rank, world, _ = dist_setup()
     if rank != 0:
         return
+    from oracle import oracle
+    w = CpuWorkload(a.workload)
+    threads = os.cpu_count()
     for _ in range(a.warmup):
-        cpu_sample(a.workload, 0.3)
-    per_step = [cpu_sample(a.workload, a.cpu_seconds / max(a.steps, 1)) for _ in range(a.steps)]
-    v = statistics.median(s["value"] for s in per_step)
-    pts = points_per_step(a.workload)
+        w.step(threads)
+    times = [w.step(threads) for _ in range(a.steps)]
+    t = statistics.mean(times)
+    v = w.points / t / 1e6
+    one, one_sample = w.single_thread(3.0)
     line = {
         "impl": "reference", "metric": "Mpoints/s", "value": v, "unit": "Mpoints/s", "n_gpus": a.gpus,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": pts / (v * 1e6) * 1e3, "higher_is_better": True,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": a.workload, "points_per_step": pts},
-        "cpu_baseline": {"value": v, "unit": "Mpoints/s", "cores": per_step[0]["cores"], "kind": "port",
-                         "sample": per_step[0]["sample"] + " (per step)"},
+        "config": {"workload": a.workload, "points_per_step": w.points,
+                   **({"requests": len(w.reqs), "rng": "numpy PCG64(20261203)"} if a.workload == "chunk-mix" else {})},
+        "cpu_baseline": {"value": v, "unit": "Mpoints/s", "cores": threads, "kind": "port",
+                         "sample": "every step one whole pass over the workload; CPU restatement of FastNoise2 "
+                                   "(oracle/) on a persistent pool of all host threads, "
+                                   + ("whole requests per thread, largest first" if a.workload == "chunk-mix"
+                                      else "one contiguous slab per thread")
+                                   + "; the reference binary needs the unvendored FastSIMD",
+                         "single_thread": {"value": one, "unit": "Mpoints/s", "sample": one_sample},
+                         "host": oracle.cpu_description(),
+                         "ms_per_step_min": min(times) * 1e3, "ms_per_step_max": max(times) * 1e3},
         "e2e": {"value": v, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -358,7 +422,7 @@ def run_chunkmix(a, rank, world, local):
     work = sum(c.points * (tree_ops[c.tree] if len(c.count) == 3 else tree_ops2[c.tree]) for c in chunks)
     achieved = work / (batch_ms * 1e-3) / 1e12
     hbm_gbs = pts * 4 / (batch_ms * 1e-3) / 1e9
-    cpu = cpu_sample("chunk-mix", a.cpu_seconds) if a.cpu_seconds > 0 else None
+    cpu = cpu_baseline("chunk-mix", a.cpu_passes, 3.0, rank) if a.cpu_passes > 0 else None
     line = {
         "metric": "Mpoints/s", "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": batch_ms_max, "higher_is_better": True, "scaling": "weak",
@@ -665,7 +729,7 @@ def run_grid(a, rank, world, local):
         "e2e": {"value": pts * world / (e2e_ms * 1e-3) / 1e6 if e2e_ms else None, "unit": "Mpoints/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": pts * 4 + 8, "ms_per_step": e2e_ms,
                 "api": "fnGenUniformGrid3D / fnGenTileable2D into pinned host memory"},
-        "cpu_baseline": cpu_sample(a.workload, a.cpu_seconds) if a.cpu_seconds > 0 else None,
+        "cpu_baseline": cpu_baseline(a.workload, a.cpu_passes, 3.0, rank) if a.cpu_passes > 0 else None,
         "clocks": clocks,
         "gpu_launches": a.steps,
     }
@@ -682,7 +746,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--kernels", default="jit", choices=["jit", "interp"],
                     help="specialised per-tree kernels (NVRTC) or the program interpreter")
-    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--cpu-passes", type=int, default=1,
+                    help="cpu_baseline: whole passes of the CPU restatement over the workload (0 = leave it out)")
     ap.add_argument("--pool-gb", type=float, default=40.0)
     ap.add_argument("--streams", type=int, default=3)
     ap.add_argument("--max-batch-requests", type=int, default=512)

@@ -324,7 +324,9 @@ __global__ void __launch_bounds__(kThreads, 4) interp_kernel(const FnProgramHead
     fne::grid_minmax(mn, mx, work, dminmax, smn, smx);
 }
 
-int g_num_sms = 0;
+// SM count per device ordinal, looked up on first use with that device current.
+constexpr int kSmCacheDevices = 64;
+std::atomic<int> g_num_sms[kSmCacheDevices];
 
 // Let a kernel stage up to 96 KB of program in dynamic shared memory, once per
 // device (the attribute is per device; `done` holds one bit per device ordinal).
@@ -413,13 +415,15 @@ int batch_occupancy(int block, uint32_t smem)
 
 int num_sms()
 {
-    if (!g_num_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_num_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_num_sms <= 0) g_num_sms = 1;
-    }
-    return g_num_sms;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    const bool cached = dev >= 0 && dev < kSmCacheDevices;
+    int n = cached ? g_num_sms[dev].load(std::memory_order_relaxed) : 0;
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 1;
+    // threads racing here look up and store the same value
+    if (cached) g_num_sms[dev].store(n, std::memory_order_relaxed);
+    return n;
 }
 
 cudaError_t launch_interpreter(const FnProgramHeader* prog, uint32_t prog_bytes, const PointArgs& args, float* out,

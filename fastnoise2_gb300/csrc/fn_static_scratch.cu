@@ -3,8 +3,6 @@
 // The ordinary device entry points keep their scratch (the tree's program blob
 // and the min/max reduction workspace) in memory that the library obtains with
 // cudaMalloc on first use.  Some callers cannot let a library allocate:
-//   * code running while a stream is being captured into a CUDA graph, where
-//     cudaMalloc / cudaFree are not legal in the default capture mode;
 //   * applications that hand all device memory to their own pool allocator at
 //     start-up, so a later cudaMalloc from a library fails or evicts their pool;
 //   * frame loops with a fixed time budget, where cudaFree synchronises the

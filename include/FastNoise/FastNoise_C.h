@@ -378,13 +378,15 @@ FASTNOISE_API int fnJitCheck(const void* const* nodes, const int* dimensions, in
 FASTNOISE_API int fnSetJitEnabled(int enabled);
 
 /* No counterpart in the reference.  fnGenUniformGrid3DDevice for callers that
- * cannot let the library allocate device memory: code running while a stream is
- * captured into a CUDA graph, applications whose own pool allocator owns all
- * device memory, frame loops that cannot absorb the device-wide synchronisation
- * of cudaFree.  It calls no cudaMalloc / cudaFree / cudaMallocHost and creates no
- * stream: the tree's program and the min/max workspace live in one fixed-size
- * static device array per device, filled by stream-ordered copies on `stream`
- * (NULL = the legacy default stream, not this thread's stream).
+ * cannot let the library allocate device memory: applications whose own pool
+ * allocator takes all device memory at start-up (a library cudaMalloc would then
+ * fail or shrink the pool), and frame loops with a fixed time budget that cannot
+ * absorb the device-wide synchronisation of cudaFree.  It calls no cudaMalloc /
+ * cudaFree / cudaMallocHost and creates no stream: the tree's program and the
+ * min/max workspace live in one fixed-size static device array per device,
+ * filled by stream-ordered copies on `stream`.
+ * - NULL stream: the legacy default stream (fnGenUniformGrid3DDevice reads NULL
+ *   as this thread's stream instead).
  * - Limit: the tree's compiled program must fit 16 KiB (several hundred nodes);
  *   larger trees return FN_ERR_CAPACITY without touching the GPU.
  * - The first call on a device looks up that device's array; make that first
@@ -392,7 +394,8 @@ FASTNOISE_API int fnSetJitEnabled(int enabled);
  * - Every call shares the array and it keeps the last call's contents; calls
  *   ordered on one stream are safe, calls that overlap on the GPU (different
  *   streams without ordering between them) race and give wrong results.
- * Arguments, outputs and the asynchronous behaviour are those of fnGenUniformGrid3DDevice. */
+ * The other arguments, the outputs and the asynchronous behaviour are those of
+ * fnGenUniformGrid3DDevice. */
 FASTNOISE_API int fnGenUniformGrid3DDeviceNoAlloc(const void* node, float* dOut, float xOffset, float yOffset,
                                                   float zOffset, int xCount, int yCount, int zCount, float xStepSize,
                                                   float yStepSize, float zStepSize, int seed, float* dMinMax,

@@ -2556,36 +2556,124 @@ static void run_range(job_t* j)
     j->mn = mn; j->mx = mx;
 }
 
-static void* run_range_thread(void* arg) { run_range((job_t*)arg); return NULL; }
+/* ------------------------------------------------------------------------- */
+/* Host worker pool (persistent: threads are created once and reused by every   */
+/* call, as an application keeps its job system).  A call hands the pool a list */
+/* of tasks; the calling thread works on them too.  Calls are serialised.       */
+/* ------------------------------------------------------------------------- */
 
+typedef struct { job_t* job; int64_t begin, end; float mn, mx; } task_t;
+
+#define OC_MAX_THREADS 256
+
+static pthread_mutex_t g_call_mu = PTHREAD_MUTEX_INITIALIZER;   /* one call at a time */
+static pthread_mutex_t g_pool_mu = PTHREAD_MUTEX_INITIALIZER;
+static pthread_cond_t g_pool_work = PTHREAD_COND_INITIALIZER;
+static pthread_cond_t g_pool_done = PTHREAD_COND_INITIALIZER;
+static int g_pool_threads = 0;           /* workers started (the caller is extra) */
+static uint64_t g_pool_gen = 0;          /* bumped per dispatch */
+static task_t* g_tasks = NULL;
+static int g_ntasks = 0, g_next_task = 0, g_active = 0, g_busy = 0;
+
+static void run_task(task_t* t)
+{
+    job_t j = *t->job;
+    j.begin = t->begin;
+    j.end = t->end;
+    run_range(&j);
+    t->mn = j.mn;
+    t->mx = j.mx;
+}
+
+/* Take tasks until none is left (pool mutex held on entry and exit). */
+static void drain_tasks_locked(void)
+{
+    while (g_next_task < g_ntasks) {
+        task_t* t = &g_tasks[g_next_task++];
+        pthread_mutex_unlock(&g_pool_mu);
+        run_task(t);
+        pthread_mutex_lock(&g_pool_mu);
+    }
+}
+
+static void* pool_worker(void* arg)
+{
+    int index = (int)(intptr_t)arg;
+    uint64_t seen = 0;
+    pthread_mutex_lock(&g_pool_mu);
+    for (;;) {
+        while (g_pool_gen == seen) pthread_cond_wait(&g_pool_work, &g_pool_mu);
+        seen = g_pool_gen;
+        if (index < g_active - 1) {      /* this dispatch asked for fewer threads than the pool has */
+            ++g_busy;
+            drain_tasks_locked();
+            if (--g_busy == 0) pthread_cond_broadcast(&g_pool_done);
+        }
+    }
+    return NULL;
+}
+
+/* Run `ntasks` tasks on `threads` threads (the caller included). */
+static void pool_run(task_t* tasks, int ntasks, int threads)
+{
+    if (threads < 1) threads = 1;
+    if (threads > OC_MAX_THREADS) threads = OC_MAX_THREADS;
+    if (threads > ntasks) threads = ntasks > 0 ? ntasks : 1;
+    pthread_mutex_lock(&g_pool_mu);
+    while (g_pool_threads < threads - 1) {
+        pthread_t tid;
+        if (pthread_create(&tid, NULL, pool_worker, (void*)(intptr_t)g_pool_threads) != 0) break;
+        pthread_detach(tid);
+        ++g_pool_threads;
+    }
+    if (threads > g_pool_threads + 1) threads = g_pool_threads + 1;
+    g_tasks = tasks;
+    g_ntasks = ntasks;
+    g_next_task = 0;
+    g_active = threads;
+    g_busy = 1;                          /* the caller */
+    ++g_pool_gen;
+    if (threads > 1) pthread_cond_broadcast(&g_pool_work);
+    drain_tasks_locked();
+    --g_busy;
+    while (g_busy > 0) pthread_cond_wait(&g_pool_done, &g_pool_mu);
+    g_tasks = NULL;
+    g_ntasks = 0;
+    pthread_mutex_unlock(&g_pool_mu);
+}
+
+/* OutputMinMax << OutputMinMax (Generator.h:99-104): min with min, max with max, so a
+   range whose values were all NaN (still +inf, -inf) leaves the result unchanged. */
+static void merge_minmax(const task_t* tasks, int ntasks, float* minmax)
+{
+    float mn = INFINITY, mx = -INFINITY;
+    for (int t = 0; t < ntasks; ++t) {
+        if (tasks[t].begin >= tasks[t].end) continue;
+        if (tasks[t].mn < mn) mn = tasks[t].mn;
+        if (mx < tasks[t].mx) mx = tasks[t].mx;
+    }
+    if (minmax) { minmax[0] = mn; minmax[1] = mx; }
+}
+
+/* One call: `total` points cut into `threads` contiguous ranges (slabs along the
+   outermost axis for grids), one task each. */
 static void run_jobs(job_t* proto, int64_t total, int threads, float* minmax)
 {
     if (threads < 1) threads = 1;
     if (total < 4096) threads = 1;
-    job_t jobs[256];
-    pthread_t tid[256];
-    if (threads > 256) threads = 256;
+    if (threads > OC_MAX_THREADS) threads = OC_MAX_THREADS;
+    task_t tasks[OC_MAX_THREADS];
     int64_t chunk = (total + threads - 1) / threads;
     for (int t = 0; t < threads; ++t) {
-        jobs[t] = *proto;
-        jobs[t].begin = (int64_t)t * chunk;
-        jobs[t].end = jobs[t].begin + chunk < total ? jobs[t].begin + chunk : total;
-        if (jobs[t].begin > total) jobs[t].begin = total;
+        int64_t b = (int64_t)t * chunk, e = b + chunk;
+        tasks[t].job = proto;
+        tasks[t].begin = b < total ? b : total;
+        tasks[t].end = e < total ? e : total;
     }
-    if (threads == 1) run_range(&jobs[0]);
-    else {
-        for (int t = 0; t < threads; ++t) pthread_create(&tid[t], NULL, run_range_thread, &jobs[t]);
-        for (int t = 0; t < threads; ++t) pthread_join(tid[t], NULL);
-    }
-    /* OutputMinMax << OutputMinMax (Generator.h:99-104): min with min, max with max, so a
-       range whose values were all NaN (still +inf, -inf) leaves the result unchanged. */
-    float mn = INFINITY, mx = -INFINITY;
-    for (int t = 0; t < threads; ++t) {
-        if (jobs[t].begin >= jobs[t].end) continue;
-        if (jobs[t].mn < mn) mn = jobs[t].mn;
-        if (mx < jobs[t].mx) mx = jobs[t].mx;
-    }
-    if (minmax) { minmax[0] = mn; minmax[1] = mx; }
+    pthread_mutex_lock(&g_call_mu);
+    pool_run(tasks, threads, threads);
+    pthread_mutex_unlock(&g_call_mu);
+    merge_minmax(tasks, threads, minmax);
 }
 
 OC_EXPORT void on_set_unfused(int unfused) { g_unfused = unfused; }
@@ -2632,6 +2720,105 @@ OC_EXPORT void on_gen_tileable(const on_node* root, float* out, int xSize, int y
     j.tmul[1] = 1 / ySizePi;
     int64_t total = (int64_t)(xSize > 0 ? xSize : 0) * (ySize > 0 ? ySize : 0);
     run_jobs(&j, total, threads, minmax);
+}
+
+/* A batch of requests (the product's fnGenRequest fields; kinds numbered as FN_KIND_*):
+ * every request is one task, so whole requests go to threads, largest first; a request
+ * of more than `split` points (split > 0) is cut into contiguous ranges of that size. */
+typedef struct {
+    const on_node* root;
+    int kind;
+    int seed;
+    int count[4];
+    float offset[4];
+    float step[4];
+    const float* positions[4];
+    float* out;
+    float* minmax;                       /* float[2]: the request's OutputMinMax */
+} on_request;
+
+static int64_t setup_request_job(job_t* j, const on_request* r)
+{
+    memset(j, 0, sizeof *j);
+    j->root = r->root;
+    j->kind = r->kind;
+    j->seed = r->seed;
+    j->out = r->out;
+    int64_t total = 1;
+    if (r->kind <= K_GRID4) {
+        int dim = r->kind + 2;
+        for (int k = 0; k < dim; ++k) {
+            j->count[k] = r->count[k]; j->offset[k] = r->offset[k]; j->step[k] = r->step[k];
+            total *= r->count[k] > 0 ? r->count[k] : 0;
+        }
+    } else if (r->kind == K_TILE2) {
+        const float pi2Recip = 0.15915493667f;             /* Generator.inl:386-392 */
+        j->count[0] = r->count[0]; j->count[1] = r->count[1];
+        float xSizePi = (float)r->count[0] * pi2Recip;
+        float ySizePi = (float)r->count[1] * pi2Recip;
+        j->tfreq[0] = xSizePi * r->step[0];
+        j->tfreq[1] = ySizePi * r->step[1];
+        j->tmul[0] = 1 / xSizePi;
+        j->tmul[1] = 1 / ySizePi;
+        total = (int64_t)(r->count[0] > 0 ? r->count[0] : 0) * (r->count[1] > 0 ? r->count[1] : 0);
+    } else {
+        int dim = r->kind - K_POS2 + 2;
+        for (int k = 0; k < dim; ++k) { j->posarr[k] = r->positions[k]; j->offset[k] = r->offset[k]; }
+        total = r->count[0] > 0 ? r->count[0] : 0;
+    }
+    return total;
+}
+
+static int cmp_task_size_desc(const void* a, const void* b)
+{
+    const task_t* x = (const task_t*)a;
+    const task_t* y = (const task_t*)b;
+    int64_t sx = x->end - x->begin, sy = y->end - y->begin;
+    return sx < sy ? 1 : sx > sy ? -1 : 0;
+}
+
+OC_EXPORT int on_gen_requests(const on_request* reqs, int n, int threads, int64_t split)
+{
+    if (n <= 0) return 0;
+    job_t* jobs = (job_t*)malloc(sizeof(job_t) * (size_t)n);
+    int64_t* totals = (int64_t*)malloc(sizeof(int64_t) * (size_t)n);
+    if (!jobs || !totals) { free(jobs); free(totals); return -1; }
+    int64_t ntasks = 0;
+    for (int i = 0; i < n; ++i) {
+        totals[i] = setup_request_job(&jobs[i], &reqs[i]);
+        ntasks += (split > 0 && totals[i] > split) ? (totals[i] + split - 1) / split : 1;
+    }
+    task_t* tasks = (task_t*)malloc(sizeof(task_t) * (size_t)ntasks);
+    if (!tasks) { free(jobs); free(totals); return -1; }
+    int64_t t = 0;
+    for (int i = 0; i < n; ++i) {
+        int64_t piece = (split > 0 && totals[i] > split) ? split : (totals[i] > 0 ? totals[i] : 1);
+        int64_t b = 0;
+        do {
+            tasks[t].job = &jobs[i];
+            tasks[t].begin = b < totals[i] ? b : totals[i];
+            tasks[t].end = b + piece < totals[i] ? b + piece : totals[i];
+            tasks[t].mn = INFINITY; tasks[t].mx = -INFINITY;
+            ++t;
+            b += piece;
+        } while (b < totals[i]);
+    }
+    qsort(tasks, (size_t)t, sizeof(task_t), cmp_task_size_desc);
+    pthread_mutex_lock(&g_call_mu);
+    pool_run(tasks, (int)t, threads);
+    pthread_mutex_unlock(&g_call_mu);
+    /* per request: min with min, max with max over its ranges (Generator.h:99-104) */
+    for (int i = 0; i < n; ++i) { jobs[i].mn = INFINITY; jobs[i].mx = -INFINITY; }
+    for (int64_t k = 0; k < t; ++k) {
+        job_t* j = tasks[k].job;
+        if (tasks[k].begin >= tasks[k].end) continue;
+        if (tasks[k].mn < j->mn) j->mn = tasks[k].mn;
+        if (j->mx < tasks[k].mx) j->mx = tasks[k].mx;
+    }
+    for (int i = 0; i < n; ++i)
+        if (reqs[i].minmax) { reqs[i].minmax[0] = jobs[i].mn; reqs[i].minmax[1] = jobs[i].mx; }
+    free(tasks); free(jobs); free(totals);
+    return 0;
 }
 
 OC_EXPORT float on_gen_single(const on_node* root, int dim, const float* pos, int seed)

@@ -1,8 +1,8 @@
 """ctypes front-end to the C oracle (TEST INFRASTRUCTURE, never shipped).
 
 Builds ``oracle/fn_oracle.c`` into ``oracle/_build/libfn_oracle.so`` with the
-recipe in :func:`build` (plain gcc, ``-ffp-contract=off`` so that only the
-explicit ``fmaf`` calls fuse), instantiates a :class:`oracle.tree.Node` tree by
+recipe in :func:`build` (gcc ``-O3`` tuned for the host CPU, ``-ffp-contract=off``
+so that only the explicit ``fmaf`` calls fuse), instantiates a :class:`oracle.tree.Node` tree by
 replaying its setter calls in order, and exposes the reference's batch drivers
 (``Generator.inl`` GenUniformGrid2D/3D/4D, GenPositionArray2D/3D/4D,
 GenTileable2D, GenSingle*), each returning ``(values, (min, max))``.
@@ -39,12 +39,50 @@ def build(force: bool = False) -> str:
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB
     flags = ["-O3", "-std=c11", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared", "-fvisibility=hidden"]
-    if platform.machine() in ("x86_64", "AMD64"):
-        flags.append("-mfma")            # hardware fmaf; the result is the same IEEE fused op
+    flags += native_cpu_flags()          # hardware fmaf and the host's vector units; IEEE results unchanged
     tmp = LIB + f".tmp{os.getpid()}"
     subprocess.run(["gcc", *flags, "-o", tmp, SRC, "-lm", "-lpthread"], check=True)
     os.replace(tmp, LIB)
     return LIB
+
+
+def native_cpu_flags():
+    """Code generation for the CPU this runs on: ``-march=native`` on x86-64,
+    ``-mcpu=native`` on AArch64 (GCC's spelling for each)."""
+    m = platform.machine()
+    if m in ("x86_64", "AMD64"):
+        return ["-march=native"]
+    if m in ("aarch64", "arm64"):
+        return ["-mcpu=native"]
+    return []
+
+
+def cpu_description() -> dict:
+    """Host CPU facts recorded beside every CPU timing: architecture, model name, threads."""
+    model = ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                key = line.split(":", 1)[0].strip().lower()
+                if key in ("model name", "cpu model", "hardware") and ":" in line:
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if not model and platform.machine() in ("aarch64", "arm64"):
+        # Arm kernels list implementer / part numbers instead of a name
+        try:
+            parts = {}
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if ":" in line:
+                        k, v = line.split(":", 1)
+                        parts.setdefault(k.strip(), v.strip())
+            model = f"implementer {parts.get('CPU implementer', '?')} part {parts.get('CPU part', '?')}"
+        except OSError:
+            pass
+    return {"uname_m": platform.machine(), "cpu_model": model, "nproc": os.cpu_count(),
+            "compiler_flags": " ".join(["-O3", "-ffp-contract=off", *native_cpu_flags()])}
 
 
 def build_count(force: bool = False) -> str:
@@ -120,6 +158,8 @@ def lib():
         L.on_gen_tileable.argtypes = [vp, fp, c_int, c_int, c_float, c_float, c_int, c_int, fp]
         L.on_gen_single.restype = c_float
         L.on_gen_single.argtypes = [vp, c_int, fp, c_int]
+        L.on_gen_requests.restype = c_int
+        L.on_gen_requests.argtypes = [ctypes.c_void_p, c_int, c_int, ctypes.c_int64]
         L.fn_sinf.restype = c_float
         L.fn_sinf.argtypes = [c_float]
         L.fn_cosf.restype = c_float
@@ -210,6 +250,44 @@ class OracleTree:
         p[:len(pos)] = pos
         self._mode()
         return float(lib().on_gen_single(self.root, len(pos), _fptr(p), int(np.int32(seed))))
+
+
+class OracleRequest(ctypes.Structure):
+    """One request of :func:`gen_requests` (the fields of the product's fnGenRequest)."""
+    _fields_ = [("root", ctypes.c_void_p), ("kind", ctypes.c_int), ("seed", ctypes.c_int),
+                ("count", ctypes.c_int * 4), ("offset", ctypes.c_float * 4), ("step", ctypes.c_float * 4),
+                ("positions", ctypes.POINTER(ctypes.c_float) * 4), ("out", ctypes.POINTER(ctypes.c_float)),
+                ("minmax", ctypes.POINTER(ctypes.c_float))]
+
+
+KIND_GRID2D, KIND_GRID3D, KIND_GRID4D, KIND_TILEABLE2D, KIND_POSITIONS2D, KIND_POSITIONS3D, KIND_POSITIONS4D = range(7)
+
+
+def request(tree: "OracleTree", kind: int, out: np.ndarray, minmax: np.ndarray, seed: int, count=(0, 0, 0, 0),
+            offset=(0, 0, 0, 0), step=(1, 1, 1, 1), positions=()) -> OracleRequest:
+    """Fill one OracleRequest; `out` (float32) and `minmax` (float32[2]) must stay alive until the call."""
+    r = OracleRequest()
+    r.root = tree.root
+    r.kind = kind
+    r.seed = int(np.int32(seed))
+    for k in range(4):
+        r.count[k] = int(count[k]) if k < len(count) else 0
+        r.offset[k] = float(offset[k]) if k < len(offset) else 0.0
+        r.step[k] = float(step[k]) if k < len(step) else 1.0
+        r.positions[k] = _fptr(positions[k]) if k < len(positions) else None
+    r.out = _fptr(out)
+    r.minmax = _fptr(minmax)
+    return r
+
+
+def gen_requests(reqs: Sequence[OracleRequest], threads: int = 0, split: int = 0, unfused: bool = False) -> None:
+    """Evaluate a batch of requests on the oracle's persistent worker pool: whole requests go
+    to threads, largest first (requests above `split` points, when split > 0, are cut into
+    ranges of that size).  Fills every request's out and minmax."""
+    arr = (OracleRequest * len(reqs))(*reqs)
+    lib().on_set_unfused(1 if unfused else 0)
+    if lib().on_gen_requests(ctypes.cast(arr, ctypes.c_void_p), len(reqs), threads or os.cpu_count(), int(split)) != 0:
+        raise MemoryError("oracle batch: allocation failed")
 
 
 def sinf(x: float) -> float:

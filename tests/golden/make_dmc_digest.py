@@ -43,7 +43,9 @@ def parse(path: str):
 
 
 def main():
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_dmc_digest.py /path/to/FastNoise2")
+    ref_root = sys.argv[1]
     table = parse(os.path.join(ref_root, "tools", "NodeEditor", "util", "DmcTable.inl"))
     out = {
         "source": "tools/NodeEditor/util/DmcTable.inl kDualPointsList",

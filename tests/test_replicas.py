@@ -52,7 +52,7 @@ def test_reference_arm_under_torchrun_prints_once():
     pytest.importorskip("torch")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(_free_port()), "bench.py", "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-seconds", "0.3", "--workload", "simplex-64"]
+           "--gpus", "2", "--steps", "1", "--warmup", "0", "--workload", "simplex-64"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -60,3 +60,5 @@ def test_reference_arm_under_torchrun_prints_once():
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
+    assert line["config"]["points_per_step"] == 64 ** 3
+    assert line["cpu_baseline"]["single_thread"]["value"] > 0 and line["cpu_baseline"]["host"]["nproc"] >= 1

@@ -18,10 +18,10 @@ from tests import trees
 FN_ERR_CAPACITY = -4
 
 
-def _call(fn, entry, node, out_ptr, offset, count, step, seed, mm_ptr):
+def _call(fn, entry, node, out_ptr, offset, count, step, seed, mm_ptr, stream=0):
     f = getattr(fn.lib(), entry)
     return f(node._h, ctypes.c_void_p(out_ptr), *map(float, offset), *map(int, count), *map(float, step),
-             int(np.int32(seed)), ctypes.c_void_p(mm_ptr), None)
+             int(np.int32(seed)), ctypes.c_void_p(mm_ptr), ctypes.c_void_p(stream) if stream else None)
 
 
 def _deep_chain(links):
@@ -67,6 +67,36 @@ def test_no_alloc_matches_device_entry_point_twice(gpu):
         rc = _call(fn, "fnGenUniformGrid3DDeviceNoAlloc", node, out.data_ptr(), off, cnt, st, seed, mm.data_ptr())
         assert rc == 0, fn.lib().fnGetLastErrorString()
     torch.cuda.synchronize()
+    for (ref, ref_mm), (out, mm) in zip(refs, gots):
+        assert torch.equal(out.view(torch.int32), ref.view(torch.int32))
+        assert torch.equal(mm.view(torch.int32), ref_mm.view(torch.int32))
+
+
+@pytest.mark.gpu
+def test_no_alloc_back_to_back_on_a_non_blocking_stream(gpu):
+    """Two calls queued on a non-blocking stream with nothing between them: the second call's
+    copies into the shared array must wait for the first call's kernel by stream order alone
+    (no implicit synchronisation of the legacy default stream helps here)."""
+    torch = pytest.importorskip("torch")
+    fn = gpu
+    cases = [
+        (trees.to_product(trees.fbm_perlin_c1()), (-40.0, 12.5, 3.0), (96, 80, 72), (1.0, 1.0, 1.0), 42),
+        (trees.to_product(trees.cellular_lookup_tree()), (7.0, -9.0, 100.0), (33, 65, 17), (0.5, 2.0, 1.0), -5),
+    ]
+    refs = []
+    for node, off, cnt, st, seed in cases:
+        ref = torch.full((int(np.prod(cnt)),), float("nan"), device="cuda")
+        ref_mm = torch.zeros(2, device="cuda")
+        assert _call(fn, "fnGenUniformGrid3DDevice", node, ref.data_ptr(), off, cnt, st, seed, ref_mm.data_ptr()) == 0
+        refs.append((ref, ref_mm))
+    gots = [(torch.full((int(np.prod(c[2])),), float("nan"), device="cuda"), torch.zeros(2, device="cuda")) for c in cases]
+    torch.cuda.synchronize()
+    stream = torch.cuda.Stream()                     # created with cudaStreamNonBlocking
+    for (node, off, cnt, st, seed), (out, mm) in zip(cases, gots):
+        rc = _call(fn, "fnGenUniformGrid3DDeviceNoAlloc", node, out.data_ptr(), off, cnt, st, seed, mm.data_ptr(),
+                   stream.cuda_stream)
+        assert rc == 0, fn.lib().fnGetLastErrorString()
+    stream.synchronize()
     for (ref, ref_mm), (out, mm) in zip(refs, gots):
         assert torch.equal(out.view(torch.int32), ref.view(torch.int32))
         assert torch.equal(mm.view(torch.int32), ref_mm.view(torch.int32))
