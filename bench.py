@@ -501,34 +501,57 @@ def run_served(fn, chunks, nodes, rank, a, dev):
     for t in [srv.submit(r) for r in serve]:           # warm the extra kinds
         srv.wait(t)
         srv.release(t)
-    open_loop = []
+    # the per-call path needs outputs of its own: one device buffer holding every distinct request's output
+    serve_total = int(sum(serve_pts))
+    pc_out = torch.empty(serve_total, dtype=torch.float32, device=dev)
+    pc_reqs, off = [], 0
+    for r, n_pts in zip(serve, serve_pts):
+        q = fn.GenRequest.from_buffer_copy(r)
+        q._keep = r._keep
+        q.out = pc_out.data_ptr() + 4 * off
+        pc_reqs.append(q)
+        off += n_pts
+    stream = torch.cuda.current_stream(dev).cuda_stream
+    fn.gen_each(pc_reqs, stream, sync=True)              # warm the per-call path
+    open_loop, per_call_open = [], []
     rng = np.random.default_rng(5)
     for rate in a.rates:
-        srv.reset_stats()
         n = min(4 * len(serve), max(200, int(rate * a.open_seconds)))
-        gaps = rng.exponential(1.0 / rate, n)
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n)) * 1e6      # microseconds after the start
+        idx = [k % len(serve) for k in range(n)]
+        served_pts = sum(serve_pts[k] for k in idx)
+        # served: one native submitter follows the arrival schedule; latency counts from arrival
+        srv.reset_stats()
+        rarr = fn.request_array([serve[k] for k in idx])
         t_start = time.perf_counter()
-        due = t_start
-        tickets = (ctypes.c_ulonglong * n)()
-        for k in range(n):
-            due += gaps[k]
-            while time.perf_counter() < due:
-                pass
-            tickets[k] = srv.submit(serve[k % len(serve)])
-        srv.wait_many(tickets, timeout_ms=60000)         # one native wait: the last completion ends the run
+        tickets = srv.submit_paced(rarr, arrivals)
+        srv.wait_many(tickets, timeout_ms=120000)
         wall = time.perf_counter() - t_start
         st = srv.stats()
         for t in tickets:
             srv.release(t)
-        served_pts = sum(serve_pts[k % len(serve)] for k in range(n))
         open_loop.append({"rate_req_s": rate, "achieved_req_s": n / wall, "requests": n,
                           "p50_ms": st["p50Micros"] / 1e3, "p99_ms": st["p99Micros"] / 1e3,
-                          "max_ms": st["maxMicros"] / 1e3, "Mpoints_s": served_pts / wall / 1e6, "batches": st["batches"]})
+                          "max_ms": st["maxMicros"] / 1e3, "Mpoints_s": served_pts / wall / 1e6, "batches": st["batches"],
+                          "overlapped_batches": st["overlappedBatches"], "max_concurrent_batches": st["maxConcurrentBatches"]})
+        # per-call: the same arrivals, one fnGen*Device launch per request on one stream
+        parr = fn.request_array([pc_reqs[k] for k in idx])
+        t_start = time.perf_counter()
+        lat = fn.gen_each_paced(parr, arrivals, stream)
+        wall = time.perf_counter() - t_start
+        per_call_open.append({"rate_req_s": rate, "achieved_req_s": n / wall, "requests": n,
+                              "p50_ms": float(np.percentile(lat, 50)) / 1e3, "p99_ms": float(np.percentile(lat, 99)) / 1e3,
+                              "max_ms": float(lat.max()) / 1e3, "Mpoints_s": served_pts / wall / 1e6})
+    del pc_out
     srv.close()
     result["open_loop"] = open_loop
+    result["per_call_open_loop"] = per_call_open
     result["config"] = {"pool_gb": a.pool_gb, "streams": a.streams, "max_batch_requests": a.max_batch_requests,
                         "open_loop_mix": f"chunk mix + per {a.extra_every} chunks one GenUniformGrid4D 32^4 and one "
-                                         "GenPositionArray3D 1M positions U[-1e4,1e4]^3; Poisson arrivals"}
+                                         "GenPositionArray3D 1M positions U[-1e4,1e4]^3; Poisson arrivals",
+                        "open_loop_latency": "arrival -> min/max on the host; served: fnServerSubmitPaced + fnServerWaitMany; "
+                                             "per_call_open_loop: fnGenEachPaced (one fnGen*Device launch per request on one "
+                                             "stream, min/max copied back, completion seen by a second host thread)"}
     return result
 
 
@@ -751,7 +774,8 @@ def main():
     ap.add_argument("--pool-gb", type=float, default=40.0)
     ap.add_argument("--streams", type=int, default=3)
     ap.add_argument("--max-batch-requests", type=int, default=512)
-    ap.add_argument("--rates", type=float, nargs="*", default=[1000.0, 5000.0, 10000.0, 20000.0, 50000.0])
+    ap.add_argument("--rates", type=float, nargs="*",
+                    default=[1000.0, 5000.0, 10000.0, 20000.0, 50000.0, 100000.0, 200000.0, 400000.0])
     ap.add_argument("--extra-every", type=int, default=64,
                     help="serving mix: one GenUniformGrid4D 32^4 and one GenPositionArray3D 1M request per this many chunks")
     ap.add_argument("--open-seconds", type=float, default=0.5)

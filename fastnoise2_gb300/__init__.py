@@ -147,6 +147,12 @@ def _declare(L):
         "fnLiveTreeDelete": (None, [vp]),
         "fnAutotuneLoad": (c_int, [cp]),
         "fnAutotuneSave": (c_int, [cp]),
+        "fnServerSubmitPaced": (c_int, [vp, vp, c_int, vp, vp]),
+        "fnGenEachPaced": (c_int, [vp, c_int, vp, vp, vp]),
+        "fnGetVariableBits": (c_int, [vp, c_int, ctypes.POINTER(c_int)]),
+        "fnGetNodeLookupRef": (vp, [vp, c_int]),
+        "fnGetHybridNodeLookupRef": (vp, [vp, c_int]),
+        "fnGetHybridFloat": (c_int, [vp, c_int, ctypes.POINTER(c_float)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -231,6 +237,18 @@ def gen_each(requests, stream: int = 0, sync: bool = True) -> None:
     arr = request_array(requests)
     if lib().fnGenEachDevice(arr, len(requests), stream or None, BATCH_SYNC if sync else 0) != 0:
         _check()
+
+
+def gen_each_paced(requests, arrivals_us, stream: int = 0) -> np.ndarray:
+    """fnGenEachPaced: the per-call path driven by arrival times; returns each request's latency
+    (microseconds from its arrival to its min/max on the host)."""
+    arr = request_array(requests)
+    times = np.ascontiguousarray(arrivals_us, np.float64)
+    assert len(times) == len(arr)
+    lat = np.zeros(len(arr), np.float64)
+    if lib().fnGenEachPaced(arr, len(arr), times.ctypes.data, stream or None, lat.ctypes.data) != 0:
+        _check()
+    return lat
 
 
 def autotune_batch(requests, stream: int = 0) -> None:
@@ -470,7 +488,8 @@ class ServerStats(ctypes.Structure):
                 ("batches", ctypes.c_ulonglong), ("points", ctypes.c_ulonglong), ("p50Micros", ctypes.c_double),
                 ("p99Micros", ctypes.c_double), ("maxMicros", ctypes.c_double), ("meanMicros", ctypes.c_double),
                 ("poolUsed", ctypes.c_ulonglong), ("poolCapacity", ctypes.c_ulonglong), ("queueDepth", ctypes.c_int),
-                ("inflight", ctypes.c_int)]
+                ("inflight", ctypes.c_int), ("overlappedBatches", ctypes.c_ulonglong), ("maxInflightBatches", ctypes.c_int),
+                ("maxConcurrentBatches", ctypes.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -511,6 +530,18 @@ class Server:
         if lib().fnServerSubmitMany(self._h, arr, n, t) != 0:
             _check()
         return t if as_array else list(t)
+
+    def submit_paced(self, requests, arrivals_us):
+        """Open-loop submission (fnServerSubmitPaced): requests[k] is queued arrivals_us[k]
+        microseconds after the call starts; returns the tickets (a ctypes array)."""
+        n = len(requests)
+        arr = request_array(requests)
+        times = np.ascontiguousarray(arrivals_us, np.float64)
+        assert len(times) == n
+        t = (ctypes.c_ulonglong * n)()
+        if lib().fnServerSubmitPaced(self._h, arr, n, times.ctypes.data, t) != 0:
+            _check()
+        return t
 
     def wait_many(self, tickets, timeout_ms: int = -1) -> None:
         """Wait until every ticket has finished; raises FastNoiseError on failure or timeout."""

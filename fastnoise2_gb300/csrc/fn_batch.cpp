@@ -264,6 +264,7 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         r.minmax = items[i].dminmax;
         r.host_minmax = items[i].host_minmax;
         r.host_done = items[i].host_done;
+        r.host_time = items[i].host_time;
         r.n_tiles = tiles_for(items[i].args.total, tp);
         states[i].mn_enc = 0xFFFFFFFFu;
         states[i].mx_enc = 0u;

@@ -20,6 +20,7 @@ struct BatchItem {
     float* dminmax = nullptr;          // device float[2] or null
     float* host_minmax = nullptr;      // mapped pinned float[2] or null
     unsigned int* host_done = nullptr; // mapped pinned completion flag or null
+    unsigned long long* host_time = nullptr;  // mapped pinned: device clock (ns) at completion, or null
 };
 
 struct BatchTuning {

@@ -5,11 +5,14 @@
 // through the program interpreter; host output arrays are filled by a
 // device->host copy on this thread's stream.
 #include <algorithm>
+#include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <limits>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/FastNoise/FastNoise_C.h"
@@ -767,6 +770,46 @@ int fnSerialiseNodeTree(const void* node, char* buffer, int bufferSize)
     return (int)s.size();
 }
 
+int fnGetVariableBits(const void* node, int variableIndex, int* bits)
+{
+    clear_error();
+    if (!node || !bits) { set_error(FN_ERR_ARG, "null node or output"); return FN_ERR_ARG; }
+    const Node* n = N(node);
+    if (variableIndex < 0 || variableIndex >= (int)n->vars.size()) { set_error(FN_ERR_ARG, "variable index out of range"); return FN_ERR_ARG; }
+    *bits = n->vars[variableIndex];
+    return FN_OK;
+}
+
+void* fnGetNodeLookupRef(const void* node, int nodeLookupIndex)
+{
+    if (!node) return nullptr;
+    const Node* n = N(node);
+    if (nodeLookupIndex < 0 || nodeLookupIndex >= (int)n->lookups.size()) return nullptr;
+    Node* c = n->lookups[nodeLookupIndex];
+    node_ref(c);
+    return c;
+}
+
+void* fnGetHybridNodeLookupRef(const void* node, int hybridIndex)
+{
+    if (!node) return nullptr;
+    const Node* n = N(node);
+    if (hybridIndex < 0 || hybridIndex >= (int)n->hnodes.size()) return nullptr;
+    Node* c = n->hnodes[hybridIndex];
+    node_ref(c);
+    return c;
+}
+
+int fnGetHybridFloat(const void* node, int hybridIndex, float* value)
+{
+    clear_error();
+    if (!node || !value) { set_error(FN_ERR_ARG, "null node or output"); return FN_ERR_ARG; }
+    const Node* n = N(node);
+    if (hybridIndex < 0 || hybridIndex >= (int)n->hvals.size()) { set_error(FN_ERR_ARG, "hybrid index out of range"); return FN_ERR_ARG; }
+    *value = n->hvals[hybridIndex];
+    return FN_OK;
+}
+
 int fnGenBatchDevice(const fnGenRequest* requests, int count, void* stream, int flags)
 {
     clear_error();
@@ -886,6 +929,75 @@ int fnGenEachDevice(const fnGenRequest* requests, int count, void* stream, int f
     return FN_OK;
 }
 
+int fnGenEachPaced(const fnGenRequest* requests, int count, const double* arrivalMicros, void* stream,
+                   double* latencyMicros)
+{
+    clear_error();
+    if (count < 0 || (count > 0 && (!requests || !arrivalMicros))) { set_error(FN_ERR_ARG, "invalid request list"); return FN_ERR_ARG; }
+    if (count == 0) return FN_OK;
+    std::vector<PointArgs> args((size_t)count);
+    for (int i = 0; i < count; ++i)
+        if (!requests[i].node || !request_args(requests[i], args[i])) { set_error(FN_ERR_ARG, "invalid request"); return FN_ERR_ARG; }
+    if (!thread_ctx()) return FN_ERR_CUDA;
+    BatchCtx* b = batch_ctx((size_t)count);
+    if (!b) return FN_ERR_CUDA;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::vector<cudaEvent_t> ev((size_t)count, nullptr);
+    for (auto& e : ev)
+        if (!cuda_ok(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event")) {
+            for (auto& x : ev) if (x) cudaEventDestroy(x);
+            return FN_ERR_CUDA;
+        }
+    using clock = std::chrono::steady_clock;
+    std::vector<clock::time_point> done((size_t)count);
+    std::atomic<int> issued{0};
+    std::atomic<int> stop{0};
+    const clock::time_point start = clock::now();
+    // completion side: requests finish in stream order, so wait on them in order
+    std::thread waiter([&] {
+        cudaSetDevice(dev);
+        for (int k = 0; k < count; ++k) {
+            while (issued.load(std::memory_order_acquire) <= k) {
+                if (stop.load(std::memory_order_acquire)) return;
+                std::this_thread::yield();
+            }
+            if (cudaEventSynchronize(ev[(size_t)k]) != cudaSuccess) { stop = 2; return; }
+            done[(size_t)k] = clock::now();
+        }
+    });
+    int rc = FN_OK;
+    for (int k = 0; k < count && rc == FN_OK; ++k) {
+        const clock::time_point due = start + std::chrono::duration_cast<clock::duration>(
+                                                  std::chrono::duration<double, std::micro>(arrivalMicros[k]));
+        while (clock::now() < due) {
+        }
+        rc = gen_device(requests[k].node, args[(size_t)k], requests[k].out, b->dminmax + 2 * k, stream);
+        if (rc == FN_OK &&
+            (!cuda_ok(cudaMemcpyAsync(b->hminmax + 2 * k, b->dminmax + 2 * k, 2 * sizeof(float), cudaMemcpyDeviceToHost, s),
+                      "copy minmax") ||
+             !cuda_ok(cudaEventRecord(ev[(size_t)k], s), "event record")))
+            rc = FN_ERR_CUDA;
+        if (rc == FN_OK) issued.store(k + 1, std::memory_order_release);
+    }
+    if (rc != FN_OK) stop = 1;
+    waiter.join();
+    if (rc == FN_OK && stop.load() == 2) { set_error(FN_ERR_CUDA, "request failed on the device"); rc = FN_ERR_CUDA; }
+    if (rc == FN_OK) {
+        for (int k = 0; k < count; ++k) {
+            if (latencyMicros)
+                latencyMicros[k] = std::chrono::duration<double, std::micro>(done[(size_t)k] - start).count() - arrivalMicros[k];
+            if (requests[k].minMax) {
+                requests[k].minMax[0] = b->hminmax[2 * k];
+                requests[k].minMax[1] = b->hminmax[2 * k + 1];
+            }
+        }
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc;
+}
+
 int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream)
 {
     clear_error();
@@ -969,6 +1081,29 @@ int fnServerSubmitMany(void* server, const fnGenRequest* requests, int count, un
     return rc;
 }
 
+int fnServerSubmitPaced(void* server, const fnGenRequest* requests, int count, const double* arrivalMicros,
+                        unsigned long long* tickets)
+{
+    clear_error();
+    if (!server || count < 0 || (count > 0 && (!requests || !tickets || !arrivalMicros))) {
+        set_error(FN_ERR_ARG, "invalid arguments");
+        return FN_ERR_ARG;
+    }
+    std::vector<BatchItem> items((size_t)count);
+    for (int i = 0; i < count; ++i) {
+        items[i].node = N(requests[i].node);
+        if (!items[i].node || !request_args(requests[i], items[i].args)) {
+            set_error(FN_ERR_ARG, "request " + std::to_string(i) + ": invalid node, kind or positions");
+            return FN_ERR_ARG;
+        }
+        items[i].dout = requests[i].out;
+    }
+    std::vector<uint64_t> t((size_t)count);
+    int rc = static_cast<Server*>(server)->submit_paced(items.data(), items.size(), arrivalMicros, t.data());
+    if (rc == 0) for (int i = 0; i < count; ++i) tickets[i] = t[i];
+    return rc;
+}
+
 int fnServerWaitMany(void* server, const unsigned long long* tickets, int count, int timeoutMs)
 {
     clear_error();
@@ -1017,6 +1152,9 @@ int fnServerGetStats(void* server, fnServerStats* out)
     out->poolCapacity = s.pool_capacity;
     out->queueDepth = s.queue_depth;
     out->inflight = s.inflight;
+    out->overlappedBatches = s.overlapped_batches;
+    out->maxInflightBatches = s.max_inflight_batches;
+    out->maxConcurrentBatches = s.max_concurrent_batches;
     return FN_OK;
 }
 

@@ -175,6 +175,11 @@ __device__ __forceinline__ void finish_tile(const fn::BatchRequest& rq, fn::Batc
             hm[0] = fmn;
             hm[1] = fmx;
         }
+        if (rq.host_time) {
+            unsigned long long t;
+            asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+            *(volatile unsigned long long*)rq.host_time = t;
+        }
         __threadfence_system();
         if (rq.host_done) atomicExch_system(rq.host_done, 1u);
         atomicAdd(&hdr->requests_done, 1u);

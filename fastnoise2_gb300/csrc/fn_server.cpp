@@ -105,9 +105,8 @@ Server::~Server()
     if (slots_) cudaFreeHost(slots_);
 }
 
-int Server::submit(const BatchItem& item, uint64_t& ticket)
+int Server::validate(const BatchItem& item)
 {
-    if (!ok_) { set_error(-6, "server is not running"); return -6; }
     if (!item.node || item.args.total < 0) { set_error(-1, "invalid request"); return -1; }
     DeviceProgram p;                      // compile now so the submitter sees tree errors
     if (!get_program(item.node, item.args.dim, p)) return last_error();
@@ -115,15 +114,47 @@ int Server::submit(const BatchItem& item, uint64_t& ticket)
     if (!jit_ensure(p.host, jerr)) { set_error(-2, jerr); return -2; }
     const size_t bytes = (size_t)std::max(0ll, item.args.total) * sizeof(float);
     if (!item.dout && bytes > pool_.capacity()) { set_error(-4, "request output larger than the device pool"); return -4; }
+    return 0;
+}
+
+int Server::enqueue_locked(const BatchItem& item, std::chrono::steady_clock::time_point t_submit, uint64_t& ticket)
+{
     node_ref(const_cast<Node*>(item.node));
-    std::lock_guard<std::mutex> lk(mu_);
     ticket = next_ticket_++;
     Record& r = recs_[ticket];
     r.item = item;
-    r.t_submit = std::chrono::steady_clock::now();
+    r.t_submit = t_submit;
     queue_.push_back(ticket);
     ++submitted_;
+    return 0;
+}
+
+int Server::submit(const BatchItem& item, uint64_t& ticket)
+{
+    if (!ok_) { set_error(-6, "server is not running"); return -6; }
+    if (int rc = validate(item)) return rc;
+    std::lock_guard<std::mutex> lk(mu_);
+    enqueue_locked(item, std::chrono::steady_clock::now(), ticket);
     cv_work_.notify_one();
+    return 0;
+}
+
+int Server::submit_paced(const BatchItem* items, size_t n, const double* arrival_us, uint64_t* tickets)
+{
+    if (!ok_) { set_error(-6, "server is not running"); return -6; }
+    for (size_t i = 0; i < n; ++i)
+        if (int rc = validate(items[i])) return rc;
+    using clock = std::chrono::steady_clock;
+    const clock::time_point start = clock::now();
+    for (size_t i = 0; i < n; ++i) {
+        const clock::time_point due = start + std::chrono::duration_cast<clock::duration>(
+                                                  std::chrono::duration<double, std::micro>(arrival_us[i]));
+        while (clock::now() < due) {
+        }
+        std::lock_guard<std::mutex> lk(mu_);
+        enqueue_locked(items[i], due, tickets[i]);
+        cv_work_.notify_one();
+    }
     return 0;
 }
 
@@ -131,30 +162,14 @@ int Server::submit_many(const BatchItem* items, size_t n, uint64_t* tickets)
 {
     if (!ok_) { set_error(-6, "server is not running"); return -6; }
     for (size_t i = 0; i < n; ++i) {        // validate and compile everything before queueing anything
-        const BatchItem& item = items[i];
-        if (!item.node || item.args.total < 0) { set_error(-1, "invalid request " + std::to_string(i)); return -1; }
-        DeviceProgram p;
-        if (!get_program(item.node, item.args.dim, p)) return last_error();
-        std::string jerr;
-        if (!jit_ensure(p.host, jerr)) { set_error(-2, jerr); return -2; }
-        const size_t bytes = (size_t)std::max(0ll, item.args.total) * sizeof(float);
-        if (!item.dout && bytes > pool_.capacity()) {
-            set_error(-4, "request " + std::to_string(i) + " output larger than the device pool");
-            return -4;
+        if (int rc = validate(items[i])) {
+            set_error(rc, "request " + std::to_string(i) + ": " + last_error_string());
+            return rc;
         }
     }
     const auto now = std::chrono::steady_clock::now();
-    for (size_t i = 0; i < n; ++i) node_ref(const_cast<Node*>(items[i].node));
     std::lock_guard<std::mutex> lk(mu_);
-    for (size_t i = 0; i < n; ++i) {
-        const uint64_t t = next_ticket_++;
-        Record& r = recs_[t];
-        r.item = items[i];
-        r.t_submit = now;
-        queue_.push_back(t);
-        tickets[i] = t;
-    }
-    submitted_ += n;
+    for (size_t i = 0; i < n; ++i) enqueue_locked(items[i], now, tickets[i]);
     cv_work_.notify_one();
     return 0;
 }
@@ -254,6 +269,9 @@ void Server::stats(ServerStats& s)
     int inflight = 0;
     for (auto& kv : recs_) inflight += kv.second.state == kInflight;
     s.inflight = inflight;
+    s.overlapped_batches = overlapped_;
+    s.max_inflight_batches = max_inflight_;
+    s.max_concurrent_batches = max_concurrent_;
 }
 
 void Server::reset_stats()
@@ -261,6 +279,31 @@ void Server::reset_stats()
     std::lock_guard<std::mutex> lk(mu_);
     lat_us_.clear();
     submitted_ = completed_ = failed_ = batches_ = points_ = 0;
+    spans_.clear();
+    overlapped_ = 0;
+    max_inflight_ = max_concurrent_ = 0;
+}
+
+// A retired batch's span of request completions on the device clock.  A batch that has
+// completed a request by time t and completes another at t or later is executing at t, so
+// two batches whose spans intersect were on the GPU together.
+void Server::record_span(unsigned long long first, unsigned long long last)
+{
+    Span mine{first, last, false};
+    for (Span& o : spans_) {
+        if (o.first <= mine.last && mine.first <= o.last) {
+            if (!o.counted) { o.counted = true; ++overlapped_; }
+            if (!mine.counted) { mine.counted = true; ++overlapped_; }
+        }
+    }
+    spans_.push_back(mine);
+    if (spans_.size() > 64) spans_.pop_front();
+    // most spans covering one moment: the maximum is reached at some span's start
+    for (const Span& a : spans_) {
+        int n = 0;
+        for (const Span& b : spans_) n += b.first <= a.first && a.first <= b.last;
+        max_concurrent_ = std::max(max_concurrent_, n);
+    }
 }
 
 void Server::retire()
@@ -283,6 +326,9 @@ void Server::retire()
             if (sl->done) {
                 r.minmax[0] = sl->minmax[0];
                 r.minmax[1] = sl->minmax[1];
+                const unsigned long long td = sl->t_done;
+                f.dev_first = std::min(f.dev_first, td);
+                f.dev_last = std::max(f.dev_last, td);
                 r.state = kDone;
                 r.t_done = now;
                 free_slots_.push_back(r.slot);
@@ -301,6 +347,8 @@ void Server::retire()
                     if (r.state == kInflight) { r.state = kFailed; free_slots_.push_back(r.slot); ++failed_; any = true; }
                 }
                 set_error(-3, "batch finished without completing every request");
+            } else if (f.dev_first <= f.dev_last) {
+                record_span(f.dev_first, f.dev_last);
             }
             f.busy = false;
             f.tickets.clear();
@@ -343,6 +391,7 @@ bool Server::admit_and_launch(std::unique_lock<std::mutex>& lk)
         slots_[r.slot].done = 0;
         r.item.host_done = &slots_dev_[r.slot].done;
         r.item.host_minmax = slots_dev_[r.slot].minmax;
+        r.item.host_time = &slots_dev_[r.slot].t_done;
         r.item.dminmax = nullptr;
         r.state = kInflight;
         items.push_back(r.item);
@@ -352,7 +401,12 @@ bool Server::admit_and_launch(std::unique_lock<std::mutex>& lk)
     if (items.empty()) return false;
     fl->busy = true;
     fl->tickets = tickets;
+    fl->dev_first = ~0ull;
+    fl->dev_last = 0;
     ++batches_;
+    int busy = 0;
+    for (auto& f : flights_) busy += f.busy;
+    max_inflight_ = std::max(max_inflight_, busy);
     lk.unlock();
     int rc = fl->runner->launch(items, fl->stream, nullptr, true);
     if (rc == 0) cudaEventRecord(fl->done, fl->stream);

@@ -61,6 +61,11 @@ struct ServerStats {
     double p50_us, p99_us, max_us, mean_us;
     size_t pool_used, pool_capacity;
     int queue_depth, inflight;
+    // Batches whose requests completed, on the device clock, within another batch's span of
+    // completions: both batches were executing on the GPU at the same moment.
+    unsigned long long overlapped_batches;
+    int max_inflight_batches;         // most batches launched and not yet retired at once
+    int max_concurrent_batches;       // most batches executing on the GPU at one moment (device clock)
 };
 
 class Server {
@@ -72,6 +77,10 @@ public:
     int submit(const BatchItem& item, uint64_t& ticket);      // item.dout null => pool-allocated output
     // All-or-nothing submission of n items under one lock (tickets[i] for items[i]).
     int submit_many(const BatchItem* items, size_t n, uint64_t* tickets);
+    // Open-loop submission: item k is submitted when the steady clock reaches start + arrival_us[k]
+    // (the calling thread waits until then), and its latency counts from that arrival time, so
+    // a submitter falling behind the schedule shows up in the latency.
+    int submit_paced(const BatchItem* items, size_t n, const double* arrival_us, uint64_t* tickets);
     // Wait until every ticket is finished (done, failed or cancelled); FN_ERR_TIMEOUT if
     // timeout_ms >= 0 runs out first.  Returns 0, or the first failure's status.
     int wait_many(const uint64_t* tickets, size_t n, int timeout_ms);
@@ -99,12 +108,22 @@ private:
         std::unique_ptr<BatchRunner> runner;
         std::vector<uint64_t> tickets;
         bool busy = false;
+        unsigned long long dev_first = ~0ull, dev_last = 0;   // device clock of the first and last completion
     };
-    struct Slot {
+    struct Slot {                      // mapped pinned, written by the kernel that completes the request
         unsigned int done;
-        float minmax[2];
         unsigned int pad;
+        float minmax[2];
+        unsigned long long t_done;     // device clock (ns)
     };
+    struct Span {
+        unsigned long long first, last;
+        bool counted;
+    };
+
+    int enqueue_locked(const BatchItem& item, std::chrono::steady_clock::time_point t_submit, uint64_t& ticket);
+    int validate(const BatchItem& item);
+    void record_span(unsigned long long first, unsigned long long last);
 
     void loop();
     bool admit_and_launch(std::unique_lock<std::mutex>& lk);
@@ -131,6 +150,9 @@ private:
     // statistics
     std::vector<double> lat_us_;
     unsigned long long submitted_ = 0, completed_ = 0, failed_ = 0, batches_ = 0, points_ = 0;
+    std::deque<Span> spans_;           // completion spans of the most recent batches
+    unsigned long long overlapped_ = 0;
+    int max_inflight_ = 0, max_concurrent_ = 0;
 };
 
 }  // namespace fn

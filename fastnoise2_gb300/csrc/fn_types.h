@@ -65,7 +65,8 @@ struct BatchRequest {
     unsigned int prog_bytes;
     unsigned int n_tiles;
     int jit_slot;                // index of this tree in a specialised batch kernel, or -1
-    unsigned int pad[3];
+    unsigned int pad;
+    unsigned long long* host_time;   // mapped pinned or null: device clock (ns) when the request completed
 };
 
 struct BatchState {              // per-request mutable state, zeroed by the host upload

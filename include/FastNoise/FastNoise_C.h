@@ -25,10 +25,12 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#ifndef FASTNOISE_API
 #if defined(_WIN32)
 #define FASTNOISE_API __declspec(dllexport)
 #else
 #define FASTNOISE_API __attribute__((visibility("default")))
+#endif
 #endif
 
 #ifdef __cplusplus
@@ -138,10 +140,20 @@ FASTNOISE_API const char* fnGetLastErrorString(void);
  * Writes a NUL-terminated string if it fits; returns its length (excluding NUL) or a negative status. */
 FASTNOISE_API int fnSerialiseNodeTree(const void* node, char* buffer, int bufferSize);
 
+/* Read a node's members back (no counterpart in the reference, whose C++ objects hold them;
+ * the C++ layer's Metadata::DeserialiseNodeData uses these).  Variables come back as the raw
+ * bits of the last value set (the reference's Metadata::MemberVariable::ValueUnion); lookups
+ * and hybrid nodes come back with a new reference the caller drops with fnDeleteNodeRef, or
+ * NULL when unset or out of range; a hybrid's float is its constant (used while no node is set). */
+FASTNOISE_API int fnGetVariableBits(const void* node, int variableIndex, int* bits);
+FASTNOISE_API void* fnGetNodeLookupRef(const void* node, int nodeLookupIndex);
+FASTNOISE_API void* fnGetHybridNodeLookupRef(const void* node, int hybridIndex);
+FASTNOISE_API int fnGetHybridFloat(const void* node, int hybridIndex, float* value);
+
 /* Device-pointer variants of the generation calls.  `dOut` is device memory
  * (count floats); `dMinMax` is NULL or device float[2]; `stream` is a
- * cudaStream_t (NULL = this thread's stream).  The call is asynchronous:
- * it returns once the work is queued on the stream. */
+ * cudaStream_t (NULL = the legacy default stream, as in CUDA's own calls).
+ * The call is asynchronous: it returns once the work is queued on the stream. */
 FASTNOISE_API int fnGenUniformGrid2DDevice(const void* node, float* dOut, float xOffset, float yOffset, int xCount,
                                            int yCount, float xStepSize, float yStepSize, int seed, float* dMinMax,
                                            void* stream);
@@ -204,6 +216,15 @@ FASTNOISE_API int fnGenBatchHost(const fnGenRequest* requests, int count, int fl
  * order on `stream` (what a caller looping over fnGen*Device would do), for comparison
  * with fnGenBatchDevice.  minMax pointers are filled when FN_BATCH_SYNC is set. */
 FASTNOISE_API int fnGenEachDevice(const fnGenRequest* requests, int count, void* stream, int flags);
+/* The per-call path driven by arrival times, for latency measurement beside the server:
+ * requests[k] is launched as one fnGen*Device call on `stream` once arrivalMicros[k]
+ * microseconds have passed since the call began (the calling thread waits in between, and
+ * issues late when it falls behind), followed by a copy of its min/max to the host; a second
+ * host thread waits for each request in order.  latencyMicros[k] (may be NULL) = the moment
+ * the request's min/max was on the host minus its arrival time.  minMax pointers are filled.
+ * Returns when every request has completed. */
+FASTNOISE_API int fnGenEachPaced(const fnGenRequest* requests, int count, const double* arrivalMicros, void* stream,
+                                 double* latencyMicros);
 /* Time each tuning candidate on this batch and remember the fastest for its signature. */
 FASTNOISE_API int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream);
 FASTNOISE_API int fnAutotuneLoad(const char* path);
@@ -224,6 +245,12 @@ typedef struct fnServerStats {
     double p50Micros, p99Micros, maxMicros, meanMicros;   /* submit -> completion latency */
     unsigned long long poolUsed, poolCapacity;
     int queueDepth, inflight;
+    /* Batches that were executing on the GPU at the same moment as another batch: the kernels
+     * stamp each request's completion with the device clock, and two batches whose spans of
+     * completions intersect were both running then. */
+    unsigned long long overlappedBatches;
+    int maxInflightBatches;         /* most batches launched and not yet retired at once */
+    int maxConcurrentBatches;       /* most batches executing at one moment (device clock) */
 } fnServerStats;
 
 /* NULL config = defaults.  Returns NULL (error set) if the device or pool is unavailable. */
@@ -236,6 +263,12 @@ FASTNOISE_API int fnServerSubmit(void* server, const fnGenRequest* request, unsi
 /* Queue `count` requests under one lock; all or nothing (nothing is queued if any request is
  * invalid).  tickets[i] receives the ticket of requests[i]. */
 FASTNOISE_API int fnServerSubmitMany(void* server, const fnGenRequest* requests, int count, unsigned long long* tickets);
+/* Open-loop submission: requests[k] is queued when arrivalMicros[k] microseconds have passed
+ * since the call began (the calling thread waits in between); its latency in the statistics
+ * counts from that arrival time.  Returns once every request is queued (all are validated
+ * first; nothing is queued if any is invalid).  Use fnServerWaitMany for completion. */
+FASTNOISE_API int fnServerSubmitPaced(void* server, const fnGenRequest* requests, int count,
+                                      const double* arrivalMicros, unsigned long long* tickets);
 /* Wait until every ticket has finished; FN_ERR_TIMEOUT when timeoutMs (>= 0) runs out first,
  * else 0 or the status of the first failed / cancelled request. */
 FASTNOISE_API int fnServerWaitMany(void* server, const unsigned long long* tickets, int count, int timeoutMs);
@@ -385,8 +418,7 @@ FASTNOISE_API int fnSetJitEnabled(int enabled);
  * cudaFree / cudaMallocHost and creates no stream: the tree's program and the
  * min/max workspace live in one fixed-size static device array per device,
  * filled by stream-ordered copies on `stream`.
- * - NULL stream: the legacy default stream (fnGenUniformGrid3DDevice reads NULL
- *   as this thread's stream instead).
+ * - NULL stream: the legacy default stream, as for fnGenUniformGrid3DDevice.
  * - Limit: the tree's compiled program must fit 16 KiB (several hundred nodes);
  *   larger trees return FN_ERR_CAPACITY without touching the GPU.
  * - The first call on a device looks up that device's array; make that first

@@ -69,6 +69,15 @@ def cpu_description() -> dict:
                     break
     except OSError:
         pass
+    if not model:
+        try:                             # util-linux names Arm cores from their part numbers
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for line in out.splitlines():
+                if line.lower().startswith("model name:"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
     if not model and platform.machine() in ("aarch64", "arm64"):
         # Arm kernels list implementer / part numbers instead of a name
         try:

@@ -188,10 +188,13 @@ def mix_oracle():
 
 
 def mix_requests(fn, torch, chunks, nodes, base, minmax):
+    """Requests whose outputs lie back to back from device address `base`; base None = every
+    output NULL (the request server then carves it from its pool)."""
     reqs, off = [], 0
     for k, c in enumerate(chunks):
         kind = fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D
-        reqs.append(fn.make_request(nodes[MIX_NAMES[c.tree]], kind, base + 4 * off, c.seed, c.count, c.offset,
+        out = 0 if base is None else base + 4 * off
+        reqs.append(fn.make_request(nodes[MIX_NAMES[c.tree]], kind, out, c.seed, c.count, c.offset,
                                     (1, 1, 1, 1), minmax=None if minmax is None else minmax[k]))
         off += c.points
     return reqs
@@ -237,7 +240,8 @@ def test_chunk_mix_512_served(specialised, torch_cuda, mix_oracle):
     pts = sum(c.points for c in chunks)
     srv = fn.Server(pool_bytes=4 * pts + (64 << 20), streams=3, max_batch_requests=128)
     try:
-        reqs = mix_requests(fn, torch, chunks, nodes, 0, None)
+        reqs = mix_requests(fn, torch, chunks, nodes, None, None)
+        assert all(r.out is None for r in reqs)
         tickets = srv.submit_many(reqs)
         got = np.empty(pts, np.float32)
         gmm = np.zeros((n, 2), np.float32)

@@ -169,3 +169,66 @@ def test_cancel_timeout_and_unknown_ticket(gpu):
         srv.release(t)
     assert srv.poll(123456789) < 0
     srv.close()
+
+
+def test_batches_overlap_on_the_gpu(gpu, torch_cuda):
+    """Continuous batching: requests submitted in waves are admitted while earlier batches run,
+    and batches execute on the GPU at the same time.  The kernels stamp each request's
+    completion with the device clock; two batches whose spans of completions intersect were
+    both executing then (server statistic overlappedBatches).  Every result is the same as the
+    request generated alone."""
+    fn = gpu
+    nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
+    chunks = chunkmix.make_mix(240, seed=5, sizes=[(32, 32, 32), (64, 64, 64), (128, 128), (512, 512)])
+    srv = fn.Server(pool_bytes=2 << 30, streams=3, max_batch_requests=8)
+    tickets = []
+    for i in range(0, len(chunks), 40):                 # waves of 40 while earlier waves run
+        tickets += srv.submit_many([request(fn, nodes[c.tree], c) for c in chunks[i:i + 40]])
+        time.sleep(0.0005)
+    srv.wait_many(tickets, timeout_ms=60000)
+    st = srv.stats()
+    assert st["completed"] == len(chunks) and st["failed"] == 0
+    assert st["maxInflightBatches"] >= 2, st
+    assert st["overlappedBatches"] >= 2 and st["maxConcurrentBatches"] >= 2, st
+    for t, c in zip(tickets, chunks):
+        mn, mx, ptr = srv.wait(t, timeout_ms=0)
+        got = device_array(torch_cuda, ptr, c.points)
+        ref, rmm = nodes[c.tree].gen_uniform_grid(c.offset, c.count, (1,) * len(c.count), c.seed)
+        assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), c
+        assert (mn, mx) == rmm
+        assert srv.release(t) == 0
+    srv.close()
+
+
+def test_paced_submission_and_per_call_paced(gpu, torch_cuda):
+    """fnServerSubmitPaced queues requests on an arrival schedule and counts latency from the
+    arrival; fnGenEachPaced drives the per-call path with the same schedule.  Both return every
+    request's result equal to the request generated alone."""
+    fn = gpu
+    torch = torch_cuda
+    nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
+    chunks = chunkmix.make_mix(120, seed=9, sizes=[(16, 16, 16), (32, 32, 32), (64, 64), (128, 128)])
+    arrivals = np.cumsum(np.random.default_rng(3).exponential(1.0 / 20000.0, len(chunks))) * 1e6
+    srv = fn.Server(pool_bytes=256 << 20, streams=3, max_batch_requests=32)
+    tickets = srv.submit_paced([request(fn, nodes[c.tree], c) for c in chunks], arrivals)
+    srv.wait_many(tickets, timeout_ms=60000)
+    st = srv.stats()
+    assert st["completed"] == len(chunks) and st["p99Micros"] >= st["p50Micros"] > 0
+    refs = []
+    for t, c in zip(tickets, chunks):
+        mn, mx, ptr = srv.wait(t, timeout_ms=0)
+        ref, rmm = nodes[c.tree].gen_uniform_grid(c.offset, c.count, (1,) * len(c.count), c.seed)
+        assert np.array_equal(device_array(torch, ptr, c.points).view(np.uint32), ref.view(np.uint32)), c
+        assert (mn, mx) == rmm
+        refs.append((ref, rmm))
+        srv.release(t)
+    srv.close()
+    outs = [torch.full((c.points,), float("nan"), device="cuda") for c in chunks]
+    mms = [np.zeros(2, np.float32) for _ in chunks]
+    reqs = [fn.make_request(nodes[c.tree], fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D, o.data_ptr(), c.seed,
+                            c.count, c.offset, (1, 1, 1, 1), minmax=m) for c, o, m in zip(chunks, outs, mms)]
+    lat = fn.gen_each_paced(reqs, arrivals)
+    assert lat.shape == (len(chunks),) and (lat > 0).all()
+    for (ref, rmm), o, m in zip(refs, outs, mms):
+        assert np.array_equal(o.cpu().numpy().view(np.uint32), ref.view(np.uint32))
+        assert (float(m[0]), float(m[1])) == rmm
