@@ -137,6 +137,54 @@ def read_traffic(name):
     return None
 
 
+def parse_cpulist(text):
+    cpus = set()
+    for part in text.strip().split(","):
+        if not part:
+            continue
+        if "-" in part:
+            a, b = part.split("-")
+            cpus.update(range(int(a), int(b) + 1))
+        else:
+            cpus.add(int(part))
+    return cpus
+
+
+def bind_near_gpu(local):
+    """Keep this process (and the pinned host buffers it allocates later) on the CPUs the PCI
+    topology lists next to GPU `local`, as numactl would: host<->device copies from a remote
+    socket's memory run at a fraction of the local rate.  Returns what was found and done."""
+    info = {"bound": False}
+    try:
+        rt = ctypes.CDLL("libcudart.so")
+        buf = ctypes.create_string_buffer(64)
+        if rt.cudaDeviceGetPCIBusId(buf, 64, int(local)) != 0:
+            return info
+        bus = buf.value.decode().lower()
+        info["pci_bus_id"] = bus
+        dev_dir = None
+        for name in os.listdir("/sys/bus/pci/devices"):
+            if name.lower().endswith(bus.split(":", 1)[1]) and int(name.split(":")[0], 16) == int(bus.split(":")[0], 16):
+                dev_dir = os.path.join("/sys/bus/pci/devices", name)
+                break
+        if dev_dir is None:
+            return info
+        with open(os.path.join(dev_dir, "numa_node")) as f:
+            info["gpu_numa_node"] = int(f.read().strip())
+        with open(os.path.join(dev_dir, "local_cpulist")) as f:
+            near = parse_cpulist(f.read())
+        allowed = os.sched_getaffinity(0)
+        both = near & allowed
+        info["near_cpus_allowed"] = len(both)
+        info["cpus_allowed"] = len(allowed)
+        if both and both != allowed:
+            os.sched_setaffinity(0, both)
+            info["bound"] = True
+    except (OSError, ValueError, AttributeError):
+        pass
+    return info
+
+
 def dist_setup():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -410,6 +458,14 @@ def run_chunkmix(a, rank, world, local):
             e2e.append((time.perf_counter() - t0) * 1e3)
     e2e_ms = allmax(statistics.median(e2e), world) if e2e else None
     hinfo = fn.batch_info()
+    # the plain copy engine rate for the same bytes (device outputs -> the pinned host buffer)
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    host.copy_(out, non_blocking=True)
+    c0.record(stream)
+    host.copy_(out, non_blocking=True)
+    c1.record(stream)
+    torch.cuda.synchronize(dev)
+    d2h_gbs = pts * 4 / (c0.elapsed_time(c1) * 1e-3) / 1e9
 
     if rank != 0:
         return
@@ -432,7 +488,7 @@ def run_chunkmix(a, rank, world, local):
                    "l2": "flushed between steps (256 MiB write outside the timed events)",
                    "path": "batched persistent launch (fnGenBatchDevice), CUDA graph, "
                            + ("specialised kernels (fnJitCompile)" if a.kernels == "jit" else "interpreter kernel"),
-                   "jit_compile_s": jit_s},
+                   "jit_compile_s": jit_s, "host_placement": a.host_placement},
         "interpreter": interp,
         "per_call": {"value": percall_value, "unit": "Mpoints/s", "ms_per_step": percall_ms,
                      "api": "fnGenEachDevice: one launch per request"},
@@ -446,7 +502,7 @@ def run_chunkmix(a, rank, world, local):
                              "frac": hbm_gbs / float(peaks.get("hbm_gbs", 6800.0)), "algorithmic_bytes_per_point": 4}},
         "e2e": {"value": pts * world / (e2e_ms * 1e-3) / 1e6 if e2e_ms else None, "unit": "Mpoints/s",
                 "h2d_bytes_per_step": hinfo["uploadBytes"], "d2h_bytes_per_step": pts * 4 + 8 * len(chunks),
-                "ms_per_step": e2e_ms,
+                "ms_per_step": e2e_ms, "d2h_copy_gbs": d2h_gbs,
                 "api": "fnGenBatchHost: host (pinned) outputs; request descriptors uploaded, every output and "
                        "min/max read back, slices of 2^25 points copied while the next slice is generated"},
         "batch": binfo,
@@ -771,6 +827,7 @@ def main():
                     help="specialised per-tree kernels (NVRTC) or the program interpreter")
     ap.add_argument("--cpu-passes", type=int, default=1,
                     help="cpu_baseline: whole passes of the CPU restatement over the workload (0 = leave it out)")
+    ap.add_argument("--cpu-seconds", type=float, default=None, help=argparse.SUPPRESS)   # older spelling: 0 = no baseline
     ap.add_argument("--pool-gb", type=float, default=40.0)
     ap.add_argument("--streams", type=int, default=3)
     ap.add_argument("--max-batch-requests", type=int, default=512)
@@ -784,12 +841,15 @@ def main():
     ap.add_argument("--no-served", dest="served", action="store_false",
                     help="chunk mix: leave out the request-server measurements")
     a = ap.parse_args()
+    if a.cpu_seconds is not None and a.cpu_seconds <= 0:
+        a.cpu_passes = 0
     if a.impl == "reference":
         run_reference(a)
         return
     import torch
     rank, world, local = dist_setup()
     torch.cuda.set_device(local)
+    a.host_placement = bind_near_gpu(local)
     if a.workload == "chunk-mix":
         run_chunkmix(a, rank, world, local)
     elif a.workload in ("mesh-bloxel-128", "mesh-dmc-128"):

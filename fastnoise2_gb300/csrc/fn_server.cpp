@@ -436,8 +436,11 @@ void Server::loop()
         for (auto& f : flights_) busy |= f.busy;
         if (!launched) {
             if (busy) {
+                // Batches are on the GPU: poll their completion flags continuously.  A timed
+                // sleep here would add the scheduler's wake-up delay (tens of microseconds)
+                // to every request's latency.
                 lk.unlock();
-                std::this_thread::sleep_for(std::chrono::microseconds(cfg_.idle_wait_us > 0 ? cfg_.idle_wait_us / 4 + 1 : 1));
+                std::this_thread::yield();
             } else {
                 cv_work_.wait_for(lk, std::chrono::microseconds(cfg_.idle_wait_us > 0 ? cfg_.idle_wait_us : 50),
                                   [&] { return stop_.load() || !queue_.empty(); });

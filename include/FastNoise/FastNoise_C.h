@@ -237,7 +237,8 @@ typedef struct fnServerConfig {
     int streams;                    /* batches in flight at once (default 3) */
     int maxBatchRequests;           /* requests per launch (default 1024) */
     long long maxBatchPoints;       /* points per launch (default 64 Mi) */
-    int idleWaitMicros;             /* request-loop poll interval when idle (default 50) */
+    int idleWaitMicros;             /* longest request-loop wait when no batch is in flight (default 50);
+                                     * while batches are in flight the loop polls continuously */
 } fnServerConfig;
 
 typedef struct fnServerStats {
