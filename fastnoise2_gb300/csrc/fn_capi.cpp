@@ -188,9 +188,11 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
         if (!gen_host_slabs(prog, args, ctx, work, out, minmax)) fill_nan(out, total, minmax);
         return;
     }
-    if (!cuda_ok(launch_points(prog, args, ctx->dbuf, work, nullptr, ctx->stream), "launch")) { fill_nan(out, total, minmax); return; }
+    // the kernel's last block stores the min/max straight into pinned host memory when it can
+    if (!cuda_ok(launch_points(prog, args, ctx->dbuf, work, ctx->hminmax_dev, ctx->stream), "launch")) { fill_nan(out, total, minmax); return; }
     if (total > 0 && !cuda_ok(cudaMemcpyAsync(out, ctx->dbuf, (size_t)total * 4, cudaMemcpyDeviceToHost, ctx->stream), "copy output")) { fill_nan(out, total, minmax); return; }
-    if (!cuda_ok(cudaMemcpyAsync(ctx->hminmax, work->result, 8, cudaMemcpyDeviceToHost, ctx->stream), "copy minmax") ||
+    if ((!ctx->hminmax_dev &&
+         !cuda_ok(cudaMemcpyAsync(ctx->hminmax, work->result, 8, cudaMemcpyDeviceToHost, ctx->stream), "copy minmax")) ||
         !cuda_ok(cudaStreamSynchronize(ctx->stream), "synchronize")) {
         fill_nan(out, total, minmax);
         return;

@@ -112,37 +112,6 @@ __device__ __forceinline__ void block_minmax(float& mn, float& mx, float* smn, f
         for (int w = 1; w < (int)(blockDim.x >> 5); ++w) { mn = fmin_(mn, smn[w]); mx = fmax_(mx, smx[w]); }
 }
 
-// Per-launch min/max: block partials, then the last block to finish folds them
-// and resets the counter so the workspace can serve the next launch.
-__device__ __forceinline__ void grid_minmax(float mn, float mx, fn::MinMaxWork* work, float* dminmax, float* smn, float* smx)
-{
-    __shared__ bool is_last;
-    block_minmax(mn, mx, smn, smx);
-    if (threadIdx.x == 0) {
-        work->partial[2 * blockIdx.x] = mn;
-        work->partial[2 * blockIdx.x + 1] = mx;
-        __threadfence();
-        const unsigned t = atomicAdd(&work->counter, 1u);
-        is_last = (t == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (!is_last) return;
-    __threadfence();
-    mn = inf(); mx = -inf();
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) {
-        mn = fmin_(mn, __ldcg(&work->partial[2 * b]));
-        mx = fmax_(mx, __ldcg(&work->partial[2 * b + 1]));
-    }
-    __syncthreads();
-    block_minmax(mn, mx, smn, smx);
-    if (threadIdx.x == 0) {
-        work->result[0] = mn;
-        work->result[1] = mx;
-        if (dminmax) { dminmax[0] = mn; dminmax[1] = mx; }
-        work->counter = 0;
-    }
-}
-
 // Order-preserving float <-> uint encoding for atomicMin / atomicMax.
 __device__ __forceinline__ unsigned int enc_ordered(float f)
 {
@@ -152,6 +121,30 @@ __device__ __forceinline__ unsigned int enc_ordered(float f)
 __device__ __forceinline__ float dec_ordered(unsigned int u)
 {
     return __uint_as_float((u & 0x80000000u) ? (u & 0x7FFFFFFFu) : ~u);
+}
+
+// Per-launch min/max: each block folds its result into the workspace keys with
+// two atomics; the block that counts itself last decodes them (no per-block
+// partials to re-read) and clears the workspace for the next launch.  A block
+// without a non-NaN output folds nothing, so an all-NaN launch gives (+inf, -inf).
+__device__ __forceinline__ void grid_minmax(float mn, float mx, fn::MinMaxWork* work, float* dminmax, float* smn, float* smx)
+{
+    block_minmax(mn, mx, smn, smx);
+    if (threadIdx.x != 0) return;
+    if (mn <= mx) {
+        atomicMax(&work->mn_key, ~enc_ordered(mn));
+        atomicMax(&work->mx_key, enc_ordered(mx));
+    }
+    __threadfence();
+    if (atomicAdd(&work->counter, 1u) != gridDim.x - 1) return;
+    __threadfence();
+    const unsigned int a = atomicExch(&work->mn_key, 0u), b = atomicExch(&work->mx_key, 0u);
+    const float fmn = a == 0u ? inf() : dec_ordered(~a);
+    const float fmx = b == 0u ? -inf() : dec_ordered(b);
+    work->result[0] = fmn;
+    work->result[1] = fmx;
+    if (dminmax) { dminmax[0] = fmn; dminmax[1] = fmx; }
+    work->counter = 0;
 }
 
 // Fold one finished tile's min/max into its request; the tile that completes

@@ -516,6 +516,14 @@ bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& er
              cudaLibraryGetKernel(&jk.positions, lib, "fnjit_pos_0") == cudaSuccess &&
              (progs[k]->dim != 4 || cudaLibraryGetKernel(&jk.tileable, lib, "fnjit_tile_0") == cudaSuccess) &&
              cudaLibraryGetKernel(&bk, mods[0]->lib, ("fnjit_batch_" + std::to_string(k)).c_str()) == cudaSuccess;
+        const cudaKernel_t kern[3] = {jk.grid, jk.positions, jk.tileable};
+        for (int j = 0; ok && j < 3; ++j) {
+            int n = 0;
+            if (kern[j] && cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)kern[j], 256, 0) == cudaSuccess && n > 0)
+                jk.resident[j] = n;
+            else
+                cudaGetLastError();
+        }
         found[progs[k]->hash] = jk;
         batch[progs[k]->hash] = bk;
     }
@@ -694,15 +702,25 @@ bool jit_launch(uint64_t hash, const PointArgs& args, float* out, MinMaxWork* wo
     err = cudaSuccess;
     JitKernels jk;
     if (args.total <= 0 || args.total > (1ll << 31) || !jit_lookup(hash, jk)) return false;
-    cudaKernel_t k = args.src == kSrcGrid ? jk.grid : args.src == kSrcPositions ? jk.positions : jk.tileable;
+    const int which = args.src == kSrcGrid ? 0 : args.src == kSrcPositions ? 1 : 2;
+    cudaKernel_t k = which == 0 ? jk.grid : which == 1 ? jk.positions : jk.tileable;
     if (!k) return false;
-    // 4 points per lane (float4 stores) when that still gives every SM a few
-    // warps; 1 point per lane for small calls, which are latency-bound.
-    unsigned ppl = args.total >= (long long)num_sms() * 8 * 128 * 4 ? 4u : 1u;
-    const long long chunks = (args.total + 32 * ppl - 1) / (32 * ppl);   // one warp per chunk
-    long long blocks = (chunks + 7) / 8;
-    const long long cap = (long long)num_sms() * 8;              // beyond this the warps stride over the chunks
-    if (blocks > cap) blocks = cap;
+    const int sms = num_sms();
+    unsigned ppl;
+    long long blocks;
+    if (args.total >= (long long)sms * 8 * 128 * 4) {
+        // large calls: 4 points per lane (float4 stores), a grid of 8 blocks per SM striding over
+        // the warp chunks
+        ppl = 4u;
+        blocks = std::min<long long>((args.total + 1023) / 1024, (long long)sms * 8);
+    } else {
+        // small calls are latency-bound: run them in one wave of the blocks that fit at once,
+        // with as few points per lane as that allows (the fixed cost of a thread -- index set-up,
+        // the min/max reduction -- is shared by its points)
+        const long long resident = (long long)sms * std::max(1, jk.resident[which]) * 256;
+        ppl = (unsigned)std::min<long long>(4, std::max<long long>(1, (args.total + resident - 1) / resident));
+        blocks = (args.total + 256ll * ppl - 1) / (256ll * ppl);
+    }
     if (blocks > kMaxReduceBlocks) blocks = kMaxReduceBlocks;
     if (blocks < 1) blocks = 1;
     PointArgs a = args;

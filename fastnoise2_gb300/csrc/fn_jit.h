@@ -28,6 +28,7 @@ struct JitKernels {
     cudaKernel_t positions = nullptr; // GenPositionArray
     cudaKernel_t tileable = nullptr;  // GenTileable2D (4D programs only)
     int slot = -1;                    // index in the module's batch kernel
+    int resident[3] = {1, 1, 1};      // 256-thread blocks per SM of grid / positions / tileable at once
 };
 
 // CUDA source of the batch module for `progs` (slot k = progs[k]) and of one

@@ -128,6 +128,11 @@ ThreadCtx* thread_ctx()
     }
     if (!cuda_ok(cudaStreamCreateWithFlags(&t_ctx.ctx.stream, cudaStreamNonBlocking), "cudaStreamCreate")) { t_ctx.failed = true; return nullptr; }
     if (!cuda_ok(cudaMallocHost(&t_ctx.ctx.hminmax, 2 * sizeof(float)), "cudaMallocHost")) { t_ctx.failed = true; return nullptr; }
+    // Pinned memory is mapped into the device's address space (unified addressing); when the
+    // device pointer cannot be had, host calls copy the min/max back instead.
+    void* mapped = nullptr;
+    if (cudaHostGetDevicePointer(&mapped, t_ctx.ctx.hminmax, 0) == cudaSuccess) t_ctx.ctx.hminmax_dev = static_cast<float*>(mapped);
+    else cudaGetLastError();
     t_ctx.init = true;
     return &t_ctx.ctx;
 }

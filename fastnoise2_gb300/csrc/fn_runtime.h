@@ -38,6 +38,7 @@ struct ThreadCtx {
     float* dpos[4] = {nullptr, nullptr, nullptr, nullptr};
     size_t dpos_cap = 0;
     float* hminmax = nullptr;                 // pinned float[2]
+    float* hminmax_dev = nullptr;             // the same memory as the device sees it (kernels store min/max there)
 };
 ThreadCtx* thread_ctx();                      // nullptr (and error set) if CUDA is unusable
 MinMaxWork* work_for_stream(cudaStream_t s);  // per (thread, stream) workspace

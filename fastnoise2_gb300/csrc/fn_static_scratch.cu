@@ -12,6 +12,7 @@
 // memory.  The price: every call shares that one array.
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstring>
 #include <mutex>
 
@@ -23,11 +24,11 @@ namespace fn {
 namespace {
 
 struct StaticScratch {
-    MinMaxWork work;                                         // reduction workspace; `counter` must start at zero
+    MinMaxWork work;                                         // reduction workspace; counter and keys must start at zero
     alignas(256) unsigned char prog[kStaticProgramBytes];     // the tree's program blob
 };
 
-// The shared scratch: one per device, sized at compile time (about 49 KB).
+// The shared scratch: one per device, sized at compile time (about 17 KB).
 static __device__ __align__(256) unsigned char g_scratch[sizeof(StaticScratch)];
 
 constexpr int kMaxDevices = 64;
@@ -66,7 +67,7 @@ cudaError_t launch_interpreter_static(const void* blob, uint32_t blob_bytes, con
     // stream has finished with the array, and before this call's kernel reads it.
     e = cudaMemcpyAsync(s->prog, blob, blob_bytes, cudaMemcpyHostToDevice, stream);
     if (e != cudaSuccess) return e;
-    e = cudaMemsetAsync(&s->work.counter, 0, sizeof(s->work.counter), stream);
+    e = cudaMemsetAsync(&s->work, 0, offsetof(MinMaxWork, result), stream);   // counter and min/max keys
     if (e != cudaSuccess) return e;
     return launch_interpreter(reinterpret_cast<const FnProgramHeader*>(s->prog), blob_bytes, args, out, &s->work, dminmax,
                               stream);

@@ -31,15 +31,20 @@ struct PointArgs {
     unsigned int base;
 };
 
-// Per-launch reduction workspace.  `counter` must be zero before the first
-// launch; the last block to finish resets it, so a workspace can be reused by
-// consecutive launches on one stream (never by overlapping launches).
+// Per-launch reduction workspace.  Every block folds its min/max into the two
+// keys with order-preserving atomics (mn_key holds the complement of the encoded
+// minimum, so that zero means "nothing folded" for both keys), then counts itself
+// in `counter`; the last block decodes the keys into `result` and clears
+// counter and keys.  The first 16 bytes must be zero before the first launch;
+// a workspace can then be reused by consecutive launches on one stream (never
+// by overlapping launches).
 struct MinMaxWork {
     unsigned int counter;
-    unsigned int pad[3];
+    unsigned int mn_key;
+    unsigned int mx_key;
+    unsigned int pad;
     float result[2];
     float pad2[2];
-    float partial[2 * 4096];
 };
 
 constexpr int kMaxReduceBlocks = 4096;
