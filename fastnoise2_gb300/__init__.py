@@ -148,6 +148,7 @@ def _declare(L):
         "fnAutotuneLoad": (c_int, [cp]),
         "fnAutotuneSave": (c_int, [cp]),
         "fnServerSubmitPaced": (c_int, [vp, vp, c_int, vp, vp]),
+        "fnJitCheckBatchVariants": (c_int, [vp, vp, c_int, ctypes.POINTER(c_int)]),
         "fnGenEachPaced": (c_int, [vp, c_int, vp, vp, vp]),
         "fnGetVariableBits": (c_int, [vp, c_int, ctypes.POINTER(c_int)]),
         "fnGetNodeLookupRef": (vp, [vp, c_int]),
@@ -268,6 +269,25 @@ def jit_compile(pairs) -> None:
     nodes, dims = _jit_arrays(pairs)
     if lib().fnJitCompile(nodes, dims, len(pairs)) != 0:
         _check()
+
+
+def jit_check_batch_variants(pairs) -> int:
+    """NVRTC-compile the other batch-kernel variants for [(node, dimension), ...] without loading them."""
+    nodes, dims = _jit_arrays(pairs)
+    n = ctypes.c_int(0)
+    if lib().fnJitCheckBatchVariants(nodes, dims, len(pairs), ctypes.byref(n)) != 0:
+        _check()
+    return n.value
+
+
+def autotune_save(path: str) -> None:
+    if lib().fnAutotuneSave(str(path).encode()) != 0:
+        raise FastNoiseError(-1, f"could not write {path}")
+
+
+def autotune_load(path: str) -> None:
+    if lib().fnAutotuneLoad(str(path).encode()) != 0:
+        raise FastNoiseError(-1, f"could not read {path}")
 
 
 def jit_check(pairs) -> int:

@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <sstream>
@@ -100,7 +101,7 @@ cudaError_t BatchRunner::launch_group(size_t g, uint32_t smem, cudaStream_t stre
     BatchState* states = d_states_;
     BatchGroup* grp = reinterpret_cast<BatchGroup*>(d_buf_ + off_groups_) + g;
     void* params[] = {&hdr, &reqs, &states, &items, &grp};
-    return cudaLaunchKernel((const void*)gr.jit, dim3((unsigned)gr.grid), dim3(256), params, 0, stream);
+    return cudaLaunchKernel((const void*)gr.jit, dim3((unsigned)gr.grid), dim3((unsigned)gr.threads), params, 0, stream);
 }
 
 // Several group kernels run concurrently: fork from `stream` onto the auxiliary
@@ -182,15 +183,30 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         points_ += (uint64_t)std::max(0ll, items[i].args.total);
     }
     signature_ = batch_signature(items, progs);
-    // Specialised batch kernels when every program of the batch has one.
-    std::vector<cudaKernel_t> kernels;
-    bool jit = false;
+    // Specialised batch kernels when every program of the batch has one: each tree's tuned
+    // variant when it is built (a variant not built yet is queued for a background build and
+    // variant 0 runs meanwhile), or the variant a tuning run forces.
+    std::vector<BatchKernel> kernels(n);
+    bool jit = true;
+    for (size_t i = 0; jit && i < n; ++i) jit = items[i].args.total < (1ll << 32);   // 32-bit point indices
     {
-        std::vector<uint64_t> hashes(n);
-        for (size_t i = 0; i < n; ++i) hashes[i] = progs[i].hash;
-        bool fits = true;                           // the specialised kernels index points with 32 bits
-        for (size_t i = 0; i < n; ++i) fits = fits && items[i].args.total < (1ll << 32);
-        jit = fits && jit_batch_kernels(hashes, kernels);
+        const int forced = tuning_in ? tuning_in->variant : -1;
+        std::map<uint64_t, BatchKernel> chosen;
+        for (size_t i = 0; jit && i < n; ++i) {
+            auto it = chosen.find(progs[i].hash);
+            if (it == chosen.end()) {
+                BatchKernel bk;
+                const int v = forced >= 0 ? forced : Autotuner::instance().tree_variant(progs[i].hash);
+                bool ok = jit_batch_kernel(progs[i].hash, v, bk);
+                if (!ok && v != 0) {
+                    if (forced < 0) jit_request_batch_variants(progs[i].host);
+                    ok = jit_batch_kernel(progs[i].hash, 0, bk);
+                }
+                if (!ok) { jit = false; break; }
+                it = chosen.emplace(progs[i].hash, bk).first;
+            }
+            kernels[i] = it->second;
+        }
     }
     if (!jit) {                                     // interpreter batch: count a use of each program
         std::vector<uint64_t> seen;
@@ -220,13 +236,13 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
     // Requests per group: all of them for the interpreter, one group per
     // distinct specialised kernel (first-appearance order) otherwise.
     std::vector<std::vector<uint32_t>> members;
-    std::vector<cudaKernel_t> gkernel;
+    std::vector<BatchKernel> gkernel;
     if (jit) {
         std::map<cudaKernel_t, size_t> index;
         for (size_t i = 0; i < n; ++i) {
-            auto it = index.find(kernels[i]);
+            auto it = index.find(kernels[i].kernel);
             if (it == index.end()) {
-                it = index.emplace(kernels[i], members.size()).first;
+                it = index.emplace(kernels[i].kernel, members.size()).first;
                 members.emplace_back();
                 gkernel.push_back(kernels[i]);
             }
@@ -234,7 +250,7 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         }
     } else {
         members.emplace_back();
-        gkernel.push_back(nullptr);
+        gkernel.push_back(BatchKernel{nullptr, 256});          // the interpreter's batch kernel: 256 threads
         for (size_t i = 0; i < n; ++i) members[0].push_back((uint32_t)i);
     }
 
@@ -278,7 +294,8 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
     int total_grid = 0;
     for (size_t g = 0; g < members.size(); ++g) {
         Group& gr = groups_[g];
-        gr.jit = gkernel[g];
+        gr.jit = gkernel[g].kernel;
+        gr.threads = gkernel[g].threads;
         gr.item_begin = (uint32_t)k;
         for (uint32_t i : members[g])
             for (uint32_t t = 0; t < reqs[i].n_tiles; ++t) its[k++] = make_uint2(i, t);
@@ -289,7 +306,7 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         grps[g].pad = 0;
         int occ = tuning.ctas_per_sm;
         if (occ <= 0 && gr.jit) {
-            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)gr.jit, 256, 0) != cudaSuccess || occ < 1) occ = 1;
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)gr.jit, gr.threads, 0) != cudaSuccess || occ < 1) occ = 1;
         } else if (occ <= 0) {
             occ = batch_occupancy(256, max_bytes);
         }
@@ -357,20 +374,51 @@ std::vector<BatchTuning> Autotuner::candidates() const
 {
     std::vector<BatchTuning> c;
     for (uint32_t tp : {1024u, 2048u, 4096u, 8192u})
-        for (int ctas : {0, 1}) c.push_back(BatchTuning{tp, ctas});
+        for (int ctas : {0, 1}) c.push_back(BatchTuning{tp, ctas, -1});
     return c;
 }
 
+int Autotuner::tree_variant(uint64_t program_hash)
+{
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = trees_.find(program_hash);
+    return it == trees_.end() ? 0 : it->second.first;
+}
+
+void Autotuner::store_tree(uint64_t program_hash, int variant, double ms)
+{
+    std::lock_guard<std::mutex> lk(mu_);
+    trees_[program_hash] = {variant, ms};
+}
+
+// Text format, one entry per line:
+//   <signature hex> <tile points> <CTAs per SM> <ms>                         a batch signature
+//   tree <program hash hex> <variant> <threads> <blocks per SM> <points> <ms>  a tree's batch kernel
 bool Autotuner::load(const std::string& path)
 {
     std::ifstream f(path);
     if (!f) return false;
     std::lock_guard<std::mutex> lk(mu_);
-    unsigned long long sig;
-    unsigned tp;
-    int ctas;
-    double ms;
-    while (f >> std::hex >> sig >> std::dec >> tp >> ctas >> ms) table_[sig] = {BatchTuning{tp, ctas}, ms};
+    std::string line;
+    while (std::getline(f, line)) {
+        std::istringstream in(line);
+        std::string first;
+        if (!(in >> first)) continue;
+        if (first == "tree") {
+            unsigned long long hash;
+            int variant, threads, blocks, points;
+            double ms;
+            if (in >> std::hex >> hash >> std::dec >> variant >> threads >> blocks >> points >> ms && variant >= 0 &&
+                (size_t)variant < batch_variants().size())
+                trees_[hash] = {variant, ms};
+        } else {
+            unsigned long long sig = std::strtoull(first.c_str(), nullptr, 16);
+            unsigned tp;
+            int ctas;
+            double ms;
+            if (in >> tp >> ctas >> ms) table_[sig] = {BatchTuning{tp, ctas, -1}, ms};
+        }
+    }
     return true;
 }
 
@@ -381,6 +429,11 @@ bool Autotuner::save(const std::string& path) const
     for (const auto& kv : table_)
         f << std::hex << kv.first << std::dec << ' ' << kv.second.first.tile_points << ' ' << kv.second.first.ctas_per_sm << ' '
           << kv.second.second << '\n';
+    for (const auto& kv : trees_) {
+        const BatchVariant& v = batch_variants()[(size_t)kv.second.first];
+        f << "tree " << std::hex << kv.first << std::dec << ' ' << kv.second.first << ' ' << v.threads << ' ' << v.min_blocks << ' '
+          << v.points << ' ' << kv.second.second << '\n';
+    }
     return true;
 }
 

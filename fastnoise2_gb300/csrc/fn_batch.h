@@ -26,6 +26,7 @@ struct BatchItem {
 struct BatchTuning {
     uint32_t tile_points = 2048;
     int ctas_per_sm = 0;               // 0 = occupancy limit
+    int variant = -1;                  // specialised kernel variant for every tree; -1 = each tree's tuned choice
 };
 
 // Owns the device/pinned descriptor buffers and a captured graph; not thread safe
@@ -60,9 +61,10 @@ private:
     // (jit null), or one tree's specialised batch kernel over that tree's items.
     struct Group {
         cudaKernel_t jit = nullptr;
+        int threads = 256;
         uint32_t item_begin = 0, item_end = 0;
         int grid = 1;
-        bool operator==(const Group& o) const { return jit == o.jit && grid == o.grid; }
+        bool operator==(const Group& o) const { return jit == o.jit && grid == o.grid && threads == o.threads; }
     };
     bool reserve(size_t n_req, size_t n_items);
     int launch_graph(cudaStream_t stream, size_t bytes, uint32_t smem);
@@ -99,19 +101,24 @@ private:
     bool specialised_ = false;
 };
 
-// Tuning cache keyed by a batch signature (program hashes and size classes).
+// Tuning cache: per batch signature (program hashes and size classes) the tile size and
+// CTAs per SM; per tree (program hash, which includes the dimensionality) the variant of its
+// specialised batch kernel.  Saved and loaded as text.
 class Autotuner {
 public:
     static Autotuner& instance();
     bool lookup(uint64_t signature, BatchTuning& out);
     void store(uint64_t signature, const BatchTuning& t, double ms);
     std::vector<BatchTuning> candidates() const;
+    int tree_variant(uint64_t program_hash);                 // 0 when the tree has not been tuned
+    void store_tree(uint64_t program_hash, int variant, double ms);
     bool load(const std::string& path);
     bool save(const std::string& path) const;
 
 private:
     std::mutex mu_;
     std::map<uint64_t, std::pair<BatchTuning, double>> table_;
+    std::map<uint64_t, std::pair<int, double>> trees_;
 };
 
 uint64_t batch_signature(const std::vector<BatchItem>& items, const std::vector<DeviceProgram>& progs);

@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <string>
 #include <thread>
 #include <vector>
@@ -1022,10 +1023,53 @@ int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream)
         sig = t_batch->runner.last_signature();
         if (ms < best_ms) { best_ms = ms; best = t; }
     }
+    Autotuner::instance().store(sig, best, best_ms / 2);
+
+    // Per tree: the variant of its specialised batch kernel (register bound, block size,
+    // points in flight per thread).  The tree's own requests run alone in every variant with
+    // the batch's tuned tile size; the fastest variant is kept for that tree.
+    int rc = FN_OK;
+    if (jit_enabled()) {
+        std::map<uint64_t, std::pair<const CompiledProgram*, std::vector<int>>> trees;
+        for (int i = 0; i < count && rc == FN_OK; ++i) {
+            PointArgs a;
+            DeviceProgram p;
+            if (!requests[i].node || !request_args(requests[i], a)) continue;
+            if (!get_program(N(requests[i].node), a.dim, p)) { rc = last_error(); break; }
+            auto& t = trees[p.hash];
+            t.first = p.host;
+            t.second.push_back(i);
+        }
+        std::vector<const CompiledProgram*> progs;
+        for (auto& kv : trees)
+            if (jit_is_specialised(kv.first)) progs.push_back(kv.second.first);
+        std::string err;
+        if (rc == FN_OK && !progs.empty() && !jit_build_batch_variants(progs, err)) { set_error(FN_ERR_COMPILE, err); rc = FN_ERR_COMPILE; }
+        for (auto& kv : trees) {
+            if (rc != FN_OK || !jit_is_specialised(kv.first)) continue;
+            std::vector<fnGenRequest> sub;
+            for (int i : kv.second.second) sub.push_back(requests[i]);
+            int best_v = 0;
+            double best_v_ms = 1e30;
+            for (int v = 0; v < (int)batch_variants().size() && rc == FN_OK; ++v) {
+                BatchTuning t = best;
+                t.variant = v;
+                rc = run_batch(sub.data(), (int)sub.size(), stream, 0, &t);   // warm: the kernel's first launch loads it
+                if (rc) break;
+                cudaEventRecord(e0, s);
+                for (int rep = 0; rep < 2 && rc == 0; ++rep) rc = run_batch(sub.data(), (int)sub.size(), stream, 0, &t);
+                cudaEventRecord(e1, s);
+                if (rc || !cuda_ok(cudaEventSynchronize(e1), "synchronize")) { rc = rc ? rc : FN_ERR_CUDA; break; }
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < best_v_ms) { best_v_ms = ms; best_v = v; }
+            }
+            if (rc == FN_OK) Autotuner::instance().store_tree(kv.first, best_v, best_v_ms / 2);
+        }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    Autotuner::instance().store(sig, best, best_ms / 2);
-    return FN_OK;
+    return rc;
 }
 
 void* fnServerCreate(const fnServerConfig* config)
@@ -1389,6 +1433,30 @@ int fnJitCheck(const void* const* nodes, const int* dims, int count, int* cubinB
     if (!jit_compile_all(progs, cubins, err)) { set_error(FN_ERR_COMPILE, err); return FN_ERR_COMPILE; }
     size_t bytes = 0;
     for (auto& c : cubins) bytes += c.size();
+    if (cubinBytes) *cubinBytes = bytes > 0x7FFFFFFF ? 0x7FFFFFFF : (int)bytes;
+    return FN_OK;
+}
+
+int fnJitCheckBatchVariants(const void* const* nodes, const int* dims, int count, int* cubinBytes)
+{
+    clear_error();
+    std::vector<CompiledProgram> store;
+    std::vector<const CompiledProgram*> progs;
+    int rc = jit_programs(nodes, dims, count, store, progs);
+    if (rc) return rc;
+    const int nv = (int)batch_variants().size();
+    std::vector<std::vector<char>> cubins((size_t)nv);
+    std::vector<std::string> logs((size_t)nv);
+    std::vector<char> ok((size_t)nv, 1);
+    std::vector<std::thread> pool;                 // one NVRTC compilation per variant, concurrently
+    for (int v = 1; v < nv; ++v)
+        pool.emplace_back([&, v] { ok[(size_t)v] = jit_compile_cubin(jit_batch_source(progs, v), cubins[(size_t)v], logs[(size_t)v]) ? 1 : 0; });
+    for (auto& t : pool) t.join();
+    size_t bytes = 0;
+    for (int v = 1; v < nv; ++v) {
+        if (!ok[(size_t)v]) { set_error(FN_ERR_COMPILE, "NVRTC: " + logs[(size_t)v].substr(0, 4000)); return FN_ERR_COMPILE; }
+        bytes += cubins[(size_t)v].size();
+    }
     if (cubinBytes) *cubinBytes = bytes > 0x7FFFFFFF ? 0x7FFFFFFF : (int)bytes;
     return FN_OK;
 }

@@ -353,31 +353,75 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
     }
 }
 
-// The batch kernels: persistent CTAs pull (request, tile) items of their tree's
-// group and run a tile loop with that tree's code inlined.
-void emit_batch(const std::vector<const CompiledProgram*>& progs, std::ostringstream& o)
+}  // namespace
+
+const std::vector<BatchVariant>& batch_variants()
 {
+    // {threads, register bound as blocks per SM, points per thread per loop iteration}
+    static const std::vector<BatchVariant> v = {
+        {256, 4, 1},     // 64 registers: the kernel fnJitCompile builds
+        {256, 3, 1},     // 80 registers: fewer spills for long cellular walks
+        {256, 2, 1},     // 128 registers
+        {128, 8, 1},     // 64 registers in smaller blocks: finer balance of the work queue
+        {256, 2, 2},     // 128 registers, two points in flight per thread
+    };
+    return v;
+}
+
+namespace {
+
+std::string batch_kernel_name(size_t k, int variant)
+{
+    return "fnjit_batch_" + std::to_string(k) + (variant ? "_v" + std::to_string(variant) : std::string());
+}
+
+// The batch kernels: persistent CTAs pull (request, tile) items of their tree's
+// group and run a tile loop with that tree's code inlined.  A variant fixes the
+// block size, the register bound and how many points a thread has in flight.
+void emit_batch(const std::vector<const CompiledProgram*>& progs, std::ostringstream& o, int variant)
+{
+    const BatchVariant bv = batch_variants()[(size_t)variant];
     for (size_t k = 0; k < progs.size(); ++k) {
         const int D = progs[k]->dim;
-        o << "__device__ __forceinline__ void fnjit_tile_" << k
-          << "(const fn::PointArgs& A, float* __restrict__ out, unsigned i, unsigned end, float& mn, float& mx)\n{\n"
-          << "    for (; i < end; i += blockDim.x) {\n"
-          << "        float p[4];\n"
-          << "        fne::root_position32<" << D << ">(A, i, p);\n"
-          << "        const float v = fnjit_eval_" << k << "(A.seed, p[0], p[1], " << (D > 2 ? "p[2]" : "0.0f") << ", "
-          << (D > 3 ? "p[3]" : "0.0f") << ");\n"
-          << "        out[i] = v;\n"
-          << "        fne::fold(v, mn, mx);\n"
-          << "    }\n}\n\n";
+        const std::string call = "fnjit_eval_" + std::to_string(k) + "(A.seed, p[0], p[1], " + (D > 2 ? "p[2]" : "0.0f") +
+                                 ", " + (D > 3 ? "p[3]" : "0.0f") + ")";
+        o << "__device__ __forceinline__ void fnjit_tile_" << k << "_v" << variant
+          << "(const fn::PointArgs& A, float* __restrict__ out, unsigned i, unsigned end, float& mn, float& mx)\n{\n";
+        if (bv.points == 1) {
+            o << "    for (; i < end; i += blockDim.x) {\n"
+              << "        float p[4];\n"
+              << "        fne::root_position32<" << D << ">(A, i, p);\n"
+              << "        const float v = " << call << ";\n"
+              << "        out[i] = v;\n"
+              << "        fne::fold(v, mn, mx);\n"
+              << "    }\n}\n\n";
+        } else {
+            o << "    for (; i < end; i += " << bv.points << "u * blockDim.x) {\n"
+              << "        float v[" << bv.points << "];\n"
+              << "#pragma unroll\n"
+              << "        for (int q = 0; q < " << bv.points << "; ++q) {\n"
+              << "            const unsigned j = i + q * blockDim.x;\n"
+              << "            float p[4];\n"
+              << "            fne::root_position32<" << D << ">(A, j < end ? j : i, p);\n"
+              << "            v[q] = " << call << ";\n"
+              << "        }\n"
+              << "#pragma unroll\n"
+              << "        for (int q = 0; q < " << bv.points << "; ++q) {\n"
+              << "            const unsigned j = i + q * blockDim.x;\n"
+              << "            if (j < end) { out[j] = v[q]; fne::fold(v[q], mn, mx); }\n"
+              << "        }\n"
+              << "    }\n}\n\n";
+        }
     }
     // one persistent kernel per tree: each gets the register allocation its own
     // code needs, and the trees of a batch run as concurrent kernels
     for (size_t k = 0; k < progs.size(); ++k) {
-        o << "extern \"C\" __global__ void __launch_bounds__(256, 4) fnjit_batch_" << k
+        o << "extern \"C\" __global__ void __launch_bounds__(" << bv.threads << ", " << bv.min_blocks << ") "
+          << batch_kernel_name(k, variant)
           << "(fn::BatchHeader* hdr, const fn::BatchRequest* __restrict__ reqs, fn::BatchState* states,\n"
              "    const uint2* __restrict__ items, fn::BatchGroup* grp)\n{\n"
              "    __shared__ unsigned int s_item;\n"
-             "    __shared__ float smn[8], smx[8];\n"
+             "    __shared__ float smn[" << bv.threads / 32 << "], smx[" << bv.threads / 32 << "];\n"
              "    const unsigned int first = grp->item_begin, last = grp->item_end;\n"
              "    const unsigned int tile_points = hdr->tile_points;\n"
              "    for (;;) {\n"
@@ -393,7 +437,7 @@ void emit_batch(const std::vector<const CompiledProgram*>& progs, std::ostringst
              "        const unsigned begin = item.y * tile_points;\n"
              "        const unsigned end = total - begin < tile_points ? total : begin + tile_points;\n"
              "        float mn = fne::inf(), mx = -fne::inf();\n"
-             "        fnjit_tile_" << k << "(args, rq.out, begin + threadIdx.x, end, mn, mx);\n"
+             "        fnjit_tile_" << k << "_v" << variant << "(args, rq.out, begin + threadIdx.x, end, mn, mx);\n"
              "        fne::block_minmax(mn, mx, smn, smx);\n"
              "        if (threadIdx.x == 0) fne::finish_tile(rq, states + item.x, hdr, mn, mx);\n"
              "    }\n}\n\n";
@@ -408,17 +452,18 @@ struct Module {
 std::mutex g_jit_mu;
 std::unordered_map<uint64_t, JitKernels> g_kernels;
 std::vector<std::unique_ptr<Module>> g_modules;
-std::unordered_map<uint64_t, cudaKernel_t> g_batch_kernels;   // per-tree batch kernel
+std::unordered_map<uint64_t, cudaKernel_t> g_batch_kernels;   // per-tree batch kernel (variant 0)
+std::unordered_map<uint64_t, std::vector<BatchKernel>> g_batch_variant_kernels;   // per tree: every variant built
 std::atomic<bool> g_enabled{true};
 
 }  // namespace
 
-std::string jit_batch_source(const std::vector<const CompiledProgram*>& progs)
+std::string jit_batch_source(const std::vector<const CompiledProgram*>& progs, int variant)
 {
     std::ostringstream o;
-    o << "// generated by fn_jit.cpp: batch module\n" << embedded_device_source() << "\n";
+    o << "// generated by fn_jit.cpp: batch module, variant " << variant << "\n" << embedded_device_source() << "\n";
     for (size_t k = 0; k < progs.size(); ++k) emit_eval(*progs[k], "fnjit_eval_" + std::to_string(k), o);
-    emit_batch(progs, o);
+    emit_batch(progs, o, variant);
     return o.str();
 }
 
@@ -436,7 +481,7 @@ bool jit_compile_all(const std::vector<const CompiledProgram*>& progs, std::vect
     // source 0 = the batch module, 1 + k = program k's per-call module; NVRTC
     // compiles independent programs concurrently, so the sources go to a pool of threads
     std::vector<std::string> srcs;
-    srcs.push_back(jit_batch_source(progs));
+    srcs.push_back(jit_batch_source(progs, 0));
     for (auto* p : progs) srcs.push_back(jit_percall_source(*p));
     cubins.assign(srcs.size(), {});
     std::vector<std::string> logs(srcs.size());
@@ -534,8 +579,84 @@ bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& er
     }
     std::lock_guard<std::mutex> lk(g_jit_mu);
     for (auto& kv : found) g_kernels[kv.first] = kv.second;
-    for (auto& kv : batch) g_batch_kernels[kv.first] = kv.second;
+    for (auto& kv : batch) {
+        g_batch_kernels[kv.first] = kv.second;
+        auto& vars = g_batch_variant_kernels[kv.first];
+        vars.resize(batch_variants().size());
+        vars[0] = BatchKernel{kv.second, batch_variants()[0].threads};
+    }
     for (auto& m : mods) g_modules.push_back(std::move(m));   // modules stay loaded: kernels may still be queued
+    return true;
+}
+
+bool jit_build_batch_variants(const std::vector<const CompiledProgram*>& progs, std::string& error)
+{
+    const size_t nv = batch_variants().size();
+    std::vector<const CompiledProgram*> todo;
+    {
+        std::lock_guard<std::mutex> lk(g_jit_mu);
+        for (auto* p : progs) {
+            auto it = g_batch_variant_kernels.find(p->hash);
+            bool all = it != g_batch_variant_kernels.end() && it->second.size() == nv;
+            for (size_t v = 1; all && v < nv; ++v) all = it->second[v].kernel != nullptr;
+            if (!all && std::find(todo.begin(), todo.end(), p) == todo.end()) todo.push_back(p);
+        }
+    }
+    if (todo.empty()) return true;
+    // one module per variant, compiled concurrently
+    std::vector<std::string> srcs;
+    for (size_t v = 1; v < nv; ++v) srcs.push_back(jit_batch_source(todo, (int)v));
+    std::vector<std::vector<char>> cubins(srcs.size());
+    std::vector<std::string> logs(srcs.size());
+    std::vector<char> ok(srcs.size(), 0);
+    std::vector<std::thread> pool;
+    for (size_t i = 0; i < srcs.size(); ++i)
+        pool.emplace_back([&, i] { ok[i] = jit_compile_cubin(srcs[i], cubins[i], logs[i]) ? 1 : 0; });
+    for (auto& t : pool) t.join();
+    for (size_t i = 0; i < srcs.size(); ++i)
+        if (!ok[i]) { error = "NVRTC: " + logs[i].substr(0, 4000); return false; }
+    std::vector<std::unique_ptr<Module>> mods;
+    std::vector<std::vector<BatchKernel>> got(todo.size(), std::vector<BatchKernel>(nv));
+    for (size_t i = 0; i < cubins.size(); ++i) {
+        auto mod = std::make_unique<Module>();
+        cudaError_t e = cudaLibraryLoadData(&mod->lib, cubins[i].data(), nullptr, nullptr, 0, nullptr, nullptr, 0);
+        if (e != cudaSuccess) {
+            error = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e);
+            for (auto& m : mods) cudaLibraryUnload(m->lib);
+            return false;
+        }
+        const int v = (int)i + 1;
+        for (size_t k = 0; k < todo.size(); ++k) {
+            cudaKernel_t kern = nullptr;
+            if (cudaLibraryGetKernel(&kern, mod->lib, batch_kernel_name(k, v).c_str()) != cudaSuccess) {
+                error = "kernel lookup failed in a batch variant module";
+                cudaLibraryUnload(mod->lib);
+                for (auto& m : mods) cudaLibraryUnload(m->lib);
+                return false;
+            }
+            got[k][(size_t)v] = BatchKernel{kern, batch_variants()[(size_t)v].threads};
+        }
+        mods.push_back(std::move(mod));
+    }
+    std::lock_guard<std::mutex> lk(g_jit_mu);
+    for (size_t k = 0; k < todo.size(); ++k) {
+        auto& vars = g_batch_variant_kernels[todo[k]->hash];
+        vars.resize(nv);
+        for (size_t v = 1; v < nv; ++v) vars[v] = got[k][v];
+    }
+    for (auto& m : mods) g_modules.push_back(std::move(m));
+    return true;
+}
+
+bool jit_batch_kernel(uint64_t hash, int variant, BatchKernel& out)
+{
+    if (!g_enabled.load(std::memory_order_relaxed)) return false;
+    std::lock_guard<std::mutex> lk(g_jit_mu);
+    auto it = g_batch_variant_kernels.find(hash);
+    if (it == g_batch_variant_kernels.end() || variant < 0 || (size_t)variant >= it->second.size() ||
+        !it->second[(size_t)variant].kernel)
+        return false;
+    out = it->second[(size_t)variant];
     return true;
 }
 
@@ -546,19 +667,6 @@ bool jit_lookup(uint64_t hash, JitKernels& out)
     auto it = g_kernels.find(hash);
     if (it == g_kernels.end()) return false;
     out = it->second;
-    return true;
-}
-
-bool jit_batch_kernels(const std::vector<uint64_t>& hashes, std::vector<cudaKernel_t>& kernels)
-{
-    if (!g_enabled.load(std::memory_order_relaxed)) return false;
-    std::lock_guard<std::mutex> lk(g_jit_mu);
-    kernels.resize(hashes.size());
-    for (size_t i = 0; i < hashes.size(); ++i) {
-        auto it = g_batch_kernels.find(hashes[i]);
-        if (it == g_batch_kernels.end()) return false;
-        kernels[i] = it->second;
-    }
     return true;
 }
 
@@ -598,7 +706,13 @@ struct AutoJit {
     std::condition_variable cv, idle_cv;
     std::unordered_map<uint64_t, int> uses;        // interpreter launches per program hash
     std::unordered_set<uint64_t> queued;           // handed to the worker once, whatever the outcome
-    std::deque<std::pair<CompiledProgram, int>> work;   // program copy, device
+    struct Job {
+        CompiledProgram prog;                      // a copy: the caller's may go away
+        int device;
+        bool variants;                             // build the batch variants, not the tree's kernels
+    };
+    std::deque<Job> work;
+    std::unordered_set<uint64_t> variants_queued;
     int running = 0;
     int threshold = -1;                            // -1 = not read from the environment yet
     bool stop = false;
@@ -637,13 +751,17 @@ void auto_worker()
     for (;;) {
         a.cv.wait(lk, [&] { return a.stop || !a.work.empty(); });
         if (a.stop) return;
-        std::pair<CompiledProgram, int> job = std::move(a.work.front());
+        AutoJit::Job job = std::move(a.work.front());
         a.work.pop_front();
         ++a.running;
         lk.unlock();
-        cudaSetDevice(job.second);
+        cudaSetDevice(job.device);
         std::string err;
-        if (!is_built(job.first.hash)) jit_build({&job.first}, err);   // a failure leaves the interpreter in use
+        if (job.variants) {
+            if (is_built(job.prog.hash)) jit_build_batch_variants({&job.prog}, err);   // a failure keeps variant 0
+        } else if (!is_built(job.prog.hash)) {
+            jit_build({&job.prog}, err);           // a failure leaves the interpreter in use
+        }
         lk.lock();
         --a.running;
         if (a.work.empty() && a.running == 0) a.idle_cv.notify_all();
@@ -670,7 +788,21 @@ void jit_note_interpreted(const CompiledProgram* prog)
     a.uses.erase(prog->hash);
     int dev = 0;
     cudaGetDevice(&dev);
-    a.work.emplace_back(*prog, dev);
+    a.work.push_back(AutoJit::Job{*prog, dev, false});
+    if (!a.worker.joinable()) a.worker = std::thread(auto_worker);
+    a.cv.notify_one();
+}
+
+void jit_request_batch_variants(const CompiledProgram* prog)
+{
+    if (!prog || !g_enabled.load(std::memory_order_relaxed)) return;
+    AutoJit& a = auto_jit();
+    std::lock_guard<std::mutex> lk(a.mu);
+    if (a.stop || a.variants_queued.count(prog->hash)) return;
+    a.variants_queued.insert(prog->hash);
+    int dev = 0;
+    cudaGetDevice(&dev);
+    a.work.push_back(AutoJit::Job{*prog, dev, true});
     if (!a.worker.joinable()) a.worker = std::thread(auto_worker);
     a.cv.notify_one();
 }

@@ -31,9 +31,26 @@ struct JitKernels {
     int resident[3] = {1, 1, 1};      // 256-thread blocks per SM of grid / positions / tileable at once
 };
 
-// CUDA source of the batch module for `progs` (slot k = progs[k]) and of one
-// program's per-call module.
-std::string jit_batch_source(const std::vector<const CompiledProgram*>& progs);
+// Variants of a tree's persistent batch kernel, among which the autotuner picks per
+// tree: threads per block, the register bound (the blocks per SM the kernel must fit,
+// __launch_bounds__) and how many points a thread has in flight per loop iteration.
+// Variant 0 is the one fnJitCompile builds; the others are built when a tuning run
+// (or a loaded tuning table) asks for them.
+struct BatchVariant {
+    int threads;
+    int min_blocks;
+    int points;
+};
+const std::vector<BatchVariant>& batch_variants();
+
+struct BatchKernel {
+    cudaKernel_t kernel = nullptr;
+    int threads = 256;
+};
+
+// CUDA source of the batch module for `progs` (slot k = progs[k]) in one variant, and of
+// one program's per-call module.
+std::string jit_batch_source(const std::vector<const CompiledProgram*>& progs, int variant);
 std::string jit_percall_source(const CompiledProgram& prog);
 
 // NVRTC-compile the batch module and every per-call module (concurrently);
@@ -45,13 +62,19 @@ bool jit_compile_all(const std::vector<const CompiledProgram*>& progs, std::vect
 // per-call kernels and a batch kernel.  Thread safe.
 bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& error);
 
+// Build variants 1.. of the batch kernels of `progs` (NVRTC, one module per variant,
+// compiled concurrently); programs whose variants exist are skipped.  Thread safe.
+bool jit_build_batch_variants(const std::vector<const CompiledProgram*>& progs, std::string& error);
+
+// The batch kernel of `hash` in `variant`, or false when it is not built (or JIT is off).
+bool jit_batch_kernel(uint64_t hash, int variant, BatchKernel& out);
+
+// Queue a background build of the batch variants of `prog` (a tuning table loaded in this
+// process may name variants that have not been built yet).
+void jit_request_batch_variants(const CompiledProgram* prog);
+
 // Kernels for a program hash, or false if none have been built.
 bool jit_lookup(uint64_t hash, JitKernels& out);
-
-// The per-tree batch kernel of every hash, all or nothing (false if JIT is off
-// or any program has none).  Kernel signature: (BatchHeader*, const
-// BatchRequest*, BatchState*, const uint2* items, BatchGroup*).
-bool jit_batch_kernels(const std::vector<uint64_t>& hashes, std::vector<cudaKernel_t>& kernels);
 
 // Launch the specialised per-call kernel for `hash` if one is loaded (and JIT
 // is enabled); returns false when the caller should use the interpreter.

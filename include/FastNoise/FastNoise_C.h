@@ -225,7 +225,12 @@ FASTNOISE_API int fnGenEachDevice(const fnGenRequest* requests, int count, void*
  * Returns when every request has completed. */
 FASTNOISE_API int fnGenEachPaced(const fnGenRequest* requests, int count, const double* arrivalMicros, void* stream,
                                  double* latencyMicros);
-/* Time each tuning candidate on this batch and remember the fastest for its signature. */
+/* Tune this batch: time each tile size / CTAs-per-SM candidate on the whole batch and remember
+ * the fastest for the batch's signature; then, for every tree of the batch that has specialised
+ * kernels, time its requests alone with each variant of its batch kernel (threads per block,
+ * register bound, points in flight per thread; built here on first use, seconds) and remember
+ * the fastest per tree.  Later batches (and the server) use both choices; fnAutotuneSave writes
+ * them out ("tree" lines for the per-tree choices). */
 FASTNOISE_API int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream);
 FASTNOISE_API int fnAutotuneLoad(const char* path);
 FASTNOISE_API int fnAutotuneSave(const char* path);
@@ -407,6 +412,9 @@ FASTNOISE_API int fnJitIsSpecialised(const void* node, int dimension);
 /* Generate and compile the module source with NVRTC without loading it (no GPU needed);
  * *cubinBytes (may be NULL) receives the size of the compiled code. */
 FASTNOISE_API int fnJitCheck(const void* const* nodes, const int* dimensions, int count, int* cubinBytes);
+/* The same for the other variants of the trees' batch kernels (block size, register bound,
+ * points in flight per thread), which fnAutotuneBatch builds and times per tree. */
+FASTNOISE_API int fnJitCheckBatchVariants(const void* const* nodes, const int* dimensions, int count, int* cubinBytes);
 /* Turn the use of specialised kernels on (1, the default) or off (0, interpreter only).
  * Returns the previous setting. */
 FASTNOISE_API int fnSetJitEnabled(int enabled);

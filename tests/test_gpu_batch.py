@@ -130,3 +130,34 @@ def test_batch_host_outputs_match_device_batch(gpu, torch_cuda, contiguous):
     for c, dout, dmm, hout, hmm in zip(chunks, douts, dmms, houts, hmms):
         assert np.array_equal(hout.view(np.uint32), dout.cpu().numpy().view(np.uint32)), c
         assert (hmm[0], hmm[1]) == (dmm[0], dmm[1]), c
+
+
+def test_autotune_picks_a_batch_kernel_variant_per_tree(gpu, torch_cuda, tmp_path):
+    """fnAutotuneBatch times every variant of each specialised tree's batch kernel (block size,
+    register bound, points in flight per thread) and keeps one per tree; fnAutotuneSave lists the
+    choices as "tree" lines.  Every variant gives the same outputs: with a table that forces
+    variant v for every tree, the batch equals the per-call results bit for bit."""
+    fn, torch = gpu, torch_cuda
+    nodes = [trees.to_product(m()) for m in trees.MIX_TREES]
+    fn.jit_compile([(n, d) for n in nodes for d in (2, 3)])
+    chunks = chunkmix.make_mix(64, seed=13, sizes=[(16, 16, 16), (32, 32, 32), (64, 64), (128, 128)])
+    reqs, outs, mms = requests_for(fn, torch, chunks, nodes)
+    refs = [nodes[c.tree].gen_uniform_grid(c.offset, c.count, (1,) * len(c.count), c.seed) for c in chunks]
+    fn.autotune_batch(reqs)
+    path = tmp_path / "tune.txt"
+    fn.autotune_save(path)
+    lines = path.read_text().splitlines()
+    tree_lines = [ln.split() for ln in lines if ln.startswith("tree ")]
+    assert len(tree_lines) == len({(c.tree, len(c.count)) for c in chunks})   # one per tree and dimensionality
+    n_variants = 5
+    for variant in range(n_variants):
+        forced = [ln for ln in lines if not ln.startswith("tree ")]
+        forced += [f"tree {t[1]} {variant} 0 0 0 1.0" for t in tree_lines]
+        path.write_text("\n".join(forced) + "\n")
+        fn.autotune_load(path)
+        for o in outs:
+            o.fill_(float("nan"))
+        fn.gen_batch(reqs, sync=True)
+        for c, o, mm, (ref, rmm) in zip(chunks, outs, mms, refs):
+            assert np.array_equal(o.cpu().numpy().view(np.uint32), ref.view(np.uint32)), (variant, c)
+            assert (mm[0], mm[1]) == rmm, (variant, c)

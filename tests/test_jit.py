@@ -21,6 +21,15 @@ def test_every_node_kind_compiles(native, dim):
     assert fn.jit_check(pairs) > 0
 
 
+def test_batch_kernel_variants_compile(native):
+    """The other variants of the per-tree batch kernels (block size, register bound, points in
+    flight per thread), which the autotuner builds and times, compile for sm_103a."""
+    fn = native
+    pairs = [(trees.to_product(m()), 3) for m in trees.MIX_TREES] + [(trees.to_product(trees.terrain_c2()), 4),
+                                                                       (trees.to_product(trees.cellular_value_tree()), 2)]
+    assert fn.jit_check_batch_variants(pairs) > 0
+
+
 def test_jit_rejects_bad_arguments(native):
     fn = native
     with pytest.raises(fn.FastNoiseError):
