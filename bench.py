@@ -418,6 +418,25 @@ def run_chunkmix(a, rank, world, local):
         batch_ms = timed(lambda: fn.gen_batch(rarr, sptr, sync=False), a.steps, "batched")
         percall_ms = timed(lambda: fn.gen_each(rarr, sptr, sync=False), max(2, a.steps // 2), "per_call")
         barrier(world)
+    # the same batch with every tree on its batch kernel's variant 0 (what runs without the
+    # per-tree tuning), then the tuned table back
+    variants_default_ms = None
+    if a.kernels == "jit":
+        with tempfile.TemporaryDirectory() as td:
+            tuned = os.path.join(td, "tuned.txt")
+            fn.autotune_save(tuned)
+            lines = open(tuned).read().splitlines()
+            trees_tuned = {ln.split()[1]: int(ln.split()[2]) for ln in lines if ln.startswith("tree ")}
+            plain = os.path.join(td, "plain.txt")
+            with open(plain, "w") as f:
+                for ln in lines:
+                    parts = ln.split()
+                    f.write((" ".join(parts[:2] + ["0"] + parts[3:]) if ln.startswith("tree ") else ln) + "\n")
+            fn.autotune_load(plain)
+            fn.gen_batch(rarr, sptr, sync=True)
+            variants_default_ms = timed(lambda: fn.gen_batch(rarr, sptr, sync=False), a.steps, "batched_variant0")
+            fn.autotune_load(tuned)
+            fn.gen_batch(rarr, sptr, sync=True)
     interp = None
     if a.kernels == "jit":                              # the same batch through the interpreter, for comparison
         fn.set_jit_enabled(False)
@@ -493,6 +512,12 @@ def run_chunkmix(a, rank, world, local):
         "per_call": {"value": percall_value, "unit": "Mpoints/s", "ms_per_step": percall_ms,
                      "api": "fnGenEachDevice: one launch per request"},
         "batched_vs_per_call": value / percall_value,
+        "batch_kernel_variants": None if variants_default_ms is None else {
+            "tuned_per_tree": {k: v for k, v in trees_tuned.items()},
+            "variant0_everywhere": {"value": pts / (variants_default_ms * 1e-3) / 1e6, "unit": "Mpoints/s",
+                                    "ms_per_step": variants_default_ms},
+            "variants": "0: 256 threads, 64 regs; 1: 256, 80 regs; 2: 256, 128 regs; 3: 128, 64 regs; "
+                        "4: 256, 128 regs, 2 points in flight"},
         "served": served,
         "roofline": {"bound": "fp32-issue", "achieved": achieved, "peak": peak_lane, "unit": "Tlane-op/s",
                      "frac": achieved / peak_lane, "traffic": read_traffic("chunk-mix"),

@@ -1025,12 +1025,14 @@ int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream)
     }
     Autotuner::instance().store(sig, best, best_ms / 2);
 
-    // Per tree: the variant of its specialised batch kernel (register bound, block size,
-    // points in flight per thread).  The tree's own requests run alone in every variant with
-    // the batch's tuned tile size; the fastest variant is kept for that tree.
+    // Per tree: the variant of its specialised batch kernel (register bound, block size, points
+    // in flight per thread).  The trees' kernels run concurrently, so a variant is judged by the
+    // whole batch: coordinate descent over the trees (most points first), each variant of one
+    // tree tried with the others' current choices, kept when the batch gets faster by more than
+    // the timing noise (0.5 %).
     int rc = FN_OK;
     if (jit_enabled()) {
-        std::map<uint64_t, std::pair<const CompiledProgram*, std::vector<int>>> trees;
+        std::map<uint64_t, std::pair<const CompiledProgram*, long long>> trees;   // hash -> program, points
         for (int i = 0; i < count && rc == FN_OK; ++i) {
             PointArgs a;
             DeviceProgram p;
@@ -1038,33 +1040,50 @@ int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream)
             if (!get_program(N(requests[i].node), a.dim, p)) { rc = last_error(); break; }
             auto& t = trees[p.hash];
             t.first = p.host;
-            t.second.push_back(i);
+            t.second += std::max(0ll, a.total);
         }
+        std::vector<std::pair<long long, uint64_t>> order;
         std::vector<const CompiledProgram*> progs;
         for (auto& kv : trees)
-            if (jit_is_specialised(kv.first)) progs.push_back(kv.second.first);
+            if (jit_is_specialised(kv.first)) {
+                progs.push_back(kv.second.first);
+                order.push_back({kv.second.second, kv.first});
+            }
+        std::sort(order.rbegin(), order.rend());
         std::string err;
         if (rc == FN_OK && !progs.empty() && !jit_build_batch_variants(progs, err)) { set_error(FN_ERR_COMPILE, err); rc = FN_ERR_COMPILE; }
-        for (auto& kv : trees) {
-            if (rc != FN_OK || !jit_is_specialised(kv.first)) continue;
-            std::vector<fnGenRequest> sub;
-            for (int i : kv.second.second) sub.push_back(requests[i]);
-            int best_v = 0;
-            double best_v_ms = 1e30;
-            for (int v = 0; v < (int)batch_variants().size() && rc == FN_OK; ++v) {
-                BatchTuning t = best;
-                t.variant = v;
-                rc = run_batch(sub.data(), (int)sub.size(), stream, 0, &t);   // warm: the kernel's first launch loads it
-                if (rc) break;
+        // the whole batch with the current choices: one warm launch (a new shape compiles and
+        // captures), then the fastest of three
+        auto time_batch = [&](double& ms_out) -> int {
+            int r = run_batch(requests, count, stream, 0, &best);
+            double fastest = 1e30;
+            for (int rep = 0; rep < 3 && r == FN_OK; ++rep) {
                 cudaEventRecord(e0, s);
-                for (int rep = 0; rep < 2 && rc == 0; ++rep) rc = run_batch(sub.data(), (int)sub.size(), stream, 0, &t);
+                r = run_batch(requests, count, stream, 0, &best);
                 cudaEventRecord(e1, s);
-                if (rc || !cuda_ok(cudaEventSynchronize(e1), "synchronize")) { rc = rc ? rc : FN_ERR_CUDA; break; }
+                if (r == FN_OK && !cuda_ok(cudaEventSynchronize(e1), "synchronize")) r = FN_ERR_CUDA;
                 float ms = 0;
-                cudaEventElapsedTime(&ms, e0, e1);
-                if (ms < best_v_ms) { best_v_ms = ms; best_v = v; }
+                if (r == FN_OK) cudaEventElapsedTime(&ms, e0, e1);
+                fastest = std::min(fastest, (double)ms);
             }
-            if (rc == FN_OK) Autotuner::instance().store_tree(kv.first, best_v, best_v_ms / 2);
+            ms_out = fastest;
+            return r;
+        };
+        double base = 0;
+        if (rc == FN_OK && !order.empty()) {
+            for (auto& o : order) Autotuner::instance().store_tree(o.second, 0, 0.0);
+            rc = time_batch(base);
+        }
+        for (auto& o : order) {
+            if (rc != FN_OK) break;
+            int keep = 0;
+            for (int v = 1; v < (int)batch_variants().size() && rc == FN_OK; ++v) {
+                Autotuner::instance().store_tree(o.second, v, 0.0);
+                double ms = 0;
+                rc = time_batch(ms);
+                if (rc == FN_OK && ms < base * 0.995) { base = ms; keep = v; }
+            }
+            Autotuner::instance().store_tree(o.second, keep, base);
         }
     }
     cudaEventDestroy(e0);

@@ -226,11 +226,12 @@ FASTNOISE_API int fnGenEachDevice(const fnGenRequest* requests, int count, void*
 FASTNOISE_API int fnGenEachPaced(const fnGenRequest* requests, int count, const double* arrivalMicros, void* stream,
                                  double* latencyMicros);
 /* Tune this batch: time each tile size / CTAs-per-SM candidate on the whole batch and remember
- * the fastest for the batch's signature; then, for every tree of the batch that has specialised
- * kernels, time its requests alone with each variant of its batch kernel (threads per block,
- * register bound, points in flight per thread; built here on first use, seconds) and remember
- * the fastest per tree.  Later batches (and the server) use both choices; fnAutotuneSave writes
- * them out ("tree" lines for the per-tree choices). */
+ * the fastest for the batch's signature; then choose, for every tree of the batch that has
+ * specialised kernels, a variant of its batch kernel (threads per block, register bound, points
+ * in flight per thread; built here on first use, seconds): tree by tree, most points first, each
+ * variant is timed on the whole batch and kept when the batch gets faster.  Later batches (and
+ * the server) use both choices; fnAutotuneSave writes them out ("tree" lines for the per-tree
+ * choices). */
 FASTNOISE_API int fnAutotuneBatch(const fnGenRequest* requests, int count, void* stream);
 FASTNOISE_API int fnAutotuneLoad(const char* path);
 FASTNOISE_API int fnAutotuneSave(const char* path);
