@@ -9,6 +9,7 @@
 
 #include "../../include/FastNoise/FastNoise_C.h"
 #include "fn_capi_internal.h"
+#include "fn_jit.h"
 #include "fn_mesh.h"
 
 using namespace fn;
@@ -27,6 +28,7 @@ struct MeshCtx {
     float* dminmax = nullptr;
     MeshScratch scratch;
     DmcScratch dmc;
+    SparseScratch sp;                  // the sparse density form (trees with specialised kernels)
     unsigned* host = nullptr;          // pinned read-back of one chunk (see enqueue_chunk)
     ~MeshCtx()
     {
@@ -34,7 +36,35 @@ struct MeshCtx {
         if (dminmax) cudaFree(dminmax);
         if (scratch.counts) cudaFree(scratch.counts);
         if (dmc.offsets) cudaFree(dmc.offsets);
+        if (sp.above) cudaFree(sp.above);
         if (host) cudaFreeHost(host);
+    }
+
+    // Bitmasks, ranks and the needed list for `densities` densities.  The index list and the
+    // value array are sized for every density, though a chunk stores only the few near its
+    // surface.
+    bool reserve_sparse(size_t densities)
+    {
+        if (densities <= sp.cap_densities) return true;
+        if (sp.above) cudaFree(sp.above);
+        sp = SparseScratch();
+        const size_t words = (densities + 31) / 32, nb = (words + 1023) / 1024;
+        char* block = nullptr;
+        if (!cuda_ok(cudaMalloc(&block, (5 * words + nb + 1 + densities) * sizeof(unsigned) + densities * sizeof(float)),
+                     "cudaMalloc(mesh sparse densities)"))
+            return false;
+        unsigned* w = reinterpret_cast<unsigned*>(block);
+        sp.above = w;
+        sp.solid = w + words;
+        sp.need = w + 2 * words;
+        sp.counts = w + 3 * words;
+        sp.rank = w + 4 * words;
+        sp.block_totals = w + 5 * words;
+        sp.total = w + 5 * words + nb;
+        sp.idx = w + 5 * words + nb + 1;
+        sp.vals = reinterpret_cast<float*>(w + 5 * words + nb + 1 + densities);
+        sp.cap_densities = densities;
+        return true;
     }
 
     bool reserve(size_t densities, size_t voxels)
@@ -154,25 +184,61 @@ bool enqueue_chunk(MeshKind kind, const DeviceProgram& prog, MeshCtx& m, cudaStr
 {
     const int apron = kind == kDmc ? 2 : 1;
     const int sg = size + 2 * apron;
-    if (!m.reserve((size_t)sg * sg * sg, kind == kBloxel ? (size_t)size * size * size : 0) || (kind == kDmc && !m.reserve_dmc(size)))
-        return false;
+    const size_t n_dens = (size_t)sg * sg * sg;
     MinMaxWork* work = work_for_stream(s);
     if (!work) return false;
     const float off[3] = {(float)(px - apron), (float)((upAxisZ ? pz : py) - apron), (float)((upAxisZ ? py : pz) - apron)};
     const int cnt[3] = {sg, sg, sg};
     const float step[3] = {1, 1, 1};
-    if (!cuda_ok(launch_points(prog, grid_args(3, off, cnt, step, seed), m.dens, work, m.dminmax, s), "densities")) return false;
+    const PointArgs args = grid_args(3, off, cnt, step, seed);
+    // A tree with specialised kernels meshes from the sparse form: its densities stay in
+    // registers, only their classification against the iso level is stored, and the few exact
+    // values the passes need are evaluated again where they are read.  Otherwise the tree's
+    // (interpreter) kernel writes the density array.
+    bool sparse = false;
+    if (jit_enabled()) {
+        if (!m.reserve(0, kind == kBloxel ? (size_t)size * size * size : 0) || (kind == kDmc && !m.reserve_dmc(size)) ||
+            !m.reserve_sparse(n_dens))
+            return false;
+        cudaError_t err = cudaSuccess;
+        sparse = jit_launch_solid(prog.hash, args, m.sp.above, m.sp.solid, work, m.dminmax, iso, s, err);
+        if (sparse && !cuda_ok(err, "densities (classification)")) return false;
+    }
+    if (!sparse) {
+        if (!m.reserve(n_dens, kind == kBloxel ? (size_t)size * size * size : 0) || (kind == kDmc && !m.reserve_dmc(size)))
+            return false;
+        if (!cuda_ok(launch_points(prog, args, m.dens, work, m.dminmax, s), "densities")) return false;
+    }
     MeshVertex* verts = reinterpret_cast<MeshVertex*>(mesh->vertices);
+    auto needed_values = [&]() {
+        cudaError_t err = cudaSuccess;
+        return jit_launch_list(prog.hash, args, m.sp.idx, m.sp.total, (unsigned)n_dens, m.sp.vals, s, err) &&
+               cuda_ok(err, "needed densities");
+    };
     if (kind == kBloxel) {
-        if (!cuda_ok(launch_bloxel(m.dens, size, upAxisZ != 0, (float)px, (float)py, (float)pz, iso, m.dminmax, m.scratch, verts,
-                                   (unsigned)mesh->vertexCapacity, mesh->indices, (unsigned)mesh->indexCapacity, s),
-                     "bloxel mesher") ||
-            !cuda_ok(cudaMemcpyAsync(host8, m.scratch.total, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read back"))
+        const bool queued =
+            sparse ? cuda_ok(launch_bloxel_sparse_prepare(m.sp, size, upAxisZ != 0, (float)px, (float)py, (float)pz, iso, m.dminmax,
+                                                          m.scratch, s), "bloxel mesher") &&
+                         needed_values() &&
+                         cuda_ok(launch_bloxel_sparse_emit(m.sp, size, upAxisZ != 0, (float)px, (float)py, (float)pz, iso, m.dminmax,
+                                                           m.scratch, verts, (unsigned)mesh->vertexCapacity, mesh->indices,
+                                                           (unsigned)mesh->indexCapacity, s), "bloxel mesher")
+                   : cuda_ok(launch_bloxel(m.dens, size, upAxisZ != 0, (float)px, (float)py, (float)pz, iso, m.dminmax, m.scratch,
+                                           verts, (unsigned)mesh->vertexCapacity, mesh->indices, (unsigned)mesh->indexCapacity, s),
+                             "bloxel mesher");
+        if (!queued || !cuda_ok(cudaMemcpyAsync(host8, m.scratch.total, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read back"))
             return false;
     } else {
-        if (!cuda_ok(launch_dmc(m.dens, size, upAxisZ != 0, px, py, pz, iso, m.dminmax, m.dmc, verts, (unsigned)mesh->vertexCapacity,
-                                mesh->indices, (unsigned)mesh->indexCapacity, s),
-                     "dual marching cubes mesher") ||
+        const bool queued =
+            sparse ? cuda_ok(launch_dmc_sparse_prepare(m.sp, size, upAxisZ != 0, iso, m.dminmax, m.dmc, s), "dual marching cubes mesher") &&
+                         needed_values() &&
+                         cuda_ok(launch_dmc_sparse_finish(m.sp, size, upAxisZ != 0, px, py, pz, iso, m.dmc, verts,
+                                                          (unsigned)mesh->vertexCapacity, mesh->indices, (unsigned)mesh->indexCapacity, s),
+                                 "dual marching cubes mesher")
+                   : cuda_ok(launch_dmc(m.dens, size, upAxisZ != 0, px, py, pz, iso, m.dminmax, m.dmc, verts,
+                                        (unsigned)mesh->vertexCapacity, mesh->indices, (unsigned)mesh->indexCapacity, s),
+                             "dual marching cubes mesher");
+        if (!queued ||
             !cuda_ok(cudaMemcpyAsync(host8, m.dmc.total, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read back") ||
             !cuda_ok(cudaMemcpyAsync(host8 + 2, m.dmc.airsolid, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, s), "read back"))
             return false;

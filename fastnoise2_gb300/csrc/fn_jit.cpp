@@ -318,6 +318,7 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
     };
 
     // grid: Generator.inl:79-254, pos_k = fma(float(i_k), step_k, offset_k), x fastest
+    std::string gridpos;
     {
         std::ostringstream pos;
         pos << "                unsigned r = i + A.base;\n";          // index in the whole request
@@ -329,7 +330,8 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
             else pos << "                const unsigned i" << ax[j] << " = r;\n";
             pos << "                const float " << pv[j] << " = fmaf(fnd::cvtf((int)i" << ax[j] << "), A.step[" << j << "], A.offset[" << j << "]);\n";
         }
-        kernel("fnjit_grid", "", pos.str());
+        gridpos = pos.str();
+        kernel("fnjit_grid", "", gridpos);
     }
     // position arrays: Generator.inl:256-350, pos_k = offset_k + array_k[i]
     {
@@ -350,6 +352,49 @@ void emit_percall(const CompiledProgram& prog, int k, std::ostringstream& o)
             << "                const float pz = fnd::sin_(xf) * A.tfreq[0];\n"
             << "                const float pw = fnd::sin_(yf) * A.tfreq[1];\n";
         kernel("fnjit_tile", "", pos.str());
+    }
+    // Chunk meshing (3D programs): the meshers need every density only as "above the iso
+    // level" / "at or below it", and exact values at a few voxels near the surface.
+    //  fnjit_solid: the grid's two classification bitmasks (bit i of word i / 32; the warp's
+    //    32 consecutive points form one word) and OutputMinMax -- no density leaves registers;
+    //  fnjit_list: the grid's values at listed point indices (count read from the device).
+    if (D == 3) {
+        o << "extern \"C\" __global__ void __launch_bounds__(256, 4) fnjit_solid_" << k
+          << "(fn::PointArgs A, unsigned* __restrict__ above, unsigned* __restrict__ solid, fn::MinMaxWork* work, float* dminmax,\n"
+          << "    float iso, unsigned ppl)\n{\n"
+          << "    __shared__ float smn[8], smx[8];\n"
+          << "    float mn = fne::inf(), mx = -fne::inf();\n"
+          << "    const unsigned total = (unsigned)A.total;\n"
+          << "    const unsigned lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;\n"
+          << "    const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;\n"
+          << "    const unsigned chunk = 32u * ppl;\n"
+          << "    for (unsigned base = (((blockIdx.x * blockDim.x) >> 5) + warp) * chunk; base < total; base += nwarps * chunk) {\n"
+          << "#pragma unroll 1\n"
+          << "        for (unsigned t = 0; t < ppl; ++t) {\n"
+          << "            const unsigned i = base + t * 32u + lane;\n"
+          << "            bool gt = false, le = false;\n"
+          << "            if (i < total) {\n"
+          << gridpos
+          << "                const float v = " << call << ";\n"
+          << "                fne::fold(v, mn, mx);\n"
+          << "                gt = v > iso;\n"
+          << "                le = v <= iso;\n"
+          << "            }\n"
+          << "            const unsigned wg = __ballot_sync(0xffffffffu, gt), wl = __ballot_sync(0xffffffffu, le);\n"
+          << "            if (lane == 0 && base + t * 32u < total) { above[(base + t * 32u) >> 5] = wg; solid[(base + t * 32u) >> 5] = wl; }\n"
+          << "        }\n"
+          << "    }\n"
+          << "    fne::grid_minmax(mn, mx, work, dminmax, smn, smx);\n"
+          << "}\n\n";
+        o << "extern \"C\" __global__ void __launch_bounds__(256, 4) fnjit_list_" << k
+          << "(fn::PointArgs A, const unsigned* __restrict__ idx, const unsigned* __restrict__ count, float* __restrict__ out)\n{\n"
+          << "    const unsigned n = *count;\n"
+          << "    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {\n"
+          << "        const unsigned i = idx[j];\n"
+          << gridpos
+          << "        out[j] = " << call << ";\n"
+          << "    }\n"
+          << "}\n\n";
     }
 }
 
@@ -560,6 +605,8 @@ bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& er
         ok = cudaLibraryGetKernel(&jk.grid, lib, "fnjit_grid_0") == cudaSuccess &&
              cudaLibraryGetKernel(&jk.positions, lib, "fnjit_pos_0") == cudaSuccess &&
              (progs[k]->dim != 4 || cudaLibraryGetKernel(&jk.tileable, lib, "fnjit_tile_0") == cudaSuccess) &&
+             (progs[k]->dim != 3 || (cudaLibraryGetKernel(&jk.solid, lib, "fnjit_solid_0") == cudaSuccess &&
+                                     cudaLibraryGetKernel(&jk.list, lib, "fnjit_list_0") == cudaSuccess)) &&
              cudaLibraryGetKernel(&bk, mods[0]->lib, ("fnjit_batch_" + std::to_string(k)).c_str()) == cudaSuccess;
         const cudaKernel_t kern[3] = {jk.grid, jk.positions, jk.tileable};
         for (int j = 0; ok && j < 3; ++j) {
@@ -858,6 +905,42 @@ bool jit_launch(uint64_t hash, const PointArgs& args, float* out, MinMaxWork* wo
     PointArgs a = args;
     void* params[] = {&a, &out, &work, &dminmax, &ppl};
     err = cudaLaunchKernel((const void*)k, dim3((unsigned)blocks), dim3(256), params, 0, stream);
+    return true;
+}
+
+bool jit_launch_solid(uint64_t hash, const PointArgs& args, unsigned* above, unsigned* solid, MinMaxWork* work, float* dminmax,
+                      float iso, cudaStream_t stream, cudaError_t& err)
+{
+    err = cudaSuccess;
+    JitKernels jk;
+    if (args.total <= 0 || args.total > (1ll << 31) || !jit_lookup(hash, jk) || !jk.solid) return false;
+    const int sms = num_sms();
+    unsigned ppl = 4u;                                     // the grid as the large per-call calls run it
+    long long blocks = std::min<long long>((args.total + 1023) / 1024, (long long)sms * 8);
+    if (args.total < (long long)sms * 8 * 128 * 4) {
+        const long long resident = (long long)sms * std::max(1, jk.resident[0]) * 256;
+        ppl = (unsigned)std::min<long long>(4, std::max<long long>(1, (args.total + resident - 1) / resident));
+        blocks = (args.total + 256ll * ppl - 1) / (256ll * ppl);
+    }
+    if (blocks > kMaxReduceBlocks) blocks = kMaxReduceBlocks;
+    if (blocks < 1) blocks = 1;
+    PointArgs a = args;
+    void* params[] = {&a, &above, &solid, &work, &dminmax, &iso, &ppl};
+    err = cudaLaunchKernel((const void*)jk.solid, dim3((unsigned)blocks), dim3(256), params, 0, stream);
+    return true;
+}
+
+bool jit_launch_list(uint64_t hash, const PointArgs& args, const unsigned* idx, const unsigned* count, unsigned max_count,
+                     float* out, cudaStream_t stream, cudaError_t& err)
+{
+    err = cudaSuccess;
+    JitKernels jk;
+    if (args.total <= 0 || args.total > (1ll << 31) || !jit_lookup(hash, jk) || !jk.list) return false;
+    long long blocks = std::min<long long>(((long long)max_count + 255) / 256, (long long)num_sms() * 8);
+    if (blocks < 1) blocks = 1;
+    PointArgs a = args;
+    void* params[] = {&a, &idx, &count, &out};
+    err = cudaLaunchKernel((const void*)jk.list, dim3((unsigned)blocks), dim3(256), params, 0, stream);
     return true;
 }
 

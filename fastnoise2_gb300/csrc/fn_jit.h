@@ -27,6 +27,8 @@ struct JitKernels {
     cudaKernel_t grid = nullptr;      // GenUniformGrid for the program's dimensionality
     cudaKernel_t positions = nullptr; // GenPositionArray
     cudaKernel_t tileable = nullptr;  // GenTileable2D (4D programs only)
+    cudaKernel_t solid = nullptr;     // chunk meshing (3D programs): classification bitmasks of a grid
+    cudaKernel_t list = nullptr;      // chunk meshing (3D programs): grid values at listed point indices
     int slot = -1;                    // index in the module's batch kernel
     int resident[3] = {1, 1, 1};      // 256-thread blocks per SM of grid / positions / tileable at once
 };
@@ -81,6 +83,15 @@ bool jit_lookup(uint64_t hash, JitKernels& out);
 // `err` carries the launch status when true is returned.
 bool jit_launch(uint64_t hash, const PointArgs& args, float* out, MinMaxWork* work, float* dminmax, cudaStream_t stream,
                 cudaError_t& err);
+
+// Chunk meshing with a specialised 3D tree (false when none is loaded): bit i of `above` /
+// `solid` = grid point i's value is > iso / <= iso (both 0 for NaN), and OutputMinMax into
+// `dminmax`; and the values at the grid point indices idx[0 .. *count) into out (max_count
+// bounds the launch).
+bool jit_launch_solid(uint64_t hash, const PointArgs& args, unsigned* above, unsigned* solid, MinMaxWork* work, float* dminmax,
+                      float iso, cudaStream_t stream, cudaError_t& err);
+bool jit_launch_list(uint64_t hash, const PointArgs& args, const unsigned* idx, const unsigned* count, unsigned max_count,
+                     float* out, cudaStream_t stream, cudaError_t& err);
 
 // Programs the interpreter cannot run (CompiledProgram::needs_specialisation)
 // get their specialised kernels built on first use; true if they exist now.

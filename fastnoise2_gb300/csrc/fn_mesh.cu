@@ -37,8 +37,36 @@ __device__ __forceinline__ unsigned enc(float f)
     return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
-struct Vox {
+// Where a mesher reads the chunk's densities.  DenseSrc: the density array.  SparseSrc: no
+// density array -- two classification bitmasks of every density (computed where the tree is
+// evaluated) and exact values only at the voxels a pass needs them (marked in `need`, stored
+// in index order; `rank` = values stored before each 32-bit word of `need`).  NaN densities are
+// neither above nor at-or-below the iso level in both forms.
+struct DenseSrc {
     const float* d;
+    __device__ __forceinline__ bool above(int i, float iso) const { return d[i] > iso; }
+    __device__ __forceinline__ bool solid(int i, float iso) const { return d[i] <= iso; }
+    __device__ __forceinline__ float value(int i) const { return d[i]; }
+};
+
+struct SparseSrc {
+    const unsigned* gt;      // bit i: density i > iso
+    const unsigned* le;      // bit i: density i <= iso
+    const unsigned* need;    // bit i: density i is stored in vals
+    const unsigned* rank;    // per word of need: values stored before it
+    const float* vals;
+    __device__ __forceinline__ bool above(int i, float) const { return (__ldg(&gt[i >> 5]) >> (i & 31)) & 1u; }
+    __device__ __forceinline__ bool solid(int i, float) const { return (__ldg(&le[i >> 5]) >> (i & 31)) & 1u; }
+    __device__ __forceinline__ float value(int i) const
+    {
+        const unsigned w = (unsigned)i >> 5, below = (1u << (i & 31)) - 1u;
+        return vals[rank[w] + __popc(need[w] & below)];
+    }
+};
+
+template <class S>
+struct Vox {
+    S src;
     int sx, sy, sz;    // density strides of the mesher's x / y / z axes
 };
 
@@ -49,21 +77,25 @@ __device__ __forceinline__ bool early_out(const float* minmax, float iso)
 }
 
 // bit k set = face k (Right, Left, Up, Down, Forward, Back) is emitted
-__device__ __forceinline__ unsigned face_mask(const Vox& v, int i, float iso)
+template <class S>
+__device__ __forceinline__ unsigned face_mask(const Vox<S>& v, int i, float iso)
 {
-    if (!(v.d[i] <= iso)) return 0u;
+    if (!v.src.solid(i, iso)) return 0u;
     unsigned m = 0;
-    m |= (v.d[i + v.sx] > iso) ? 1u : 0u;
-    m |= (v.d[i - v.sx] > iso) ? 2u : 0u;
-    m |= (v.d[i + v.sy] > iso) ? 4u : 0u;
-    m |= (v.d[i - v.sy] > iso) ? 8u : 0u;
-    m |= (v.d[i + v.sz] > iso) ? 16u : 0u;
-    m |= (v.d[i - v.sz] > iso) ? 32u : 0u;
+    m |= v.src.above(i + v.sx, iso) ? 1u : 0u;
+    m |= v.src.above(i - v.sx, iso) ? 2u : 0u;
+    m |= v.src.above(i + v.sy, iso) ? 4u : 0u;
+    m |= v.src.above(i - v.sy, iso) ? 8u : 0u;
+    m |= v.src.above(i + v.sz, iso) ? 16u : 0u;
+    m |= v.src.above(i - v.sz, iso) ? 32u : 0u;
     return m;
 }
 
-__global__ void bloxel_count(Vox v, int size, float3 pos, float iso, const float* minmax, unsigned* counts,
-                             unsigned* airsolid)
+// Faces per voxel and the min air / max solid heights.  `need` (sparse form, else null):
+// every voxel with a face is marked, since emitting its faces reads its density.
+template <class S>
+__global__ void bloxel_count(Vox<S> v, int size, float3 pos, float iso, const float* minmax, unsigned* counts,
+                             unsigned* airsolid, unsigned* need)
 {
     const unsigned n = (unsigned)size * size * size;
     const bool skip = early_out(minmax, iso);
@@ -74,9 +106,10 @@ __global__ void bloxel_count(Vox v, int size, float3 pos, float iso, const float
         unsigned c = 0;
         if (!skip) {
             const float yf = (float)y + pos.y;
-            if (v.d[i] <= iso) {
+            if (v.src.solid(i, iso)) {
                 c = __popc(face_mask(v, i, iso));
                 solid = max(solid, enc(yf));
+                if (c && need) atomicOr(&need[i >> 5], 1u << (i & 31));
             } else {
                 air = min(air, enc(yf));
             }
@@ -193,22 +226,23 @@ struct Quad {
     float3 p00, p01, p11, p10;
 };
 
-__device__ __forceinline__ void emit_quad(const Vox& v, int i, float iso, const Quad& q, unsigned face, MeshVertex* verts,
-                                          unsigned* idx, unsigned vcap, unsigned icap)
+template <class S>
+__device__ __forceinline__ void emit_quad(const Vox<S>& v, int i, float iso, float density, const Quad& q, unsigned face,
+                                          MeshVertex* verts, unsigned* idx, unsigned vcap, unsigned icap)
 {
     const int f = i + q.facing;
-    const unsigned sa0 = v.d[f - q.oa] <= iso, sa1 = v.d[f + q.oa] <= iso;
-    const unsigned sb0 = v.d[f - q.ob] <= iso, sb1 = v.d[f + q.ob] <= iso;
-    const unsigned c00 = (sa0 & sb0) || v.d[f - q.oa - q.ob] <= iso;
-    const unsigned c01 = (sa0 & sb1) || v.d[f - q.oa + q.ob] <= iso;
-    const unsigned c10 = (sa1 & sb0) || v.d[f + q.oa - q.ob] <= iso;
-    const unsigned c11 = (sa1 & sb1) || v.d[f + q.oa + q.ob] <= iso;
+    const unsigned sa0 = v.src.solid(f - q.oa, iso), sa1 = v.src.solid(f + q.oa, iso);
+    const unsigned sb0 = v.src.solid(f - q.ob, iso), sb1 = v.src.solid(f + q.ob, iso);
+    const unsigned c00 = (sa0 & sb0) || v.src.solid(f - q.oa - q.ob, iso);
+    const unsigned c01 = (sa0 & sb1) || v.src.solid(f - q.oa + q.ob, iso);
+    const unsigned c10 = (sa1 & sb0) || v.src.solid(f + q.oa - q.ob, iso);
+    const unsigned c11 = (sa1 & sb1) || v.src.solid(f + q.oa + q.ob, iso);
     constexpr float aoAdjust = kAoStrength / 3.0f;
     const float ao00 = (float)(sa0 + sb0 + c00) * aoAdjust;
     const float ao01 = (float)(sa1 + sb0 + c10) * aoAdjust;
     const float ao10 = (float)(sa0 + sb1 + c01) * aoAdjust;
     const float ao11 = (float)(sa1 + sb1 + c11) * aoAdjust;
-    float light = q.light - (iso - v.d[i]) * 4.0f;
+    float light = q.light - (iso - density) * 4.0f;
     light = light * fabsf(light);
     light = kAmbient < light ? light : kAmbient;              // std::max(AMBIENT_LIGHT, light)
     const unsigned base = face * 4u;
@@ -230,7 +264,8 @@ __device__ __forceinline__ void emit_quad(const Vox& v, int i, float iso, const 
     }
 }
 
-__global__ void bloxel_emit(Vox v, int size, float3 pos, float iso, const float* minmax, const unsigned* offsets,
+template <class S>
+__global__ void bloxel_emit(Vox<S> v, int size, float3 pos, float iso, const float* minmax, const unsigned* offsets,
                             MeshVertex* verts, unsigned* idx, unsigned vcap, unsigned icap)
 {
     if (early_out(minmax, iso)) return;
@@ -243,18 +278,19 @@ __global__ void bloxel_emit(Vox v, int size, float3 pos, float iso, const float*
         if (!m) continue;
         const float xf = (float)x + pos.x, yf = (float)y + pos.y, zf = (float)z + pos.z;
         const float x1 = xf + 1.0f, y1 = yf + 1.0f, z1 = zf + 1.0f;
+        const float dens = v.src.value(i);
         unsigned face = offsets[t];
-        if (m & 1u) emit_quad(v, i, iso, Quad{v.sx, v.sy, v.sz, sunX + kAmbient, {x1, yf, zf}, {x1, y1, zf}, {x1, y1, z1}, {x1, yf, z1}},
+        if (m & 1u) emit_quad(v, i, iso, dens, Quad{v.sx, v.sy, v.sz, sunX + kAmbient, {x1, yf, zf}, {x1, y1, zf}, {x1, y1, z1}, {x1, yf, z1}},
                               face++, verts, idx, vcap, icap);
-        if (m & 2u) emit_quad(v, i, iso, Quad{-v.sx, -v.sy, v.sz, 1.0f - sunX, {xf, y1, zf}, {xf, yf, zf}, {xf, yf, z1}, {xf, y1, z1}},
+        if (m & 2u) emit_quad(v, i, iso, dens, Quad{-v.sx, -v.sy, v.sz, 1.0f - sunX, {xf, y1, zf}, {xf, yf, zf}, {xf, yf, z1}, {xf, y1, z1}},
                               face++, verts, idx, vcap, icap);
-        if (m & 4u) emit_quad(v, i, iso, Quad{v.sy, v.sz, v.sx, sunY + kAmbient, {xf, y1, zf}, {xf, y1, z1}, {x1, y1, z1}, {x1, y1, zf}},
+        if (m & 4u) emit_quad(v, i, iso, dens, Quad{v.sy, v.sz, v.sx, sunY + kAmbient, {xf, y1, zf}, {xf, y1, z1}, {x1, y1, z1}, {x1, y1, zf}},
                               face++, verts, idx, vcap, icap);
-        if (m & 8u) emit_quad(v, i, iso, Quad{-v.sy, -v.sz, v.sx, 1.0f - sunY, {xf, yf, z1}, {xf, yf, zf}, {x1, yf, zf}, {x1, yf, z1}},
+        if (m & 8u) emit_quad(v, i, iso, dens, Quad{-v.sy, -v.sz, v.sx, 1.0f - sunY, {xf, yf, z1}, {xf, yf, zf}, {x1, yf, zf}, {x1, yf, z1}},
                               face++, verts, idx, vcap, icap);
-        if (m & 16u) emit_quad(v, i, iso, Quad{v.sz, v.sx, v.sy, sunZ + kAmbient, {xf, yf, z1}, {x1, yf, z1}, {x1, y1, z1}, {xf, y1, z1}},
+        if (m & 16u) emit_quad(v, i, iso, dens, Quad{v.sz, v.sx, v.sy, sunZ + kAmbient, {xf, yf, z1}, {x1, yf, z1}, {x1, y1, z1}, {xf, y1, z1}},
                                face++, verts, idx, vcap, icap);
-        if (m & 32u) emit_quad(v, i, iso, Quad{-v.sz, -v.sx, v.sy, 1.0f - sunZ, {x1, yf, zf}, {xf, yf, zf}, {xf, y1, zf}, {x1, y1, zf}},
+        if (m & 32u) emit_quad(v, i, iso, dens, Quad{-v.sz, -v.sx, v.sy, 1.0f - sunZ, {x1, yf, zf}, {xf, yf, zf}, {xf, y1, zf}, {x1, y1, zf}},
                                face++, verts, idx, vcap, icap);
     }
 }
@@ -468,37 +504,40 @@ static_assert(dmc_use_slot(1) == 10 && dmc_use_off(10, 0) == 1 && dmc_use_off(10
               "quad slot tables");
 static_assert(make_dmc_table().first[1][0] == 0 && make_dmc_table().first[255 - 64][0] == 7, "first-use edges");
 
+template <class S>
 struct DmcGrid {
-    const float* d;
+    S src;                        // the densities (DenseSrc or SparseSrc)
     int sx, sy, sz;               // density strides of the mesher's x / y / z axes
     int size;                     // cells per axis
     unsigned char* cases;         // marching-cubes case of each vertex cell, (size + 1)^3, from -1
 };
 
-__device__ __forceinline__ int dmc_index(const DmcGrid& g, int x, int y, int z)
+template <class S>
+__device__ __forceinline__ int dmc_index(const DmcGrid<S>& g, int x, int y, int z)
 {
     return (x + 2) * g.sx + (y + 2) * g.sy + (z + 2) * g.sz;
 }
 
-__device__ __forceinline__ unsigned dmc_case_at(const DmcGrid& g, int x, int y, int z)
+template <class S>
+__device__ __forceinline__ unsigned dmc_case_at(const DmcGrid<S>& g, int x, int y, int z)
 {
     const unsigned s1 = (unsigned)g.size + 1u;
     return g.cases[((unsigned)(z + 1) * s1 + (unsigned)(y + 1)) * s1 + (unsigned)(x + 1)];
 }
 
 // DmcGetVertIndex's cell code (:774-790)
-__device__ __forceinline__ unsigned dmc_case(const DmcGrid& g, int i, float iso)
+template <class S>
+__device__ __forceinline__ unsigned dmc_case(const DmcGrid<S>& g, int i, float iso)
 {
-    const float* d = g.d;
     unsigned c = 0;
-    c |= d[i] > iso ? 1u : 0u;
-    c |= d[i + g.sx] > iso ? 2u : 0u;
-    c |= d[i + g.sy] > iso ? 4u : 0u;
-    c |= d[i + g.sx + g.sy] > iso ? 8u : 0u;
-    c |= d[i + g.sz] > iso ? 16u : 0u;
-    c |= d[i + g.sx + g.sz] > iso ? 32u : 0u;
-    c |= d[i + g.sy + g.sz] > iso ? 64u : 0u;
-    c |= d[i + g.sx + g.sy + g.sz] > iso ? 128u : 0u;
+    c |= g.src.above(i, iso) ? 1u : 0u;
+    c |= g.src.above(i + g.sx, iso) ? 2u : 0u;
+    c |= g.src.above(i + g.sy, iso) ? 4u : 0u;
+    c |= g.src.above(i + g.sx + g.sy, iso) ? 8u : 0u;
+    c |= g.src.above(i + g.sz, iso) ? 16u : 0u;
+    c |= g.src.above(i + g.sx + g.sz, iso) ? 32u : 0u;
+    c |= g.src.above(i + g.sy + g.sz, iso) ? 64u : 0u;
+    c |= g.src.above(i + g.sx + g.sy + g.sz, iso) ? 128u : 0u;
     return c;
 }
 
@@ -513,7 +552,8 @@ __device__ __forceinline__ int dmc_slot_offset(int a, int s, int k)
     return -((k == (a + 2) % 3 ? (s & 1) : 0) + (k == (a + 1) % 3 ? (s >> 1) & 1 : 0));
 }
 
-__device__ __forceinline__ unsigned dmc_key(const DmcGrid& g, unsigned cx, unsigned cy, unsigned cz, unsigned slot)
+template <class S>
+__device__ __forceinline__ unsigned dmc_key(const DmcGrid<S>& g, unsigned cx, unsigned cy, unsigned cz, unsigned slot)
 {
     const unsigned n = (unsigned)g.size;
     return ((cz * n + cy) * n + cx) * 12u + slot;
@@ -524,7 +564,8 @@ __device__ __forceinline__ unsigned dmc_key(const DmcGrid& g, unsigned cx, unsig
 // DmcGetVertIndex call is the one that creates the vertex in the reference's map.  Away
 // from the chunk's faces every quad around w lies in the chunk and the table knows the
 // first; next to them the quads that fall outside are skipped.
-__device__ __forceinline__ unsigned dmc_first_use(const DmcGrid& g, int wx, int wy, int wz, unsigned c, unsigned p)
+template <class S>
+__device__ __forceinline__ unsigned dmc_first_use(const DmcGrid<S>& g, int wx, int wy, int wz, unsigned c, unsigned p)
 {
     const unsigned n = (unsigned)g.size;
     if ((unsigned)wx < n - 1u && (unsigned)wy < n - 1u && (unsigned)wz < n - 1u) {
@@ -552,7 +593,8 @@ struct DmcRef {
     unsigned c, p;
 };
 
-__device__ __forceinline__ DmcRef dmc_ref(const DmcGrid& g, int x, int y, int z, int a, int s)
+template <class S>
+__device__ __forceinline__ DmcRef dmc_ref(const DmcGrid<S>& g, int x, int y, int z, int a, int s)
 {
     DmcRef r;
     r.wx = x + dmc_slot_offset(a, s, 0);
@@ -565,11 +607,14 @@ __device__ __forceinline__ DmcRef dmc_ref(const DmcGrid& g, int x, int y, int z,
 }
 
 // mean of the piece's edge crossings, relative to the cell's base corner (:810-890)
-__device__ __forceinline__ float3 dmc_point(const DmcGrid& g, int i, unsigned code, float iso)
+template <class S>
+__device__ __forceinline__ float3 dmc_point(const DmcGrid<S>& g, int i, unsigned code, float iso)
 {
-    const float* d = g.d;
     const int X = g.sx, Y = g.sy, Z = g.sz;
-    auto t = [&](int a, int b) { return (iso - d[a]) / (d[b] - d[a]); };
+    auto t = [&](int a, int b) {
+        const float da = g.src.value(a);
+        return (iso - da) / (g.src.value(b) - da);
+    };
     float x = 0.0f, y = 0.0f, z = 0.0f;
     if (code & 1u) x += t(i, i + X);
     if (code & 2u) { x += 1.0f; z += t(i + X, i + X + Z); }
@@ -612,9 +657,10 @@ __device__ __forceinline__ float dmc_offset(int pos, int cell, int vcell)
 __device__ __forceinline__ float lerp_(float a, float b, float t) { return a + (b - a) * t; }   // ImLerp
 
 // the vertex light: trilinear central-difference gradient at the point (:902-948)
-__device__ __forceinline__ float dmc_light(const DmcGrid& g, int i, float3 v, float3 nl)
+template <class S>
+__device__ __forceinline__ float dmc_light(const DmcGrid<S>& g, int i, float3 v, float3 nl)
 {
-    const float* d = g.d;
+    auto d = [&](int k) { return g.src.value(k); };
     const int X = g.sx, Y = g.sy, Z = g.sz;
     // STEP & (int)lroundf(-v): v lies in [0, 1], so lroundf gives -1 (offset one step) or 0
     const int ox = lroundf(-v.x) == -1 ? X : 0, oy = lroundf(-v.y) == -1 ? Y : 0, oz = lroundf(-v.z) == -1 ? Z : 0;
@@ -633,15 +679,15 @@ __device__ __forceinline__ float dmc_light(const DmcGrid& g, int i, float3 v, fl
                 const float cx = fabsf((float)x + v.x);
                 if (x) {
                     const int k = cur + ox;
-                    der.x += cy * cz * lerp_(d[k - X] - d[k], d[k] - d[k + X], dd.x);
+                    der.x += cy * cz * lerp_(d(k - X) - d(k), d(k) - d(k + X), dd.x);
                 }
                 if (y) {
                     const int k = cur + oy;
-                    der.y += cx * cz * lerp_(d[k - Y] - d[k], d[k] - d[k + Y], dd.y);
+                    der.y += cx * cz * lerp_(d(k - Y) - d(k), d(k) - d(k + Y), dd.y);
                 }
                 if (z) {
                     const int k = cur + oz;
-                    der.z += cx * cy * lerp_(d[k - Z] - d[k], d[k] - d[k + Z], dd.z);
+                    der.z += cx * cy * lerp_(d(k - Z) - d(k), d(k) - d(k + Z), dd.z);
                 }
                 cur += X;
             }
@@ -690,7 +736,8 @@ __device__ __forceinline__ unsigned warp_append(unsigned* counter, unsigned n)
 
 // Case pass: the marching-cubes case of every vertex cell (-1 .. size-1 per axis); for the
 // chunk's own cells also their quads (one per cut axis): tile sums and work items.
-__global__ void dmc_cases(DmcGrid g, float iso, const float* minmax, unsigned* masks, DmcLists lists)
+template <class S>
+__global__ void dmc_cases(DmcGrid<S> g, float iso, const float* minmax, unsigned* masks, DmcLists lists)
 {
     if (early_out(minmax, iso)) return;
     const unsigned s1 = (unsigned)g.size + 1u, n = s1 * s1 * s1, lane = threadIdx.x & 31u;
@@ -716,7 +763,8 @@ __global__ void dmc_cases(DmcGrid g, float iso, const float* minmax, unsigned* m
 
 // Count pass: one thread per quad; each of its 4 references that is the vertex's first
 // use creates the vertex (bit axis * 4 + slot of the cell's mask) and becomes a vertex item.
-__global__ void dmc_count(DmcGrid g, unsigned* masks, DmcLists lists)
+template <class S>
+__global__ void dmc_count(DmcGrid<S> g, unsigned* masks, DmcLists lists)
 {
     const unsigned items = lists.counters[1];
     unsigned* vert_sums = &lists.tile_sums[0].x;
@@ -761,7 +809,8 @@ __global__ void __launch_bounds__(kScanBlock) dmc_scan_tiles(uint2* tile_sums, u
 // Cell offsets within each tile that holds quads (256 threads x 8 cells, staged through
 // shared memory so that global loads and stores stay coalesced).  A cell's counts come from
 // its case (one quad per cut axis) and its mask (the vertices it creates).
-__global__ void __launch_bounds__(256) dmc_scan_cells(DmcGrid g, const unsigned* masks, uint2* offsets, const uint2* tile_offsets,
+template <class S>
+__global__ void __launch_bounds__(256) dmc_scan_cells(DmcGrid<S> g, const unsigned* masks, uint2* offsets, const uint2* tile_offsets,
                                                       const uint2* total)
 {
     __shared__ uint2 tile[kDmcTile];
@@ -799,7 +848,8 @@ __global__ void __launch_bounds__(256) dmc_scan_cells(DmcGrid g, const unsigned*
 }
 
 // Vertex pass: one thread per created vertex, written at its cell's scanned offset.
-__global__ void dmc_vertices(DmcGrid g, int3 pos, float iso, const unsigned* masks, const uint2* offsets, const uint2* total,
+template <class S>
+__global__ void dmc_vertices(DmcGrid<S> g, int3 pos, float iso, const unsigned* masks, const uint2* offsets, const uint2* total,
                              DmcLists lists, MeshVertex* verts, unsigned vcap)
 {
     __shared__ float3 s_nl;
@@ -826,7 +876,8 @@ __global__ void dmc_vertices(DmcGrid g, int3 pos, float iso, const unsigned* mas
 // Quad pass: one thread per cut edge, 6 indices (:662-674) with the vertex indices found
 // through each vertex's first use; the y-edge quads also give the min air / max solid
 // heights (:706-724).
-__global__ void dmc_quads(DmcGrid g, int3 pos, float iso, const unsigned* masks, const uint2* offsets, const uint2* total,
+template <class S>
+__global__ void dmc_quads(DmcGrid<S> g, int3 pos, float iso, const unsigned* masks, const uint2* offsets, const uint2* total,
                           DmcLists lists, const MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap, unsigned* airsolid)
 {
     const uint2 tot = *total;
@@ -882,6 +933,61 @@ __global__ void dmc_quads(DmcGrid g, int3 pos, float iso, const unsigned* masks,
     }
 }
 
+// ---- the sparse density form: which densities a pass reads, and where their values land
+
+// Set bits [start, start + len) of `need`, clipped to the chunk's n densities.
+__device__ __forceinline__ void mark_run(unsigned* need, int start, int len, unsigned n)
+{
+    int a = start < 0 ? 0 : start;
+    const int b = start + len < (int)n ? start + len : (int)n;
+    while (a < b) {
+        const int lo = a & 31, cnt = min(b - a, 32 - lo);
+        const unsigned mask = (cnt == 32 ? 0xFFFFFFFFu : ((1u << cnt) - 1u)) << lo;
+        atomicOr(&need[a >> 5], mask);
+        a += cnt;
+    }
+}
+
+// The densities the vertex and quad passes read around each created vertex's cell (base
+// corner index i): its corners (dmc_point) and dmc_light's central differences at them,
+// which the vertex position may shift one step up each axis -- i + [-1, 3] along the
+// differentiated axis and i + [0, 2] along the other two, with the passes' own index
+// arithmetic.
+template <class S>
+__global__ void dmc_mark_needed(DmcGrid<S> g, DmcLists lists, unsigned* need, unsigned n_dens)
+{
+    const unsigned items = lists.counters[0];
+    for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < items; j += gridDim.x * blockDim.x) {
+        const unsigned it = lists.vert_items[j];
+        const unsigned t = it >> 4, bit = it & 15u;
+        const int a = (int)(bit >> 2), s = (int)(bit & 3u);
+        const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
+        const DmcRef r = dmc_ref(g, x, y, z, a, s);
+        const int wi = dmc_index(g, r.wx, r.wy, r.wz);
+        for (int dz = -1; dz <= 3; ++dz)
+            for (int dy = -1; dy <= 3; ++dy) {
+                const bool iny = dy >= 0 && dy <= 2, inz = dz >= 0 && dz <= 2;
+                if (!iny && !inz) continue;
+                const int lo = iny && inz ? -1 : 0, hi = iny && inz ? 3 : 2;
+                mark_run(need, wi + dy * g.sy + dz * g.sz + lo, hi - lo + 1, n_dens);
+            }
+    }
+}
+
+__global__ void need_counts(const unsigned* need, unsigned* counts, unsigned nwords)
+{
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) counts[w] = __popc(need[w]);
+}
+
+// The marked density indices in ascending order: word w's go to idx[rank[w] ..].
+__global__ void need_compact(const unsigned* need, const unsigned* rank, unsigned nwords, unsigned* idx)
+{
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        unsigned o = rank[w];
+        for (unsigned m = need[w]; m; m &= m - 1u) idx[o++] = w * 32u + (unsigned)(__ffs(m) - 1);
+    }
+}
+
 // Grid-stride launches: one thread per element up to 8 waves of 256-thread blocks per SM.
 int grid_for(unsigned n, int block)
 {
@@ -902,16 +1008,63 @@ cudaError_t launch_bloxel(const float* dens, int size, bool up_axis_z, float px,
                           MeshScratch& s, MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap, cudaStream_t stream)
 {
     const int sg = size + 2;
-    Vox v{dens, 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg};
+    Vox<DenseSrc> v{DenseSrc{dens}, 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg};
     const unsigned n = (unsigned)size * size * size;
     cudaError_t e = cudaMemsetAsync(s.airsolid, 0, 2 * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(s.airsolid, 0xFF, sizeof(unsigned), stream);           // min air starts at "none"
     if (e != cudaSuccess) return e;
     const float3 pos = make_float3(px, py, pz);
-    bloxel_count<<<grid_for(n, 256), 256, 0, stream>>>(v, size, pos, iso, dminmax, s.counts, s.airsolid);
+    bloxel_count<<<grid_for(n, 256), 256, 0, stream>>>(v, size, pos, iso, dminmax, s.counts, s.airsolid, nullptr);
     exclusive_scan<unsigned>(s.counts, s.offsets, s.block_totals, s.total, n, stream);
     bloxel_emit<<<grid_for(n, 256), 256, 0, stream>>>(v, size, pos, iso, dminmax, s.offsets, verts, idx, vcap, icap);
+    return cudaGetLastError();
+}
+
+namespace {
+
+SparseSrc sparse_src(const SparseScratch& sp)
+{
+    return SparseSrc{sp.above, sp.solid, sp.need, sp.rank, sp.vals};
+}
+
+// The marked densities' ranks and their index list (total in sp.total).
+void need_list(SparseScratch& sp, unsigned n_dens, cudaStream_t stream)
+{
+    const unsigned nwords = (n_dens + 31u) / 32u;
+    need_counts<<<grid_for(nwords, 256), 256, 0, stream>>>(sp.need, sp.counts, nwords);
+    exclusive_scan<unsigned>(sp.counts, sp.rank, sp.block_totals, sp.total, nwords, stream);
+    need_compact<<<grid_for(nwords, 256), 256, 0, stream>>>(sp.need, sp.rank, nwords, sp.idx);
+}
+
+}  // namespace
+
+cudaError_t launch_bloxel_sparse_prepare(SparseScratch& sp, int size, bool up_axis_z, float px, float py, float pz, float iso,
+                                         const float* dminmax, MeshScratch& s, cudaStream_t stream)
+{
+    const int sg = size + 2;
+    const unsigned n_dens = (unsigned)sg * sg * sg;
+    Vox<SparseSrc> v{sparse_src(sp), 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg};
+    const unsigned n = (unsigned)size * size * size;
+    cudaError_t e = cudaMemsetAsync(s.airsolid, 0, 2 * sizeof(unsigned), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.airsolid, 0xFF, sizeof(unsigned), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sp.need, 0, ((n_dens + 31u) / 32u) * sizeof(unsigned), stream);
+    if (e != cudaSuccess) return e;
+    bloxel_count<<<grid_for(n, 256), 256, 0, stream>>>(v, size, make_float3(px, py, pz), iso, dminmax, s.counts, s.airsolid, sp.need);
+    exclusive_scan<unsigned>(s.counts, s.offsets, s.block_totals, s.total, n, stream);
+    need_list(sp, n_dens, stream);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bloxel_sparse_emit(const SparseScratch& sp, int size, bool up_axis_z, float px, float py, float pz, float iso,
+                                      const float* dminmax, MeshScratch& s, MeshVertex* verts, unsigned vcap, unsigned* idx,
+                                      unsigned icap, cudaStream_t stream)
+{
+    const int sg = size + 2;
+    Vox<SparseSrc> v{sparse_src(sp), 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg};
+    const unsigned n = (unsigned)size * size * size;
+    bloxel_emit<<<grid_for(n, 256), 256, 0, stream>>>(v, size, make_float3(px, py, pz), iso, dminmax, s.offsets, verts, idx, vcap,
+                                                      icap);
     return cudaGetLastError();
 }
 
@@ -927,7 +1080,7 @@ cudaError_t launch_dmc(const float* dens, int size, bool up_axis_z, int px, int 
                        DmcScratch& s, MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap, cudaStream_t stream)
 {
     const int sg = size + 4;
-    const DmcGrid g{dens, 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg, size, s.cases};
+    const DmcGrid<DenseSrc> g{DenseSrc{dens}, 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg, size, s.cases};
     const DmcLists lists{s.vert_items, s.quad_items, s.counters, s.tile_sums};
     const unsigned n = (unsigned)size * size * size, s1 = (unsigned)size + 1u;
     const unsigned tiles = (n + kDmcTile - 1) / kDmcTile;
@@ -946,6 +1099,45 @@ cudaError_t launch_dmc(const float* dens, int size, bool up_axis_z, int px, int 
     dmc_count<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, s.masks, lists);
     dmc_scan_tiles<<<1, kScanBlock, 0, stream>>>(s.tile_sums, tiles, s.total);
     dmc_scan_cells<<<tiles, 256, 0, stream>>>(g, s.masks, s.offsets, s.tile_sums, s.total);
+    dmc_vertices<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, pos, iso, s.masks, s.offsets, s.total, lists, verts, vcap);
+    dmc_quads<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, pos, iso, s.masks, s.offsets, s.total, lists, verts, vcap, idx, icap,
+                                                        s.airsolid);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dmc_sparse_prepare(SparseScratch& sp, int size, bool up_axis_z, float iso, const float* dminmax, DmcScratch& s,
+                                      cudaStream_t stream)
+{
+    const int sg = size + 4;
+    const unsigned n_dens = (unsigned)sg * sg * sg;
+    const DmcGrid<SparseSrc> g{sparse_src(sp), 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg, size, s.cases};
+    const DmcLists lists{s.vert_items, s.quad_items, s.counters, s.tile_sums};
+    const unsigned n = (unsigned)size * size * size, s1 = (unsigned)size + 1u;
+    const unsigned tiles = (n + kDmcTile - 1) / kDmcTile;
+    cudaError_t e = cudaMemsetAsync(s.airsolid, 0, 2 * sizeof(unsigned), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.airsolid, 0xFF, sizeof(unsigned), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.counters, 0, 2 * sizeof(unsigned), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.tile_sums, 0, tiles * sizeof(uint2), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sp.need, 0, ((n_dens + 31u) / 32u) * sizeof(unsigned), stream);
+    if (e != cudaSuccess) return e;
+    dmc_cases<<<grid_for(s1 * s1 * s1, 256), 256, 0, stream>>>(g, iso, dminmax, s.masks, lists);
+    dmc_count<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, s.masks, lists);
+    dmc_scan_tiles<<<1, kScanBlock, 0, stream>>>(s.tile_sums, tiles, s.total);
+    dmc_scan_cells<<<tiles, 256, 0, stream>>>(g, s.masks, s.offsets, s.tile_sums, s.total);
+    dmc_mark_needed<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, lists, sp.need, n_dens);
+    need_list(sp, n_dens, stream);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_dmc_sparse_finish(const SparseScratch& sp, int size, bool up_axis_z, int px, int py, int pz, float iso,
+                                     DmcScratch& s, MeshVertex* verts, unsigned vcap, unsigned* idx, unsigned icap,
+                                     cudaStream_t stream)
+{
+    const int sg = size + 4;
+    const DmcGrid<SparseSrc> g{sparse_src(sp), 1, up_axis_z ? sg * sg : sg, up_axis_z ? sg : sg * sg, size, s.cases};
+    const DmcLists lists{s.vert_items, s.quad_items, s.counters, s.tile_sums};
+    const unsigned n = (unsigned)size * size * size;
+    const int3 pos = make_int3(px, py, pz);
     dmc_vertices<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, pos, iso, s.masks, s.offsets, s.total, lists, verts, vcap);
     dmc_quads<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, pos, iso, s.masks, s.offsets, s.total, lists, verts, vcap, idx, icap,
                                                         s.airsolid);

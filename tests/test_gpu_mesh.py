@@ -1,6 +1,9 @@
-"""Chunk meshing on the GPU (fnBuildChunkMeshBloxel / fnBuildChunkMeshHeightmap)
-against the CPU restatement of the Node Editor's meshers (oracle/mesh.py): the
-same vertices, indices, heights and OutputMinMax, bit for bit."""
+"""Chunk meshing on the GPU (fnBuildChunkMeshBloxel / Dmc / Heightmap) against the CPU
+restatement of the Node Editor's meshers (oracle/mesh.py): the same vertices, indices, heights
+and OutputMinMax, bit for bit.  Each 3D case runs on both kernel tiers: the interpreter, which
+writes the chunk's density array, and the tree's specialised kernels, with which the meshers
+work from the sparse form (the densities' classification bitmasks, and values evaluated again
+only at the voxels the light and vertex passes read)."""
 import numpy as np
 import pytest
 
@@ -29,8 +32,18 @@ def caves_tree():
     return N("CellularDistance", Feature_Scale=9.0, Return_Type="Index0Sub1")
 
 
-def run_bloxel(fn, torch, root, size, pos, seed, iso, up_z, vcap=None, icap=None):
+TIERS = ["interpreter", "specialised"]
+
+
+def product_node(fn, root, tier):
     node = trees.to_product(root)
+    if tier == "specialised":
+        fn.jit_compile([(node, 3)])
+    return node
+
+
+def run_bloxel(fn, torch, root, size, pos, seed, iso, up_z, vcap=None, icap=None, tier="interpreter"):
+    node = product_node(fn, root, tier)
     vcap = vcap if vcap is not None else size ** 3 * 24
     icap = icap if icap is not None else size ** 3 * 36
     v = torch.zeros(max(vcap, 1) * 4, dtype=torch.float32, device="cuda")
@@ -50,9 +63,10 @@ def oracle_bloxel(root, size, pos, seed, iso, up_z):
     (surface_tree, 16, (16, -16, 0), 42, 0.0, True),
     (caves_tree, 12, (-12, 24, 36), -5, -0.8, False),
 ])
-def test_bloxel_matches_oracle(gpu, torch_cuda, case):
+@pytest.mark.parametrize("tier", TIERS)
+def test_bloxel_matches_oracle(gpu, torch_cuda, case, tier):
     make, size, pos, seed, iso, up_z = case
-    res, gv, gi = run_bloxel(gpu, torch_cuda, make(), size, pos, seed, iso, up_z)
+    res, gv, gi = run_bloxel(gpu, torch_cuda, make(), size, pos, seed, iso, up_z, tier=tier)
     ov, oi, oair, osolid, omm = oracle_bloxel(make(), size, pos, seed, iso, up_z)
     assert res["fits"] and res["vertexCount"] == len(ov) and res["indexCount"] == len(oi) > 0
     assert np.array_equal(gv[:len(ov)].view(np.uint32), ov.view(np.uint32))
@@ -61,10 +75,11 @@ def test_bloxel_matches_oracle(gpu, torch_cuda, case):
     assert res["minMax"] == (float(omm[0]), float(omm[1]))
 
 
+@pytest.mark.parametrize("tier", TIERS)
 @pytest.mark.parametrize("value, expect", [(1.0, "air"), (-1.0, "solid")])
-def test_bloxel_early_out(gpu, torch_cuda, value, expect):
+def test_bloxel_early_out(gpu, torch_cuda, value, expect, tier):
     """OutputMinMax entirely above / below the iso level: no faces, only the height."""
-    res, _, _ = run_bloxel(gpu, torch_cuda, N("Constant", Value=value), 16, (0, 32, 0), 1, 0.0, False)
+    res, _, _ = run_bloxel(gpu, torch_cuda, N("Constant", Value=value), 16, (0, 32, 0), 1, 0.0, False, tier=tier)
     assert res["vertexCount"] == 0 and res["indexCount"] == 0
     if expect == "air":
         assert res["minAirY"] == 32.0 and res["maxSolidY"] == float("-inf")
@@ -72,8 +87,9 @@ def test_bloxel_early_out(gpu, torch_cuda, value, expect):
         assert res["maxSolidY"] == 32.0 - 1.0 + 16 and res["minAirY"] == float("inf")
 
 
-def test_bloxel_reports_capacity(gpu, torch_cuda):
-    res, _, _ = run_bloxel(gpu, torch_cuda, surface_tree(), 16, (32, -8, 16), 1337, 0.0, False, vcap=8, icap=12)
+@pytest.mark.parametrize("tier", TIERS)
+def test_bloxel_reports_capacity(gpu, torch_cuda, tier):
+    res, _, _ = run_bloxel(gpu, torch_cuda, surface_tree(), 16, (32, -8, 16), 1337, 0.0, False, vcap=8, icap=12, tier=tier)
     ov, oi, _, _, _ = oracle_bloxel(surface_tree(), 16, (32, -8, 16), 1337, 0.0, False)
     assert not res["fits"] and res["vertexCount"] == len(ov) and res["indexCount"] == len(oi)
 
@@ -99,8 +115,8 @@ def white_tree():
     return N("White", Seed_Offset=5)
 
 
-def run_dmc(fn, torch, root, size, pos, seed, iso, up_z, vcap=None, icap=None):
-    node = trees.to_product(root)
+def run_dmc(fn, torch, root, size, pos, seed, iso, up_z, vcap=None, icap=None, tier="interpreter"):
+    node = product_node(fn, root, tier)
     vcap = vcap if vcap is not None else (size + 1) ** 3 * 4
     icap = icap if icap is not None else size ** 3 * 18
     v = torch.zeros(max(vcap, 1) * 4, dtype=torch.float32, device="cuda")
@@ -122,9 +138,10 @@ def oracle_dmc(root, size, pos, seed, iso, up_z):
     (white_tree, 10, (100, -3, 7), 99, 0.0, False),
     (white_tree, 9, (0, 0, 0), -1234, 0.3, True),
 ])
-def test_dmc_matches_oracle(gpu, torch_cuda, case):
+@pytest.mark.parametrize("tier", TIERS)
+def test_dmc_matches_oracle(gpu, torch_cuda, case, tier):
     make, size, pos, seed, iso, up_z = case
-    res, gv, gi = run_dmc(gpu, torch_cuda, make(), size, pos, seed, iso, up_z)
+    res, gv, gi = run_dmc(gpu, torch_cuda, make(), size, pos, seed, iso, up_z, tier=tier)
     ov, oi, oair, osolid, omm = oracle_dmc(make(), size, pos, seed, iso, up_z)
     assert res["fits"] and res["vertexCount"] == len(ov) and res["indexCount"] == len(oi) > 0
     assert np.array_equal(gv[:len(ov)].view(np.uint32), ov.view(np.uint32))
@@ -133,9 +150,10 @@ def test_dmc_matches_oracle(gpu, torch_cuda, case):
     assert res["minMax"] == (float(omm[0]), float(omm[1]))
 
 
+@pytest.mark.parametrize("tier", TIERS)
 @pytest.mark.parametrize("value, expect", [(1.0, "air"), (-1.0, "solid")])
-def test_dmc_early_out(gpu, torch_cuda, value, expect):
-    res, _, _ = run_dmc(gpu, torch_cuda, N("Constant", Value=value), 16, (0, 32, 0), 1, 0.0, False)
+def test_dmc_early_out(gpu, torch_cuda, value, expect, tier):
+    res, _, _ = run_dmc(gpu, torch_cuda, N("Constant", Value=value), 16, (0, 32, 0), 1, 0.0, False, tier=tier)
     assert res["vertexCount"] == 0 and res["indexCount"] == 0
     if expect == "air":
         assert res["minAirY"] == 32.0 and res["maxSolidY"] == float("-inf")
@@ -143,21 +161,23 @@ def test_dmc_early_out(gpu, torch_cuda, value, expect):
         assert res["maxSolidY"] == 32.0 - 1.0 + 16 and res["minAirY"] == float("inf")
 
 
-def test_dmc_reports_capacity(gpu, torch_cuda):
-    res, _, _ = run_dmc(gpu, torch_cuda, surface_tree(), 16, (32, -8, 16), 1337, 0.0, False, vcap=8, icap=12)
+@pytest.mark.parametrize("tier", TIERS)
+def test_dmc_reports_capacity(gpu, torch_cuda, tier):
+    res, _, _ = run_dmc(gpu, torch_cuda, surface_tree(), 16, (32, -8, 16), 1337, 0.0, False, vcap=8, icap=12, tier=tier)
     ov, oi, oair, osolid, _ = oracle_dmc(surface_tree(), 16, (32, -8, 16), 1337, 0.0, False)
     assert not res["fits"] and res["vertexCount"] == len(ov) and res["indexCount"] == len(oi)
     assert (res["minAirY"], res["maxSolidY"]) == (float(oair), float(osolid))
 
 
+@pytest.mark.parametrize("tier", TIERS)
 @pytest.mark.parametrize("kind", ["dmc", "bloxel"])
-def test_many_chunks_match_single_calls(gpu, torch_cuda, kind):
+def test_many_chunks_match_single_calls(gpu, torch_cuda, kind, tier):
     """fnBuildChunkMeshes*: chunks spread over internal streams give each chunk exactly the
     single-call mesh; a chunk with too small buffers reports its counts, the others complete."""
     fn, torch = gpu, torch_cuda
     size = 16
     positions = [(16 * k - 40, -8 + 4 * (k % 3), 16 * (k % 2)) for k in range(7)]
-    node = trees.to_product(surface_tree())
+    node = product_node(fn, surface_tree(), tier)
     vcap, icap = (size + 1) ** 3 * 4, size ** 3 * 18
     single = {"dmc": fn.build_chunk_mesh_dmc, "bloxel": fn.build_chunk_mesh_bloxel}[kind]
     bufs, tensors = [], []
@@ -182,3 +202,25 @@ def test_many_chunks_match_single_calls(gpu, torch_cuda, kind):
         v, i = tensors[k]
         assert torch.equal(v[:nv * 4].view(torch.int32), v1[:nv * 4].view(torch.int32)), k
         assert torch.equal(i[:ni], i1[:ni]), k
+
+
+@pytest.mark.parametrize("kind", ["dmc", "bloxel"])
+def test_sparse_form_equals_density_array_on_editor_chunks(gpu, torch_cuda, kind):
+    """The Node Editor's chunk size (128^3) on a terrain surface: the mesh from the sparse form
+    (specialised kernels) equals the mesh from the density array (interpreter) bit for bit."""
+    fn, torch = gpu, torch_cuda
+    root = N("Add", LHS=N("FractalFBm", Source=N("Simplex", Feature_Scale=60.0), Octaves=4),
+             RHS=N("Gradient").set("Multiplier", 0.02, 1))
+    run = run_dmc if kind == "dmc" else run_bloxel
+    size, vcap, icap = 128, 1 << 20, 3 << 20
+    got = run(fn, torch, root, size, (-64, -64, 128), 1337, 0.0, False, vcap=vcap, icap=icap, tier="specialised")
+    fn.set_jit_enabled(False)
+    try:
+        ref = run(fn, torch, root, size, (-64, -64, 128), 1337, 0.0, False, vcap=vcap, icap=icap, tier="interpreter")
+    finally:
+        fn.set_jit_enabled(True)
+    (r1, v1, i1), (r2, v2, i2) = got, ref
+    assert r1 == r2 and r1["fits"] and r1["indexCount"] > 10000
+    nv, ni = r1["vertexCount"], r1["indexCount"]
+    assert np.array_equal(v1[:nv].view(np.uint32), v2[:nv].view(np.uint32))
+    assert np.array_equal(i1[:ni], i2[:ni])
