@@ -36,7 +36,7 @@ struct MeshCtx {
         if (dminmax) cudaFree(dminmax);
         if (scratch.counts) cudaFree(scratch.counts);
         if (dmc.offsets) cudaFree(dmc.offsets);
-        if (sp.above) cudaFree(sp.above);
+        if (sp.stored) cudaFree(sp.stored);
         if (host) cudaFreeHost(host);
     }
 
@@ -46,23 +46,27 @@ struct MeshCtx {
     bool reserve_sparse(size_t densities)
     {
         if (densities <= sp.cap_densities) return true;
-        if (sp.above) cudaFree(sp.above);
+        if (sp.stored) cudaFree(sp.stored);
         sp = SparseScratch();
         const size_t words = (densities + 31) / 32, nb = (words + 1023) / 1024;
         char* block = nullptr;
-        if (!cuda_ok(cudaMalloc(&block, (5 * words + nb + 1 + densities) * sizeof(unsigned) + densities * sizeof(float)),
+        // stored (uint2) | above | solid | need | cells | counts | rank | block totals | total | idx | vals
+        const size_t uwords = 6 * words + nb + 1 + densities;
+        if (!cuda_ok(cudaMalloc(&block, words * sizeof(uint2) + uwords * sizeof(unsigned) + densities * sizeof(float)),
                      "cudaMalloc(mesh sparse densities)"))
             return false;
-        unsigned* w = reinterpret_cast<unsigned*>(block);
+        sp.stored = reinterpret_cast<uint2*>(block);
+        unsigned* w = reinterpret_cast<unsigned*>(block + words * sizeof(uint2));
         sp.above = w;
         sp.solid = w + words;
         sp.need = w + 2 * words;
-        sp.counts = w + 3 * words;
-        sp.rank = w + 4 * words;
-        sp.block_totals = w + 5 * words;
-        sp.total = w + 5 * words + nb;
-        sp.idx = w + 5 * words + nb + 1;
-        sp.vals = reinterpret_cast<float*>(w + 5 * words + nb + 1 + densities);
+        sp.cells = w + 3 * words;
+        sp.counts = w + 4 * words;
+        sp.rank = w + 5 * words;
+        sp.block_totals = w + 6 * words;
+        sp.total = w + 6 * words + nb;
+        sp.idx = w + 6 * words + nb + 1;
+        sp.vals = reinterpret_cast<float*>(w + 6 * words + nb + 1 + densities);
         sp.cap_densities = densities;
         return true;
     }

@@ -52,15 +52,14 @@ struct DenseSrc {
 struct SparseSrc {
     const unsigned* gt;      // bit i: density i > iso
     const unsigned* le;      // bit i: density i <= iso
-    const unsigned* need;    // bit i: density i is stored in vals
-    const unsigned* rank;    // per word of need: values stored before it
+    const uint2* stored;     // per 32 densities: (values stored before them, bit k: density 32w + k is stored)
     const float* vals;
     __device__ __forceinline__ bool above(int i, float) const { return (__ldg(&gt[i >> 5]) >> (i & 31)) & 1u; }
     __device__ __forceinline__ bool solid(int i, float) const { return (__ldg(&le[i >> 5]) >> (i & 31)) & 1u; }
     __device__ __forceinline__ float value(int i) const
     {
-        const unsigned w = (unsigned)i >> 5, below = (1u << (i & 31)) - 1u;
-        return vals[rank[w] + __popc(need[w] & below)];
+        const uint2 w = stored[(unsigned)i >> 5];
+        return vals[w.x + __popc(w.y & ((1u << (i & 31)) - 1u))];
     }
 };
 
@@ -900,9 +899,11 @@ __global__ void dmc_quads(DmcGrid<S> g, int3 pos, float iso, const unsigned* mas
             const unsigned c = first / 12u, bit = first - c * 12u;
             q[s] = offsets[c].x + __popc(masks[c] & ((1u << bit) - 1u));
             if (a == 1) {                       // the stored vertex's y: offset of the quad that created it
+                // the vertex pass wrote exactly this value when the buffers fit
                 const int cy = (int)((c / (unsigned)g.size) % (unsigned)g.size);
-                const float vy = dmc_point(g, dmc_index(g, r.wx, r.wy, r.wz), __ldg(&kDmc.code[r.c][r.p]), iso).y +
-                                 dmc_offset(pos.y, cy, r.wy);
+                const float vy = fits ? verts[q[s]].y
+                                      : dmc_point(g, dmc_index(g, r.wx, r.wy, r.wz), __ldg(&kDmc.code[r.c][r.p]), iso).y +
+                                            dmc_offset(pos.y, cy, r.wy);
                 if (inside) solid = max(solid, enc(vy));
                 else air = min(air, enc(vy));
             }
@@ -948,29 +949,58 @@ __device__ __forceinline__ void mark_run(unsigned* need, int start, int len, uns
     }
 }
 
-// The densities the vertex and quad passes read around each created vertex's cell (base
-// corner index i): its corners (dmc_point) and dmc_light's central differences at them,
-// which the vertex position may shift one step up each axis -- i + [-1, 3] along the
-// differentiated axis and i + [0, 2] along the other two, with the passes' own index
-// arithmetic.
+// The density index of every created vertex's cell (its base corner) -- marked in `cells`;
+// need_dilate then adds the densities the vertex and quad passes read around them.
 template <class S>
-__global__ void dmc_mark_needed(DmcGrid<S> g, DmcLists lists, unsigned* need, unsigned n_dens)
+__global__ void dmc_mark_cells(DmcGrid<S> g, DmcLists lists, unsigned* cells)
 {
     const unsigned items = lists.counters[0];
     for (unsigned j = blockIdx.x * blockDim.x + threadIdx.x; j < items; j += gridDim.x * blockDim.x) {
         const unsigned it = lists.vert_items[j];
         const unsigned t = it >> 4, bit = it & 15u;
-        const int a = (int)(bit >> 2), s = (int)(bit & 3u);
         const int x = t % g.size, y = (t / g.size) % g.size, z = t / ((unsigned)g.size * g.size);
-        const DmcRef r = dmc_ref(g, x, y, z, a, s);
+        const DmcRef r = dmc_ref(g, x, y, z, (int)(bit >> 2), (int)(bit & 3u));
         const int wi = dmc_index(g, r.wx, r.wy, r.wz);
+        atomicOr(&cells[wi >> 5], 1u << (wi & 31));
+    }
+}
+
+// 64 bits of a bit array starting at bit b (bits outside [0, 32 nwords) read as 0).
+__device__ __forceinline__ unsigned long long bits64(const unsigned* a, long long b, unsigned nwords)
+{
+    const long long w = b >> 5;                       // floor
+    const unsigned sh = (unsigned)(b & 31);
+    unsigned v[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) v[k] = (w + k >= 0 && w + k < (long long)nwords) ? __ldg(&a[w + k]) : 0u;
+    const unsigned long long lo = (unsigned long long)v[0] | ((unsigned long long)v[1] << 32);
+    return sh ? (lo >> sh) | ((unsigned long long)v[2] << (64 - sh)) : lo;
+}
+
+// The densities dmc_point and dmc_light read around a vertex cell with base corner i: the
+// corners, and the central differences at them, which the vertex position may shift one step
+// up each axis -- i + [-1, 3] along the differentiated axis and i + [0, 2] along the other
+// two (offsets in the passes' own index arithmetic).  need = cells dilated by that stencil,
+// 32 densities per thread: for each stencil row (dy, dz) and its x range [lo, hi],
+// need bit j |= cells bit (32w + j - dx - dy sy - dz sz) for dx in [lo, hi].  Also the set bits
+// per word, for the scan.
+__global__ void need_dilate(const unsigned* cells, unsigned* need, unsigned* counts, unsigned n_dens, int sy, int sz)
+{
+    const unsigned nwords = (n_dens + 31u) / 32u;
+    for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        unsigned out = 0;
         for (int dz = -1; dz <= 3; ++dz)
             for (int dy = -1; dy <= 3; ++dy) {
                 const bool iny = dy >= 0 && dy <= 2, inz = dz >= 0 && dz <= 2;
                 if (!iny && !inz) continue;
                 const int lo = iny && inz ? -1 : 0, hi = iny && inz ? 3 : 2;
-                mark_run(need, wi + dy * g.sy + dz * g.sz + lo, hi - lo + 1, n_dens);
+                const long long b = 32ll * w - (long long)dy * sy - (long long)dz * sz - hi;
+                const unsigned long long win = bits64(cells, b, nwords);
+                for (int m = 0; m <= hi - lo; ++m) out |= (unsigned)(win >> m);
             }
+        if (w == nwords - 1u && (n_dens & 31u)) out &= (1u << (n_dens & 31u)) - 1u;   // past the last density
+        need[w] = out;
+        counts[w] = __popc(out);
     }
 }
 
@@ -979,12 +1009,15 @@ __global__ void need_counts(const unsigned* need, unsigned* counts, unsigned nwo
     for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) counts[w] = __popc(need[w]);
 }
 
-// The marked density indices in ascending order: word w's go to idx[rank[w] ..].
-__global__ void need_compact(const unsigned* need, const unsigned* rank, unsigned nwords, unsigned* idx)
+// The marked density indices in ascending order (word w's go to idx[rank[w] ..]), and each
+// word's rank packed with its bits for the passes' value lookups.
+__global__ void need_compact(const unsigned* need, const unsigned* rank, unsigned nwords, unsigned* idx, uint2* stored)
 {
     for (unsigned w = blockIdx.x * blockDim.x + threadIdx.x; w < nwords; w += gridDim.x * blockDim.x) {
+        const unsigned bits = need[w];
         unsigned o = rank[w];
-        for (unsigned m = need[w]; m; m &= m - 1u) idx[o++] = w * 32u + (unsigned)(__ffs(m) - 1);
+        stored[w] = make_uint2(o, bits);
+        for (unsigned m = bits; m; m &= m - 1u) idx[o++] = w * 32u + (unsigned)(__ffs(m) - 1);
     }
 }
 
@@ -1025,16 +1058,17 @@ namespace {
 
 SparseSrc sparse_src(const SparseScratch& sp)
 {
-    return SparseSrc{sp.above, sp.solid, sp.need, sp.rank, sp.vals};
+    return SparseSrc{sp.above, sp.solid, sp.stored, sp.vals};
 }
 
-// The marked densities' ranks and their index list (total in sp.total).
-void need_list(SparseScratch& sp, unsigned n_dens, cudaStream_t stream)
+// The marked densities' ranks and their index list (total in sp.total); `counted` = the
+// counts per word are already in sp.counts.
+void need_list(SparseScratch& sp, unsigned n_dens, bool counted, cudaStream_t stream)
 {
     const unsigned nwords = (n_dens + 31u) / 32u;
-    need_counts<<<grid_for(nwords, 256), 256, 0, stream>>>(sp.need, sp.counts, nwords);
+    if (!counted) need_counts<<<grid_for(nwords, 256), 256, 0, stream>>>(sp.need, sp.counts, nwords);
     exclusive_scan<unsigned>(sp.counts, sp.rank, sp.block_totals, sp.total, nwords, stream);
-    need_compact<<<grid_for(nwords, 256), 256, 0, stream>>>(sp.need, sp.rank, nwords, sp.idx);
+    need_compact<<<grid_for(nwords, 256), 256, 0, stream>>>(sp.need, sp.rank, nwords, sp.idx, sp.stored);
 }
 
 }  // namespace
@@ -1052,7 +1086,7 @@ cudaError_t launch_bloxel_sparse_prepare(SparseScratch& sp, int size, bool up_ax
     if (e != cudaSuccess) return e;
     bloxel_count<<<grid_for(n, 256), 256, 0, stream>>>(v, size, make_float3(px, py, pz), iso, dminmax, s.counts, s.airsolid, sp.need);
     exclusive_scan<unsigned>(s.counts, s.offsets, s.block_totals, s.total, n, stream);
-    need_list(sp, n_dens, stream);
+    need_list(sp, n_dens, false, stream);
     return cudaGetLastError();
 }
 
@@ -1114,18 +1148,20 @@ cudaError_t launch_dmc_sparse_prepare(SparseScratch& sp, int size, bool up_axis_
     const DmcLists lists{s.vert_items, s.quad_items, s.counters, s.tile_sums};
     const unsigned n = (unsigned)size * size * size, s1 = (unsigned)size + 1u;
     const unsigned tiles = (n + kDmcTile - 1) / kDmcTile;
+    const unsigned nwords = (n_dens + 31u) / 32u;
     cudaError_t e = cudaMemsetAsync(s.airsolid, 0, 2 * sizeof(unsigned), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.airsolid, 0xFF, sizeof(unsigned), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.counters, 0, 2 * sizeof(unsigned), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.tile_sums, 0, tiles * sizeof(uint2), stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(sp.need, 0, ((n_dens + 31u) / 32u) * sizeof(unsigned), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(sp.cells, 0, nwords * sizeof(unsigned), stream);
     if (e != cudaSuccess) return e;
     dmc_cases<<<grid_for(s1 * s1 * s1, 256), 256, 0, stream>>>(g, iso, dminmax, s.masks, lists);
     dmc_count<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, s.masks, lists);
     dmc_scan_tiles<<<1, kScanBlock, 0, stream>>>(s.tile_sums, tiles, s.total);
     dmc_scan_cells<<<tiles, 256, 0, stream>>>(g, s.masks, s.offsets, s.tile_sums, s.total);
-    dmc_mark_needed<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, lists, sp.need, n_dens);
-    need_list(sp, n_dens, stream);
+    dmc_mark_cells<<<grid_for(n / 8, 256), 256, 0, stream>>>(g, lists, sp.cells);
+    need_dilate<<<grid_for(nwords, 256), 256, 0, stream>>>(sp.cells, sp.need, sp.counts, n_dens, g.sy, g.sz);
+    need_list(sp, n_dens, true, stream);
     return cudaGetLastError();
 }
 

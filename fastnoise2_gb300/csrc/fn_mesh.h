@@ -42,8 +42,10 @@ struct SparseScratch {
     unsigned* above = nullptr;         // density > iso
     unsigned* solid = nullptr;         // density <= iso
     unsigned* need = nullptr;
+    unsigned* cells = nullptr;         // dual marching cubes: base corners of the created vertices' cells
     unsigned* counts = nullptr;        // set bits per word of need
     unsigned* rank = nullptr;          // exclusive scan of counts
+    uint2* stored = nullptr;           // per word of need: (rank, bits), for value lookups
     unsigned* block_totals = nullptr;
     unsigned* total = nullptr;         // needed densities
     unsigned* idx = nullptr;           // their density indices, ascending
