@@ -664,6 +664,7 @@ def run_mesh(a, rank, world, local):
         fn.jit_compile([(node, 3)])
     else:
         fn.set_jit_enabled(False)
+    fn.set_mesh_density_form(fn.MESH_DENSITY_SPARSE if a.mesh_densities == "sparse" else fn.MESH_DENSITY_ARRAY)
     dev = torch.device("cuda", local)
     vcap, icap = 2 << 20, 4 << 20                       # per chunk: a 128^3 surface chunk needs ~0.5 M / 0.7 M
     bufs = [(torch.empty(vcap * 4, dtype=torch.float32, device=dev), torch.empty(icap, dtype=torch.int32, device=dev))
@@ -729,7 +730,10 @@ def run_mesh(a, rank, world, local):
                    "path": api + ": densities (" + ("specialised kernel" if a.kernels == "jit" else "interpreter")
                            + (") + cases/count/scan/vertex/quad mesher" if dmc else ") + count/scan/emit mesher")
                            + f", {chunks} chunks per call over 4 internal streams",
-                   "l2": f"densities of a chunk ({(size + apron) ** 3 * 4 / 1e6:.1f} MB) stay in L2 between generation and meshing"},
+                   "density_form": a.mesh_densities,
+                   "l2": (f"densities of a chunk ({(size + apron) ** 3 * 4 / 1e6:.1f} MB) stay in L2 between generation and meshing"
+                          if a.mesh_densities == "array" else
+                          "no density array: 2 classification bits per density, exact values only where the passes read them")},
         "e2e": {"value": value, "unit": "Mpoints/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": (24 if dmc else 20) * chunks,
                 "api": api + " (device mesh buffers; counts, heights and min/max read back per chunk)"},
         "single_chunk_calls": {"value": voxels / (single_ms * 1e-3) / 1e6, "unit": "Mpoints/s", "ms_per_step": single_ms,
@@ -863,6 +867,8 @@ def main():
     ap.add_argument("--open-seconds", type=float, default=0.5)
     ap.add_argument("--requests", type=int, default=4096,
                     help="chunk mix: use the first N requests of the 4096-request mix (smaller cases for profiling)")
+    ap.add_argument("--mesh-densities", default="array", choices=["array", "sparse"],
+                    help="mesh workloads: the chunk's density array, or the sparse form (fnSetMeshDensityForm)")
     ap.add_argument("--no-served", dest="served", action="store_false",
                     help="chunk mix: leave out the request-server measurements")
     a = ap.parse_args()

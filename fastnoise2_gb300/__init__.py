@@ -148,6 +148,7 @@ def _declare(L):
         "fnAutotuneLoad": (c_int, [cp]),
         "fnAutotuneSave": (c_int, [cp]),
         "fnServerSubmitPaced": (c_int, [vp, vp, c_int, vp, vp]),
+        "fnSetMeshDensityForm": (c_int, [c_int]),
         "fnJitCheckBatchVariants": (c_int, [vp, vp, c_int, ctypes.POINTER(c_int)]),
         "fnGenEachPaced": (c_int, [vp, c_int, vp, vp, vp]),
         "fnGetVariableBits": (c_int, [vp, c_int, ctypes.POINTER(c_int)]),
@@ -269,6 +270,17 @@ def jit_compile(pairs) -> None:
     nodes, dims = _jit_arrays(pairs)
     if lib().fnJitCompile(nodes, dims, len(pairs)) != 0:
         _check()
+
+
+MESH_DENSITY_ARRAY, MESH_DENSITY_SPARSE = 0, 1
+
+
+def set_mesh_density_form(form: int) -> int:
+    """fnSetMeshDensityForm: MESH_DENSITY_ARRAY (default) or MESH_DENSITY_SPARSE; returns the previous."""
+    rc = lib().fnSetMeshDensityForm(int(form))
+    if rc < 0:
+        raise FastNoiseError(rc, "invalid mesh density form")
+    return rc
 
 
 def jit_check_batch_variants(pairs) -> int:

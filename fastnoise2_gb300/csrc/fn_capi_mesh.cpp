@@ -3,6 +3,7 @@
 // multi-chunk calls, and the host side of the meshers in fn_mesh.cu.  They restate the Node
 // Editor's chunk meshers (reference tools/NodeEditor/MeshNoisePreview.cpp) on the GPU.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -127,6 +128,9 @@ struct MeshCtx {
 };
 thread_local MeshCtx t_mesh;
 
+// FN_MESH_DENSITY_ARRAY (default) or FN_MESH_DENSITY_SPARSE (fnSetMeshDensityForm).
+std::atomic<int> g_mesh_form{FN_MESH_DENSITY_ARRAY};
+
 constexpr int kMeshLanes = 4;
 
 struct MeshLanes {
@@ -195,12 +199,13 @@ bool enqueue_chunk(MeshKind kind, const DeviceProgram& prog, MeshCtx& m, cudaStr
     const int cnt[3] = {sg, sg, sg};
     const float step[3] = {1, 1, 1};
     const PointArgs args = grid_args(3, off, cnt, step, seed);
-    // A tree with specialised kernels meshes from the sparse form: its densities stay in
-    // registers, only their classification against the iso level is stored, and the few exact
-    // values the passes need are evaluated again where they are read.  Otherwise the tree's
-    // (interpreter) kernel writes the density array.
+    // The density array (default): the tree's kernel writes every density of the chunk (9 MB
+    // for the editor's 128^3, which stays in L2 between generation and meshing).  The sparse
+    // form (fnSetMeshDensityForm, trees with specialised kernels): the densities stay in
+    // registers, only their classification against the iso level is stored, and the exact
+    // values the passes read are evaluated again at those voxels only.
     bool sparse = false;
-    if (jit_enabled()) {
+    if (g_mesh_form.load(std::memory_order_relaxed) == FN_MESH_DENSITY_SPARSE && jit_enabled()) {
         if (!m.reserve(0, kind == kBloxel ? (size_t)size * size * size : 0) || (kind == kDmc && !m.reserve_dmc(size)) ||
             !m.reserve_sparse(n_dens))
             return false;
@@ -335,6 +340,12 @@ int build_chunk_meshes(MeshKind kind, const void* node, int size, int count, con
 }  // namespace
 
 extern "C" {
+
+int fnSetMeshDensityForm(int form)
+{
+    if (form != FN_MESH_DENSITY_ARRAY && form != FN_MESH_DENSITY_SPARSE) return FN_ERR_ARG;
+    return g_mesh_form.exchange(form);
+}
 
 int fnBuildChunkMeshBloxel(const void* node, int size, int posX, int posY, int posZ, int seed, float isoSurface, int upAxisZ,
                            fnChunkMesh* mesh, void* stream)

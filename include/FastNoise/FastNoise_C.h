@@ -339,6 +339,19 @@ typedef struct fnChunkMesh {
     float minAirY, maxSolidY;       /* out (bloxel, dmc): lowest air / highest solid height, +-inf if none */
     float minMax[2];                /* out: OutputMinMax of the densities */
 } fnChunkMesh;
+/* Where the chunk meshers keep a chunk's densities (no counterpart in the reference).
+ * FN_MESH_DENSITY_ARRAY (default): the tree's kernel writes every density of the chunk into a
+ * device array that the mesher passes read ((size+2)^3 or (size+4)^3 floats; for the editor's
+ * 128^3 chunks 9 MB, which stays in L2).  FN_MESH_DENSITY_SPARSE: for trees with specialised
+ * kernels the densities never leave registers; the tree's kernel stores only their
+ * classification against the iso level (2 bits each), and the exact values the light and
+ * vertex passes read are evaluated again at those voxels only (the bloxel mesher's surface
+ * voxels; a gradient stencil around every dual marching cubes vertex).  Same meshes bit for
+ * bit; the array form measures faster on a GB300.  Returns the previous setting (or
+ * FN_ERR_ARG). */
+#define FN_MESH_DENSITY_ARRAY 0
+#define FN_MESH_DENSITY_SPARSE 1
+FASTNOISE_API int fnSetMeshDensityForm(int form);
 /* BuildBloxel3DMesh (MeshNoisePreview.cpp:443-590): block faces between solid (density <=
  * isoSurface) and air voxels of a size^3 chunk at (posX, posY, posZ), with ambient occlusion
  * and directional light; size <= 256 (every index fits 32 bits).  upAxisZ swaps the y and z noise axes. */

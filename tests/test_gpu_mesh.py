@@ -32,12 +32,22 @@ def caves_tree():
     return N("CellularDistance", Feature_Scale=9.0, Return_Type="Index0Sub1")
 
 
-TIERS = ["interpreter", "specialised"]
+# interpreter: the density array; specialised: the density array from the tree's specialised
+# kernel; sparse: the sparse density form (fnSetMeshDensityForm)
+TIERS = ["interpreter", "specialised", "sparse"]
+
+
+@pytest.fixture(autouse=True)
+def density_form(request, gpu):
+    tier = request.node.callspec.params.get("tier") if hasattr(request.node, "callspec") else None
+    prev = gpu.set_mesh_density_form(gpu.MESH_DENSITY_SPARSE if tier == "sparse" else gpu.MESH_DENSITY_ARRAY)
+    yield
+    gpu.set_mesh_density_form(prev)
 
 
 def product_node(fn, root, tier):
     node = trees.to_product(root)
-    if tier == "specialised":
+    if tier in ("specialised", "sparse"):
         fn.jit_compile([(node, 3)])
     return node
 
@@ -213,7 +223,11 @@ def test_sparse_form_equals_density_array_on_editor_chunks(gpu, torch_cuda, kind
              RHS=N("Gradient").set("Multiplier", 0.02, 1))
     run = run_dmc if kind == "dmc" else run_bloxel
     size, vcap, icap = 128, 1 << 20, 3 << 20
-    got = run(fn, torch, root, size, (-64, -64, 128), 1337, 0.0, False, vcap=vcap, icap=icap, tier="specialised")
+    prev = fn.set_mesh_density_form(fn.MESH_DENSITY_SPARSE)
+    try:
+        got = run(fn, torch, root, size, (-64, -64, 128), 1337, 0.0, False, vcap=vcap, icap=icap, tier="specialised")
+    finally:
+        fn.set_mesh_density_form(prev)
     fn.set_jit_enabled(False)
     try:
         ref = run(fn, torch, root, size, (-64, -64, 128), 1337, 0.0, False, vcap=vcap, icap=icap, tier="interpreter")
