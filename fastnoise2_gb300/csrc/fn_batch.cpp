@@ -97,7 +97,7 @@ cudaError_t BatchRunner::launch_group(size_t g, uint32_t smem, cudaStream_t stre
     auto* reqs = reinterpret_cast<BatchRequest*>(d_buf_ + off_req_);
     auto* items = reinterpret_cast<uint2*>(d_buf_ + off_items_);
     const Group& gr = groups_[g];
-    if (!gr.jit) return launch_batch(hdr, reqs, d_states_, items, smem, max_regs_, gr.grid, 256, stream);
+    if (!gr.jit) return launch_batch(hdr, reqs, d_states_, items, smem, gr.grid, 256, stream);
     BatchState* states = d_states_;
     BatchGroup* grp = reinterpret_cast<BatchGroup*>(d_buf_ + off_groups_) + g;
     void* params[] = {&hdr, &reqs, &states, &items, &grp};
@@ -129,7 +129,7 @@ int BatchRunner::launch_graph(cudaStream_t stream, size_t bytes, uint32_t smem)
     // Recapture when the launch shape (kernels, grids, dynamic shared memory)
     // changed; otherwise only the upload node is updated -- the kernel arguments
     // are the fixed buffer addresses, the work lists travel in the upload.
-    if (exec_ && (graph_groups_ != groups_ || graph_smem_ != smem || graph_regs_ != max_regs_)) {
+    if (exec_ && (graph_groups_ != groups_ || graph_smem_ != smem)) {
         cudaGraphExecDestroy(exec_);
         exec_ = nullptr;
         if (graph_) { cudaGraphDestroy(graph_); graph_ = nullptr; }
@@ -137,7 +137,6 @@ int BatchRunner::launch_graph(cudaStream_t stream, size_t bytes, uint32_t smem)
     if (!exec_) {
         graph_groups_ = groups_;
         graph_smem_ = smem;
-        graph_regs_ = max_regs_;
         copy_node_ = nullptr;
         if (!capture_stream_ && !cuda_ok(cudaStreamCreateWithFlags(&capture_stream_, cudaStreamNonBlocking), "stream")) return -3;
         if (!cuda_ok(cudaStreamBeginCapture(capture_stream_, cudaStreamCaptureModeThreadLocal), "begin capture")) return -3;
@@ -171,7 +170,6 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
     if (n == 0) return 0;
     std::vector<DeviceProgram> progs(n);
     uint32_t max_bytes = 16;
-    int max_regs = 1;
     points_ = 0;
     for (size_t i = 0; i < n; ++i) {
         if (!items[i].node || items[i].args.total < 0 || (items[i].args.total > 0 && !items[i].dout)) {
@@ -182,7 +180,6 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         std::string err;
         if (!jit_ensure(progs[i].host, err)) { set_error(-2, "batch request " + std::to_string(i) + ": " + err); return -2; }
         max_bytes = std::max(max_bytes, progs[i].bytes);
-        max_regs = std::max(max_regs, progs[i].host->n_regs);
         points_ += (uint64_t)std::max(0ll, items[i].args.total);
     }
     signature_ = batch_signature(items, progs);
@@ -311,7 +308,7 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
         if (occ <= 0 && gr.jit) {
             if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)gr.jit, gr.threads, 0) != cudaSuccess || occ < 1) occ = 1;
         } else if (occ <= 0) {
-            occ = batch_occupancy(256, interpreter_smem(max_bytes, max_regs));
+            occ = batch_occupancy(256, max_bytes);
         }
         long long grid = (long long)sms * occ;
         const long long group_items = (long long)(gr.item_end - gr.item_begin);
@@ -322,15 +319,13 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
     }
     const size_t bytes = off_items_ + n_items * sizeof(uint2);
     const uint32_t smem = jit ? 0 : max_bytes;
-    max_regs_ = max_regs;
     // A graph pays off for a launch shape that repeats (the same batch every frame); batches
     // whose shape keeps changing (a server's admissions) would pay a capture each time, so a
     // new shape is captured only when it comes twice in a row and runs as plain launches until then.
-    const bool same_as_graph = exec_ && graph_groups_ == groups_ && graph_smem_ == smem && graph_regs_ == max_regs_;
-    const bool repeated = last_groups_ == groups_ && last_smem_ == smem && last_regs_ == max_regs_;
+    const bool same_as_graph = exec_ && graph_groups_ == groups_ && graph_smem_ == smem;
+    const bool repeated = last_groups_ == groups_ && last_smem_ == smem;
     last_groups_ = groups_;
     last_smem_ = smem;
-    last_regs_ = max_regs_;
     int rc;
     if (use_graph && (same_as_graph || repeated)) {
         rc = launch_graph(stream, bytes, smem);

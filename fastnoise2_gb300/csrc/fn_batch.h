@@ -90,8 +90,6 @@ private:
     cudaGraphNode_t copy_node_ = nullptr;
     std::vector<Group> graph_groups_;   // launch shape the graph was captured with
     uint32_t graph_smem_ = 0;
-    int max_regs_ = 1;                  // interpreter batches: register file slots of the largest program
-    int graph_regs_ = 0, last_regs_ = 0;
     std::vector<Group> last_groups_;    // shape of the previous launch (a graph is captured for a repeated shape)
     uint32_t last_smem_ = 0;
     std::vector<float*> last_minmax_;

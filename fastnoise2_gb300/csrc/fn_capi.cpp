@@ -71,7 +71,7 @@ cudaError_t launch_points(const DeviceProgram& prog, const PointArgs& args, floa
     // points there is nothing to evaluate and the interpreter only writes min/max.
     if (prog.host->needs_specialisation() && args.total > 0) return cudaErrorNotSupported;
     if (args.total > 0) jit_note_interpreted(prog.host);      // may queue a background specialisation
-    return launch_interpreter(prog.dptr, prog.bytes, prog.host->n_regs, args, out, work, dminmax, stream);
+    return launch_interpreter(prog.dptr, prog.bytes, args, out, work, dminmax, stream);
 }
 
 // Specialise trees the interpreter cannot run before their first launch.

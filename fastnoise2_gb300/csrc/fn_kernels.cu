@@ -25,21 +25,10 @@ namespace {
 constexpr int kThreads = 256;
 constexpr float kInf = __builtin_huge_valf();
 
-// The per-point register file, in shared memory after the staged program: slot k of this
-// thread at base[k * kThreads], so a warp touching one slot hits 32 consecutive banks.  Its
-// size follows the program (n_regs slots), not the largest possible program.
-struct Regs {
-    float* base;
-    __device__ __forceinline__ float& operator[](int k) const { return base[k * kThreads]; }
-};
-
-// Byte offset of the register file in the dynamic shared memory (after the program area).
-__host__ __device__ constexpr uint32_t reg_file_offset(uint32_t prog_bytes) { return (prog_bytes + 15u) & ~15u; }
-
 __device__ __forceinline__ int sadd(int a, int b) { return (int)((unsigned)a + (unsigned)b); }
 
 template <int D>
-__device__ __forceinline__ float noise_at(int kind, int seed, const Regs& R, int a, float f)
+__device__ __forceinline__ float noise_at(int kind, int seed, const float* R, int a, float f)
 {
     float p[4];
 #pragma unroll
@@ -69,7 +58,7 @@ __device__ __forceinline__ float noise_at(int kind, int seed, const Regs& R, int
 }
 
 template <int D>
-__device__ __forceinline__ CellParams cell_params(const FnInstr& I, const float* P, const Regs& R)
+__device__ __forceinline__ CellParams cell_params(const FnInstr& I, const float* P, const float* R)
 {
     CellParams cp;
     cp.freq = P[I.prm];
@@ -82,7 +71,7 @@ __device__ __forceinline__ CellParams cell_params(const FnInstr& I, const float*
 }
 
 template <int D>
-__device__ __forceinline__ void exec_dim(const FnInstr& I, const float* P, const Regs& R, int seed)
+__device__ __forceinline__ void exec_dim(const FnInstr& I, const float* P, float* R, int seed)
 {
     const int sd = sadd(seed, I.seed);
     switch (I.op) {
@@ -221,7 +210,7 @@ __device__ __forceinline__ void exec_dim(const FnInstr& I, const float* P, const
     }
 }
 
-__device__ __noinline__ void exec_program(const FnInstr* ins, int n, const float* P, Regs R, int seed)
+__device__ __noinline__ void exec_program(const FnInstr* ins, int n, const float* P, float* R, int seed)
 {
     for (int pc = 0; pc < n; ++pc) {
         const FnInstr I = ins[pc];
@@ -323,12 +312,10 @@ __global__ void __launch_bounds__(kThreads, 4) interp_kernel(const FnProgramHead
     const int outr = h->out_reg;
 
     float mn = kInf, mx = -kInf;
-    const Regs R{reinterpret_cast<float*>(reinterpret_cast<char*>(sprog) + reg_file_offset(bytes)) + threadIdx.x};
+    float R[FN_MAX_REGS];
     const long long stride = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < args.total; i += stride) {
-        float p[4];
-        fne::root_position(args, i, p);
-        for (int k = 0; k < args.dim; ++k) R[k] = p[k];
+        fne::root_position(args, i, R);
         exec_program(ins, n, P, R, args.seed);
         const float v = R[outr];
         out[i] = v;
@@ -341,9 +328,8 @@ __global__ void __launch_bounds__(kThreads, 4) interp_kernel(const FnProgramHead
 constexpr int kSmCacheDevices = 64;
 std::atomic<int> g_num_sms[kSmCacheDevices];
 
-// Let a kernel stage up to 96 KB of program plus a 64-slot register file (64 KB) in dynamic
-// shared memory, once per device (the attribute is per device; `done` holds one bit per
-// device ordinal).
+// Let a kernel stage up to 96 KB of program in dynamic shared memory, once per
+// device (the attribute is per device; `done` holds one bit per device ordinal).
 cudaError_t allow_program_smem(const void* kernel, std::atomic<unsigned long long>& done)
 {
     int dev = 0;
@@ -351,7 +337,7 @@ cudaError_t allow_program_smem(const void* kernel, std::atomic<unsigned long lon
     if (e != cudaSuccess) return e;
     const unsigned long long bit = 1ull << (dev & 63);
     if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
-    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024 + FN_MAX_REGS * kThreads * 4);
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
     if (e == cudaSuccess) done.fetch_or(bit, std::memory_order_release);
     return e;
 }
@@ -391,11 +377,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(BatchHeader* hd
         if (end > args.total) end = args.total;
 
         float mn = kInf, mx = -kInf;
-        const Regs R{reinterpret_cast<float*>(reinterpret_cast<char*>(sprog) + reg_file_offset(hdr->max_prog_bytes)) + threadIdx.x};
+        float R[FN_MAX_REGS];
         for (long long i = begin + threadIdx.x; i < end; i += blockDim.x) {
-            float p[4];
-            fne::root_position(args, i, p);
-            for (int k = 0; k < args.dim; ++k) R[k] = p[k];
+            fne::root_position(args, i, R);
             exec_program(ins, h->n_instr, P, R, args.seed);
             const float v = R[h->out_reg];
             rq.out[i] = v;
@@ -409,19 +393,14 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_kernel(BatchHeader* hd
 
 }  // namespace
 
-uint32_t interpreter_smem(uint32_t prog_bytes, int n_regs)
-{
-    return reg_file_offset(prog_bytes) + (uint32_t)n_regs * kThreads * 4u;
-}
-
 cudaError_t launch_batch(BatchHeader* hdr, const BatchRequest* reqs, BatchState* states, const uint2* items,
-                         uint32_t max_prog_bytes, int max_regs, int grid, int block, cudaStream_t stream)
+                         uint32_t max_prog_bytes, int grid, int block, cudaStream_t stream)
 {
     static std::atomic<unsigned long long> attr_set{0};      // one bit per device
     cudaError_t e = allow_program_smem((const void*)batch_kernel, attr_set);
     if (e != cudaSuccess) return e;
-    if (block != kBatchThreads || max_prog_bytes > 96 * 1024 || max_regs < 1 || max_regs > FN_MAX_REGS) return cudaErrorInvalidValue;
-    batch_kernel<<<grid, block, interpreter_smem(max_prog_bytes, max_regs), stream>>>(hdr, reqs, states, items);
+    if (block != kBatchThreads || max_prog_bytes > 96 * 1024) return cudaErrorInvalidValue;
+    batch_kernel<<<grid, block, max_prog_bytes, stream>>>(hdr, reqs, states, items);
     return cudaGetLastError();
 }
 
@@ -447,20 +426,19 @@ int num_sms()
     return n;
 }
 
-cudaError_t launch_interpreter(const FnProgramHeader* prog, uint32_t prog_bytes, int n_regs, const PointArgs& args, float* out,
+cudaError_t launch_interpreter(const FnProgramHeader* prog, uint32_t prog_bytes, const PointArgs& args, float* out,
                                MinMaxWork* work, float* dminmax, cudaStream_t stream)
 {
     static std::atomic<unsigned long long> attr_set{0};      // one bit per device
     cudaError_t e = allow_program_smem((const void*)interp_kernel, attr_set);
     if (e != cudaSuccess) return e;
-    if (prog_bytes > 96 * 1024 || (prog_bytes & 15) || n_regs < 1 || n_regs > FN_MAX_REGS) return cudaErrorInvalidValue;
+    if (prog_bytes > 96 * 1024 || (prog_bytes & 15)) return cudaErrorInvalidValue;
     long long blocks = (args.total + kThreads - 1) / kThreads;
     long long cap = (long long)num_sms() * 8;
     if (blocks > cap) blocks = cap;
     if (blocks > kMaxReduceBlocks) blocks = kMaxReduceBlocks;
     if (blocks < 1) blocks = 1;
-    interp_kernel<<<(unsigned)blocks, kThreads, interpreter_smem(prog_bytes, n_regs), stream>>>(prog, prog_bytes, args, out, work,
-                                                                                              dminmax);
+    interp_kernel<<<(unsigned)blocks, kThreads, prog_bytes, stream>>>(prog, prog_bytes, args, out, work, dminmax);
     return cudaGetLastError();
 }
 

@@ -69,8 +69,8 @@ cudaError_t launch_interpreter_static(const void* blob, uint32_t blob_bytes, con
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(&s->work, 0, offsetof(MinMaxWork, result), stream);   // counter and min/max keys
     if (e != cudaSuccess) return e;
-    return launch_interpreter(reinterpret_cast<const FnProgramHeader*>(s->prog), blob_bytes,
-                              static_cast<const FnProgramHeader*>(blob)->n_regs, args, out, &s->work, dminmax, stream);
+    return launch_interpreter(reinterpret_cast<const FnProgramHeader*>(s->prog), blob_bytes, args, out, &s->work, dminmax,
+                              stream);
 }
 
 }  // namespace fn
