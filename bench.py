@@ -498,6 +498,8 @@ def run_chunkmix(a, rank, world, local):
     achieved = work / (batch_ms * 1e-3) / 1e12
     hbm_gbs = pts * 4 / (batch_ms * 1e-3) / 1e9
     cpu = cpu_baseline("chunk-mix", a.cpu_passes, 3.0, rank) if a.cpu_passes > 0 else None
+    if cpu is not None and served is not None and a.cpu_rates:
+        served["cpu_open_loop"] = cpu_open_loop(chunks, a, rank)
     line = {
         "metric": "Mpoints/s", "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": batch_ms_max, "higher_is_better": True, "scaling": "weak",
@@ -634,6 +636,47 @@ def run_served(fn, chunks, nodes, rank, a, dev):
                                              "per_call_open_loop: fnGenEachPaced (one fnGen*Device launch per request on one "
                                              "stream, min/max copied back, completion seen by a second host thread)"}
     return result
+
+
+def cpu_open_loop(chunks, a, rank=0):
+    """The same open-loop serving mix on the host cores: the CPU restatement (oracle/) serves
+    requests in arrival order on every host thread, whole requests per thread; latency counts
+    from arrival to the request's output and min/max written."""
+    from oracle import oracle
+    from tests import trees
+    otrees = [oracle.OracleTree(m()) for m in trees.MIX_TREES]
+    prng = np.random.default_rng(20261203)
+    pos = [prng.uniform(-1e4, 1e4, 1 << 20).astype(np.float32) for _ in range(3)]
+    serve = []                                            # (tree, kind, count, offset, seed, positions, points)
+    for k, c in enumerate(chunks):
+        kind = oracle.KIND_GRID3D if len(c.count) == 3 else oracle.KIND_GRID2D
+        serve.append((c.tree, kind, tuple(c.count), tuple(c.offset), c.seed + rank, (), c.points))
+        if a.extra_every > 0 and k % a.extra_every == a.extra_every - 1:
+            serve.append((c.tree, oracle.KIND_GRID4D, (32, 32, 32, 32), tuple(c.offset) + (0.0,) * (4 - len(c.offset)),
+                          c.seed + 1, (), 32 ** 4))
+            serve.append((c.tree, oracle.KIND_POSITIONS3D, (1 << 20,), (0, 0, 0), c.seed + 2, pos, 1 << 20))
+    threads = os.cpu_count()
+    rng = np.random.default_rng(5)
+    result = []
+    for rate in a.cpu_rates:
+        n = min(len(serve), max(100, int(rate * a.cpu_open_seconds)))
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, n)) * 1e6
+        outs, mms, reqs = [], [], []
+        for k in range(n):
+            tree, kind, cnt, off, seed, p, npts = serve[k]
+            outs.append(np.empty(npts, np.float32))
+            mms.append(np.zeros(2, np.float32))
+            reqs.append(oracle.request(otrees[tree], kind, outs[-1], mms[-1], seed, cnt, off, (1.0,) * len(cnt), p))
+        t0 = time.perf_counter()
+        lat = oracle.serve_paced(reqs, arrivals, threads)
+        wall = time.perf_counter() - t0
+        npts = sum(serve[k][-1] for k in range(n))
+        result.append({"rate_req_s": rate, "achieved_req_s": n / wall, "requests": n,
+                       "p50_ms": float(np.percentile(lat, 50)) / 1e3, "p99_ms": float(np.percentile(lat, 99)) / 1e3,
+                       "max_ms": float(lat.max()) / 1e3, "Mpoints_s": npts / wall / 1e6})
+    return {"threads": threads, "rates": result, "host": oracle.cpu_description(),
+            "api": "oracle on_serve_paced: Poisson arrivals (same mix and generator as the served open loop), "
+                   "a FIFO served by every host thread, whole requests per thread"}
 
 
 # ---------------------------------------------------------------- GPU: chunk meshing
@@ -862,6 +905,10 @@ def main():
     ap.add_argument("--max-batch-requests", type=int, default=512)
     ap.add_argument("--rates", type=float, nargs="*",
                     default=[1000.0, 5000.0, 10000.0, 20000.0, 50000.0, 100000.0, 200000.0, 400000.0])
+    ap.add_argument("--cpu-rates", type=float, nargs="*", default=[100.0, 250.0, 500.0, 1000.0],
+                    help="open-loop request rates for the CPU restatement's serving latency (none = leave it out)")
+    ap.add_argument("--cpu-open-seconds", type=float, default=1.0,
+                    help="seconds of Poisson arrivals per CPU open-loop rate")
     ap.add_argument("--extra-every", type=int, default=64,
                     help="serving mix: one GenUniformGrid4D 32^4 and one GenPositionArray3D 1M request per this many chunks")
     ap.add_argument("--open-seconds", type=float, default=0.5)

@@ -34,12 +34,16 @@
  * compiled with a counting scalar type (see opcount.h) to measure FS-level
  * operations per point.
  */
+#if !defined(__cplusplus) && !defined(_POSIX_C_SOURCE)
+#define _POSIX_C_SOURCE 200809L /* clock_gettime under -std=c11 */
+#endif
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 #include <float.h>
 #include <pthread.h>
+#include <time.h>
 
 #ifdef OC_COUNT
 #include "opcount.h"
@@ -2818,6 +2822,74 @@ OC_EXPORT int on_gen_requests(const on_request* reqs, int n, int threads, int64_
     for (int i = 0; i < n; ++i)
         if (reqs[i].minmax) { reqs[i].minmax[0] = jobs[i].mn; reqs[i].minmax[1] = jobs[i].mx; }
     free(tasks); free(jobs); free(totals);
+    return 0;
+}
+
+/* Open-loop serving on the host cores: request k arrives arrival_us[k] microseconds after the
+ * call starts; `threads` workers take the requests in arrival order (a shared FIFO), each
+ * waiting for its request's arrival, and latency_us[k] = the request's completion minus its
+ * arrival.  Whole requests per worker, as an application's job system would serve them. */
+typedef struct {
+    const on_request* reqs;
+    const double* arrival;
+    double* latency;
+    int n;
+    int next;                            /* guarded by mu */
+    pthread_mutex_t mu;
+    struct timespec start;
+} serve_t;
+
+static double us_since(const struct timespec* t0)
+{
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return (double)(t.tv_sec - t0->tv_sec) * 1e6 + (double)(t.tv_nsec - t0->tv_nsec) * 1e-3;
+}
+
+static void* serve_worker(void* arg)
+{
+    serve_t* sv = (serve_t*)arg;
+    for (;;) {
+        pthread_mutex_lock(&sv->mu);
+        const int k = sv->next < sv->n ? sv->next++ : -1;
+        pthread_mutex_unlock(&sv->mu);
+        if (k < 0) return NULL;
+        while (us_since(&sv->start) < sv->arrival[k]) {
+            /* spin: arrivals are microseconds apart */
+        }
+        job_t j;
+        const int64_t total = setup_request_job(&j, &sv->reqs[k]);
+        j.begin = 0;
+        j.end = total;
+        run_range(&j);
+        if (sv->reqs[k].minmax) {
+            sv->reqs[k].minmax[0] = total > 0 ? j.mn : INFINITY;
+            sv->reqs[k].minmax[1] = total > 0 ? j.mx : -INFINITY;
+        }
+        sv->latency[k] = us_since(&sv->start) - sv->arrival[k];
+    }
+}
+
+OC_EXPORT int on_serve_paced(const on_request* reqs, int n, const double* arrival_us, int threads, double* latency_us)
+{
+    if (n <= 0) return 0;
+    if (threads < 1) threads = 1;
+    if (threads > OC_MAX_THREADS) threads = OC_MAX_THREADS;
+    serve_t sv;
+    sv.reqs = reqs;
+    sv.arrival = arrival_us;
+    sv.latency = latency_us;
+    sv.n = n;
+    sv.next = 0;
+    pthread_mutex_init(&sv.mu, NULL);
+    pthread_t tid[OC_MAX_THREADS];
+    clock_gettime(CLOCK_MONOTONIC, &sv.start);
+    int started = 0;
+    for (int t = 0; t < threads; ++t)
+        if (pthread_create(&tid[t], NULL, serve_worker, &sv) == 0) ++started;
+    if (started == 0) serve_worker(&sv);
+    for (int t = 0; t < started; ++t) pthread_join(tid[t], NULL);
+    pthread_mutex_destroy(&sv.mu);
     return 0;
 }
 

@@ -169,6 +169,8 @@ def lib():
         L.on_gen_single.argtypes = [vp, c_int, fp, c_int]
         L.on_gen_requests.restype = c_int
         L.on_gen_requests.argtypes = [ctypes.c_void_p, c_int, c_int, ctypes.c_int64]
+        L.on_serve_paced.restype = c_int
+        L.on_serve_paced.argtypes = [ctypes.c_void_p, c_int, ctypes.c_void_p, c_int, ctypes.c_void_p]
         L.fn_sinf.restype = c_float
         L.fn_sinf.argtypes = [c_float]
         L.fn_cosf.restype = c_float
@@ -297,6 +299,19 @@ def gen_requests(reqs: Sequence[OracleRequest], threads: int = 0, split: int = 0
     lib().on_set_unfused(1 if unfused else 0)
     if lib().on_gen_requests(ctypes.cast(arr, ctypes.c_void_p), len(reqs), threads or os.cpu_count(), int(split)) != 0:
         raise MemoryError("oracle batch: allocation failed")
+
+
+def serve_paced(reqs: Sequence[OracleRequest], arrivals_us, threads: int = 0) -> np.ndarray:
+    """Open-loop serving on the host cores: request k arrives arrivals_us[k] microseconds after
+    the start; `threads` workers serve the requests in arrival order.  Returns each request's
+    latency (completion minus arrival, microseconds)."""
+    arr = (OracleRequest * len(reqs))(*reqs)
+    times = np.ascontiguousarray(arrivals_us, np.float64)
+    lat = np.zeros(len(reqs), np.float64)
+    lib().on_set_unfused(0)
+    lib().on_serve_paced(ctypes.cast(arr, ctypes.c_void_p), len(reqs), times.ctypes.data, threads or os.cpu_count(),
+                         lat.ctypes.data)
+    return lat
 
 
 def sinf(x: float) -> float:

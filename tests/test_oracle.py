@@ -74,6 +74,30 @@ def test_thread_count_does_not_change_results():
     assert np.array_equal(a.view(np.uint32), b.view(np.uint32)) and ma == mb
 
 
+def test_request_batch_and_paced_serving_match_single_grids():
+    """gen_requests (whole-request batch) and serve_paced (open-loop FIFO) write the same bits
+    and min/max as one grid call per request."""
+    ts = [O.OracleTree(m()) for m in trees.MIX_TREES[:3]]
+    shapes = [(9, 7, 5), (16, 16), (4, 3, 2, 2)]
+    kinds = [O.KIND_GRID3D, O.KIND_GRID2D, O.KIND_GRID4D]
+    rng = np.random.default_rng(3)
+    cases = [(k % 3, k % 3, tuple(rng.uniform(-50, 50, len(shapes[k % 3]))), 11 + k) for k in range(12)]
+    for serve in (False, True):
+        outs, mms, reqs = [], [], []
+        for tree, shape_k, off, seed in cases:
+            outs.append(np.empty(int(np.prod(shapes[shape_k])), np.float32))
+            mms.append(np.zeros(2, np.float32))
+            reqs.append(O.request(ts[tree], kinds[shape_k], outs[-1], mms[-1], seed, shapes[shape_k], off))
+        if serve:
+            lat = O.serve_paced(reqs, np.arange(len(reqs)) * 50.0, threads=3)
+            assert lat.shape == (len(reqs),) and np.all(lat >= 0)
+        else:
+            O.gen_requests(reqs, threads=3)
+        for (tree, shape_k, off, seed), o, mm in zip(cases, outs, mms):
+            ref, rmm = ts[tree].grid(off, shapes[shape_k], (1,) * len(shapes[shape_k]), seed)
+            assert np.array_equal(ref.view(np.uint32), o.view(np.uint32)) and (float(mm[0]), float(mm[1])) == rmm
+
+
 def test_noise_outputs_are_normalised():
     """Each coherent noise's bounding constant maps its output into [-1, 1]."""
     for name in ("Simplex", "SuperSimplex", "Perlin", "Value"):
