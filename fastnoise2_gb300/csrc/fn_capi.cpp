@@ -16,6 +16,8 @@
 #include <thread>
 #include <vector>
 
+#include <cuda.h>   // CUpointer_attribute: the range query below goes through the runtime's driver entry point
+
 #include "../../include/FastNoise/FastNoise_C.h"
 #include "fn_capi_internal.h"
 #include "fn_batch.h"
@@ -46,6 +48,66 @@ void fill_nan(float* out, long long n, float* mm)
     const float q = std::numeric_limits<float>::quiet_NaN();
     if (out) for (long long i = 0; i < n; ++i) out[i] = q;
     store_minmax(mm, q, q);
+}
+
+// Page-locked host memory (cudaHostAlloc, cudaMallocHost, cudaHostRegister): the end of the
+// allocation holding `p`, in host addresses; 0 for pageable memory or where the driver does not
+// report the allocation's extent.  A device-to-host copy that starts in such an allocation must
+// end inside it (the runtime rejects the copy otherwise), so copies are cut there.
+using PointerAttrFn = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+
+PointerAttrFn pointer_attr_fn()
+{
+    static const PointerAttrFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess) {
+            cudaGetLastError();
+            return PointerAttrFn(nullptr);
+        }
+        return reinterpret_cast<PointerAttrFn>(f);
+    }();
+    return fn;
+}
+
+uintptr_t pinned_end(const void* p)
+{
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) { cudaGetLastError(); return 0; }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return 0;
+    const PointerAttrFn attr = pointer_attr_fn();
+    if (!attr) return 0;
+    const CUdeviceptr dp = (CUdeviceptr)(uintptr_t)at.devicePointer;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    if (attr(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, dp) != CUDA_SUCCESS ||
+        attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, dp) != CUDA_SUCCESS || dp < start || dp - start >= size)
+        return 0;
+    return (uintptr_t)p + (size_t)(start + size - dp);
+}
+
+// Copy of `bytes` between device memory and host memory that may start in one page-locked
+// allocation and continue past it (into pageable memory, or another allocation).
+bool copy_host(const void* host, const void* dev, size_t bytes, bool to_host, cudaStream_t s, const char* what)
+{
+    uintptr_t h = (uintptr_t)host, d = (uintptr_t)dev;
+    while (bytes) {
+        const uintptr_t end = pinned_end(reinterpret_cast<const void*>(h));
+        const size_t n = (end > h && end - h < bytes) ? (size_t)(end - h) : bytes;
+        const cudaError_t e = to_host ? cudaMemcpyAsync(reinterpret_cast<void*>(h), reinterpret_cast<const void*>(d), n, cudaMemcpyDeviceToHost, s)
+                                      : cudaMemcpyAsync(reinterpret_cast<void*>(d), reinterpret_cast<const void*>(h), n, cudaMemcpyHostToDevice, s);
+        if (!cuda_ok(e, what)) return false;
+        h += n;
+        d += n;
+        bytes -= n;
+    }
+    return true;
+}
+
+bool copy_to_host(float* dst, const float* src, size_t bytes, cudaStream_t s)
+{
+    return copy_host(dst, src, bytes, true, s, "copy output");
 }
 
 bool ensure(float*& buf, size_t& cap, size_t n)
@@ -142,8 +204,7 @@ bool gen_host_slabs(const DeviceProgram& prog, const PointArgs& args, ThreadCtx*
     for (int s = 0; s < slabs; ++s) {
         const long long r0 = (long long)s * per, r1 = std::min<long long>(rows, r0 + per);
         if (!cuda_ok(cudaStreamWaitEvent(sc->copy, sc->done[s], 0), "wait") ||
-            !cuda_ok(cudaMemcpyAsync(out + r0 * row, ctx->dbuf + r0 * row, (size_t)((r1 - r0) * row) * 4, cudaMemcpyDeviceToHost,
-                                     sc->copy), "copy output"))
+            !copy_to_host(out + r0 * row, ctx->dbuf + r0 * row, (size_t)((r1 - r0) * row) * 4, sc->copy))
             return false;
     }
     if (!cuda_ok(cudaMemcpyAsync(sc->hmm, sc->dmm, 2 * slabs * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream), "copy minmax") ||
@@ -178,7 +239,7 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
         }
         for (int k = 0; k < args.dim; ++k) {
             if (!hpos[k]) { set_error(FN_ERR_ARG, "null position array"); fill_nan(out, total, minmax); return; }
-            if (!cuda_ok(cudaMemcpyAsync(ctx->dpos[k], hpos[k], (size_t)total * 4, cudaMemcpyHostToDevice, ctx->stream), "copy positions")) {
+            if (!copy_host(hpos[k], ctx->dpos[k], (size_t)total * 4, false, ctx->stream, "copy positions")) {
                 fill_nan(out, total, minmax);
                 return;
             }
@@ -191,7 +252,7 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
     }
     // the kernel's last block stores the min/max straight into pinned host memory when it can
     if (!cuda_ok(launch_points(prog, args, ctx->dbuf, work, ctx->hminmax_dev, ctx->stream), "launch")) { fill_nan(out, total, minmax); return; }
-    if (total > 0 && !cuda_ok(cudaMemcpyAsync(out, ctx->dbuf, (size_t)total * 4, cudaMemcpyDeviceToHost, ctx->stream), "copy output")) { fill_nan(out, total, minmax); return; }
+    if (total > 0 && !copy_to_host(out, ctx->dbuf, (size_t)total * 4, ctx->stream)) { fill_nan(out, total, minmax); return; }
     if ((!ctx->hminmax_dev &&
          !cuda_ok(cudaMemcpyAsync(ctx->hminmax, work->result, 8, cudaMemcpyDeviceToHost, ctx->stream), "copy minmax")) ||
         !cuda_ok(cudaStreamSynchronize(ctx->stream), "synchronize")) {
@@ -889,9 +950,7 @@ int fnGenBatchHost(const fnGenRequest* requests, int count, int flags)
             size_t n = points[(size_t)j];
             int e = j + 1;
             while (e < i1 && points[(size_t)e] && requests[e].out == dst + n) n += points[(size_t)e++];
-            if (n && !cuda_ok(cudaMemcpyAsync(dst, h->stage[buf] + src, n * sizeof(float), cudaMemcpyDeviceToHost, h->copy),
-                              "copy output"))
-                return FN_ERR_CUDA;
+            if (n && !copy_to_host(dst, h->stage[buf] + src, n * sizeof(float), h->copy)) return FN_ERR_CUDA;
             src += n;
             j = e;
         }

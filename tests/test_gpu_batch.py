@@ -102,11 +102,12 @@ def test_bad_request_fails_loudly(gpu, torch_cuda):
         fn.gen_batch([fn.make_request(node, fn.KIND_GRID2D, out.data_ptr(), 1, (4, 4))])
 
 
-@pytest.mark.parametrize("contiguous", [True, False])
-def test_batch_host_outputs_match_device_batch(gpu, torch_cuda, contiguous):
-    """fnGenBatchHost: host outputs (contiguous runs copied together, or separate arrays), slices
-    across both staging buffers (the mix is larger than one 2^25-point slice), a request larger
-    than a slice, and empty requests; outputs and min/max equal the device batch's."""
+@pytest.mark.parametrize("mode", ["pinned", "pageable", "pinned-and-pageable"])
+def test_batch_host_outputs_match_device_batch(gpu, torch_cuda, mode):
+    """fnGenBatchHost: outputs in one page-locked block (contiguous runs copied together),
+    separate pageable arrays, or one request outside the page-locked block; slices across both
+    staging buffers (the mix is larger than one 2^25-point slice), a request larger than a
+    slice, and empty requests; outputs and min/max equal the device batch's."""
     fn, torch = gpu, torch_cuda
     chunks = chunkmix.make_mix(40, seed=19, sizes=[(128, 128, 64), (96, 80, 70), (0, 5, 5), (17, 3)])
     chunks.append(chunkmix.Chunk(tree=1, count=(384, 320, 300), offset=(-5.0, 7.0, 3.0), seed=77))   # 36.9 M points
@@ -115,9 +116,11 @@ def test_batch_host_outputs_match_device_batch(gpu, torch_cuda, contiguous):
     fn.gen_batch(dreqs, sync=True)
     total = sum(c.points for c in chunks)
     block = torch.empty(max(total, 1), dtype=torch.float32, pin_memory=True).numpy()
+    block[:] = np.nan
     hreqs, houts, hmms, off = [], [], [], 0
-    for c in chunks:
-        out = block[off:off + c.points] if contiguous else np.empty(c.points, np.float32)
+    for k, c in enumerate(chunks):
+        pinned = mode.startswith("pinned") and not (mode == "pinned-and-pageable" and k == 7)
+        out = block[off:off + c.points] if pinned else np.empty(c.points, np.float32)
         off += c.points
         mm = np.zeros(2, np.float32)
         kind = fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D
@@ -130,6 +133,29 @@ def test_batch_host_outputs_match_device_batch(gpu, torch_cuda, contiguous):
     for c, dout, dmm, hout, hmm in zip(chunks, douts, dmms, houts, hmms):
         assert np.array_equal(hout.view(np.uint32), dout.cpu().numpy().view(np.uint32)), c
         assert (hmm[0], hmm[1]) == (dmm[0], dmm[1]), c
+
+
+def test_batch_host_outputs_across_a_registered_range(gpu, torch_cuda):
+    """Host outputs in an application buffer page-locked in part by cudaHostRegister: inside the
+    registered bytes, and starting inside them but running past their end (the copy is cut at
+    the end of the registered range; the rest goes to pageable memory)."""
+    fn, torch = gpu, torch_cuda
+    cudart = torch.cuda.cudart()
+    node = trees.to_product(trees.MIX_TREES[2]())
+    n = 96 * 80 * 70
+    buf = np.empty(2 * n + 1024, np.float32)
+    assert int(cudart.cudaHostRegister(buf.ctypes.data, (n + 512) * 4, 0)) == 0
+    try:
+        ref, rmm = node.gen_uniform_grid((1.0, 2.0, 3.0), (96, 80, 70), (1, 1, 1), 5)
+        for start in (0, 512, n // 2, n + 1024):    # inside; inside; running past the registered end; pageable
+            out = buf[start:start + n]
+            out[:] = np.nan
+            mm = np.zeros(2, np.float32)
+            fn.gen_batch_host([fn.make_request(node, fn.KIND_GRID3D, out.ctypes.data, 5, (96, 80, 70), (1.0, 2.0, 3.0),
+                                               (1, 1, 1, 1), minmax=mm)])
+            assert np.array_equal(out.view(np.uint32), ref.view(np.uint32)) and (float(mm[0]), float(mm[1])) == rmm
+    finally:
+        cudart.cudaHostUnregister(buf.ctypes.data)
 
 
 def test_autotune_picks_a_batch_kernel_variant_per_tree(gpu, torch_cuda, tmp_path):
