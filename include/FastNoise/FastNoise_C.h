@@ -444,8 +444,8 @@ FASTNOISE_API int fnSetJitEnabled(int enabled);
  * - NULL stream: the legacy default stream, as for fnGenUniformGrid3DDevice.
  * - Limit: the tree's compiled program must fit 16 KiB (several hundred nodes);
  *   larger trees return FN_ERR_CAPACITY without touching the GPU.
- * - The first call on a device looks up that device's array; make that first
- *   call before any stream capture begins.
+ * - Not for use while `stream` is being captured into a CUDA graph: each call
+ *   uploads the program from pageable host memory that the next call reuses.
  * - Every call shares the array and it keeps the last call's contents; calls
  *   ordered on one stream are safe, calls that overlap on the GPU (different
  *   streams without ordering between them) race and give wrong results.
