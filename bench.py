@@ -91,7 +91,14 @@ class ClockSampler:
                                           "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
-        time.sleep(0.3)
+        # nvidia-smi's start-up can take seconds on a fresh host and stalls GPU work while it
+        # runs: wait for its first sample so that the start-up stays outside the timed region
+        t0 = time.time()
+        while self.proc and self.proc.poll() is None and time.time() - t0 < 30.0:
+            if os.path.getsize(self.path) > 0:
+                break
+            time.sleep(0.05)
+        time.sleep(0.2)
         return self
 
     def __exit__(self, *exc):
@@ -408,8 +415,11 @@ def run_chunkmix(a, rank, world, local):
             en[i].record(stream)
             torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize(dev)
-        return statistics.mean(s.elapsed_time(e) for s, e in zip(st, en))
+        ms = [s.elapsed_time(e) for s, e in zip(st, en)]
+        spread[label] = {"min": min(ms), "median": statistics.median(ms), "max": max(ms)}
+        return statistics.mean(ms)
 
+    spread = {}
     sampler = ClockSampler(local)
     with sampler:
         barrier(world)
@@ -503,7 +513,7 @@ def run_chunkmix(a, rank, world, local):
     line = {
         "metric": "Mpoints/s", "value": value, "unit": "Mpoints/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": batch_ms_max, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "step_ms": spread.get("batched"),
         "config": {"workload": "chunk-mix", "requests": len(chunks), "points_per_step": pts,
                    "trees": [m.__name__ for m in trees.MIX_TREES], "rng": "numpy PCG64(20261203)",
                    "l2": "flushed between steps (256 MiB write outside the timed events)",
