@@ -107,6 +107,8 @@ def _declare(L):
         "fnBuildChunkMeshHeightmap": (c_int, [vp, c_int, c_int, c_int, c_int, c_float, vp, vp]),
         "fnGetBatchInfo": (c_int, [vp]),
         "fnJitCheck": (c_int, [vp, vp, c_int, ctypes.POINTER(c_int)]),
+        "fnJitSetCacheDir": (c_int, [ctypes.c_char_p]),
+        "fnJitGetCacheInfo": (c_int, [ctypes.c_char_p, c_int, ctypes.POINTER(ctypes.c_ulonglong), ctypes.POINTER(ctypes.c_ulonglong)]),
         "fnSetJitEnabled": (c_int, [c_int]),
         "fnSetAutoSpecialise": (c_int, [c_int]),
         "fnAutoSpecialiseWait": (c_int, [c_int]),
@@ -300,6 +302,19 @@ def autotune_save(path: str) -> None:
 def autotune_load(path: str) -> None:
     if lib().fnAutotuneLoad(str(path).encode()) != 0:
         raise FastNoiseError(-1, f"could not read {path}")
+
+
+def jit_set_cache_dir(path) -> None:
+    """fnJitSetCacheDir: the on-disk cache of specialised modules for this process (None = off)."""
+    lib().fnJitSetCacheDir(None if path is None else str(path).encode())
+
+
+def jit_cache_info() -> dict:
+    """fnJitGetCacheInfo: the cache directory in use ("" = off) and this process's hits and misses."""
+    buf = ctypes.create_string_buffer(4096)
+    hits, misses = ctypes.c_ulonglong(0), ctypes.c_ulonglong(0)
+    lib().fnJitGetCacheInfo(buf, len(buf), ctypes.byref(hits), ctypes.byref(misses))
+    return {"dir": buf.value.decode(), "hits": hits.value, "misses": misses.value}
 
 
 def jit_check(pairs) -> int:

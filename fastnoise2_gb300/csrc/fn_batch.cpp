@@ -189,6 +189,8 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
     std::vector<BatchKernel> kernels(n);
     bool jit = true;
     for (size_t i = 0; jit && i < n; ++i) jit = items[i].args.total < (1ll << 32);   // 32-bit point indices
+    for (size_t i = 0; jit && i < n; ++i)               // trees an earlier process specialised: from the cache
+        if (!jit_is_specialised(progs[i].hash)) jit_try_cached(progs[i].host);
     {
         const int forced = tuning_in ? tuning_in->variant : -1;
         std::map<uint64_t, BatchKernel> chosen;

@@ -129,6 +129,8 @@ cudaError_t launch_points(const DeviceProgram& prog, const PointArgs& args, floa
 {
     cudaError_t e;
     if (jit_launch(prog.hash, args, out, work, dminmax, stream, e)) return e;
+    // the first call on a tree that an earlier process specialised: its kernels from the cache
+    if (args.total > 0 && jit_try_cached(prog.host) && jit_launch(prog.hash, args, out, work, dminmax, stream, e)) return e;
     // A tree with per-cell sub-programs cannot run on the interpreter; with no
     // points there is nothing to evaluate and the interpreter only writes min/max.
     if (prog.host->needs_specialisation() && args.total > 0) return cudaErrorNotSupported;
@@ -1497,6 +1499,26 @@ int fnJitIsSpecialised(const void* node, int dimension)
     std::string err;
     if (!compile_program(N(node), dimension, prog, err)) { set_error(FN_ERR_COMPILE, err); return FN_ERR_COMPILE; }
     return jit_is_specialised(prog.hash) ? 1 : 0;
+}
+
+int fnJitSetCacheDir(const char* dir)
+{
+    clear_error();
+    jit_cache_set_dir(dir);
+    return FN_OK;
+}
+
+int fnJitGetCacheInfo(char* dir, int dirBytes, unsigned long long* hits, unsigned long long* misses)
+{
+    clear_error();
+    const std::string d = jit_cache_dir();
+    if (dir && dirBytes > 0) {
+        const size_t n = std::min(d.size(), (size_t)dirBytes - 1);
+        std::memcpy(dir, d.data(), n);
+        dir[n] = '\0';
+    }
+    jit_cache_stats(hits, misses);
+    return (int)std::min<size_t>(d.size(), 0x7FFFFFFF);
 }
 
 int fnJitCheck(const void* const* nodes, const int* dims, int count, int* cubinBytes)

@@ -13,11 +13,15 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <mutex>
 #include <sstream>
 #include <thread>
 #include <unordered_map>
 #include <unordered_set>
+
+#include <sys/stat.h>
+#include <unistd.h>
 
 #include "fn_kernels.cuh"
 #include "fn_runtime.h"
@@ -521,6 +525,141 @@ std::string jit_percall_source(const CompiledProgram& prog)
     return o.str();
 }
 
+// ---------------------------------------------------------------- on-disk module cache
+// Compiled modules are kept on disk, keyed by their CUDA source (which embeds the node
+// library's device code), the NVRTC options and the NVRTC version, so a module that any
+// earlier process built loads in milliseconds instead of being compiled again.  File:
+// "FNJC", format version, the 128-bit key, payload size, the cubin, a checksum of the cubin;
+// a file that does not check out is ignored (and replaced by the next compile).
+namespace {
+
+constexpr uint32_t kCacheFormat = 1;
+const char* const kNvrtcOptions[] = {"--gpu-architecture=sm_103a", "-fmad=false", "--std=c++17", "-default-device",
+                                     "-lineinfo", "-diag-suppress=177"};
+
+struct CacheKey {
+    uint64_t a = 0, b = 0;
+};
+
+uint64_t fnv1a(const void* data, size_t n, uint64_t h)
+{
+    const unsigned char* p = static_cast<const unsigned char*>(data);
+    for (size_t i = 0; i < n; ++i) h = (h ^ p[i]) * 0x100000001B3ull;
+    return h;
+}
+
+CacheKey cache_key(const std::string& src)
+{
+    int major = 0, minor = 0;
+    nvrtcVersion(&major, &minor);
+    std::string salt = "nvrtc " + std::to_string(major) + "." + std::to_string(minor) + " format " + std::to_string(kCacheFormat);
+    for (const char* o : kNvrtcOptions) salt += std::string(" ") + o;
+    CacheKey k;
+    k.a = fnv1a(src.data(), src.size(), fnv1a(salt.data(), salt.size(), 0xCBF29CE484222325ull));
+    k.b = fnv1a(src.data(), src.size(), fnv1a(salt.data(), salt.size(), 0x84222325CBF29CE4ull ^ 0x9E3779B97F4A7C15ull));
+    return k;
+}
+
+std::mutex g_cache_mu;
+bool g_cache_resolved = false;
+std::string g_cache_dir;                  // empty: off
+std::atomic<unsigned long long> g_cache_hits{0}, g_cache_misses{0};
+
+void make_dirs(const std::string& dir)
+{
+    for (size_t i = 1; i <= dir.size(); ++i)
+        if (i == dir.size() || dir[i] == '/') mkdir(dir.substr(0, i).c_str(), 0755);   // existing parts fail harmlessly
+}
+
+std::string cache_dir()
+{
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    if (!g_cache_resolved) {
+        g_cache_resolved = true;
+        // off unless the application names a directory: a library writes no files of its own
+        const char* env = std::getenv("FASTNOISE_JIT_CACHE");
+        if (env && *env && std::strcmp(env, "off") != 0) g_cache_dir = env;
+        if (!g_cache_dir.empty()) make_dirs(g_cache_dir);
+    }
+    return g_cache_dir;
+}
+
+std::string cache_path(const std::string& dir, const CacheKey& k)
+{
+    char name[64];
+    std::snprintf(name, sizeof name, "/%016llx%016llx.cubin", (unsigned long long)k.a, (unsigned long long)k.b);
+    return dir + name;
+}
+
+bool cache_read(const std::string& path, const CacheKey& k, std::vector<char>& cubin)
+{
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    char magic[4];
+    uint32_t format = 0;
+    uint64_t ka = 0, kb = 0, size = 0, sum = 0;
+    if (!f.read(magic, 4) || std::memcmp(magic, "FNJC", 4) != 0 || !f.read(reinterpret_cast<char*>(&format), 4) ||
+        format != kCacheFormat || !f.read(reinterpret_cast<char*>(&ka), 8) || !f.read(reinterpret_cast<char*>(&kb), 8) ||
+        ka != k.a || kb != k.b || !f.read(reinterpret_cast<char*>(&size), 8) || size == 0 || size > (uint64_t(1) << 30))
+        return false;
+    std::vector<char> data((size_t)size);
+    if (!f.read(data.data(), (std::streamsize)size) || !f.read(reinterpret_cast<char*>(&sum), 8) ||
+        sum != fnv1a(data.data(), data.size(), 0xCBF29CE484222325ull))
+        return false;
+    cubin.swap(data);
+    return true;
+}
+
+void cache_write(const std::string& path, const CacheKey& k, const std::vector<char>& cubin)
+{
+    // written under a name of its own, then renamed: readers see a whole file or none
+    const std::string tmp = path + ".tmp" + std::to_string((long long)getpid()) + "_" +
+                            std::to_string(std::hash<std::thread::id>()(std::this_thread::get_id()));
+    {
+        std::ofstream f(tmp, std::ios::binary | std::ios::trunc);
+        if (!f) return;
+        const uint64_t size = cubin.size(), sum = fnv1a(cubin.data(), cubin.size(), 0xCBF29CE484222325ull);
+        f.write("FNJC", 4);
+        f.write(reinterpret_cast<const char*>(&kCacheFormat), 4);
+        f.write(reinterpret_cast<const char*>(&k.a), 8);
+        f.write(reinterpret_cast<const char*>(&k.b), 8);
+        f.write(reinterpret_cast<const char*>(&size), 8);
+        f.write(cubin.data(), (std::streamsize)cubin.size());
+        f.write(reinterpret_cast<const char*>(&sum), 8);
+        if (!f) { f.close(); std::remove(tmp.c_str()); return; }
+    }
+    if (std::rename(tmp.c_str(), path.c_str()) != 0) std::remove(tmp.c_str());
+}
+
+// A module from the cache only (no compile); false on a miss.
+bool cached_cubin(const std::string& src, std::vector<char>& cubin)
+{
+    const std::string dir = cache_dir();
+    if (dir.empty()) return false;
+    const CacheKey k = cache_key(src);
+    if (!cache_read(cache_path(dir, k), k, cubin)) return false;
+    g_cache_hits.fetch_add(1);
+    return true;
+}
+
+}  // namespace
+
+void jit_cache_set_dir(const char* dir)
+{
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    g_cache_resolved = true;
+    g_cache_dir = (!dir || !*dir || std::strcmp(dir, "off") == 0) ? std::string() : std::string(dir);
+    if (!g_cache_dir.empty()) make_dirs(g_cache_dir);
+}
+
+std::string jit_cache_dir() { return cache_dir(); }
+
+void jit_cache_stats(unsigned long long* hits, unsigned long long* misses)
+{
+    if (hits) *hits = g_cache_hits.load();
+    if (misses) *misses = g_cache_misses.load();
+}
+
 bool jit_compile_all(const std::vector<const CompiledProgram*>& progs, std::vector<std::vector<char>>& cubins, std::string& error)
 {
     // source 0 = the batch module, 1 + k = program k's per-call module; NVRTC
@@ -548,17 +687,18 @@ bool jit_compile_all(const std::vector<const CompiledProgram*>& progs, std::vect
 
 bool jit_compile_cubin(const std::string& src, std::vector<char>& cubin, std::string& log)
 {
+    // FASTNOISE_JIT_VERBOSE=1 prints ptxas' register / spill report of every
+    // specialised kernel to stderr (useful when tuning trees); it always compiles.
+    const char* verbose = std::getenv("FASTNOISE_JIT_VERBOSE");
+    const bool v = verbose && verbose[0] == '1';
+    if (!v && cached_cubin(src, cubin)) return true;
+    const std::string dir = cache_dir();
     nvrtcProgram prog;
     if (nvrtcCreateProgram(&prog, src.c_str(), "fastnoise_jit.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
         log = "nvrtcCreateProgram failed";
         return false;
     }
-    // FASTNOISE_JIT_VERBOSE=1 prints ptxas' register / spill report of every
-    // specialised kernel to stderr (useful when tuning trees).
-    const char* verbose = std::getenv("FASTNOISE_JIT_VERBOSE");
-    const bool v = verbose && verbose[0] == '1';
-    std::vector<const char*> opts = {"--gpu-architecture=sm_103a", "-fmad=false", "--std=c++17", "-default-device",
-                                     "-lineinfo", "-diag-suppress=177"};
+    std::vector<const char*> opts(std::begin(kNvrtcOptions), std::end(kNvrtcOptions));
     if (v) opts.push_back("--ptxas-options=-v");
     nvrtcResult rc = nvrtcCompileProgram(prog, (int)opts.size(), opts.data());
     size_t loglen = 0;
@@ -575,14 +715,20 @@ bool jit_compile_cubin(const std::string& src, std::vector<char>& cubin, std::st
     cubin.resize(n);
     nvrtcGetCUBIN(prog, cubin.data());
     nvrtcDestroyProgram(&prog);
+    g_cache_misses.fetch_add(1);
+    if (!dir.empty() && n > 0) {
+        const CacheKey k = cache_key(src);
+        cache_write(cache_path(dir, k), k, cubin);
+    }
     return true;
 }
 
-bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& error)
+namespace {
+
+// Load the batch module (cubins[0]) and the per-call modules (cubins[1 + k]) of `progs` and
+// register their kernels.
+bool jit_load(const std::vector<const CompiledProgram*>& progs, const std::vector<std::vector<char>>& cubins, std::string& error)
 {
-    if (progs.empty()) return true;
-    std::vector<std::vector<char>> cubins;
-    if (!jit_compile_all(progs, cubins, error)) return false;
     std::vector<std::unique_ptr<Module>> mods;
     for (auto& c : cubins) {
         auto mod = std::make_unique<Module>();
@@ -634,6 +780,38 @@ bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& er
     }
     for (auto& m : mods) g_modules.push_back(std::move(m));   // modules stay loaded: kernels may still be queued
     return true;
+}
+
+std::mutex g_build_mu;                           // one build per program, even with concurrent first calls
+
+}  // namespace
+
+bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& error)
+{
+    if (progs.empty()) return true;
+    std::vector<std::vector<char>> cubins;
+    if (!jit_compile_all(progs, cubins, error)) return false;
+    return jit_load(progs, cubins, error);
+}
+
+bool jit_try_cached(const CompiledProgram* prog)
+{
+    if (!prog || !g_enabled.load(std::memory_order_relaxed) || cache_dir().empty()) return false;
+    static std::mutex tried_mu;
+    static std::unordered_set<uint64_t> tried;          // one look per program and process
+    {
+        std::lock_guard<std::mutex> lk(tried_mu);
+        if (!tried.insert(prog->hash).second) return false;
+    }
+    std::lock_guard<std::mutex> lk(g_build_mu);
+    {
+        std::lock_guard<std::mutex> rk(g_jit_mu);
+        if (g_kernels.count(prog->hash) && g_batch_kernels.count(prog->hash)) return true;
+    }
+    std::vector<std::vector<char>> cubins(2);
+    if (!cached_cubin(jit_batch_source({prog}, 0), cubins[0]) || !cached_cubin(jit_percall_source(*prog), cubins[1])) return false;
+    std::string err;
+    return jit_load({prog}, cubins, err);
 }
 
 bool jit_build_batch_variants(const std::vector<const CompiledProgram*>& progs, std::string& error)
@@ -733,8 +911,7 @@ bool jit_ensure(const CompiledProgram* prog, std::string& error)
                 "can do, and specialisation is disabled";
         return false;
     }
-    static std::mutex build_mu;                 // one build per program, even with concurrent first calls
-    std::lock_guard<std::mutex> lk(build_mu);
+    std::lock_guard<std::mutex> lk(g_build_mu);
     {
         std::lock_guard<std::mutex> rk(g_jit_mu);
         if (g_kernels.count(prog->hash) && g_batch_kernels.count(prog->hash)) return true;

@@ -64,6 +64,16 @@ bool jit_compile_all(const std::vector<const CompiledProgram*>& progs, std::vect
 // per-call kernels and a batch kernel.  Thread safe.
 bool jit_build(const std::vector<const CompiledProgram*>& progs, std::string& error);
 
+// On-disk module cache (see fn_jit.cpp): the directory in use ("" = off, the default; the
+// environment variable FASTNOISE_JIT_CACHE names one),
+// its hit / miss counts in this process, and the tree's kernels loaded straight from the
+// cache when an earlier process built them alone (the way automatic specialisation does):
+// true when they are loaded now.  Looks once per program and process.
+void jit_cache_set_dir(const char* dir);
+std::string jit_cache_dir();
+void jit_cache_stats(unsigned long long* hits, unsigned long long* misses);
+bool jit_try_cached(const CompiledProgram* prog);
+
 // Build variants 1.. of the batch kernels of `progs` (NVRTC, one module per variant,
 // compiled concurrently); programs whose variants exist are skipped.  Thread safe.
 bool jit_build_batch_variants(const std::vector<const CompiledProgram*>& progs, std::string& error);

@@ -423,6 +423,19 @@ FASTNOISE_API int fnAutoSpecialiseWait(int timeoutMs);
 /* 1 when the tree's specialised kernels for `dimension` are loaded, 0 when calls run on the
  * interpreter, FN_ERR_* on error. */
 FASTNOISE_API int fnJitIsSpecialised(const void* node, int dimension);
+/* On-disk cache of the specialised modules: each compiled module is kept in a directory,
+ * keyed by its CUDA source, the NVRTC options and the NVRTC version.  A later process loads
+ * it instead of compiling (milliseconds instead of seconds), and a tree that an earlier
+ * process specialised alone (as automatic specialisation does) runs its specialised kernels
+ * from its first call, without interpreted calls.  Off by default (the library writes no
+ * files of its own); the environment variable FASTNOISE_JIT_CACHE names a directory, created
+ * if missing, and fnJitSetCacheDir sets or replaces it for this process (NULL, "" or "off":
+ * off).
+ * fnJitGetCacheInfo copies the directory in use into dir (dirBytes with the terminating zero;
+ * dir may be NULL), fills this process's cache hits and misses (either may be NULL), and
+ * returns the directory's length (0 = off). */
+FASTNOISE_API int fnJitSetCacheDir(const char* dir);
+FASTNOISE_API int fnJitGetCacheInfo(char* dir, int dirBytes, unsigned long long* hits, unsigned long long* misses);
 /* Generate and compile the module source with NVRTC without loading it (no GPU needed);
  * *cubinBytes (may be NULL) receives the size of the compiled code. */
 FASTNOISE_API int fnJitCheck(const void* const* nodes, const int* dimensions, int count, int* cubinBytes);

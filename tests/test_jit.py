@@ -185,6 +185,79 @@ def test_automatic_specialisation(gpu):
         fn.set_auto_specialise(old)
 
 
+def test_module_cache(native, tmp_path):
+    """The on-disk cache of specialised modules: a compile writes each module (batch and
+    per-call) once; the same sources later load from the cache; a damaged file is ignored
+    and rewritten; with the cache off nothing is read."""
+    fn = native
+    pairs = [(trees.to_product(N("FractalFBm", Source=N("Perlin", Feature_Scale=31.0), Octaves=2)), 3)]
+    fn.jit_set_cache_dir(tmp_path)
+    try:
+        assert fn.jit_cache_info()["dir"] == str(tmp_path)
+        i0 = fn.jit_cache_info()
+        size = fn.jit_check(pairs)
+        i1 = fn.jit_cache_info()
+        assert (i1["misses"] - i0["misses"], i1["hits"] - i0["hits"]) == (2, 0)
+        files = sorted(tmp_path.glob("*.cubin"))
+        assert len(files) == 2 and not list(tmp_path.glob("*.tmp*"))
+        assert fn.jit_check(pairs) == size
+        i2 = fn.jit_cache_info()
+        assert (i2["misses"] - i1["misses"], i2["hits"] - i1["hits"]) == (0, 2)
+        whole = files[0].read_bytes()
+        files[0].write_bytes(whole[: len(whole) // 2])
+        assert fn.jit_check(pairs) == size
+        i3 = fn.jit_cache_info()
+        assert (i3["misses"] - i2["misses"], i3["hits"] - i2["hits"]) == (1, 1)
+        assert files[0].read_bytes() == whole
+        fn.jit_set_cache_dir(None)
+        assert fn.jit_cache_info()["dir"] == ""
+        fn.jit_check(pairs)
+        i4 = fn.jit_cache_info()
+        assert (i4["misses"] - i3["misses"], i4["hits"] - i3["hits"]) == (2, 0)
+    finally:
+        fn.jit_set_cache_dir(None)
+
+
+_CACHE_CHILD = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+import fastnoise2_gb300 as fn
+from oracle.tree import N
+from tests import trees
+fn.jit_set_cache_dir(sys.argv[2])
+node = trees.to_product(N("FractalRidged", Source=N("Simplex", Feature_Scale=17.0), Octaves=3))
+args = ((2.0, -5.0, 9.0), (40, 36, 30), (1.0, 1.0, 1.0), 11)
+if sys.argv[3] == "warm":                      # specialise in the background, which writes the cache
+    fn.set_auto_specialise(1)
+    node.gen_uniform_grid(*args)
+    assert fn.auto_specialise_wait(120000) and fn.is_specialised(node, 3)
+else:                                          # a fresh process: specialised from the first call
+    fn.set_auto_specialise(0)
+    assert not fn.is_specialised(node, 3)
+    first, fmm = node.gen_uniform_grid(*args)
+    assert fn.is_specialised(node, 3), "not loaded from the cache"
+    assert fn.jit_cache_info()["hits"] == 2
+    fn.set_jit_enabled(False)
+    ref, rmm = node.gen_uniform_grid(*args)
+    assert np.array_equal(first.view(np.uint32), ref.view(np.uint32)) and fmm == rmm
+print("ok")
+"""
+
+
+@pytest.mark.gpu
+def test_cached_modules_specialise_the_first_call(gpu, tmp_path):
+    """A tree specialised by one process runs its specialised kernels from the first call in
+    the next process that uses the same cache directory, with the interpreter's results."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    for phase in ("warm", "cold"):
+        r = subprocess.run([sys.executable, "-c", _CACHE_CHILD, root, str(tmp_path), phase], capture_output=True, text=True,
+                           timeout=600, cwd=root)
+        assert r.returncode == 0 and r.stdout.strip().endswith("ok"), (phase, r.stdout, r.stderr)
+
+
 def test_automatic_specialisation_controls(native):
     fn = native
     old = fn.set_auto_specialise(0)
