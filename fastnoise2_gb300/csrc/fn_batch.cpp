@@ -189,8 +189,6 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
     std::vector<BatchKernel> kernels(n);
     bool jit = true;
     for (size_t i = 0; jit && i < n; ++i) jit = items[i].args.total < (1ll << 32);   // 32-bit point indices
-    for (size_t i = 0; jit && i < n; ++i)               // trees an earlier process specialised: from the cache
-        if (!jit_is_specialised(progs[i].hash)) jit_try_cached(progs[i].host);
     {
         const int forced = tuning_in ? tuning_in->variant : -1;
         std::map<uint64_t, BatchKernel> chosen;
@@ -200,6 +198,8 @@ int BatchRunner::launch(const std::vector<BatchItem>& items, cudaStream_t stream
                 BatchKernel bk;
                 const int v = forced >= 0 ? forced : Autotuner::instance().tree_variant(progs[i].hash);
                 bool ok = jit_batch_kernel(progs[i].hash, v, bk);
+                if (!ok && !jit_is_specialised(progs[i].hash) && jit_try_cached(progs[i].host))   // an earlier process built it
+                    ok = jit_batch_kernel(progs[i].hash, v, bk);
                 if (!ok && v != 0) {
                     if (forced < 0) jit_request_batch_variants(progs[i].host);
                     ok = jit_batch_kernel(progs[i].hash, 0, bk);
