@@ -225,29 +225,41 @@ import fastnoise2_gb300 as fn
 from oracle.tree import N
 from tests import trees
 fn.jit_set_cache_dir(sys.argv[2])
+import torch
 node = trees.to_product(N("FractalRidged", Source=N("Simplex", Feature_Scale=17.0), Octaves=3))
+other = trees.to_product(N("CellularDistance", Feature_Scale=13.0))
 args = ((2.0, -5.0, 9.0), (40, 36, 30), (1.0, 1.0, 1.0), 11)
+out = torch.empty(40 * 36 * 30, dtype=torch.float32, device="cuda")
+batch = [fn.make_request(other, fn.KIND_GRID3D, out.data_ptr(), 12, args[1], args[0], (1, 1, 1))]
 if sys.argv[3] == "warm":                      # specialise in the background, which writes the cache
     fn.set_auto_specialise(1)
     node.gen_uniform_grid(*args)
-    assert fn.auto_specialise_wait(120000) and fn.is_specialised(node, 3)
+    fn.gen_batch(batch, sync=True)
+    assert fn.auto_specialise_wait(120000) and fn.is_specialised(node, 3) and fn.is_specialised(other, 3)
 else:                                          # a fresh process: specialised from the first call
     fn.set_auto_specialise(0)
-    assert not fn.is_specialised(node, 3)
+    assert not fn.is_specialised(node, 3) and not fn.is_specialised(other, 3)
     first, fmm = node.gen_uniform_grid(*args)
-    assert fn.is_specialised(node, 3), "not loaded from the cache"
-    assert fn.jit_cache_info()["hits"] == 2
+    assert fn.is_specialised(node, 3), "per-call: not loaded from the cache"
+    fn.gen_batch(batch, sync=True)
+    assert fn.batch_info()["specialised"] == 1, "batch: not loaded from the cache"
+    assert fn.jit_cache_info()["hits"] == 4
+    got = out.cpu().numpy().copy()
     fn.set_jit_enabled(False)
     ref, rmm = node.gen_uniform_grid(*args)
     assert np.array_equal(first.view(np.uint32), ref.view(np.uint32)) and fmm == rmm
+    fn.gen_batch(batch, sync=True)
+    assert fn.batch_info()["specialised"] == 0
+    assert np.array_equal(got.view(np.uint32), out.cpu().numpy().view(np.uint32))
 print("ok")
 """
 
 
 @pytest.mark.gpu
 def test_cached_modules_specialise_the_first_call(gpu, tmp_path):
-    """A tree specialised by one process runs its specialised kernels from the first call in
-    the next process that uses the same cache directory, with the interpreter's results."""
+    """Trees specialised by one process run their specialised kernels from the first call
+    (per-call and batch) in the next process that uses the same cache directory, with the
+    interpreter's results."""
     import os
     import subprocess
     import sys
