@@ -87,6 +87,18 @@ uintptr_t pinned_end(const void* p)
     return (uintptr_t)p + (size_t)(start + size - dp);
 }
 
+// The device address of host memory [p, p + bytes) when the whole range lies in one
+// page-locked allocation the device addresses (cudaHostAlloc, cudaMallocHost, cudaHostRegister),
+// else nullptr.
+float* pinned_device_view(float* p, size_t bytes)
+{
+    cudaPointerAttributes at{};
+    if (!p || cudaPointerGetAttributes(&at, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    const uintptr_t a = (uintptr_t)p, end = pinned_end(p);
+    return (end > a && bytes <= end - a) ? static_cast<float*>(at.devicePointer) : nullptr;
+}
+
 // Copy of `bytes` between device memory and host memory that may start in one page-locked
 // allocation and continue past it (into pageable memory, or another allocation).
 bool copy_host(const void* host, const void* dev, size_t bytes, bool to_host, cudaStream_t s, const char* what)
@@ -230,7 +242,11 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
     DeviceProgram prog;
     if (!ctx || !get_program(N(node), args.dim, prog) || !ensure_runnable(prog)) { fill_nan(out, total, minmax); return; }
     MinMaxWork* work = work_for_stream(ctx->stream);
-    if (!work || !ensure(ctx->dbuf, ctx->dbuf_cap, (size_t)total)) { fill_nan(out, total, minmax); return; }
+    // Outputs in page-locked host memory: the kernel stores into them directly.  One tree's
+    // kernel produces output slower than the host link carries it, so the stores overlap the
+    // generation; there is no device buffer, no copy and no slab pipeline to fill and drain.
+    float* direct = total > 0 ? pinned_device_view(out, (size_t)total * 4) : nullptr;
+    if (!work || (!direct && !ensure(ctx->dbuf, ctx->dbuf_cap, (size_t)total))) { fill_nan(out, total, minmax); return; }
     if (args.src == kSrcPositions && total > 0) {
         if ((size_t)total > ctx->dpos_cap) {
             for (float*& p : ctx->dpos) { if (p) cudaFree(p); p = nullptr; }
@@ -248,13 +264,16 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
             args.pos[k] = ctx->dpos[k];
         }
     }
-    if (args.src == kSrcGrid && total >= 2 * kSlabMinPoints && total < (1ll << 32)) {
+    if (!direct && args.src == kSrcGrid && total >= 2 * kSlabMinPoints && total < (1ll << 32)) {
         if (!gen_host_slabs(prog, args, ctx, work, out, minmax)) fill_nan(out, total, minmax);
         return;
     }
     // the kernel's last block stores the min/max straight into pinned host memory when it can
-    if (!cuda_ok(launch_points(prog, args, ctx->dbuf, work, ctx->hminmax_dev, ctx->stream), "launch")) { fill_nan(out, total, minmax); return; }
-    if (total > 0 && !copy_to_host(out, ctx->dbuf, (size_t)total * 4, ctx->stream)) { fill_nan(out, total, minmax); return; }
+    if (!cuda_ok(launch_points(prog, args, direct ? direct : ctx->dbuf, work, ctx->hminmax_dev, ctx->stream), "launch")) {
+        fill_nan(out, total, minmax);
+        return;
+    }
+    if (!direct && total > 0 && !copy_to_host(out, ctx->dbuf, (size_t)total * 4, ctx->stream)) { fill_nan(out, total, minmax); return; }
     if ((!ctx->hminmax_dev &&
          !cuda_ok(cudaMemcpyAsync(ctx->hminmax, work->result, 8, cudaMemcpyDeviceToHost, ctx->stream), "copy minmax")) ||
         !cuda_ok(cudaStreamSynchronize(ctx->stream), "synchronize")) {

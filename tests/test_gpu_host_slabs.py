@@ -52,3 +52,56 @@ def test_slabbed_host_grid_equals_one_launch(gpu, case, jit):
         pos = float(np.float32(float(r) * float(np.float32(step[-1])) + float(np.float32(offset[-1]))))
         o, _ = OracleTree(root).grid(tuple(offset[:-1]) + (pos,), tuple(count[:-1]) + (1,), step, 42)
         assert np.array_equal(host[r * plane:(r + 1) * plane].view(np.uint32), np.asarray(o, np.float32).view(np.uint32)), r
+
+
+@pytest.mark.parametrize("jit", [True, False])
+def test_host_calls_into_page_locked_memory(gpu, jit):
+    """Host outputs in page-locked memory are written by the kernel directly (no device buffer,
+    no copy, no slabs); outputs and OutputMinMax equal those of the same calls into pageable
+    memory, for grids below and above the slab size, tileable images and position arrays, and
+    an application buffer registered in part (the call whose output runs past the registered
+    bytes takes the staged path)."""
+    torch = pytest.importorskip("torch")
+    fn = gpu
+    root = trees.terrain_c2()
+    node = trees.to_product(root)
+    if jit:
+        fn.jit_compile([(node, d) for d in (2, 3, 4)])
+    old = fn.set_jit_enabled(jit)
+    try:
+        for offset, count, step in [((1.0, 2.0), (300, 200), (1.0, 1.0)), ((-3.0, 4.0, 5.0), (64, 48, 40), (1.0, 0.5, 2.0)),
+                                    ((-100.0, 20.5, -7.0), (200, 160, 300), (1.0, 0.5, 2.0)),
+                                    ((0.0, 0.0, 0.0, 5.0), (16, 12, 10, 7), (1.0, 1.0, 1.0, 1.0))]:
+            n = int(np.prod(count))
+            pinned = torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+            pinned[:] = np.nan
+            a, amm = node.gen_uniform_grid(offset, count, step, 42, out=pinned)
+            b, bmm = node.gen_uniform_grid(offset, count, step, 42)
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)) and amm == bmm, count
+        pinned = torch.empty(96 * 80, dtype=torch.float32, pin_memory=True).numpy()
+        a, amm = node.gen_tileable_2d((96, 80), (1.0, 1.0), 7, out=pinned)
+        b, bmm = node.gen_tileable_2d((96, 80), (1.0, 1.0), 7)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)) and amm == bmm
+        rng = np.random.default_rng(5)
+        xyz = [rng.uniform(-1e4, 1e4, 5000).astype(np.float32) for _ in range(3)]
+        pinned = torch.empty(5000, dtype=torch.float32, pin_memory=True).numpy()
+        a, amm = node.gen_position_array(xyz, (0.5, 0.25, -1.0), 2024, out=pinned)
+        b, bmm = node.gen_position_array(xyz, (0.5, 0.25, -1.0), 2024)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32)) and amm == bmm
+        # an application buffer registered in part: inside the registered bytes, and past them
+        cudart = torch.cuda.cudart()
+        count = (64, 48, 40)
+        n = int(np.prod(count))
+        buf = np.empty(2 * n + 1024, np.float32)
+        assert int(cudart.cudaHostRegister(buf.ctypes.data, (n + 512) * 4, 0)) == 0
+        try:
+            ref, rmm = node.gen_uniform_grid((-3.0, 4.0, 5.0), count, (1.0, 0.5, 2.0), 42)
+            for start in (0, 512, n // 2):
+                out = buf[start:start + n]
+                out[:] = np.nan
+                got, gmm = node.gen_uniform_grid((-3.0, 4.0, 5.0), count, (1.0, 0.5, 2.0), 42, out=out)
+                assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)) and gmm == rmm, start
+        finally:
+            cudart.cudaHostUnregister(buf.ctypes.data)
+    finally:
+        fn.set_jit_enabled(old)
