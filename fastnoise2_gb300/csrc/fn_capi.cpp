@@ -9,12 +9,16 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <map>
 #include <string>
 #include <thread>
 #include <vector>
+
+#include <sys/mman.h>
+#include <unistd.h>
 
 #include <cuda.h>   // CUpointer_attribute: the range query below goes through the runtime's driver entry point
 
@@ -97,6 +101,65 @@ float* pinned_device_view(float* p, size_t bytes)
     if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
     const uintptr_t a = (uintptr_t)p, end = pinned_end(p);
     return (end > a && bytes <= end - a) ? static_cast<float*>(at.devicePointer) : nullptr;
+}
+
+// Host memory the generation kernels may store into directly: page-locked memory (above), or,
+// on devices that access pageable memory coherently through the host's page tables (a Grace
+// host over NVLink-C2C reports both attributes), any host memory.  FASTNOISE_HOST_DIRECT=0
+// turns direct stores off (every host output is then staged in device memory and copied).
+bool pageable_direct_supported()
+{
+    static std::atomic<int> cached[64];                 // per device: 0 unknown, 1 no, 2 yes
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) { cudaGetLastError(); return false; }
+    int v = cached[dev].load(std::memory_order_relaxed);
+    if (v == 0) {
+        int pageable = 0, host_tables = 0;
+        const bool ok = cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) == cudaSuccess &&
+                        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) == cudaSuccess;
+        if (!ok) cudaGetLastError();
+        v = ok && pageable == 1 && host_tables == 1 ? 2 : 1;
+        cached[dev].store(v, std::memory_order_relaxed);
+    }
+    return v == 2;
+}
+
+// True when the pages of [p, p + bytes) are resident (one mincore call; above 64 Ki pages, the
+// first, middle and last page).  A kernel storing into pages nobody has touched yet would
+// populate them one device fault at a time (a fresh 64 MB buffer took 20 ms that way), so such
+// outputs are staged instead and the host touches them.
+bool pages_resident(const void* p, size_t bytes)
+{
+    static const uintptr_t page = (uintptr_t)sysconf(_SC_PAGESIZE);
+    const uintptr_t a = (uintptr_t)p, first = a & ~(page - 1), last = (a + bytes - 1) & ~(page - 1);
+    const size_t pages = (size_t)((last - first) / page) + 1;
+    if (pages <= 65536) {
+        thread_local std::vector<unsigned char> v;
+        v.resize(pages);
+        if (mincore(reinterpret_cast<void*>(first), (size_t)(last - first) + page, v.data()) != 0) return false;
+        for (unsigned char c : v)
+            if (!(c & 1)) return false;
+        return true;
+    }
+    const uintptr_t probes[3] = {first, (a + bytes / 2) & ~(page - 1), last};
+    for (uintptr_t q : probes) {
+        unsigned char c = 0;
+        if (mincore(reinterpret_cast<void*>(q), 1, &c) != 0 || !(c & 1)) return false;
+    }
+    return true;
+}
+
+float* host_direct_view(float* p, size_t bytes)
+{
+    static const bool allowed = [] {
+        const char* env = std::getenv("FASTNOISE_HOST_DIRECT");
+        return !(env && env[0] == '0');
+    }();
+    if (!p || !allowed) return nullptr;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+    if (at.type == cudaMemoryTypeHost) return pinned_device_view(p, bytes);
+    return at.type == cudaMemoryTypeUnregistered && pageable_direct_supported() && pages_resident(p, bytes) ? p : nullptr;
 }
 
 // Copy of `bytes` between device memory and host memory that may start in one page-locked
@@ -242,10 +305,11 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
     DeviceProgram prog;
     if (!ctx || !get_program(N(node), args.dim, prog) || !ensure_runnable(prog)) { fill_nan(out, total, minmax); return; }
     MinMaxWork* work = work_for_stream(ctx->stream);
-    // Outputs in page-locked host memory: the kernel stores into them directly.  One tree's
-    // kernel produces output slower than the host link carries it, so the stores overlap the
+    // Host outputs the device can store into (page-locked memory; any host memory on devices
+    // with coherent pageable access): the kernel stores into them directly.  One tree's kernel
+    // produces output slower than the host link carries it, so the stores overlap the
     // generation; there is no device buffer, no copy and no slab pipeline to fill and drain.
-    float* direct = total > 0 ? pinned_device_view(out, (size_t)total * 4) : nullptr;
+    float* direct = total > 0 ? host_direct_view(out, (size_t)total * 4) : nullptr;
     if (!work || (!direct && !ensure(ctx->dbuf, ctx->dbuf_cap, (size_t)total))) { fill_nan(out, total, minmax); return; }
     if (args.src == kSrcPositions && total > 0) {
         if ((size_t)total > ctx->dpos_cap) {

@@ -56,11 +56,13 @@ def test_slabbed_host_grid_equals_one_launch(gpu, case, jit):
 
 @pytest.mark.parametrize("jit", [True, False])
 def test_host_calls_into_page_locked_memory(gpu, jit):
-    """Host outputs in page-locked memory are written by the kernel directly (no device buffer,
-    no copy, no slabs); outputs and OutputMinMax equal those of the same calls into pageable
-    memory, for grids below and above the slab size, tileable images and position arrays, and
-    an application buffer registered in part (the call whose output runs past the registered
-    bytes takes the staged path)."""
+    """Host outputs the device can store into are written by the kernel directly (no device
+    buffer, no copy, no slabs): page-locked memory, and pageable memory whose pages are
+    resident where the device reads host page tables.  Outputs and OutputMinMax equal those of
+    the same calls into fresh (untouched, so staged) pageable arrays, for grids below and above
+    the slab size, tileable images and position arrays, and an application buffer registered
+    in part (the call whose output runs past the registered bytes does not store into it as
+    page-locked memory)."""
     torch = pytest.importorskip("torch")
     fn = gpu
     root = trees.terrain_c2()
@@ -78,6 +80,9 @@ def test_host_calls_into_page_locked_memory(gpu, jit):
             a, amm = node.gen_uniform_grid(offset, count, step, 42, out=pinned)
             b, bmm = node.gen_uniform_grid(offset, count, step, 42)
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32)) and amm == bmm, count
+            touched = np.full(n, np.nan, np.float32)
+            c, cmm = node.gen_uniform_grid(offset, count, step, 42, out=touched)
+            assert np.array_equal(c.view(np.uint32), b.view(np.uint32)) and cmm == bmm, count
         pinned = torch.empty(96 * 80, dtype=torch.float32, pin_memory=True).numpy()
         a, amm = node.gen_tileable_2d((96, 80), (1.0, 1.0), 7, out=pinned)
         b, bmm = node.gen_tileable_2d((96, 80), (1.0, 1.0), 7)
@@ -105,3 +110,35 @@ def test_host_calls_into_page_locked_memory(gpu, jit):
             cudart.cudaHostUnregister(buf.ctypes.data)
     finally:
         fn.set_jit_enabled(old)
+
+
+_STAGED_CHILD = r"""
+import sys, numpy as np
+sys.path.insert(0, sys.argv[1])
+import fastnoise2_gb300 as fn
+from tests import trees
+node = trees.to_product(trees.terrain_c2())
+out = np.full(64 * 48 * 40, np.nan, np.float32)
+got, mm = node.gen_uniform_grid((-3.0, 4.0, 5.0), (64, 48, 40), (1.0, 0.5, 2.0), 42, out=out)
+np.save(sys.argv[2], np.concatenate([got, np.array(mm, np.float32)]))
+"""
+
+
+def test_host_direct_stores_can_be_turned_off(gpu, tmp_path):
+    """FASTNOISE_HOST_DIRECT=0 stages every host output in device memory and copies it; the
+    results equal the direct stores of this process."""
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    path = tmp_path / "staged.npy"
+    env = dict(os.environ, FASTNOISE_HOST_DIRECT="0")
+    r = subprocess.run([sys.executable, "-c", _STAGED_CHILD, root, str(path)], capture_output=True, text=True, timeout=600,
+                       cwd=root, env=env)
+    assert r.returncode == 0, r.stderr
+    staged = np.load(path)
+    node = trees.to_product(trees.terrain_c2())
+    out = np.full(64 * 48 * 40, np.nan, np.float32)
+    got, mm = node.gen_uniform_grid((-3.0, 4.0, 5.0), (64, 48, 40), (1.0, 0.5, 2.0), 42, out=out)
+    assert np.array_equal(staged[:-2].view(np.uint32), got.view(np.uint32))
+    assert (float(staged[-2]), float(staged[-1])) == mm
