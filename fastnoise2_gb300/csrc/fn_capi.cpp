@@ -311,7 +311,14 @@ void gen_host(const void* node, PointArgs args, float* out, float* minmax, const
     // generation; there is no device buffer, no copy and no slab pipeline to fill and drain.
     float* direct = total > 0 ? host_direct_view(out, (size_t)total * 4) : nullptr;
     if (!work || (!direct && !ensure(ctx->dbuf, ctx->dbuf_cap, (size_t)total))) { fill_nan(out, total, minmax); return; }
-    if (args.src == kSrcPositions && total > 0) {
+    // Position arrays the device can read in place (the same rule as for outputs) are not copied.
+    bool pos_direct = args.src == kSrcPositions && total > 0;
+    for (int k = 0; pos_direct && k < args.dim; ++k) {
+        const float* v = hpos[k] ? host_direct_view(const_cast<float*>(hpos[k]), (size_t)total * 4) : nullptr;
+        pos_direct = v != nullptr;
+        args.pos[k] = v;
+    }
+    if (args.src == kSrcPositions && total > 0 && !pos_direct) {
         if ((size_t)total > ctx->dpos_cap) {
             for (float*& p : ctx->dpos) { if (p) cudaFree(p); p = nullptr; }
             ctx->dpos_cap = 0;

@@ -120,13 +120,17 @@ from tests import trees
 node = trees.to_product(trees.terrain_c2())
 out = np.full(64 * 48 * 40, np.nan, np.float32)
 got, mm = node.gen_uniform_grid((-3.0, 4.0, 5.0), (64, 48, 40), (1.0, 0.5, 2.0), 42, out=out)
-np.save(sys.argv[2], np.concatenate([got, np.array(mm, np.float32)]))
+rng = np.random.default_rng(5)
+xyz = [rng.uniform(-1e4, 1e4, 5000).astype(np.float32) for _ in range(3)]
+pos, pmm = node.gen_position_array(xyz, (0.5, 0.25, -1.0), 2024, out=np.full(5000, np.nan, np.float32))
+np.save(sys.argv[2], np.concatenate([got, np.array(mm, np.float32), pos, np.array(pmm, np.float32)]))
 """
 
 
 def test_host_direct_stores_can_be_turned_off(gpu, tmp_path):
-    """FASTNOISE_HOST_DIRECT=0 stages every host output in device memory and copies it; the
-    results equal the direct stores of this process."""
+    """FASTNOISE_HOST_DIRECT=0 stages every host output in device memory and copies it (and
+    copies position arrays to the device); the results equal the direct stores and in-place
+    position reads of this process."""
     import os
     import subprocess
     import sys
@@ -140,5 +144,11 @@ def test_host_direct_stores_can_be_turned_off(gpu, tmp_path):
     node = trees.to_product(trees.terrain_c2())
     out = np.full(64 * 48 * 40, np.nan, np.float32)
     got, mm = node.gen_uniform_grid((-3.0, 4.0, 5.0), (64, 48, 40), (1.0, 0.5, 2.0), 42, out=out)
-    assert np.array_equal(staged[:-2].view(np.uint32), got.view(np.uint32))
-    assert (float(staged[-2]), float(staged[-1])) == mm
+    rng = np.random.default_rng(5)
+    xyz = [rng.uniform(-1e4, 1e4, 5000).astype(np.float32) for _ in range(3)]      # resident: read in place
+    pos, pmm = node.gen_position_array(xyz, (0.5, 0.25, -1.0), 2024, out=np.full(5000, np.nan, np.float32))
+    n = got.size
+    assert np.array_equal(staged[:n].view(np.uint32), got.view(np.uint32))
+    assert (float(staged[n]), float(staged[n + 1])) == mm
+    assert np.array_equal(staged[n + 2:n + 2 + 5000].view(np.uint32), pos.view(np.uint32))
+    assert (float(staged[-2]), float(staged[-1])) == pmm
