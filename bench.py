@@ -851,9 +851,7 @@ def run_grid(a, rank, world, local):
     ms_max = allmax(ms, world)
     value = pts * world / (ms_max * 1e-3) / 1e6
 
-    e2e_ms = None
-    if a.e2e_steps > 0:
-        host = torch.empty(pts, dtype=torch.float32, pin_memory=True).numpy()
+    def host_ms(host):
         samples = []
         for i in range(3 + a.e2e_steps):
             t0 = time.perf_counter()
@@ -863,7 +861,12 @@ def run_grid(a, rank, world, local):
                 node.gen_tileable_2d(args[0], args[1], seed + rank, out=host)
             if i >= 3:
                 samples.append((time.perf_counter() - t0) * 1e3)
-        e2e_ms = allmax(statistics.median(samples), world)
+        return allmax(statistics.median(samples), world)
+
+    e2e_ms = pageable_ms = None
+    if a.e2e_steps > 0:
+        e2e_ms = host_ms(torch.empty(pts, dtype=torch.float32, pin_memory=True).numpy())
+        pageable_ms = host_ms(np.zeros(pts, np.float32) + 0.0)    # an ordinary (written) array, as a drop-in caller passes
     if rank != 0:
         return
     peaks, peak_src = load_peaks()
@@ -889,7 +892,10 @@ def run_grid(a, rank, world, local):
                              "frac": hbm_gbs / float(peaks.get("hbm_gbs", 6800.0)), "algorithmic_bytes_per_point": 4}},
         "e2e": {"value": pts * world / (e2e_ms * 1e-3) / 1e6 if e2e_ms else None, "unit": "Mpoints/s",
                 "h2d_bytes_per_step": 0, "d2h_bytes_per_step": pts * 4 + 8, "ms_per_step": e2e_ms,
-                "api": "fnGenUniformGrid3D / fnGenTileable2D into pinned host memory"},
+                "api": "fnGenUniformGrid3D / fnGenTileable2D into pinned host memory",
+                "pageable": {"value": pts * world / (pageable_ms * 1e-3) / 1e6 if pageable_ms else None,
+                             "unit": "Mpoints/s", "ms_per_step": pageable_ms,
+                             "api": "the same calls into an ordinary (pageable, written) numpy array"}},
         "cpu_baseline": cpu_baseline(a.workload, a.cpu_passes, 3.0, rank) if a.cpu_passes > 0 else None,
         "clocks": clocks,
         "gpu_launches": a.steps,
