@@ -124,27 +124,24 @@ bool pageable_direct_supported()
     return v == 2;
 }
 
-// True when the pages of [p, p + bytes) are resident (one mincore call; above 64 Ki pages, the
-// first, middle and last page).  A kernel storing into pages nobody has touched yet would
-// populate them one device fault at a time (a fresh 64 MB buffer took 20 ms that way), so such
-// outputs are staged instead and the host touches them.
+// True when every page of [p, p + bytes) is mapped and resident (mincore, in windows of 64 Ki
+// pages; it fails on unmapped addresses).  A kernel storing into pages nobody has touched yet
+// would populate them one device fault at a time (a fresh 64 MB buffer took 20 ms that way), so
+// such outputs are staged instead and the host touches them.
 bool pages_resident(const void* p, size_t bytes)
 {
     static const uintptr_t page = (uintptr_t)sysconf(_SC_PAGESIZE);
+    constexpr size_t kWindow = size_t(1) << 16;           // pages per mincore call
     const uintptr_t a = (uintptr_t)p, first = a & ~(page - 1), last = (a + bytes - 1) & ~(page - 1);
     const size_t pages = (size_t)((last - first) / page) + 1;
-    if (pages <= 65536) {
-        thread_local std::vector<unsigned char> v;
-        v.resize(pages);
-        if (mincore(reinterpret_cast<void*>(first), (size_t)(last - first) + page, v.data()) != 0) return false;
-        for (unsigned char c : v)
-            if (!(c & 1)) return false;
-        return true;
-    }
-    const uintptr_t probes[3] = {first, (a + bytes / 2) & ~(page - 1), last};
-    for (uintptr_t q : probes) {
-        unsigned char c = 0;
-        if (mincore(reinterpret_cast<void*>(q), 1, &c) != 0 || !(c & 1)) return false;
+    thread_local std::vector<unsigned char> v;
+    v.resize(std::min(pages, kWindow));
+    for (size_t done = 0; done < pages;) {
+        const size_t n = std::min(pages - done, kWindow);
+        if (mincore(reinterpret_cast<void*>(first + done * page), n * page, v.data()) != 0) return false;
+        for (size_t i = 0; i < n; ++i)
+            if (!(v[i] & 1)) return false;
+        done += n;
     }
     return true;
 }
