@@ -47,7 +47,7 @@ def test_two_gloo_ranks_barrier_and_max():
 
 
 def test_reference_arm_under_torchrun_prints_once():
-    """`bench.py --impl reference` launched like the driver's N>1 runs: rank 0 prints the
+    """`bench.py --impl reference` launched as an N>1 job under torchrun: rank 0 prints the
     single JSON line, the other rank exits 0 without work."""
     pytest.importorskip("torch")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
