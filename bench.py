@@ -407,6 +407,8 @@ def run_chunkmix(a, rank, world, local):
         # (ncu --nvtx --nvtx-include "<label>/")
         st = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
         en = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+        flush.zero_()
+        fnc()                                       # one more untimed step: clocks back up after the idle wait
         for i in range(steps):
             flush.zero_()
             torch.cuda.nvtx.range_push(label)
@@ -746,6 +748,9 @@ def run_mesh(a, rank, world, local):
     sampler = ClockSampler(local)
     with sampler:
         barrier(world)
+        step()                                      # one more untimed step: clocks back up after the idle wait
+        torch.cuda.synchronize(dev)
+        faces.clear()
         st = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
         en = [torch.cuda.Event(enable_timing=True) for _ in range(a.steps)]
         for i in range(a.steps):
@@ -836,6 +841,8 @@ def run_grid(a, rank, world, local):
     sampler = ClockSampler(local)
     with sampler:
         barrier(world)
+        flush.zero_()
+        step()                                      # one more untimed step: clocks back up after the idle wait
         torch.cuda.synchronize(dev)
         for i in range(a.steps):
             flush.zero_()
