@@ -472,23 +472,27 @@ def run_chunkmix(a, rank, world, local):
 
     # end to end: the same requests with host outputs (fnGenBatchHost: descriptors up, every
     # output and min/max down, slices copied while the next slice is generated)
+    def host_batch_ms(base):
+        hreqs, off = [], 0
+        for c in chunks:
+            kind = fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D
+            hreqs.append(fn.make_request(nodes[c.tree], kind, base + 4 * off, c.seed + rank, c.count, c.offset, (1, 1, 1, 1)))
+            off += c.points
+        harr = fn.request_array(hreqs)
+        e2e = []
+        for i in range(2 + a.e2e_steps):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            fn.gen_batch_host(harr)
+            if i >= 2:
+                e2e.append((time.perf_counter() - t0) * 1e3)
+        return (allmax(statistics.median(e2e), world) if e2e else None), fn.batch_info()
+
     host = torch.empty(pts, dtype=torch.float32, pin_memory=True)
-    hreqs, off = [], 0
-    for c in chunks:
-        kind = fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D
-        hreqs.append(fn.make_request(nodes[c.tree], kind, host.data_ptr() + 4 * off, c.seed + rank, c.count, c.offset,
-                                     (1, 1, 1, 1)))
-        off += c.points
-    harr = fn.request_array(hreqs)
-    e2e = []
-    for i in range(2 + a.e2e_steps):
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        fn.gen_batch_host(harr)
-        if i >= 2:
-            e2e.append((time.perf_counter() - t0) * 1e3)
-    e2e_ms = allmax(statistics.median(e2e), world) if e2e else None
-    hinfo = fn.batch_info()
+    e2e_ms, hinfo = host_batch_ms(host.data_ptr())
+    pageable = np.zeros(pts, np.float32) + 0.0                 # an ordinary (written) array, as most callers pass
+    pageable_ms, _ = host_batch_ms(pageable.ctypes.data)
+    del pageable
     # the plain copy engine rate for the same bytes (device outputs -> the pinned host buffer)
     c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     host.copy_(out, non_blocking=True)
@@ -543,7 +547,11 @@ def run_chunkmix(a, rank, world, local):
                 "h2d_bytes_per_step": hinfo["uploadBytes"], "d2h_bytes_per_step": pts * 4 + 8 * len(chunks),
                 "ms_per_step": e2e_ms, "d2h_copy_gbs": d2h_gbs,
                 "api": "fnGenBatchHost: host (pinned) outputs; request descriptors uploaded, every output and "
-                       "min/max read back, slices of 2^25 points copied while the next slice is generated"},
+                       "min/max read back, slices of 2^25 points copied while the next slice is generated",
+                "pageable": {"value": pts * world / (pageable_ms * 1e-3) / 1e6 if pageable_ms else None, "unit": "Mpoints/s",
+                             "ms_per_step": pageable_ms,
+                             "api": "the same call into an ordinary (pageable, written) array: on a Grace host the batch "
+                                    "kernels store into it directly"}},
         "batch": binfo,
         "cpu_baseline": cpu,
         "clocks": clocks,

@@ -146,13 +146,27 @@ bool pages_resident(const void* p, size_t bytes)
     return true;
 }
 
-float* host_direct_view(float* p, size_t bytes)
+bool host_direct_allowed()
 {
     static const bool allowed = [] {
         const char* env = std::getenv("FASTNOISE_HOST_DIRECT");
         return !(env && env[0] == '0');
     }();
-    if (!p || !allowed) return nullptr;
+    return allowed;
+}
+
+// Ordinary (pageable) host memory the device stores into coherently, with every page resident.
+bool pageable_direct(float* p, size_t bytes)
+{
+    if (!p || !host_direct_allowed()) return false;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) { cudaGetLastError(); return false; }
+    return at.type == cudaMemoryTypeUnregistered && pageable_direct_supported() && pages_resident(p, bytes);
+}
+
+float* host_direct_view(float* p, size_t bytes)
+{
+    if (!p || !host_direct_allowed()) return nullptr;
     cudaPointerAttributes at{};
     if (cudaPointerGetAttributes(&at, p) != cudaSuccess) { cudaGetLastError(); return nullptr; }
     if (at.type == cudaMemoryTypeHost) return pinned_device_view(p, bytes);
@@ -988,11 +1002,51 @@ int fnGenBatchHost(const fnGenRequest* requests, int count, int flags)
         points[(size_t)i] = (size_t)a.total;
         largest = std::max(largest, points[(size_t)i]);
     }
+    // Outputs in ordinary (pageable, resident) memory on a device that stores into it coherently:
+    // the batch kernels store into them directly.  Copies into pageable memory run at about half
+    // the speed of copies into page-locked memory (the chunk mix: 18.1 ms staged, 13.5 ms direct;
+    // into page-locked memory staging stays faster, 9.5 ms).  Checked per run of requests whose
+    // outputs are contiguous, for at most 256 runs.
+    bool direct = host_direct_allowed();
+    int runs = 0;
+    for (int j = 0; direct && j < count;) {
+        if (!points[(size_t)j]) { ++j; continue; }
+        float* dst = requests[j].out;
+        size_t n = points[(size_t)j];
+        int e = j + 1;
+        while (e < count && (!points[(size_t)e] || requests[e].out == dst + n)) n += points[(size_t)e++];
+        direct = ++runs <= 256 && pageable_direct(dst, n * sizeof(float));
+        j = e;
+    }
     const size_t cap = std::max(kHostSlicePoints, largest);
-    HostBatchCtx* h = host_batch_ctx(cap, (size_t)count);
+    HostBatchCtx* h = host_batch_ctx(direct ? 0 : cap, (size_t)count);
     if (!h) return FN_ERR_CUDA;
     h->info = fnBatchInfo{};
     h->info_valid = false;
+    if (direct) {
+        std::vector<fnGenRequest> dreqs(requests, requests + count);
+        for (auto& r : dreqs) r.minMax = nullptr;
+        BatchCtx* lane = &h->lane[0];
+        const int rc = run_batch(dreqs.data(), count, h->gen[0], 0, nullptr, lane);
+        if (rc) return rc;
+        const BatchRunner& r = lane->runner;
+        h->info.requests = count;
+        h->info.specialised = r.last_specialised() ? 1 : 0;
+        h->info.tilePoints = (int)r.last_tile_points();
+        h->info.ctas = r.last_grid();
+        h->info.workItems = r.last_items();
+        h->info.points = r.last_points();
+        h->info.uploadBytes = r.last_upload_bytes();
+        h->info.kernels = r.last_kernels();
+        if (!cuda_ok(cudaMemcpyAsync(h->hmm, lane->dminmax, (size_t)count * 2 * sizeof(float), cudaMemcpyDeviceToHost, h->gen[0]),
+                     "copy minmax") ||
+            !cuda_ok(cudaStreamSynchronize(h->gen[0]), "synchronize"))
+            return FN_ERR_CUDA;
+        for (int i = 0; i < count; ++i)
+            if (requests[i].minMax) { requests[i].minMax[0] = h->hmm[2 * i]; requests[i].minMax[1] = h->hmm[2 * i + 1]; }
+        h->info_valid = true;
+        return FN_OK;
+    }
     std::vector<fnGenRequest> slice;
     size_t remaining = 0;
     for (size_t p : points) remaining += p;

@@ -210,7 +210,10 @@ FASTNOISE_API int fnGenBatchDevice(const fnGenRequest* requests, int count, void
  * most 2^25 points (smaller at the start and the end) through two device staging buffers, each
  * slice's copy to the host overlapping the next slice's generation; requests whose outputs are
  * adjacent in host memory are copied together.  fnGetBatchInfo then reports the slices summed.
- * flags: reserved, pass 0. */
+ * Exception: when every output lies in ordinary (pageable) memory whose pages are resident, on
+ * a device that accesses pageable memory through the host's page tables (a Grace host), the
+ * batch kernels store into the outputs directly (copies into pageable memory are slower);
+ * FASTNOISE_HOST_DIRECT=0 turns this off.  flags: reserved, pass 0. */
 FASTNOISE_API int fnGenBatchHost(const fnGenRequest* requests, int count, int flags);
 /* The per-call path for the same request list: one plain launch per request, queued in
  * order on `stream` (what a caller looping over fnGen*Device would do), for comparison

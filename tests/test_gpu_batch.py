@@ -102,12 +102,14 @@ def test_bad_request_fails_loudly(gpu, torch_cuda):
         fn.gen_batch([fn.make_request(node, fn.KIND_GRID2D, out.data_ptr(), 1, (4, 4))])
 
 
-@pytest.mark.parametrize("mode", ["pinned", "pageable", "pinned-and-pageable"])
+@pytest.mark.parametrize("mode", ["pinned", "pageable", "pinned-and-pageable", "pageable-written", "block-written"])
 def test_batch_host_outputs_match_device_batch(gpu, torch_cuda, mode):
     """fnGenBatchHost: outputs in one page-locked block (contiguous runs copied together),
-    separate pageable arrays, or one request outside the page-locked block; slices across both
-    staging buffers (the mix is larger than one 2^25-point slice), a request larger than a
-    slice, and empty requests; outputs and min/max equal the device batch's."""
+    separate fresh pageable arrays, or one request outside the page-locked block (all staged:
+    slices across both staging buffers, the mix being larger than one 2^25-point slice); and
+    separate or contiguous pageable arrays already written (stored into directly by the batch
+    kernels where the device reads host page tables); a request larger than a slice and empty
+    requests; outputs and min/max equal the device batch's."""
     fn, torch = gpu, torch_cuda
     chunks = chunkmix.make_mix(40, seed=19, sizes=[(128, 128, 64), (96, 80, 70), (0, 5, 5), (17, 3)])
     chunks.append(chunkmix.Chunk(tree=1, count=(384, 320, 300), offset=(-5.0, 7.0, 3.0), seed=77))   # 36.9 M points
@@ -115,12 +117,20 @@ def test_batch_host_outputs_match_device_batch(gpu, torch_cuda, mode):
     dreqs, douts, dmms = requests_for(fn, torch, chunks, nodes)
     fn.gen_batch(dreqs, sync=True)
     total = sum(c.points for c in chunks)
-    block = torch.empty(max(total, 1), dtype=torch.float32, pin_memory=True).numpy()
-    block[:] = np.nan
+    if mode == "block-written":
+        block = np.full(max(total, 1), np.nan, np.float32)
+    else:
+        block = torch.empty(max(total, 1), dtype=torch.float32, pin_memory=True).numpy()
+        block[:] = np.nan
     hreqs, houts, hmms, off = [], [], [], 0
     for k, c in enumerate(chunks):
-        pinned = mode.startswith("pinned") and not (mode == "pinned-and-pageable" and k == 7)
-        out = block[off:off + c.points] if pinned else np.empty(c.points, np.float32)
+        in_block = mode in ("pinned", "block-written") or (mode == "pinned-and-pageable" and k != 7)
+        if in_block:
+            out = block[off:off + c.points]
+        elif mode == "pageable-written":
+            out = np.full(c.points, np.nan, np.float32)
+        else:
+            out = np.empty(c.points, np.float32)
         off += c.points
         mm = np.zeros(2, np.float32)
         kind = fn.KIND_GRID3D if len(c.count) == 3 else fn.KIND_GRID2D
