@@ -16,6 +16,7 @@ import fails; if a call cannot run on the GPU, :class:`FastNoiseError` is raised
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 from typing import Optional, Sequence, Tuple, Union
 
@@ -51,13 +52,13 @@ def _declare(L):
         "fnDeleteNodeRef": (None, [vp]),
         "fnGetActiveFeatureSet": (c_uint, [vp]),
         "fnGetMetadataID": (c_int, [vp]),
-        "fnGenUniformGrid2D": (None, [vp, _FP, c_float, c_float, c_int, c_int, c_float, c_float, c_int, _FP]),
-        "fnGenUniformGrid3D": (None, [vp, _FP, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, _FP]),
-        "fnGenUniformGrid4D": (None, [vp, _FP] + [c_float] * 4 + [c_int] * 4 + [c_float] * 4 + [c_int, _FP]),
-        "fnGenPositionArray2D": (None, [vp, _FP, c_int, _FP, _FP, c_float, c_float, c_int, _FP]),
-        "fnGenPositionArray3D": (None, [vp, _FP, c_int, _FP, _FP, _FP, c_float, c_float, c_float, c_int, _FP]),
-        "fnGenPositionArray4D": (None, [vp, _FP, c_int, _FP, _FP, _FP, _FP, c_float, c_float, c_float, c_float, c_int, _FP]),
-        "fnGenTileable2D": (None, [vp, _FP, c_int, c_int, c_float, c_float, c_int, _FP]),
+        "fnGenUniformGrid2D": (None, [vp, vp, c_float, c_float, c_int, c_int, c_float, c_float, c_int, vp]),
+        "fnGenUniformGrid3D": (None, [vp, vp, c_float, c_float, c_float, c_int, c_int, c_int, c_float, c_float, c_float, c_int, vp]),
+        "fnGenUniformGrid4D": (None, [vp, vp] + [c_float] * 4 + [c_int] * 4 + [c_float] * 4 + [c_int, vp]),
+        "fnGenPositionArray2D": (None, [vp, vp, c_int, vp, vp, c_float, c_float, c_int, vp]),
+        "fnGenPositionArray3D": (None, [vp, vp, c_int, vp, vp, vp, c_float, c_float, c_float, c_int, vp]),
+        "fnGenPositionArray4D": (None, [vp, vp, c_int, vp, vp, vp, vp, c_float, c_float, c_float, c_float, c_int, vp]),
+        "fnGenTileable2D": (None, [vp, vp, c_int, c_int, c_float, c_float, c_int, vp]),
         "fnGenSingle2D": (c_float, [vp, c_float, c_float, c_int]),
         "fnGenSingle3D": (c_float, [vp, c_float, c_float, c_float, c_int]),
         "fnGenSingle4D": (c_float, [vp, c_float, c_float, c_float, c_float, c_int]),
@@ -185,6 +186,11 @@ def _check():
 
 def _fp(a: np.ndarray):
     return a.ctypes.data_as(_FP)
+
+
+def _i32(v) -> int:
+    """An integer wrapped to int32 (seeds are int32 in the C interface)."""
+    return ((int(v) + 0x80000000) & 0xFFFFFFFF) - 0x80000000
 
 
 KIND_GRID2D, KIND_GRID3D, KIND_GRID4D, KIND_TILEABLE2D, KIND_POSITIONS2D, KIND_POSITIONS3D, KIND_POSITIONS4D = range(7)
@@ -742,19 +748,15 @@ class Node:
     def gen_uniform_grid(self, offset: Sequence[float], count: Sequence[int], step: Sequence[float], seed: int,
                          out: Optional[np.ndarray] = None) -> Tuple[np.ndarray, Tuple[float, float]]:
         dim = len(count)
-        total = int(np.prod([max(int(c), 0) for c in count]))
+        total = math.prod(max(int(c), 0) for c in count)
         if out is None:
             out = np.empty(max(total, 1), np.float32)
         mm = np.zeros(2, np.float32)
         L = lib()
-        if dim == 2:
-            L.fnGenUniformGrid2D(self._h, _fp(out), *map(float, offset), *map(int, count), *map(float, step), int(np.int32(seed)), _fp(mm))
-        elif dim == 3:
-            L.fnGenUniformGrid3D(self._h, _fp(out), *map(float, offset), *map(int, count), *map(float, step), int(np.int32(seed)), _fp(mm))
-        elif dim == 4:
-            L.fnGenUniformGrid4D(self._h, _fp(out), *map(float, offset), *map(int, count), *map(float, step), int(np.int32(seed)), _fp(mm))
-        else:
+        f = {2: L.fnGenUniformGrid2D, 3: L.fnGenUniformGrid3D, 4: L.fnGenUniformGrid4D}.get(dim)
+        if f is None:
             raise ValueError("dimension must be 2, 3 or 4")
+        f(self._h, out.ctypes.data, *offset, *count, *step, _i32(seed), mm.ctypes.data)
         _check()
         return out[:total], (float(mm[0]), float(mm[1]))
 
@@ -776,15 +778,10 @@ class Node:
             out = np.empty(max(count, 1), np.float32)
         mm = np.zeros(2, np.float32)
         L = lib()
-        s = int(np.int32(seed))
-        if dim == 2:
-            L.fnGenPositionArray2D(self._h, _fp(out), count, *map(_fp, arrs), *map(float, offset), s, _fp(mm))
-        elif dim == 3:
-            L.fnGenPositionArray3D(self._h, _fp(out), count, *map(_fp, arrs), *map(float, offset), s, _fp(mm))
-        elif dim == 4:
-            L.fnGenPositionArray4D(self._h, _fp(out), count, *map(_fp, arrs), *map(float, offset), s, _fp(mm))
-        else:
+        f = {2: L.fnGenPositionArray2D, 3: L.fnGenPositionArray3D, 4: L.fnGenPositionArray4D}.get(dim)
+        if f is None:
             raise ValueError("dimension must be 2, 3 or 4")
+        f(self._h, out.ctypes.data, count, *(a.ctypes.data for a in arrs), *offset, _i32(seed), mm.ctypes.data)
         _check()
         return out[:count], (float(mm[0]), float(mm[1]))
 
@@ -794,7 +791,8 @@ class Node:
         if out is None:
             out = np.empty(max(total, 1), np.float32)
         mm = np.zeros(2, np.float32)
-        lib().fnGenTileable2D(self._h, _fp(out), int(size[0]), int(size[1]), float(step[0]), float(step[1]), int(np.int32(seed)), _fp(mm))
+        lib().fnGenTileable2D(self._h, out.ctypes.data, int(size[0]), int(size[1]), float(step[0]), float(step[1]), _i32(seed),
+                              mm.ctypes.data)
         _check()
         return out[:total], (float(mm[0]), float(mm[1]))
 
