@@ -91,3 +91,14 @@ def test_one_tree_many_threads(gpu):
     r = subprocess.run([exe, "threads", "8"], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "0 mismatches" in r.stdout
+
+
+def test_drop_in_call_latency(gpu):
+    """The C interface called from C++ (tests/cpp/latency_check.cpp): the config-0 grid into
+    device, page-locked and std::vector outputs, all bit-identical; the per-call medians are
+    printed (pytest -s) beside the round trip of an empty GPU operation."""
+    exe = build_check.build("latency_check")
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "0 mismatches" in r.stdout
+    print(r.stdout.strip().splitlines()[0])
