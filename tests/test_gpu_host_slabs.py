@@ -123,14 +123,18 @@ got, mm = node.gen_uniform_grid((-3.0, 4.0, 5.0), (64, 48, 40), (1.0, 0.5, 2.0),
 rng = np.random.default_rng(5)
 xyz = [rng.uniform(-1e4, 1e4, 5000).astype(np.float32) for _ in range(3)]
 pos, pmm = node.gen_position_array(xyz, (0.5, 0.25, -1.0), 2024, out=np.full(5000, np.nan, np.float32))
-np.save(sys.argv[2], np.concatenate([got, np.array(mm, np.float32), pos, np.array(pmm, np.float32)]))
+batch = np.full(2 * 32 ** 3, np.nan, np.float32)              # one ordinary array, two requests
+bmm = np.zeros(4, np.float32)
+fn.gen_batch_host([fn.make_request(node, fn.KIND_GRID3D, batch.ctypes.data + 4 * k * 32 ** 3, 5 + k, (32, 32, 32),
+                                   (float(k), 1.0, 2.0), (1, 1, 1), minmax=bmm[2 * k:2 * k + 2]) for k in range(2)])
+np.save(sys.argv[2], np.concatenate([got, np.array(mm, np.float32), pos, np.array(pmm, np.float32), batch, bmm]))
 """
 
 
 def test_host_direct_stores_can_be_turned_off(gpu, tmp_path):
     """FASTNOISE_HOST_DIRECT=0 stages every host output in device memory and copies it (and
-    copies position arrays to the device); the results equal the direct stores and in-place
-    position reads of this process."""
+    copies position arrays to the device), for the per-call host calls and fnGenBatchHost; the
+    results equal the direct stores and in-place position reads of this process."""
     import os
     import subprocess
     import sys
@@ -147,8 +151,16 @@ def test_host_direct_stores_can_be_turned_off(gpu, tmp_path):
     rng = np.random.default_rng(5)
     xyz = [rng.uniform(-1e4, 1e4, 5000).astype(np.float32) for _ in range(3)]      # resident: read in place
     pos, pmm = node.gen_position_array(xyz, (0.5, 0.25, -1.0), 2024, out=np.full(5000, np.nan, np.float32))
+    batch = np.full(2 * 32 ** 3, np.nan, np.float32)          # resident: the batch kernels store into it
+    bmm = np.zeros(4, np.float32)
+    fn = gpu
+    fn.gen_batch_host([fn.make_request(node, fn.KIND_GRID3D, batch.ctypes.data + 4 * k * 32 ** 3, 5 + k, (32, 32, 32),
+                                       (float(k), 1.0, 2.0), (1, 1, 1), minmax=bmm[2 * k:2 * k + 2]) for k in range(2)])
     n = got.size
     assert np.array_equal(staged[:n].view(np.uint32), got.view(np.uint32))
     assert (float(staged[n]), float(staged[n + 1])) == mm
     assert np.array_equal(staged[n + 2:n + 2 + 5000].view(np.uint32), pos.view(np.uint32))
-    assert (float(staged[-2]), float(staged[-1])) == pmm
+    assert (float(staged[n + 5002]), float(staged[n + 5003])) == pmm
+    tail = staged[n + 5004:]
+    assert np.array_equal(tail[:batch.size].view(np.uint32), batch.view(np.uint32))
+    assert np.array_equal(tail[batch.size:].view(np.uint32), bmm.view(np.uint32))
