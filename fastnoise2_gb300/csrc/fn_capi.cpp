@@ -597,6 +597,19 @@ struct HostBatchCtx {
 };
 thread_local HostBatchCtx* t_hbatch = nullptr;
 
+// Add one launch of `r` (over `requests` requests) to the summary of a host batch call.
+void add_launch(fnBatchInfo& info, const BatchRunner& r, int requests)
+{
+    info.requests += requests;
+    info.specialised = r.last_specialised() ? 1 : 0;
+    info.tilePoints = (int)r.last_tile_points();
+    info.ctas = r.last_grid();
+    info.workItems += r.last_items();
+    info.points += r.last_points();
+    info.uploadBytes += r.last_upload_bytes();
+    info.kernels += r.last_kernels();
+}
+
 HostBatchCtx* host_batch_ctx(size_t stage_floats, size_t requests)
 {
     if (!t_hbatch) {
@@ -1029,15 +1042,7 @@ int fnGenBatchHost(const fnGenRequest* requests, int count, int flags)
         BatchCtx* lane = &h->lane[0];
         const int rc = run_batch(dreqs.data(), count, h->gen[0], 0, nullptr, lane);
         if (rc) return rc;
-        const BatchRunner& r = lane->runner;
-        h->info.requests = count;
-        h->info.specialised = r.last_specialised() ? 1 : 0;
-        h->info.tilePoints = (int)r.last_tile_points();
-        h->info.ctas = r.last_grid();
-        h->info.workItems = r.last_items();
-        h->info.points = r.last_points();
-        h->info.uploadBytes = r.last_upload_bytes();
-        h->info.kernels = r.last_kernels();
+        add_launch(h->info, lane->runner, count);
         if (!cuda_ok(cudaMemcpyAsync(h->hmm, lane->dminmax, (size_t)count * 2 * sizeof(float), cudaMemcpyDeviceToHost, h->gen[0]),
                      "copy minmax") ||
             !cuda_ok(cudaStreamSynchronize(h->gen[0]), "synchronize"))
@@ -1072,15 +1077,7 @@ int fnGenBatchHost(const fnGenRequest* requests, int count, int flags)
         if (!cuda_ok(cudaStreamWaitEvent(gen, h->copy_done[buf], 0), "wait")) return FN_ERR_CUDA;
         const int rc = run_batch(slice.data(), (int)slice.size(), gen, FN_BATCH_NO_GRAPH, nullptr, lane);
         if (rc) return rc;
-        const BatchRunner& r = lane->runner;
-        h->info.requests += (int)slice.size();
-        h->info.specialised = r.last_specialised() ? 1 : 0;
-        h->info.tilePoints = (int)r.last_tile_points();
-        h->info.ctas = r.last_grid();
-        h->info.workItems += r.last_items();
-        h->info.points += r.last_points();
-        h->info.uploadBytes += r.last_upload_bytes();
-        h->info.kernels += r.last_kernels();
+        add_launch(h->info, lane->runner, (int)slice.size());
         if (!cuda_ok(cudaMemcpyAsync(h->hmm + 2 * (size_t)i0, lane->dminmax, slice.size() * 2 * sizeof(float),
                                      cudaMemcpyDeviceToHost, gen), "copy minmax") ||
             !cuda_ok(cudaEventRecord(h->gen_done[buf], gen), "record") ||
